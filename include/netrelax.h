@@ -1,0 +1,301 @@
+/*
+ * netrelax.h — C ABI of the GB300 (sm_103a) implementation of the
+ * quasi-static strain-and-relax loop for 2D elastic fiber networks
+ * (FIRE minimisation of bond stretch + fiber bending).
+ *
+ * Reference: jmichelstl/network_relaxation, src/large_strain_relax.cu.
+ * Every entry point names the reference interface it replaces.  Arrays keep
+ * the reference's layouts: positions are 2*N doubles, xy interleaved; a bond
+ * is (i, j, l0, wrap) with the periodic image of j at x + wrap*width; a
+ * bending triple is (hinge, j, k, wrap_j, wrap_k); fcodes are 0 (clamped) or
+ * 3 (free in x and y), bit 0 = x free, bit 1 = y free.
+ *
+ * Threading: no global mutable state except where stated; distinct handles
+ * may be used from distinct host threads.  Device work is queued on the
+ * stream passed in (a cudaStream_t, NULL = legacy default stream).
+ *
+ * The library needs a CUDA device for every entry point that touches device
+ * memory; there is no CPU fallback.  Host-only entry points (network IO,
+ * topology, generators, batch-file parsing) work without a GPU.
+ */
+#ifndef NETRELAX_H
+#define NETRELAX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NR_ABI_VERSION 1
+
+/* Replaces the reference's bool returns (true = ran, false = cudaMalloc
+ * failed; large_strain_relax.cu:541-548, :596).  NR_OK and
+ * NR_NOT_CONVERGED both correspond to the reference's `true`. */
+typedef enum {
+    NR_OK = 0,
+    NR_NOT_CONVERGED = 1, /* step cap reached before the force criterion */
+    NR_ERR_INVALID = -1,  /* bad argument */
+    NR_ERR_IO = -2,       /* file could not be opened / written */
+    NR_ERR_PARSE = -3,    /* malformed .dat or batch file */
+    NR_ERR_CUDA = -4,     /* CUDA runtime error (message in nr_last_error) */
+    NR_ERR_OOM = -5,      /* device allocation failed */
+    NR_ERR_NONFINITE = -6,/* a force or position became NaN/inf */
+    NR_ERR_TIMEOUT = -7,  /* a grid barrier exceeded its wait budget */
+    NR_ERR_CAPACITY = -8  /* request exceeds a fixed capacity */
+} nr_status;
+
+const char *nr_status_string(int status);
+/* Message of the last error raised on the calling host thread. */
+const char *nr_last_error(void);
+int nr_abi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Host-side networks                                                  */
+/* ------------------------------------------------------------------ */
+
+typedef struct nr_host_network nr_host_network;
+
+typedef struct {
+    int n_points, n_edges, n_triples;
+    double offset;     /* x period ("width", the header's third field) */
+    double miny, maxy; /* as computed by the reader (max starts at FLT_MIN) */
+    int has_bond_k, has_tri_kb, has_tri_phi0;
+} nr_host_info;
+
+/* read_network (large_strain_relax.cu:42-114): same parsing rules, same
+ * rest lengths l0 = sqrt(dx*dx + dy*dy), same error cases.  On NR_ERR_PARSE
+ * the partially read network is still returned in *out (the reference keeps
+ * going with whatever it read); the caller frees it. */
+int nr_read_network(const char *path, nr_host_network **out);
+
+/* get_triples (large_strain_relax.cu:116-184): the collinear (antiparallel
+ * to absolute tolerance 1e-10) bond pairs at each hinge, same set and order.
+ * Replaces any triples already held. */
+int nr_get_triples(nr_host_network *net);
+
+/* Builds a network from arrays.  edge_l0 may be NULL: rest lengths are then
+ * computed from the points exactly as read_network does. */
+int nr_host_network_from_arrays(int n_points, const double *points, int n_edges, const int *edge_ij,
+                                const double *edge_l0, const signed char *edge_wrap, double offset,
+                                nr_host_network **out);
+/* Extensions with no reference counterpart (the reference hard-wires one
+ * ks, one kb and theta0 = pi): explicit triples with optional per-triple kb
+ * and rest-angle offset phi0 = theta0 - pi, and per-bond stiffness. */
+int nr_host_network_set_triples(nr_host_network *net, int n_triples, const int *tri_hjk, const signed char *tri_wrap,
+                                const double *tri_kb, const double *tri_phi0);
+int nr_host_network_set_bond_k(nr_host_network *net, const double *bond_k);
+void nr_host_network_info(const nr_host_network *net, nr_host_info *info);
+/* Copies out the arrays; any pointer may be NULL. */
+void nr_host_network_arrays(const nr_host_network *net, double *points, int *edge_ij, double *edge_l0,
+                            signed char *edge_wrap, int *tri_hjk, signed char *tri_wrap, double *bond_k,
+                            double *tri_kb, double *tri_phi0);
+/* fcodes (large_strain_relax.cu:895-901): 0 for y < miny+1e-10 or
+ * y > maxy-1e-10, else 3. */
+void nr_host_network_fcodes(const nr_host_network *net, unsigned char *fcodes);
+/* Writes the .dat format read_network reads (%.17g, round-trips exactly). */
+int nr_write_network(const nr_host_network *net, const char *path);
+void nr_host_network_free(nr_host_network *net);
+
+/* Synthetic inputs (no reference counterpart; the reference ships none).
+ * Diluted triangular lattice, nx columns x ny rows, unit spacing, rows at
+ * y = j*sqrt(3)/2, odd rows shifted by +0.5, x-periodic with period nx.
+ * Node (i,j) owns its right, up-left and up-right bonds, each kept with
+ * probability p (SplitMix64 stream from seed).  jitter > 0 moves every node
+ * by U(-jitter, jitter) in x and y (top and bottom rows in x only, so they
+ * stay clamped) before rest lengths are taken.  line_triples != 0 adds
+ * bending triples along the three lattice directions wherever both
+ * collinear bonds survive, with phi0 = rest angle - pi (exactly 0 force at
+ * rest); line_triples == 0 leaves triples to nr_get_triples. */
+int nr_gen_lattice(int nx, int ny, double p, double jitter, uint64_t seed, int line_triples,
+                   nr_host_network **out);
+/* Mikado network in the unit box: n_fibers straight fibers of length
+ * fiber_len with uniform centres and angles, x-periodic, cut at y = 0 and
+ * y = 1; every crossing becomes a node, segments between consecutive nodes
+ * on a fiber become bonds with per-bond k = k0 / l0; dangling ends are
+ * pruned repeatedly; consecutive segment pairs along a fiber become triples
+ * with kb = kappa0 / mean(l0 of the two segments) and their rest angle. */
+int nr_gen_mikado(int n_fibers, double fiber_len, double k0, double kappa0, uint64_t seed,
+                  nr_host_network **out);
+
+/* ------------------------------------------------------------------ */
+/* FIRE parameters and reports                                         */
+/* ------------------------------------------------------------------ */
+
+enum { NR_CRIT_RMS = 0, NR_CRIT_MAX = 1 };
+enum { NR_FP64 = 0, NR_MIXED = 1 };
+
+typedef struct {
+    /* fire_params[5] of run_fire_md (large_strain_relax.cu:610-614) */
+    double alpha0, falpha, dt_max, finc, fdec;
+    int nmin;
+    double mass;
+    double fcut;
+    int max_steps;
+    /* NR_CRIT_RMS: |F|/sqrt(2N) < fcut (large_strain_relax.cu:716);
+     * NR_CRIT_MAX: max_i |F_i| < fcut. */
+    int criterion;
+    /* NR_FP64 (plain, bit-reproducible) or NR_MIXED (FP32 bulk with FP64
+     * anchors, reductions and a final FP64 certification). */
+    int precision;
+} nr_fire_params;
+
+/* report_data[3] of run_fire_md plus the step count and extras. */
+typedef struct {
+    double rms_force; /* report_data[0]: |F|/sqrt(2N) */
+    double e_stretch; /* report_data[1] */
+    double e_bend;    /* report_data[2] */
+    double max_force; /* max_i |F_i| */
+    int steps;        /* step_count */
+    int status;       /* nr_status of this relaxation */
+    int fp64_steps;   /* iterations taken in FP64 (mixed precision only) */
+    int reserved;
+} nr_report;
+
+/* ------------------------------------------------------------------ */
+/* Device-resident network                                             */
+/* ------------------------------------------------------------------ */
+
+typedef struct nr_network nr_network;
+
+/* Uploads topology and positions, builds the per-node incidence lists
+ * (copy_bond_data / copy_triple_data, large_strain_relax.cu:552-594, plus
+ * the fcodes of :895-902).  Bonds are used when ks > 0 and triples when
+ * kb > 0 (:629, :634).  Stream may be NULL. */
+int nr_network_create(const nr_host_network *net, double ks, double kb, void *stream, nr_network **out);
+int nr_network_destroy(nr_network *dnet);
+int nr_network_n_points(const nr_network *dnet);
+int nr_network_set_positions(nr_network *dnet, const double *host_xy, void *stream);
+int nr_network_get_positions(const nr_network *dnet, double *host_xy, void *stream);
+/* Device pointer to the 2*N positions (valid until destroy). */
+double *nr_network_positions_device(nr_network *dnet);
+
+/* affine_displace (large_strain_relax.cu:527-537) over the N nodes:
+ * x += xdisp*(y-miny)/yrange; y += ydisp*(y-miny)/yrange, bit-exact. */
+int nr_affine_displace(nr_network *dnet, double miny, double yrange, double xdisp, double ydisp, void *stream);
+
+/* run_fire_md (large_strain_relax.cu:596-762) on a device network: v and F
+ * reset, FIRE to the force criterion or max_steps, energies at the end.
+ * Blocks until the report is on the host. */
+int nr_relax(nr_network *dnet, const nr_fire_params *params, nr_report *report, void *stream);
+
+/* Forces at the current positions (axial_forces + bending_forces,
+ * large_strain_relax.cu:386-469), copied to host_f (2*N doubles). */
+int nr_forces(nr_network *dnet, double *host_f, void *stream);
+/* axial_energies + bending_energies summed (large_strain_relax.cu:472-523,
+ * :743, :751). */
+int nr_energies(nr_network *dnet, double *e_stretch, double *e_bend, void *stream);
+
+/* One record per relaxation of the strain protocol (the values
+ * do_relaxation_run prints, large_strain_relax.cu:942-954, :983-994). */
+typedef struct {
+    double curr_disp; /* shear displacement (compression rows: 0) */
+    double max_comp;  /* compression displacement (compression rows: curr) */
+    double e_stretch, e_bend, rms_force, max_force;
+    int steps;
+    int is_shear;
+    int status;
+    int fp64_steps;
+} nr_step_record;
+
+/* The compression-then-shear loops of do_relaxation_run
+ * (large_strain_relax.cu:917-999) in strain mode: displacements are
+ * strain * yrange; each step applies the increment with affine_displace and
+ * relaxes.  compr / shear = {min, max, inc}.  Writes up to max_records
+ * records; shear_positions (host, may be NULL) receives the relaxed
+ * positions of each shear step (2*N doubles per record). */
+int nr_sweep(nr_network *dnet, double miny, double yrange, const nr_fire_params *params, const double compr[3],
+             const double shear[3], nr_step_record *records, int max_records, int *n_records,
+             double *shear_positions, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in for run_fire_md with the reference's own device arrays      */
+/* ------------------------------------------------------------------ */
+
+/* bool run_fire_md(...) (large_strain_relax.cu:596): same arguments in the
+ * same order and meaning, minus the dim3 launch shapes (the library picks
+ * its own).  d_pos is updated in place; d_vel and d_forces receive the final
+ * velocities and forces.  report_data = {RMS F, E_stretch, E_bend}.  Runs
+ * the FP64 path with the RMS criterion.  Returns NR_OK / NR_NOT_CONVERGED
+ * where the reference returns true. */
+int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double ks, double kb, double *d_pos,
+                   double *d_vel, double *d_forces, const int *d_pair_list, const double *d_lengths,
+                   const signed char *d_e_offsets, const int *d_triples, const signed char *d_t_offsets,
+                   const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
+                   int max_steps, int nmin, double report_data[3], int *step_count, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Batched relaxation of many independent networks in one launch       */
+/* ------------------------------------------------------------------ */
+
+typedef struct nr_batch nr_batch;
+
+/* Uploads n networks into one set of device arrays.  ks[i], kb[i] per
+ * network. */
+int nr_batch_create(int n, const nr_host_network *const *nets, const double *ks, const double *kb, void *stream,
+                    nr_batch **out);
+int nr_batch_destroy(nr_batch *b);
+int nr_batch_size(const nr_batch *b);
+int nr_batch_total_points(const nr_batch *b);
+/* Positions of all networks, concatenated in network order (host). */
+int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream);
+int nr_batch_get_positions(const nr_batch *b, double *host_xy, void *stream);
+/* Device pointer to the concatenated positions. */
+double *nr_batch_positions_device(nr_batch *b);
+/* Per-network affine_displace with per-network miny, yrange, xdisp, ydisp
+ * (host arrays of length n). */
+int nr_batch_affine_displace(nr_batch *b, const double *miny, const double *yrange, const double *xdisp,
+                             const double *ydisp, void *stream);
+/* Relaxes every network (one persistent launch; each network's FIRE state
+ * lives on the device; a network retires when it meets its criterion).
+ * params: one nr_fire_params for all.  reports: n entries (host). */
+int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Driver, batch files and CLI                                         */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+    char base[1024];
+    char tag[256];
+    double ks, kb;
+    double fire_params[5];
+    int nmin;
+    double mass, fcut;
+    int nmax;
+    double compr[3], shear[3];
+    /* 0: displacements are strain * (maxy - miny) (the reference's only
+     * reachable mode); 1: absolute displacements (lsrelax -a). */
+    int absolute;
+} nr_batch_spec;
+
+/* parse_batch_file (large_strain_relax.cu:297-383): six non-comment lines. */
+int nr_parse_batch_file(const char *path, nr_batch_spec *spec);
+
+/* get_file_lists (file_lists.cpp:80-138): the sorted .dat files matching
+ * base*.dat and their _log.txt / _edata.txt / displacement-base names.
+ * Returns the count, or a negative nr_status.  Names are written as
+ * NUL-separated strings into buf (cap bytes); entry i occupies four
+ * consecutive strings: dat, log, disp, edata. */
+int nr_get_file_lists(const char *base, const char *ext, const char *tag, char *buf, size_t cap);
+
+/* do_relaxation_run (large_strain_relax.cu:792-1010) on one network file:
+ * reads it, builds triples when kb > 0, runs the protocol on the GPU and
+ * writes the log, edata and NNN.pos files in the reference's formats.
+ * precision / criterion select the path (the reference: NR_FP64, RMS). */
+int nr_do_relaxation_run(const char *net_file, const char *log_name, const char *edata_name, const char *disp_base,
+                         const nr_batch_spec *spec, int precision, int criterion);
+
+/* relaxation_batch (large_strain_relax.cu:1016-1044). */
+int nr_relaxation_batch(const char *batch_file, int precision, int criterion);
+
+/* The lsrelax command line (large_strain_relax.cu:1047-1126):
+ * -b batch [-x bx] [-y by] [-a] [-i], plus --precision fp64|mixed and
+ * --criterion rms|max. */
+int nr_lsrelax_main(int argc, char **argv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

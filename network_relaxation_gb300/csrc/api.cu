@@ -1,0 +1,565 @@
+/*
+ * C ABI implementation: device images of networks and batches, relaxation
+ * entry points, the strain sweep and the run_fire_md drop-in.
+ *
+ * Every network (or batch of networks) lives in ONE device allocation built
+ * from a host staging image: node state first (x, v, f of all networks
+ * contiguous, so a batch's positions are one array), then the FIRE states,
+ * then per network its topology, incidence lists and reduction scratch.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fire_launch.h"
+#include "nr_device.cuh"
+#include "nr_internal.h"
+
+namespace nr {
+
+#define NR_CUDA_TRY(call)                                                                        \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            return fail(NR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+/* Wait budget of every grid barrier: NR_BARRIER_BUDGET_MS (default 2000). */
+static unsigned long long barrier_budget_ns() {
+    const char *env = getenv("NR_BARRIER_BUDGET_MS");
+    double ms = env ? atof(env) : 2000.0;
+    if (!(ms > 0)) ms = 2000.0;
+    return (unsigned long long)(ms * 1e6);
+}
+
+struct Image {
+    std::vector<char> bytes;
+    size_t add(size_t nbytes, size_t align = 256) {
+        const size_t off = (bytes.size() + align - 1) / align * align;
+        bytes.resize(off + nbytes);
+        return off;
+    }
+    template <class T>
+    size_t put(const T *src, size_t n) {
+        const size_t off = add(n * sizeof(T));
+        if (n) memcpy(bytes.data() + off, src, n * sizeof(T));
+        return off;
+    }
+};
+
+struct NetOff {
+    size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
+    bool has_bond_k, has_tri_kb, has_tri_phi0;
+};
+
+/* Device image of n networks (n = 1 for nr_network). */
+struct DeviceSet {
+    int n_nets = 0;
+    long total_nodes = 0;
+    std::vector<long> node_off;
+    std::vector<NetDev> dev;
+    std::vector<double> miny, maxy;
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    NetDev *dev_array = nullptr;
+    FireState *st = nullptr;
+    int *queue = nullptr;
+    double4 *affine_prm = nullptr;
+    double2 *x_all = nullptr, *v_all = nullptr, *f_all = nullptr;
+    ~DeviceSet() {
+        if (arena) cudaFree(arena);
+    }
+};
+
+static int build_set(int n, const nr_host_network *const *nets, const double *ks, const double *kb,
+                     const unsigned char *const *fcodes_in, cudaStream_t stream, DeviceSet &S) {
+    if (n <= 0) return fail(NR_ERR_INVALID, "network count must be positive");
+    Image img;
+    S.n_nets = n;
+    S.node_off.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        if (!nets[i] || nets[i]->n_points <= 0) return fail(NR_ERR_INVALID, "empty network");
+        S.node_off[i + 1] = S.node_off[i] + nets[i]->n_points;
+    }
+    S.total_nodes = S.node_off[n];
+    const size_t x_off = img.add(sizeof(double2) * S.total_nodes);
+    const size_t v_off = img.add(sizeof(double2) * S.total_nodes);
+    const size_t f_off = img.add(sizeof(double2) * S.total_nodes);
+    const size_t st_off = img.add(sizeof(FireState) * n);
+    const size_t q_off = img.add(256);
+    const size_t aff_off = img.add(sizeof(double4) * n);
+    const size_t dev_off = img.add(sizeof(NetDev) * n);
+    std::vector<NetOff> off(n);
+    for (int i = 0; i < n; ++i) {
+        const nr_host_network &h = *nets[i];
+        memcpy(img.bytes.data() + x_off + sizeof(double2) * S.node_off[i], h.points.data(),
+               sizeof(double) * 2 * h.n_points);
+        std::vector<unsigned char> fc(h.n_points);
+        if (fcodes_in && fcodes_in[i]) memcpy(fc.data(), fcodes_in[i], h.n_points);
+        else nr_host_network_fcodes(&h, fc.data());
+        const int ne = h.n_edges(), nt = h.n_triples();
+        std::vector<int4> bond(ne);
+        for (int e = 0; e < ne; ++e) bond[e] = make_int4(h.edge_ij[2 * e], h.edge_ij[2 * e + 1], h.edge_wrap[e], 0);
+        std::vector<int4> tri(nt);
+        for (int t = 0; t < nt; ++t)
+            tri[t] = make_int4(h.tri_hjk[3 * t], h.tri_hjk[3 * t + 1], h.tri_hjk[3 * t + 2],
+                               (h.tri_wrap[2 * t] & 255) | ((h.tri_wrap[2 * t + 1] & 255) << 8));
+        Incidence inc;
+        build_incidence(h.n_points, h.edge_ij.data(), ne, h.tri_hjk.data(), nt, ks[i] > 0, kb[i] > 0, inc);
+        NetOff &o = off[i];
+        o.fcode = img.put(fc.data(), fc.size());
+        o.bond = img.put(bond.data(), bond.size());
+        o.bond_l0 = img.put(h.edge_l0.data(), h.edge_l0.size());
+        o.has_bond_k = !h.bond_k.empty();
+        o.bond_k = img.put(h.bond_k.data(), h.bond_k.size());
+        o.tri = img.put(tri.data(), tri.size());
+        o.has_tri_kb = !h.tri_kb.empty();
+        o.tri_kb = img.put(h.tri_kb.data(), h.tri_kb.size());
+        o.has_tri_phi0 = !h.tri_phi0.empty();
+        o.tri_phi0 = img.put(h.tri_phi0.data(), h.tri_phi0.size());
+        o.bptr = img.put(inc.bptr.data(), inc.bptr.size());
+        o.bent = img.put(inc.bent.data(), inc.bent.size());
+        o.tptr = img.put(inc.tptr.data(), inc.tptr.size());
+        o.tent = img.put(inc.tent.data(), inc.tent.size());
+        const int tiles = (h.n_points + kTile - 1) / kTile;
+        o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
+        const int tb = (ne + kTile - 1) / kTile, tt = (nt + kTile - 1) / kTile;
+        o.epart = img.add(sizeof(double) * 2 * (size_t)std::max(1, std::max(tb, tt)));
+        S.miny.push_back(h.miny);
+        S.maxy.push_back(h.maxy);
+    }
+    S.arena_bytes = img.bytes.size();
+    cudaError_t e = cudaMalloc((void **)&S.arena, S.arena_bytes);
+    if (e != cudaSuccess) {
+        S.arena = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? NR_ERR_OOM : NR_ERR_CUDA,
+                    std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    char *base = S.arena;
+    S.x_all = (double2 *)(base + x_off);
+    S.v_all = (double2 *)(base + v_off);
+    S.f_all = (double2 *)(base + f_off);
+    S.st = (FireState *)(base + st_off);
+    S.queue = (int *)(base + q_off);
+    S.affine_prm = (double4 *)(base + aff_off);
+    S.dev_array = (NetDev *)(base + dev_off);
+    S.dev.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const nr_host_network &h = *nets[i];
+        const NetOff &o = off[i];
+        NetDev &d = S.dev[i];
+        memset(&d, 0, sizeof(d));
+        d.n = h.n_points;
+        d.n_edges = h.n_edges();
+        d.n_triples = h.n_triples();
+        d.n_tiles = (d.n + kTile - 1) / kTile;
+        d.use_bonds = ks[i] > 0;
+        d.use_triples = kb[i] > 0;
+        d.sub = 8;
+        d.n_units = d.n_tiles;
+        d.width = h.offset;
+        d.ks = ks[i];
+        d.kb = kb[i];
+        d.sqrt_dof = std::sqrt((double)(2L * d.n));
+        d.x = S.x_all + S.node_off[i];
+        d.v = S.v_all + S.node_off[i];
+        d.f = S.f_all + S.node_off[i];
+        d.fcode = (const unsigned char *)(base + o.fcode);
+        d.bond = (const int4 *)(base + o.bond);
+        d.bond_l0 = (const double *)(base + o.bond_l0);
+        d.bond_k = o.has_bond_k ? (const double *)(base + o.bond_k) : nullptr;
+        d.tri = (const int4 *)(base + o.tri);
+        d.tri_kb = o.has_tri_kb ? (const double *)(base + o.tri_kb) : nullptr;
+        d.tri_phi0 = o.has_tri_phi0 ? (const double *)(base + o.tri_phi0) : nullptr;
+        d.bptr = (const int *)(base + o.bptr);
+        d.bent = (const int *)(base + o.bent);
+        d.tptr = (const int *)(base + o.tptr);
+        d.tent = (const int *)(base + o.tent);
+        d.part = (double *)(base + o.part);
+        d.epart = (double *)(base + o.epart);
+        d.st = S.st + i;
+    }
+    memcpy(img.bytes.data() + dev_off, S.dev.data(), sizeof(NetDev) * n);
+    NR_CUDA_TRY(cudaMemcpyAsync(S.arena, img.bytes.data(), S.arena_bytes, cudaMemcpyHostToDevice, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    return NR_OK;
+}
+
+static FireParamsDev to_dev(const nr_fire_params &p) {
+    FireParamsDev q;
+    q.alpha0 = p.alpha0;
+    q.falpha = p.falpha;
+    q.dt_max = p.dt_max;
+    q.finc = p.finc;
+    q.fdec = p.fdec;
+    q.mass = p.mass;
+    q.fcut = p.fcut;
+    q.nmin = p.nmin;
+    q.max_steps = p.max_steps;
+    q.criterion = p.criterion;
+    q.precision = p.precision;
+    return q;
+}
+
+static int check_params(const nr_fire_params *p) {
+    if (!p) return fail(NR_ERR_INVALID, "null FIRE parameters");
+    if (!(p->mass > 0) || !(p->dt_max > 0) || p->max_steps < 0 || (p->criterion != NR_CRIT_RMS && p->criterion != NR_CRIT_MAX) ||
+        (p->precision != NR_FP64 && p->precision != NR_MIXED))
+        return fail(NR_ERR_INVALID, "invalid FIRE parameters");
+    return NR_OK;
+}
+
+static void fill_report(const FireState &st, const NetDev &d, nr_report *rep) {
+    rep->rms_force = st.fmag / d.sqrt_dof;
+    rep->e_stretch = st.e_stretch;
+    rep->e_bend = st.e_bend;
+    rep->max_force = st.maxf;
+    rep->steps = st.step;
+    rep->fp64_steps = st.fp64_steps;
+    rep->reserved = 0;
+    if (st.abort_flag) rep->status = NR_ERR_TIMEOUT;
+    else if (st.status != 0) rep->status = st.status;
+    else rep->status = st.converged ? NR_OK : NR_NOT_CONVERGED;
+}
+
+static int sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+/* One network over the whole GPU (FP64 cooperative kernel + energies). */
+static int relax_single_fp64(DeviceSet &S, int i, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
+    NetDev d = S.dev[i];
+    const int sms = sm_count();
+    int sub = 8;
+    while (sub > 1 && d.n_tiles * (8 / sub) < sms) sub /= 2;
+    d.sub = sub;
+    d.n_units = d.n_tiles * (8 / sub);
+    int max_blocks = 0;
+    NR_CUDA_TRY(fp64_grid_max_blocks(sub, &max_blocks));
+    const int blocks = std::max(1, std::min(d.n_units, max_blocks));
+    NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
+    NR_CUDA_TRY(launch_fp64_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
+    const int eblocks = std::max(1, std::min(2 * sms, (std::max(d.n_edges, d.n_triples) + kTile - 1) / kTile * 2));
+    NR_CUDA_TRY(launch_energies(d, eblocks, stream));
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    fill_report(st, d, rep);
+    if (rep->status == NR_ERR_TIMEOUT) return fail(NR_ERR_TIMEOUT, "grid barrier wait budget exceeded");
+    if (rep->status < 0) return fail(rep->status, "relaxation produced non-finite forces");
+    return rep->status;
+}
+
+static int relax_set_fp64_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
+    int max_blocks = 0;
+    NR_CUDA_TRY(fp64_batch_max_blocks(&max_blocks));
+    const int blocks = std::max(1, std::min(S.n_nets, max_blocks));
+    NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
+    NR_CUDA_TRY(launch_fp64_batch(S.dev_array, S.n_nets, to_dev(prm), S.queue, blocks, stream));
+    std::vector<FireState> st(S.n_nets);
+    NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    int worst = NR_OK;
+    for (int i = 0; i < S.n_nets; ++i) {
+        fill_report(st[i], S.dev[i], &reps[i]);
+        if (reps[i].status < 0) worst = reps[i].status;
+        else if (worst == NR_OK && reps[i].status == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+    }
+    if (worst < 0) return fail(worst, "a network in the batch failed");
+    return worst;
+}
+
+}  // namespace nr
+
+using namespace nr;
+
+struct nr_network {
+    DeviceSet set;
+};
+struct nr_batch {
+    DeviceSet set;
+};
+
+static cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+extern "C" {
+
+int nr_network_create(const nr_host_network *net, double ks, double kb, void *stream, nr_network **out) {
+    if (!net || !out) return fail(NR_ERR_INVALID, "nr_network_create: null argument");
+    *out = nullptr;
+    auto *d = new nr_network();
+    const nr_host_network *nets[1] = {net};
+    int rc = build_set(1, nets, &ks, &kb, nullptr, as_stream(stream), d->set);
+    if (rc != NR_OK) {
+        delete d;
+        return rc;
+    }
+    *out = d;
+    return NR_OK;
+}
+
+int nr_network_destroy(nr_network *d) {
+    delete d;
+    return NR_OK;
+}
+
+int nr_network_n_points(const nr_network *d) { return d ? d->set.dev[0].n : 0; }
+
+int nr_network_set_positions(nr_network *d, const double *host_xy, void *stream) {
+    if (!d || !host_xy) return fail(NR_ERR_INVALID, "nr_network_set_positions: null argument");
+    NR_CUDA_TRY(cudaMemcpyAsync(d->set.x_all, host_xy, sizeof(double2) * d->set.total_nodes, cudaMemcpyHostToDevice,
+                                as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_network_get_positions(const nr_network *d, double *host_xy, void *stream) {
+    if (!d || !host_xy) return fail(NR_ERR_INVALID, "nr_network_get_positions: null argument");
+    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, d->set.x_all, sizeof(double2) * d->set.total_nodes, cudaMemcpyDeviceToHost,
+                                as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+double *nr_network_positions_device(nr_network *d) { return d ? (double *)d->set.x_all : nullptr; }
+
+int nr_affine_displace(nr_network *d, double miny, double yrange, double xdisp, double ydisp, void *stream) {
+    if (!d) return fail(NR_ERR_INVALID, "nr_affine_displace: null network");
+    NR_CUDA_TRY(launch_affine(d->set.x_all, (int)d->set.total_nodes, miny, yrange, xdisp, ydisp, as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_relax(nr_network *d, const nr_fire_params *params, nr_report *report, void *stream) {
+    if (!d || !report) return fail(NR_ERR_INVALID, "nr_relax: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    clear_error();
+    if (params->precision == NR_MIXED) return fail(NR_ERR_INVALID, "mixed precision is not available in this build");
+    return relax_single_fp64(d->set, 0, *params, as_stream(stream), report);
+}
+
+int nr_forces(nr_network *d, double *host_f, void *stream) {
+    if (!d || !host_f) return fail(NR_ERR_INVALID, "nr_forces: null argument");
+    NR_CUDA_TRY(launch_forces(d->set.dev[0], as_stream(stream)));
+    NR_CUDA_TRY(cudaMemcpyAsync(host_f, d->set.f_all, sizeof(double2) * d->set.total_nodes, cudaMemcpyDeviceToHost,
+                                as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_energies(nr_network *d, double *e_stretch, double *e_bend, void *stream) {
+    if (!d || !e_stretch || !e_bend) return fail(NR_ERR_INVALID, "nr_energies: null argument");
+    const NetDev &dv = d->set.dev[0];
+    const int sms = sm_count();
+    const int eblocks = std::max(1, std::min(2 * sms, (std::max(dv.n_edges, dv.n_triples) + kTile - 1) / kTile * 2));
+    NR_CUDA_TRY(launch_energies(dv, eblocks, as_stream(stream)));
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, dv.st, sizeof(FireState), cudaMemcpyDeviceToHost, as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    *e_stretch = st.e_stretch;
+    *e_bend = st.e_bend;
+    return NR_OK;
+}
+
+int nr_sweep(nr_network *d, double miny, double yrange, const nr_fire_params *params, const double compr[3],
+             const double shear[3], nr_step_record *records, int max_records, int *n_records,
+             double *shear_positions, void *stream) {
+    if (!d || !compr || !shear || !n_records || (max_records > 0 && !records))
+        return fail(NR_ERR_INVALID, "nr_sweep: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    if (!(yrange > 0)) return fail(NR_ERR_INVALID, "nr_sweep: yrange must be positive");
+    *n_records = 0;
+    const double smult = yrange;
+    const size_t n2 = 2 * (size_t)d->set.total_nodes;
+    int worst = NR_OK;
+    auto one = [&](double xdisp, double ydisp, double curr, double maxc, int is_shear) -> int {
+        int r = nr_affine_displace(d, miny, yrange, xdisp, ydisp, stream);
+        if (r != NR_OK) return r;
+        nr_report rep;
+        r = nr_relax(d, params, &rep, stream);
+        if (r < 0) return r;
+        if (r == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+        if (*n_records < max_records) {
+            nr_step_record &R = records[*n_records];
+            R.curr_disp = curr;
+            R.max_comp = maxc;
+            R.e_stretch = rep.e_stretch;
+            R.e_bend = rep.e_bend;
+            R.rms_force = rep.rms_force;
+            R.max_force = rep.max_force;
+            R.steps = rep.steps;
+            R.is_shear = is_shear;
+            R.status = rep.status;
+            R.fp64_steps = rep.fp64_steps;
+            if (is_shear && shear_positions) {
+                r = nr_network_get_positions(d, shear_positions + n2 * (size_t)(*n_records), stream);
+                if (r != NR_OK) return r;
+            }
+            (*n_records)++;
+        }
+        return NR_OK;
+    };
+    double min_disp = compr[0] * smult, max_disp = compr[1] * smult, inc = compr[2] * smult;
+    double curr_disp = 0.0;
+    if (max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            rc = one(0, -inc, 0.0, curr_disp, 0);
+            if (rc < 0) return rc;
+            if (!(inc > 0)) break; /* the reference loops forever when inc == 0 */
+        }
+    }
+    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
+    min_disp = shear[0] * smult;
+    max_disp = shear[1] * smult;
+    inc = shear[2] * smult;
+    if (max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            rc = one(inc, 0, curr_disp, max_comp, 1);
+            if (rc < 0) return rc;
+            if (!(inc > 0)) break;
+        }
+    }
+    return worst;
+}
+
+int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double ks, double kb, double *d_pos,
+                   double *d_vel, double *d_forces, const int *d_pair_list, const double *d_lengths,
+                   const signed char *d_e_offsets, const int *d_triples, const signed char *d_t_offsets,
+                   const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
+                   int max_steps, int nmin, double report_data[3], int *step_count, void *stream) {
+    if (num_dof <= 0 || (num_dof & 1) || npairs < 0 || ntriples < 0 || !d_pos || !d_fcodes || !fire_params ||
+        !report_data || !step_count || (npairs > 0 && ks > 0 && (!d_pair_list || !d_lengths || !d_e_offsets)) ||
+        (ntriples > 0 && kb > 0 && (!d_triples || !d_t_offsets)))
+        return fail(NR_ERR_INVALID, "nr_run_fire_md: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    const int n = num_dof / 2;
+    nr_host_network h;
+    h.n_points = n;
+    h.offset = width;
+    h.points.resize(num_dof);
+    NR_CUDA_TRY(cudaMemcpyAsync(h.points.data(), d_pos, sizeof(double) * num_dof, cudaMemcpyDeviceToHost, s));
+    std::vector<unsigned char> fc(n);
+    NR_CUDA_TRY(cudaMemcpyAsync(fc.data(), d_fcodes, n, cudaMemcpyDeviceToHost, s));
+    if (ks > 0 && npairs > 0) {
+        h.edge_ij.resize(2 * (size_t)npairs);
+        h.edge_l0.resize(npairs);
+        h.edge_wrap.resize(npairs);
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_ij.data(), d_pair_list, sizeof(int) * 2 * npairs, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_l0.data(), d_lengths, sizeof(double) * npairs, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_wrap.data(), d_e_offsets, npairs, cudaMemcpyDeviceToHost, s));
+    }
+    if (kb > 0 && ntriples > 0) {
+        h.tri_hjk.resize(3 * (size_t)ntriples);
+        h.tri_wrap.resize(2 * (size_t)ntriples);
+        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_hjk.data(), d_triples, sizeof(int) * 3 * ntriples, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_wrap.data(), d_t_offsets, 2 * (size_t)ntriples, cudaMemcpyDeviceToHost, s));
+    }
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < h.edge_ij.size(); ++i)
+        if (h.edge_ij[i] < 0 || h.edge_ij[i] >= n) return fail(NR_ERR_INVALID, "nr_run_fire_md: bond index out of range");
+    for (size_t i = 0; i < h.tri_hjk.size(); ++i)
+        if (h.tri_hjk[i] < 0 || h.tri_hjk[i] >= n) return fail(NR_ERR_INVALID, "nr_run_fire_md: triple index out of range");
+    y_range(h.points, h.miny, h.maxy);
+    DeviceSet S;
+    const nr_host_network *nets[1] = {&h};
+    const unsigned char *fcs[1] = {fc.data()};
+    int rc = build_set(1, nets, &ks, &kb, fcs, s, S);
+    if (rc != NR_OK) return rc;
+    nr_fire_params p;
+    p.alpha0 = fire_params[0];
+    p.falpha = fire_params[1];
+    p.dt_max = fire_params[2];
+    p.finc = fire_params[3];
+    p.fdec = fire_params[4];
+    p.nmin = nmin;
+    p.mass = mass;
+    p.fcut = fcut;
+    p.max_steps = max_steps;
+    p.criterion = NR_CRIT_RMS;
+    p.precision = NR_FP64;
+    rc = check_params(&p);
+    if (rc != NR_OK) return rc;
+    nr_report rep;
+    rc = relax_single_fp64(S, 0, p, s, &rep);
+    if (rc < 0) return rc;
+    NR_CUDA_TRY(cudaMemcpyAsync(d_pos, S.x_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    if (d_vel) NR_CUDA_TRY(cudaMemcpyAsync(d_vel, S.v_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    if (d_forces) NR_CUDA_TRY(cudaMemcpyAsync(d_forces, S.f_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    report_data[0] = rep.rms_force;
+    report_data[1] = rep.e_stretch;
+    report_data[2] = rep.e_bend;
+    *step_count = rep.steps;
+    return rc;
+}
+
+int nr_batch_create(int n, const nr_host_network *const *nets, const double *ks, const double *kb, void *stream,
+                    nr_batch **out) {
+    if (n <= 0 || !nets || !ks || !kb || !out) return fail(NR_ERR_INVALID, "nr_batch_create: bad arguments");
+    *out = nullptr;
+    auto *b = new nr_batch();
+    int rc = build_set(n, nets, ks, kb, nullptr, as_stream(stream), b->set);
+    if (rc != NR_OK) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return NR_OK;
+}
+
+int nr_batch_destroy(nr_batch *b) {
+    delete b;
+    return NR_OK;
+}
+int nr_batch_size(const nr_batch *b) { return b ? b->set.n_nets : 0; }
+int nr_batch_total_points(const nr_batch *b) { return b ? (int)b->set.total_nodes : 0; }
+
+int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream) {
+    if (!b || !host_xy) return fail(NR_ERR_INVALID, "nr_batch_set_positions: null argument");
+    NR_CUDA_TRY(cudaMemcpyAsync(b->set.x_all, host_xy, sizeof(double2) * b->set.total_nodes, cudaMemcpyHostToDevice,
+                                as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_batch_get_positions(const nr_batch *b, double *host_xy, void *stream) {
+    if (!b || !host_xy) return fail(NR_ERR_INVALID, "nr_batch_get_positions: null argument");
+    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, b->set.x_all, sizeof(double2) * b->set.total_nodes, cudaMemcpyDeviceToHost,
+                                as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+double *nr_batch_positions_device(nr_batch *b) { return b ? (double *)b->set.x_all : nullptr; }
+
+int nr_batch_affine_displace(nr_batch *b, const double *miny, const double *yrange, const double *xdisp,
+                             const double *ydisp, void *stream) {
+    if (!b || !miny || !yrange || !xdisp || !ydisp) return fail(NR_ERR_INVALID, "nr_batch_affine_displace: null argument");
+    std::vector<double4> prm(b->set.n_nets);
+    for (int i = 0; i < b->set.n_nets; ++i) prm[i] = make_double4(miny[i], yrange[i], xdisp[i], ydisp[i]);
+    NR_CUDA_TRY(cudaMemcpyAsync(b->set.affine_prm, prm.data(), sizeof(double4) * prm.size(), cudaMemcpyHostToDevice,
+                                as_stream(stream)));
+    NR_CUDA_TRY(launch_affine_batch(b->set.dev_array, b->set.affine_prm, b->set.n_nets, as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports, void *stream) {
+    if (!b || !reports) return fail(NR_ERR_INVALID, "nr_batch_relax: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    clear_error();
+    if (params->precision == NR_MIXED) return fail(NR_ERR_INVALID, "mixed precision is not available in this build");
+    return relax_set_fp64_batch(b->set, *params, as_stream(stream), reports);
+}
+
+}  // extern "C"

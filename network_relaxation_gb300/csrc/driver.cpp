@@ -1,0 +1,386 @@
+/*
+ * The lsrelax-compatible driver: batch files (parse_batch_file,
+ * large_strain_relax.cu:263-383), file lists (file_lists.cpp:11-138), the
+ * per-network run with the reference's output files (do_relaxation_run,
+ * large_strain_relax.cu:792-1010), relaxation_batch (:1016-1044) and the
+ * command line (:1047-1126).
+ *
+ * Output formats are the reference's, byte for byte:
+ *   _log.txt    "Convergence [not ]reached: Steps: %d, RMS Force: %12.8le"
+ *               per relaxation, then "Elapsed time: %f seconds" (clock())
+ *   _edata.txt  compression "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le"
+ *               shear       "%12.10lf\t%12.10lf\t%12.10le\t%12.10le\t%12.10le"
+ *   _NNN.pos    "%2.10le\t%2.10le" per node after each shear step
+ * Deliberate differences: a network file that fails to parse is skipped
+ * with an error instead of being relaxed half-read; an increment of 0 runs
+ * one step instead of looping forever; -a selects absolute displacements
+ * instead of falling through into -b with no argument.
+ */
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <filesystem>
+#include <fstream>
+#include <regex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "nr_internal.h"
+
+using nr::fail;
+
+namespace {
+
+/* read_line, large_strain_relax.cu:263-283: next line that is neither empty
+ * nor a '#' comment. */
+bool read_line(std::ifstream &input, std::string &line) {
+    if (input.eof()) {
+        fprintf(stderr, "Not enough information was provided in the batch file.\n");
+        return false;
+    }
+    while (!input.eof()) {
+        std::getline(input, line);
+        if (line.empty() || line[0] == '#') continue;
+        break;
+    }
+    return !(line.empty() || line[0] == '#');
+}
+
+std::vector<std::string> split_ws(const std::string &line) {
+    std::vector<std::string> out;
+    std::string cur;
+    for (char c : line) {
+        if (c == ' ' || c == '\t') {
+            if (!cur.empty()) out.push_back(cur);
+            cur.clear();
+        } else {
+            cur += c;
+        }
+    }
+    if (!cur.empty()) out.push_back(cur);
+    return out;
+}
+
+int get_dec_digits(int value) {
+    int digits = 0;
+    do {
+        digits++;
+        value /= 10;
+    } while (value > 0);
+    return digits;
+}
+
+std::string report_name(const std::string &base, int num_digits, int count, const char *ext) {
+    std::ostringstream oss;
+    oss << base << "_";
+    for (int i = 0; i < num_digits - get_dec_digits(count); ++i) oss << 0;
+    oss << count << "." << ext;
+    return oss.str();
+}
+
+struct FileLists {
+    std::vector<std::string> dat, log, disp, edat;
+};
+
+bool file_lists(const std::string &input, const std::string &ext, const std::string &tag, FileLists &fl) {
+    if (input.empty()) return false;
+    std::vector<std::string> parts;
+    std::string cur;
+    for (char c : input) {
+        if (c == '/') {
+            if (!cur.empty()) parts.push_back(cur);
+            cur.clear();
+        } else {
+            cur += c;
+        }
+    }
+    if (!cur.empty()) parts.push_back(cur);
+    if (parts.empty()) return false;
+    std::string base = parts.back(), dir;
+    if (parts.size() > 1) {
+        if (input[0] == '/') dir = "/";
+        for (size_t i = 0; i + 1 < parts.size(); ++i) dir += parts[i] + "/";
+    } else {
+        dir = "./";
+    }
+    if (base == "*") base = "";
+    std::regex expr("^(" + base + ".*)\\." + ext);
+    const std::string suffix = tag.empty() ? std::string() : "_" + tag;
+    std::error_code ec;
+    if (std::filesystem::exists(dir, ec)) {
+        for (const auto &entry : std::filesystem::directory_iterator(dir, ec)) {
+            if (entry.is_directory()) continue;
+            const std::string name = entry.path().filename().string();
+            std::smatch m;
+            if (std::regex_search(name, m, expr)) {
+                fl.dat.push_back(dir + m[0].str());
+                fl.log.push_back(dir + m[1].str() + suffix + "_log.txt");
+                fl.disp.push_back(dir + m[1].str() + suffix);
+                fl.edat.push_back(dir + m[1].str() + suffix + "_edata.txt");
+            }
+        }
+    }
+    std::sort(fl.dat.begin(), fl.dat.end());
+    std::sort(fl.log.begin(), fl.log.end());
+    std::sort(fl.disp.begin(), fl.disp.end());
+    std::sort(fl.edat.begin(), fl.edat.end());
+    return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nr_parse_batch_file(const char *path, nr_batch_spec *spec) {
+    if (!path || !spec) return fail(NR_ERR_INVALID, "nr_parse_batch_file: null argument");
+    memset(spec, 0, sizeof(*spec));
+    std::ifstream input(path);
+    if (!input.is_open()) {
+        fprintf(stderr, "The file %s could not be read.\n", path);
+        return fail(NR_ERR_IO, std::string("cannot open ") + path);
+    }
+    std::string line;
+    if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing base name");
+    std::vector<std::string> tok = split_ws(line);
+    snprintf(spec->base, sizeof(spec->base), "%s", tok.empty() ? "" : tok[0].c_str());
+    if (tok.size() > 1) snprintf(spec->tag, sizeof(spec->tag), "%s", tok[1].c_str());
+    if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing stiffness line");
+    if (sscanf(line.c_str(), "%lf %lf", &spec->ks, &spec->kb) < 2 || spec->ks < 0 || spec->kb < 0) {
+        fprintf(stderr, "Error: invalid format for mechanical attributes.");
+        return fail(NR_ERR_PARSE, "batch file: invalid mechanical attributes");
+    }
+    if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing FIRE parameters");
+    std::vector<double> fp;
+    for (const std::string &s : split_ws(line)) {
+        double v;
+        if (sscanf(s.c_str(), "%lf", &v) == 1) fp.push_back(v);
+    }
+    if (fp.size() < 5) {
+        fprintf(stderr, "Too few FIRE parameters were supplied. 8 are needed.\n");
+        return fail(NR_ERR_PARSE, "batch file: too few FIRE parameters");
+    }
+    for (int i = 0; i < 5; ++i) spec->fire_params[i] = fp[i];
+    if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing nmin/mass/fcut/nmax");
+    if (sscanf(line.c_str(), "%d %lf %lf %d", &spec->nmin, &spec->mass, &spec->fcut, &spec->nmax) < 4 ||
+        spec->mass < 0 || spec->fcut < 0 || spec->nmax < 0) {
+        fprintf(stderr, "On or more of nmin, mass, cutoff force and step limit were invalid.\n");
+        return fail(NR_ERR_PARSE, "batch file: invalid nmin/mass/fcut/nmax");
+    }
+    for (int which = 0; which < 2; ++which) {
+        double *r = which == 0 ? spec->compr : spec->shear;
+        if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing strain range");
+        if (sscanf(line.c_str(), "%lf %lf %lf", &r[0], &r[1], &r[2]) < 3 || r[0] < 0 || r[1] < 0 || r[2] < 0 ||
+            r[1] < r[0]) {
+            fprintf(stderr, which == 0 ? "Error: invalid specification of compression."
+                                       : "Error: invalid specification of shear.");
+            return fail(NR_ERR_PARSE, "batch file: invalid strain range");
+        }
+    }
+    return NR_OK;
+}
+
+int nr_get_file_lists(const char *base, const char *ext, const char *tag, char *buf, size_t cap) {
+    if (!base || !ext) return fail(NR_ERR_INVALID, "nr_get_file_lists: null argument");
+    FileLists fl;
+    if (!file_lists(base, ext, tag ? tag : "", fl)) return fail(NR_ERR_INVALID, "nr_get_file_lists: empty base");
+    size_t pos = 0;
+    for (size_t i = 0; i < fl.dat.size(); ++i) {
+        for (const std::string *s : {&fl.dat[i], &fl.log[i], &fl.disp[i], &fl.edat[i]}) {
+            if (buf) {
+                if (pos + s->size() + 1 > cap) return fail(NR_ERR_CAPACITY, "nr_get_file_lists: buffer too small");
+                memcpy(buf + pos, s->c_str(), s->size() + 1);
+            }
+            pos += s->size() + 1;
+        }
+    }
+    return (int)fl.dat.size();
+}
+
+int nr_do_relaxation_run(const char *net_file, const char *log_name, const char *edata_name, const char *disp_base,
+                         const nr_batch_spec *spec, int precision, int criterion) {
+    if (!net_file || !log_name || !edata_name || !disp_base || !spec)
+        return fail(NR_ERR_INVALID, "nr_do_relaxation_run: null argument");
+    const clock_t ct0 = clock();
+    nr_host_network *hn = nullptr;
+    int rc = nr_read_network(net_file, &hn);
+    if (rc != NR_OK) {
+        fprintf(stderr, "%s: %s\n", net_file, nr_last_error());
+        nr_host_network_free(hn);
+        return rc;
+    }
+    if (spec->kb > 0) nr_get_triples(hn);
+    const double miny = hn->miny, range = hn->maxy - hn->miny;
+    const double smult = spec->absolute ? 1.0 : range;
+    const double s_inc = spec->shear[2];
+    const int num_digits =
+        get_dec_digits(1 + (s_inc > 0 ? (int)((spec->shear[1] - spec->shear[0]) / s_inc) : 0));
+    nr_network *net = nullptr;
+    rc = nr_network_create(hn, spec->ks, spec->kb, nullptr, &net);
+    const int n_points = hn->n_points;
+    nr_host_network_free(hn);
+    if (rc != NR_OK) return rc;
+    nr_fire_params p;
+    p.alpha0 = spec->fire_params[0];
+    p.falpha = spec->fire_params[1];
+    p.dt_max = spec->fire_params[2];
+    p.finc = spec->fire_params[3];
+    p.fdec = spec->fire_params[4];
+    p.nmin = spec->nmin;
+    p.mass = spec->mass;
+    p.fcut = spec->fcut;
+    p.max_steps = spec->nmax;
+    p.criterion = criterion;
+    p.precision = precision;
+    FILE *log_file = fopen(log_name, "w");
+    FILE *edata_file = fopen(edata_name, "w");
+    std::vector<double> pos(2 * (size_t)n_points);
+    int disp_count = 1;
+    int worst = NR_OK;
+    auto relax = [&](double xd, double yd, nr_report &rep) -> int {
+        int r = nr_affine_displace(net, miny, range, xd, yd, nullptr);
+        if (r != NR_OK) return r;
+        r = nr_relax(net, &p, &rep, nullptr);
+        if (r < 0) return r;
+        if (r == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+        const double measure = criterion == NR_CRIT_MAX ? rep.max_force : rep.rms_force;
+        if (log_file) {
+            fprintf(log_file, measure <= spec->fcut ? "Convergence reached: " : "Convergence not reached: ");
+            fprintf(log_file, "Steps: %d, RMS Force: %12.8le\n", rep.steps, rep.rms_force);
+        }
+        printf("Steps: %d, RMS Force: %12.8le\n", rep.steps, rep.rms_force);
+        return NR_OK;
+    };
+    double min_disp = spec->compr[0] * smult, max_disp = spec->compr[1] * smult, inc = spec->compr[2] * smult;
+    double curr_disp = 0.0;
+    if (max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            nr_report rep;
+            rc = relax(0, -inc, rep);
+            if (rc < 0) break;
+            if (edata_file)
+                fprintf(edata_file, "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le\n", 0., curr_disp, rep.e_stretch,
+                        rep.e_bend, rep.e_stretch + rep.e_bend);
+            if (!(inc > 0)) break;
+        }
+    }
+    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
+    min_disp = spec->shear[0] * smult;
+    max_disp = spec->shear[1] * smult;
+    inc = spec->shear[2] * smult;
+    if (rc >= 0 && max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            nr_report rep;
+            rc = relax(inc, 0, rep);
+            if (rc < 0) break;
+            if (edata_file)
+                fprintf(edata_file, "%12.10lf\t%12.10lf\t%12.10le\t%12.10le\t%12.10le\n", curr_disp, max_comp,
+                        rep.e_stretch, rep.e_bend, rep.e_stretch + rep.e_bend);
+            rc = nr_network_get_positions(net, pos.data(), nullptr);
+            if (rc != NR_OK) break;
+            const std::string name = report_name(disp_base, num_digits, disp_count++, "pos");
+            FILE *f = fopen(name.c_str(), "w");
+            if (f) {
+                for (int i = 0; i < n_points; ++i) fprintf(f, "%2.10le\t%2.10le\n", pos[2 * i], pos[2 * i + 1]);
+                fclose(f);
+            }
+            if (!(inc > 0)) break;
+        }
+    }
+    const clock_t ct = clock() - ct0;
+    if (log_file) {
+        fprintf(log_file, "Elapsed time: %f seconds\n", ((float)ct) / CLOCKS_PER_SEC);
+        fclose(log_file);
+    }
+    if (edata_file) fclose(edata_file);
+    nr_network_destroy(net);
+    if (rc < 0) {
+        fprintf(stderr, "Relaxation failed: %s\n", nr_last_error());
+        return rc;
+    }
+    return worst;
+}
+
+}  // extern "C"
+
+static int relaxation_batch(const char *batch_file, int precision, int criterion, int absolute) {
+    nr_batch_spec spec;
+    int rc = nr_parse_batch_file(batch_file, &spec);
+    spec.absolute = absolute;
+    if (rc != NR_OK) {
+        fprintf(stderr, "Parsing of the batch file failed.\n");
+        return rc;
+    }
+    FileLists fl;
+    if (!file_lists(spec.base, "dat", spec.tag, fl)) {
+        fprintf(stderr, "File lists could not be read.\n");
+        return fail(NR_ERR_IO, "file lists could not be read");
+    }
+    int worst = NR_OK;
+    for (size_t i = 0; i < fl.dat.size(); ++i) {
+        rc = nr_do_relaxation_run(fl.dat[i].c_str(), fl.log[i].c_str(), fl.edat[i].c_str(), fl.disp[i].c_str(), &spec,
+                                  precision, criterion);
+        if (rc < 0) worst = rc;
+        else if (rc == NR_NOT_CONVERGED && worst == NR_OK) worst = rc;
+    }
+    return worst;
+}
+
+extern "C" {
+
+int nr_relaxation_batch(const char *batch_file, int precision, int criterion) {
+    return relaxation_batch(batch_file, precision, criterion, 0);
+}
+
+int nr_lsrelax_main(int argc, char **argv) {
+    const char *batch_file = nullptr;
+    int precision = NR_FP64, criterion = NR_CRIT_RMS, absolute = 0;
+    for (int i = 1; i < argc; ++i) {
+        const std::string a = argv[i];
+        auto need = [&](const char *what) -> const char * {
+            if (i + 1 >= argc) {
+                fprintf(stderr, "Option \"%s\" requires %s.\n", a.c_str() + 1, what);
+                return nullptr;
+            }
+            return argv[++i];
+        };
+        if (a == "-b") {
+            batch_file = need("a file name");
+            if (!batch_file) return -1;
+        } else if (a == "-x" || a == "-y") {
+            const char *v = need("a block dimension");
+            int bx = 0;
+            if (v && sscanf(v, "%d", &bx) == 1 && bx >= 1)
+                printf("Block %s dimension: %d\n", a == "-x" ? "x" : "y", bx);
+        } else if (a == "-a") {
+            absolute = 1;
+        } else if (a == "-i") {
+            /* itemize: accepted and unused, as in the reference */
+        } else if (a == "--precision") {
+            const char *v = need("fp64 or mixed");
+            if (!v) return -1;
+            precision = strcmp(v, "mixed") == 0 ? NR_MIXED : NR_FP64;
+        } else if (a == "--criterion") {
+            const char *v = need("rms or max");
+            if (!v) return -1;
+            criterion = strcmp(v, "max") == 0 ? NR_CRIT_MAX : NR_CRIT_RMS;
+        } else {
+            fprintf(stderr, "Unrecognized option: %s\n", a.c_str());
+        }
+    }
+    if (!batch_file) {
+        fprintf(stderr, "No batch file was specified.\n");
+        return -1;
+    }
+    const int rc = relaxation_batch(batch_file, precision, criterion, absolute);
+    return rc < 0 ? 1 : 0;
+}
+
+int nr_gen_mikado(int, double, double, double, uint64_t, nr_host_network **out) {
+    if (out) *out = nullptr;
+    return fail(NR_ERR_INVALID, "nr_gen_mikado is not available in this build");
+}
+
+}  // extern "C"

@@ -1,0 +1,498 @@
+/*
+ * Plain FP64 FIRE on sm_103a: the drop-in for run_fire_md
+ * (large_strain_relax.cu:596-762) with axial_forces / bending_forces
+ * (:386-469) fused into a deterministic per-node gather.
+ *
+ * Compiled with --fmad=false: every fused multiply-add is an explicit fma()
+ * in canon_math.h or below, so results are bit-identical to the CPU oracle.
+ *
+ * One FIRE iteration is two passes over the nodes:
+ *   pass A  v mixing / zeroing from the previous step's scalars, then drift
+ *           x += dt v; x += dt^2/2m F; half kick v += dt/2m F
+ *   pass B  force gather at the new x, half kick, per-node terms of
+ *           P = v.F, |v|^2, |F|^2, max|F|^2 -> canonical unit partials
+ * separated by barriers; after pass B one CTA finishes the reductions and
+ * advances the FIRE scalars (dt, alpha, N+, convergence).  Two kernels share
+ * this code:
+ *   k_fire_grid   one network over many CTAs (cooperative launch, software
+ *                 grid barrier with a wait budget -> NR_ERR_TIMEOUT);
+ *   k_fire_batch  many networks, one CTA per network, persistent over a
+ *                 device work queue; __syncthreads only.
+ */
+#include <cuda_runtime.h>
+
+#include "../../include/netrelax.h"
+#include "canon_math.h"
+#include "fire_launch.h"
+#include "nr_device.cuh"
+
+namespace nr {
+
+constexpr int kGroup = 16; /* reduction units buffered in shared memory per flush */
+
+__device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &fx, double &fy) {
+    fx = 0.0;
+    fy = 0.0;
+    const unsigned c = d.fcode[i];
+    if (c == 0) return;
+    const double W = d.width;
+    if (d.use_bonds) {
+        const int e1 = d.bptr[i + 1];
+        for (int e = d.bptr[i]; e < e1; ++e) {
+            const int code = d.bent[e];
+            const int b = code >> 1;
+            const int4 r = d.bond[b];
+            const double2 p1 = d.x[r.x], p2 = d.x[r.y];
+            const double k = d.bond_k ? d.bond_k[b] : d.ks;
+            double bfx, bfy;
+            bond_force(p1.x, p1.y, p2.x, p2.y, wrap_shift(r.z, W), d.bond_l0[b], k, bfx, bfy);
+            if (code & 1) {
+                fx = fx + (-bfx);
+                fy = fy + (-bfy);
+            } else {
+                fx = fx + bfx;
+                fy = fy + bfy;
+            }
+        }
+    }
+    if (d.use_triples) {
+        const int e1 = d.tptr[i + 1];
+        for (int e = d.tptr[i]; e < e1; ++e) {
+            const int code = d.tent[e];
+            const int t = code >> 2, role = code & 3;
+            const int4 r = d.tri[t];
+            const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
+            const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+            const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+            const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
+            const double kb = d.tri_kb ? d.tri_kb[t] : d.kb;
+            const double phi0 = d.tri_phi0 ? d.tri_phi0[t] : 0.0;
+            double fjx, fjy, fkx, fky;
+            bend_force(ax, ay, bx, by, kb, phi0, fjx, fjy, fkx, fky);
+            if (role == 0) {
+                fx = fx + ((-fjx) - fkx);
+                fy = fy + ((-fjy) - fky);
+            } else if (role == 1) {
+                fx = fx + fjx;
+                fy = fy + fjy;
+            } else {
+                fx = fx + fkx;
+                fy = fy + fky;
+            }
+        }
+    }
+    if (!(c & 1)) fx = 0.0;
+    if (!(c & 2)) fy = 0.0;
+}
+
+/* FIRE scalars, advanced identically by whoever holds them. */
+struct Scal {
+    double dt, dtm, dtsq, alpha, mix_na, mix_a, fmag, maxf, power, vmag;
+    int mix_pending, zero_v, since, step, done, converged, status;
+};
+
+__device__ __forceinline__ bool crit_met(const FireParamsDev &p, double fmag, double maxf, double sqrt_dof) {
+    return p.criterion == 1 ? (maxf < p.fcut) : (fmag / sqrt_dof < p.fcut);
+}
+
+/* State at the top of run_fire_md (large_strain_relax.cu:616-643). */
+__device__ void scal_init(Scal &s, const FireParamsDev &p, double F2, double M2, double sqrt_dof) {
+    s.alpha = p.alpha0;
+    s.dt = p.dt_max;
+    s.dtsq = .5 * s.dt * s.dt / p.mass;
+    s.dtm = .5 * s.dt / p.mass;
+    s.mix_na = 0.0;
+    s.mix_a = 0.0;
+    s.power = 0.0;
+    s.vmag = 0.0;
+    s.fmag = sqrt(F2);
+    s.maxf = sqrt(M2);
+    s.mix_pending = 0;
+    s.zero_v = 0;
+    s.since = 0;
+    s.step = 0;
+    s.converged = crit_met(p, s.fmag, s.maxf, sqrt_dof);
+    s.status = isfinite(s.fmag) ? 0 : NR_ERR_NONFINITE;
+    s.done = p.max_steps <= 0 || s.status != 0;
+}
+
+/* End of one loop iteration (large_strain_relax.cu:683-718): mixing
+ * coefficients with the current alpha, then the dt / alpha adaption, then
+ * the convergence test. */
+__device__ void scal_step(Scal &s, const FireParamsDev &p, double P, double V2, double F2, double M2,
+                          double sqrt_dof) {
+    s.step++;
+    s.power = P;
+    s.vmag = sqrt(V2);
+    s.fmag = sqrt(F2);
+    s.maxf = sqrt(M2);
+    s.mix_a = s.alpha * s.vmag / s.fmag;
+    s.mix_na = -s.alpha;
+    s.mix_pending = 1;
+    if (P > 0) {
+        s.since++;
+        if (s.since > p.nmin) {
+            s.dt = fmin(s.dt * p.finc, p.dt_max);
+            s.dtm = .5 * s.dt / p.mass;
+            s.dtsq = .5 * s.dt * s.dt / p.mass;
+            s.alpha *= p.falpha;
+        }
+        s.zero_v = 0;
+    } else {
+        s.since = 0;
+        s.dt *= p.fdec;
+        s.dtm = .5 * s.dt / p.mass;
+        s.dtsq = s.dt * s.dt * .5 / p.mass;
+        s.alpha = p.alpha0;
+        s.zero_v = 1;
+    }
+    s.converged = crit_met(p, s.fmag, s.maxf, sqrt_dof);
+    if (!isfinite(s.fmag) || !isfinite(s.power)) s.status = NR_ERR_NONFINITE;
+    s.done = s.converged || s.step >= p.max_steps || s.status != 0;
+}
+
+__device__ __forceinline__ void scal_store(FireState *st, const Scal &s) {
+    st->dt = s.dt; st->dtm = s.dtm; st->dtsq = s.dtsq; st->alpha = s.alpha;
+    st->mix_na = s.mix_na; st->mix_a = s.mix_a;
+    st->fmag = s.fmag; st->maxf = s.maxf; st->power = s.power; st->vmag = s.vmag;
+    st->mix_pending = s.mix_pending; st->zero_v = s.zero_v; st->since = s.since; st->step = s.step;
+    st->done = s.done; st->converged = s.converged; st->status = s.status;
+}
+__device__ __forceinline__ void scal_load(Scal &s, const FireState *st_) {
+    const volatile FireState *st = st_;
+    s.dt = st->dt; s.dtm = st->dtm; s.dtsq = st->dtsq; s.alpha = st->alpha;
+    s.mix_na = st->mix_na; s.mix_a = st->mix_a;
+    s.fmag = st->fmag; s.maxf = st->maxf; s.power = st->power; s.vmag = st->vmag;
+    s.mix_pending = st->mix_pending; s.zero_v = st->zero_v; s.since = st->since; s.step = st->step;
+    s.done = st->done; s.converged = st->converged; s.status = st->status;
+}
+
+/* Pass A over the nodes of units u = u0, u0+ustride, ... */
+__device__ void pass_a(const NetDev &d, const Scal &s, int u0, int ustride) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int u = u0; u < d.n_units; u += ustride) {
+        const int i = (u * d.sub + warp) * kChunk + lane;
+        if (i >= d.n) continue;
+        double2 xi = d.x[i], vi = d.v[i];
+        const double2 fi = d.f[i];
+        if (s.mix_pending) {
+            vi.x = fma(s.mix_na, vi.x, vi.x);
+            vi.y = fma(s.mix_na, vi.y, vi.y);
+            vi.x = fma(s.mix_a, fi.x, vi.x);
+            vi.y = fma(s.mix_a, fi.y, vi.y);
+            if (s.zero_v) vi = make_double2(0.0, 0.0);
+        }
+        if (!s.done) {
+            xi.x = fma(s.dt, vi.x, xi.x);
+            xi.y = fma(s.dt, vi.y, xi.y);
+            xi.x = fma(s.dtsq, fi.x, xi.x);
+            xi.y = fma(s.dtsq, fi.y, xi.y);
+            vi.x = fma(s.dtm, fi.x, vi.x);
+            vi.y = fma(s.dtm, fi.y, vi.y);
+            d.x[i] = xi;
+        }
+        d.v[i] = vi;
+    }
+}
+
+/* Pass B: forces at the current x, half kick (or v = 0 when init), and the
+ * canonical unit partials of P, |v|^2, |F|^2, max|F|^2 into d.part. */
+__device__ void pass_b(const NetDev &d, double dtm, bool init, int u0, int ustride, double *s_units) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, sub = d.sub;
+    for (int ubase = u0; ubase < d.n_units; ubase += ustride * kGroup) {
+        int gn = 0;
+        for (int u = ubase; u < d.n_units && gn < kGroup; u += ustride, ++gn) {
+            const int i = (u * sub + warp) * kChunk + lane;
+            double tP = 0.0, tV = 0.0, tF = 0.0;
+            if (i < d.n) {
+                double fx, fy;
+                node_force_fp64(d, i, fx, fy);
+                double2 vi;
+                if (init) {
+                    vi = make_double2(0.0, 0.0);
+                } else {
+                    vi = d.v[i];
+                    vi.x = fma(dtm, fx, vi.x);
+                    vi.y = fma(dtm, fy, vi.y);
+                }
+                d.v[i] = vi;
+                d.f[i] = make_double2(fx, fy);
+                tP = dot2(vi.x, vi.y, fx, fy);
+                tV = dot2(vi.x, vi.y, vi.x, vi.y);
+                tF = dot2(fx, fy, fx, fy);
+            }
+            const double sP = warp_sum(tP), sV = warp_sum(tV), sF = warp_sum(tF), sM = warp_max(tF);
+            if (lane == 0) {
+                double *w = s_units + (size_t)gn * 4 * sub;
+                w[0 * sub + warp] = sP;
+                w[1 * sub + warp] = sV;
+                w[2 * sub + warp] = sF;
+                w[3 * sub + warp] = sM;
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < gn * 4; idx += blockDim.x) {
+            const int g = idx >> 2, q = idx & 3;
+            const int u = ubase + g * ustride;
+            const double *w = s_units + (size_t)g * 4 * sub + q * sub;
+            double val;
+            if (q < 3) {
+                val = subtree(w, sub);
+            } else {
+                val = w[0];
+                for (int k = 1; k < sub; ++k) val = fmax(val, w[k]);
+            }
+            d.part[(size_t)q * d.n_units + u] = val;
+        }
+        __syncthreads();
+    }
+}
+
+/* Final reductions of d.part by the calling CTA (all threads get them). */
+__device__ void reduce_parts(const NetDev &d, double *s_red, double &P, double &V2, double &F2, double &M2) {
+    P = final_sum(d.part, d.n_tiles, d.sub, s_red);
+    V2 = final_sum(d.part + d.n_units, d.n_tiles, d.sub, s_red);
+    F2 = final_sum(d.part + 2 * (size_t)d.n_units, d.n_tiles, d.sub, s_red);
+    M2 = final_max(d.part + 3 * (size_t)d.n_units, d.n_units, s_red);
+}
+
+/* Energy partials of bond tiles [t0, ...) and triple tiles, sub = 8 (256
+ * threads), tiles of 256 items. */
+__device__ void energy_tiles(const NetDev &d, int t0, int tstride, double *s_red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double W = d.width;
+    const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
+    const int total = (d.use_bonds ? tb : 0) + (d.use_triples ? tt : 0);
+    for (int t = t0; t < total; t += tstride) {
+        const bool is_bond = d.use_bonds && t < tb;
+        const int tile = is_bond ? t : t - (d.use_bonds ? tb : 0);
+        const int item = tile * kTile + threadIdx.x;
+        double e = 0.0;
+        if (is_bond) {
+            if (item < d.n_edges) {
+                const int4 r = d.bond[item];
+                const double2 p1 = d.x[r.x], p2 = d.x[r.y];
+                const double k = d.bond_k ? d.bond_k[item] : d.ks;
+                e = bond_energy(p1.x, p1.y, p2.x, p2.y, wrap_shift(r.z, W), d.bond_l0[item], k);
+            }
+        } else if (item < d.n_triples) {
+            const int4 r = d.tri[item];
+            const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
+            const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+            const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+            const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
+            const double kb = d.tri_kb ? d.tri_kb[item] : d.kb;
+            const double phi0 = d.tri_phi0 ? d.tri_phi0[item] : 0.0;
+            e = bend_energy(ax, ay, bx, by, kb, phi0);
+        }
+        e = warp_sum(e);
+        if (lane == 0) s_red[warp] = e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const size_t off = is_bond ? 0 : (size_t)(tb > tt ? tb : tt);
+            d.epart[off + tile] = tree8(s_red);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ void energy_final(const NetDev &d, double *s_red, double &es, double &eb) {
+    const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
+    es = 0.0;
+    eb = 0.0;
+    if (d.use_bonds && d.n_edges > 0) es = final_sum(d.epart, tb, 8, s_red);
+    if (d.use_triples && d.n_triples > 0) eb = final_sum(d.epart + (tb > tt ? tb : tt), tt, 8, s_red);
+}
+
+/* ------------------------------------------------------------------ */
+
+__global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget_ns) {
+    extern __shared__ double s_units[];
+    __shared__ double s_red[8];
+    const unsigned G = gridDim.x;
+    Scal s;
+    bool last;
+    pass_b(d, 0.0, true, blockIdx.x, G, s_units);
+    if (!barrier_arrive(d.st, G, budget_ns, last, 1)) return;
+    if (last) {
+        double P, V2, F2, M2;
+        reduce_parts(d, s_red, P, V2, F2, M2);
+        scal_init(s, p, F2, M2, d.sqrt_dof);
+        if (threadIdx.x == 0) scal_store(d.st, s);
+        barrier_release(d.st);
+    }
+    for (;;) {
+        scal_load(s, d.st);
+        pass_a(d, s, blockIdx.x, G);
+        if (s.done) break;
+        if (!barrier_arrive(d.st, G, budget_ns, last, 2)) return;
+        if (last) barrier_release(d.st);
+        pass_b(d, s.dtm, false, blockIdx.x, G, s_units);
+        if (!barrier_arrive(d.st, G, budget_ns, last, 3)) return;
+        if (last) {
+            double P, V2, F2, M2;
+            reduce_parts(d, s_red, P, V2, F2, M2);
+            scal_step(s, p, P, V2, F2, M2, d.sqrt_dof);
+            if (threadIdx.x == 0) scal_store(d.st, s);
+            barrier_release(d.st);
+        }
+    }
+}
+
+__global__ void k_energy_tiles(NetDev d) {
+    __shared__ double s_red[8];
+    energy_tiles(d, blockIdx.x, gridDim.x, s_red);
+}
+
+__global__ void k_energy_final(NetDev d) {
+    __shared__ double s_red[8];
+    double es, eb;
+    energy_final(d, s_red, es, eb);
+    if (threadIdx.x == 0) {
+        d.st->e_stretch = es;
+        d.st->e_bend = eb;
+    }
+}
+
+/* One CTA per network, networks taken from *queue until exhausted. */
+__global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_nets, FireParamsDev p, int *queue) {
+    extern __shared__ double s_units[];
+    __shared__ double s_red[8];
+    __shared__ int s_net;
+    for (;;) {
+        if (threadIdx.x == 0) s_net = atomicAdd(queue, 1);
+        __syncthreads();
+        const int net = s_net;
+        __syncthreads();
+        if (net >= n_nets) return;
+        const NetDev d = nets[net];
+        Scal s;
+        double P, V2, F2, M2;
+        pass_b(d, 0.0, true, 0, 1, s_units);
+        reduce_parts(d, s_red, P, V2, F2, M2);
+        scal_init(s, p, F2, M2, d.sqrt_dof);
+        for (;;) {
+            pass_a(d, s, 0, 1);
+            if (s.done) break;
+            __syncthreads();
+            pass_b(d, s.dtm, false, 0, 1, s_units);
+            reduce_parts(d, s_red, P, V2, F2, M2);
+            scal_step(s, p, P, V2, F2, M2, d.sqrt_dof);
+        }
+        __syncthreads();
+        energy_tiles(d, 0, 1, s_red);
+        double es, eb;
+        energy_final(d, s_red, es, eb);
+        if (threadIdx.x == 0) {
+            scal_store(d.st, s);
+            d.st->e_stretch = es;
+            d.st->e_bend = eb;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_forces(NetDev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    double fx, fy;
+    node_force_fp64(d, i, fx, fy);
+    d.f[i] = make_double2(fx, fy);
+}
+
+/* affine_displace (large_strain_relax.cu:527-537) over N nodes; with
+ * --fmad=false the operations round exactly as the reference's. */
+__global__ void k_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 p = x[i];
+    const double dy = p.y - miny;
+    p.x = p.x + xdisp * dy / yrange;
+    p.y = p.y + ydisp * dy / yrange;
+    x[i] = p;
+}
+
+/* Per-network affine map for a batch: one CTA per network. */
+__global__ void k_affine_batch(const NetDev *nets, const double4 *prm) {
+    const NetDev d = nets[blockIdx.x];
+    const double4 q = prm[blockIdx.x]; /* miny, yrange, xdisp, ydisp */
+    for (int i = threadIdx.x; i < d.n; i += blockDim.x) {
+        double2 p = d.x[i];
+        const double dy = p.y - q.x;
+        p.x = p.x + q.z * dy / q.y;
+        p.y = p.y + q.w * dy / q.y;
+        d.x[i] = p;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Host launchers                                                       */
+/* ------------------------------------------------------------------ */
+
+static size_t grid_smem_bytes(int sub) { return (size_t)kGroup * 4 * sub * sizeof(double); }
+
+cudaError_t fp64_grid_max_blocks(int sub, int *max_blocks) {
+    int dev, sms, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_grid, 32 * sub, grid_smem_bytes(sub));
+    if (e != cudaSuccess) return e;
+    *max_blocks = per_sm * sms;
+    return cudaSuccess;
+}
+
+cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
+                             cudaStream_t stream) {
+    NetDev dd = d;
+    FireParamsDev pp = p;
+    unsigned long long bb = budget_ns;
+    void *args[] = {&dd, &pp, &bb};
+    return cudaLaunchCooperativeKernel((const void *)k_fire_grid, dim3(blocks), dim3(32 * d.sub), args,
+                                       grid_smem_bytes(d.sub), stream);
+}
+
+cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream) {
+    k_energy_tiles<<<blocks, kTile, 0, stream>>>(d);
+    k_energy_final<<<1, kTile, 0, stream>>>(d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_batch(const NetDev *nets_dev, int n_nets, const FireParamsDev &p, int *queue_dev,
+                              int blocks, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    k_fire_batch<<<blocks, kTile, grid_smem_bytes(8), stream>>>(nets_dev, n_nets, p, queue_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t fp64_batch_max_blocks(int *max_blocks) {
+    int dev, sms, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_batch, kTile, grid_smem_bytes(8));
+    if (e != cudaSuccess) return e;
+    *max_blocks = per_sm * sms;
+    return cudaSuccess;
+}
+
+cudaError_t launch_forces(const NetDev &d, cudaStream_t stream) {
+    k_forces<<<(d.n + 255) / 256, 256, 0, stream>>>(d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
+                          cudaStream_t stream) {
+    k_affine<<<(n + 255) / 256, 256, 0, stream>>>(x, n, miny, yrange, xdisp, ydisp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_affine_batch(const NetDev *nets_dev, const double4 *prm_dev, int n_nets, cudaStream_t stream) {
+    k_affine_batch<<<n_nets, 256, 0, stream>>>(nets_dev, prm_dev);
+    return cudaGetLastError();
+}
+
+}  // namespace nr

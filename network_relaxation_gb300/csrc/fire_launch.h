@@ -1,0 +1,26 @@
+/* Host-side launchers of the FIRE kernels (defined in fire_fp64.cu and
+ * fire_mixed.cu). */
+#ifndef NR_FIRE_LAUNCH_H
+#define NR_FIRE_LAUNCH_H
+
+#include <cuda_runtime.h>
+
+#include "nr_device.cuh"
+
+namespace nr {
+
+cudaError_t fp64_grid_max_blocks(int sub, int *max_blocks);
+cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
+                             cudaStream_t stream);
+cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream);
+cudaError_t fp64_batch_max_blocks(int *max_blocks);
+cudaError_t launch_fp64_batch(const NetDev *nets_dev, int n_nets, const FireParamsDev &p, int *queue_dev,
+                              int blocks, cudaStream_t stream);
+cudaError_t launch_forces(const NetDev &d, cudaStream_t stream);
+cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
+                          cudaStream_t stream);
+cudaError_t launch_affine_batch(const NetDev *nets_dev, const double4 *prm_dev, int n_nets, cudaStream_t stream);
+
+}  // namespace nr
+
+#endif

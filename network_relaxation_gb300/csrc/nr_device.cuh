@@ -1,0 +1,205 @@
+/*
+ * Device-side layout of a network and the pieces every FIRE kernel shares:
+ * the canonical reductions and the grid barrier with a wait budget.
+ *
+ * HBM layout of one network (all arrays 16-byte aligned):
+ *   x, v, f        double2[N]   positions, velocities, forces (xy pairs; the
+ *                               reference's d_pos layout)
+ *   fcode          uint8[N]
+ *   bond           int4[E]      {i, j, wrap, 0}
+ *   bond_l0        double[E]    rest length
+ *   bond_k         double[E]    optional per-bond stiffness
+ *   tri            int4[T]      {hinge, j, k, (wrap_j & 255) | (wrap_k & 255) << 8}
+ *   tri_kb, tri_phi0 double[T]  optional per-triple stiffness, rest offset
+ *   bptr/bent      int[N+1]/int[2E]  incidence: (bond << 1) | role
+ *   tptr/tent      int[N+1]/int[3T]  incidence: (triple << 2) | role
+ *   part           double[4 * n_units]  reduction partials
+ * Canonical reduction (identical to the oracle's or_canon_sum): items are
+ * grouped in tiles of 256 (8 chunks of 32, one warp each); a chunk is reduced
+ * by an xor butterfly (16, 8, 4, 2, 1), the 8 chunk sums of a tile by the tree
+ * ((c0+c1)+(c2+c3))+((c4+c5)+(c6+c7)); tile sums are accumulated per lane
+ * k = t mod 256 in increasing t and the 256 lane sums are reduced like a tile.
+ */
+#ifndef NR_DEVICE_CUH
+#define NR_DEVICE_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nr {
+
+constexpr int kTile = 256;
+constexpr int kChunk = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+struct FireParamsDev {
+    double alpha0, falpha, dt_max, finc, fdec, mass, fcut;
+    int nmin, max_steps, criterion, precision;
+};
+
+/* Per-network FIRE state, written by one CTA after each reduction and read by
+ * all CTAs of the network.  The barrier words sit on their own 128-byte line. */
+struct __align__(128) FireState {
+    double dt, dtm, dtsq, alpha;
+    double mix_na, mix_a;
+    double fmag, maxf, power, vmag;
+    double e_stretch, e_bend;
+    int mix_pending, zero_v, since, step;
+    int done, converged, status, fp64_steps;
+    int pad[8];
+    unsigned int bar_count, bar_gen, abort_flag, timeout_site;
+    unsigned int pad2[28];
+};
+
+struct NetDev {
+    int n, n_edges, n_triples, n_tiles;
+    int use_bonds, use_triples, sub, n_units; /* sub = chunks per reduction unit (1,2,4,8) */
+    double width, ks, kb, sqrt_dof;
+    double2 *x, *v, *f;
+    const unsigned char *fcode;
+    const int4 *bond;
+    const double *bond_l0, *bond_k;
+    const int4 *tri;
+    const double *tri_kb, *tri_phi0;
+    const int *bptr, *bent, *tptr, *tent;
+    double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
+    double *epart;  /* 2 * max(bond tiles, triple tiles) energy partials */
+    FireState *st;
+};
+
+/* ----- reductions ----- */
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(kFull, v, off);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, off));
+    return v;
+}
+__device__ __forceinline__ double tree2(const double *w) { return w[0] + w[1]; }
+__device__ __forceinline__ double tree4(const double *w) { return (w[0] + w[1]) + (w[2] + w[3]); }
+__device__ __forceinline__ double tree8(const double *w) {
+    return ((w[0] + w[1]) + (w[2] + w[3])) + ((w[4] + w[5]) + (w[6] + w[7]));
+}
+/* Combines `sub` consecutive chunk sums with the lower levels of tree8. */
+__device__ __forceinline__ double subtree(const double *w, int sub) {
+    return sub == 8 ? tree8(w) : sub == 4 ? tree4(w) : sub == 2 ? tree2(w) : w[0];
+}
+/* Tile sum from the units of tile t (8/sub units, each a subtree of sub
+ * chunks), finishing tree8's upper levels. */
+__device__ __forceinline__ double tile_from_units(const double *p, int sub) {
+    double u[8];
+    const int upt = 8 / sub;
+    for (int i = 0; i < upt; ++i) u[i] = __ldcg(p + i);
+    if (sub == 8) return u[0];
+    if (sub == 4) return u[0] + u[1];
+    if (sub == 2) return (u[0] + u[1]) + (u[2] + u[3]);
+    return ((u[0] + u[1]) + (u[2] + u[3])) + ((u[4] + u[5]) + (u[6] + u[7]));
+}
+
+/* Final stage of the canonical sum for the calling CTA: units[] holds
+ * n_units unit partials (sub chunks each) of n_tiles tiles.  Every thread of
+ * the CTA returns the same value.  smem: >= 8 doubles. */
+__device__ inline double final_sum(const double *units, int n_tiles, int sub, double *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int upt = 8 / sub; /* units per tile */
+    for (int g = warp; g < 8; g += nwarps) {
+        const int k = 32 * g + lane;
+        double acc = 0.0;
+        if (k < n_tiles) {
+            acc = tile_from_units(units + (size_t)k * upt, sub);
+            for (int t = k + kTile; t < n_tiles; t += kTile) acc = acc + tile_from_units(units + (size_t)t * upt, sub);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) smem[g] = acc;
+    }
+    __syncthreads();
+    const double r = tree8(smem);
+    __syncthreads();
+    return r;
+}
+__device__ inline double final_max(const double *units, int n_units, double *smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    double m = 0.0;
+    for (int u = threadIdx.x; u < n_units; u += blockDim.x) m = fmax(m, __ldcg(units + u));
+    m = warp_max(m);
+    if (lane == 0) smem[warp] = m;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < nwarps; ++w) r = fmax(r, smem[w]);
+    __syncthreads();
+    return r;
+}
+
+/* ----- grid barrier with a wait budget ----- */
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+/* Arrive-and-wait across the `nblocks` CTAs sharing `st`.  The last CTA to
+ * arrive returns is_last = true WITHOUT releasing the others: it must call
+ * barrier_release() after finishing its serial work.  Returns false (and sets
+ * st->abort_flag / st->status) when the wait exceeds budget_ns or another CTA
+ * aborted; every thread of the CTA sees the same result. */
+__device__ inline bool barrier_arrive(FireState *st, unsigned nblocks, unsigned long long budget_ns, bool &is_last,
+                               unsigned site) {
+    __shared__ int s_flag;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &st->bar_gen;
+        volatile unsigned *abort_flag = &st->abort_flag;
+        int flag = -1;
+        const unsigned g = *gen;
+        if (!*abort_flag) {
+            __threadfence();
+            const unsigned prev = atomicAdd(&st->bar_count, 1u);
+            if (prev == nblocks - 1) {
+                atomicExch(&st->bar_count, 0u);
+                __threadfence();
+                flag = 1;
+            } else {
+                flag = 0;
+                const unsigned long long t0 = global_ns();
+                unsigned spins = 0;
+                while (*gen == g) {
+                    if (*abort_flag) {
+                        flag = -1;
+                        break;
+                    }
+                    if ((++spins & 63u) == 0 && global_ns() - t0 > budget_ns) {
+                        atomicExch(&st->abort_flag, 1u);
+                        atomicExch(&st->timeout_site, site);
+                        flag = -1;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                __threadfence();
+            }
+        }
+        s_flag = flag;
+    }
+    __syncthreads();
+    const int flag = s_flag;
+    __syncthreads();
+    is_last = flag == 1;
+    return flag >= 0;
+}
+
+__device__ __forceinline__ void barrier_release(FireState *st) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&st->bar_gen, 1u);
+    }
+}
+
+}  // namespace nr
+
+#endif

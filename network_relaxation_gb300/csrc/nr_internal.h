@@ -1,0 +1,49 @@
+/* Internal declarations shared by the host C++ and CUDA translation units. */
+#ifndef NR_INTERNAL_H
+#define NR_INTERNAL_H
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/netrelax.h"
+
+struct nr_host_network {
+    int n_points = 0;
+    double offset = 0, miny = 0, maxy = 0;
+    std::vector<double> points;       // 2N
+    std::vector<int> edge_ij;         // 2E
+    std::vector<double> edge_l0;      // E
+    std::vector<signed char> edge_wrap;
+    std::vector<int> tri_hjk;         // 3T
+    std::vector<signed char> tri_wrap;// 2T
+    std::vector<double> bond_k;       // empty or E
+    std::vector<double> tri_kb;       // empty or T
+    std::vector<double> tri_phi0;     // empty or T
+    int n_edges() const { return (int)edge_l0.size(); }
+    int n_triples() const { return (int)(tri_hjk.size() / 3); }
+};
+
+namespace nr {
+
+/* Thread-local error message + status helper. */
+int fail(int status, const std::string &msg);
+void clear_error();
+
+/* Per-node incidence lists in canonical order: every bond (in index order,
+ * first endpoint before second) and every triple (in index order, hinge, j,
+ * k) touching the node.  Entry encodings: bond (b << 1) | role,
+ * triple (t << 2) | role. */
+struct Incidence {
+    std::vector<int> bptr, bent, tptr, tent;
+};
+void build_incidence(int n_points, const int *edge_ij, int n_edges, const int *tri_hjk, int n_triples, bool use_bonds,
+                     bool use_triples, Incidence &inc);
+
+/* Min/max y in the reader's convention (min starts at FLT_MAX, max at
+ * FLT_MIN). */
+void y_range(const std::vector<double> &points, double &miny, double &maxy);
+
+}  // namespace nr
+
+#endif

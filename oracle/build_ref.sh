@@ -1,0 +1,35 @@
+#!/usr/bin/env bash
+# Builds oracle/_ref/liblsr_ref.so: the reference's own large_strain_relax.cu
+# compiled as host C++ (kernels run as sequential loops, cuBLAS Level-1 and the
+# CUDA runtime replaced by the stand-ins in oracle/refshim/include).
+#
+# The source is read where it lies and piped to the compiler with two textual
+# rewrites.  The first is the kernel-launch syntax, `k<<<grid, block>>>(args)`
+# -> `nr_ref_launch(grid, block, k, args)`, which plain C++ cannot parse.
+# The second is the one-token fix at large_strain_relax.cu:349,
+# `mass < 0 || fcut < 0 || nmax < 0` compares pointers with 0, which GCC 13
+# rejects; the parsed values `*mass`, `*fcut`, `*nmax` are what it means.
+# main is renamed so the library can expose the CLI.
+#
+# Needs the reference checkout (default /root/reference, or $NR_REFERENCE).
+# Outputs go only to oracle/_ref/ (git-ignored).  Exits 0 without building
+# when the reference is absent.
+set -euo pipefail
+HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
+REF="${NR_REFERENCE:-/root/reference}"
+SRC="$REF/src/large_strain_relax.cu"
+OUT="$HERE/_ref"
+if [ ! -f "$SRC" ]; then
+    echo "build_ref: $SRC not present; skipping"
+    exit 0
+fi
+mkdir -p "$OUT"
+CXX="${CXX:-g++}"
+sed -E -e 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/nr_ref_launch(\2, \1, /g' \
+    -e 's/\|\| mass < 0 \|\| fcut < 0 \|\| nmax < 0/|| *mass < 0 || *fcut < 0 || *nmax < 0/' "$SRC" |
+    "$CXX" -x c++ -std=c++17 -O2 -fPIC -w \
+        -I "$HERE/refshim/include" -I "$REF/src" -Dmain=lsr_reference_main \
+        -c - -o "$OUT/lsr_ref.o"
+"$CXX" -std=c++17 -O2 -fPIC -I "$HERE/refshim/include" -c "$HERE/refshim/ref_api.cpp" -o "$OUT/ref_api.o"
+"$CXX" -shared -o "$OUT/liblsr_ref.so" "$OUT/lsr_ref.o" "$OUT/ref_api.o"
+echo "build_ref: built $OUT/liblsr_ref.so"

@@ -1,0 +1,114 @@
+/*
+ * nr_oracle — CPU restatement of the reference's FIRE strain-and-relax path
+ * (jmichelstl/network_relaxation, src/large_strain_relax.cu), in plain C.
+ *
+ * TEST INFRASTRUCTURE ONLY.  The test suite, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline leg use it as the checker; the product never links,
+ * loads or calls it.
+ *
+ * Parity pin: tests/test_oracle_vs_reference.py checks this restatement
+ * against the reference's own code compiled for the host
+ * (oracle/build_ref.sh -> oracle/_ref/liblsr_ref.so) where the reference
+ * checkout is present, and against tests/golden/ fixtures produced by that
+ * build (tests/golden/make_golden.py) everywhere else.
+ *
+ * Arithmetic is "canonical": every operation, fused multiply-add and
+ * summation order is fixed so the GPU kernels reproduce the same bits:
+ *  - forces are summed per node in the reference's kernel order, all bonds in
+ *    index order then all triples in index order (hinge, j, k roles), which is
+ *    the reference's atomicAdd scatter (large_strain_relax.cu:386-469) with the
+ *    atomics serialised in index order;
+ *  - reductions over nodes / bonds / triples use or_canon_sum's fixed tree;
+ *  - the bending angle uses or_atan2, a polynomial atan with fixed
+ *    coefficients (no libm transcendental).
+ * Build with -ffp-contract=off so the compiler adds no fused operations.
+ */
+#ifndef NR_ORACLE_H
+#define NR_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Topology + positions as read from a .dat file (large_strain_relax.cu:42-114)
+ * with triples from get_triples (:116-184). */
+typedef struct {
+    int n_points, n_edges, n_triples;
+    double offset; /* x period ("width") */
+    double miny, maxy;
+    double *points;        /* 2*n_points, xy interleaved */
+    int *edge_ij;          /* 2*n_edges */
+    double *edge_l0;       /* n_edges */
+    signed char *edge_wrap;/* n_edges: periodic image multiplier */
+    int *tri_hjk;          /* 3*n_triples: hinge, j, k */
+    signed char *tri_wrap; /* 2*n_triples: wrap of hinge->j, hinge->k */
+} or_net;
+
+/* Model seen by the force / energy / FIRE functions.  bond_k, tri_kb and
+ * tri_phi0 are optional extensions (NULL = the reference's global ks, kb and
+ * rest angle pi); tri_phi0 holds theta0 - pi per triple. */
+typedef struct {
+    int n_points, n_edges, n_triples;
+    double width, ks, kb;
+    const int *edge_ij;
+    const double *edge_l0;
+    const signed char *edge_wrap;
+    const int *tri_hjk;
+    const signed char *tri_wrap;
+    const unsigned char *fcodes;
+    const double *bond_k;
+    const double *tri_kb;
+    const double *tri_phi0;
+} or_model;
+
+enum { OR_CRIT_RMS = 0, OR_CRIT_MAX = 1 };
+
+typedef struct {
+    double alpha0, falpha, dt_max, finc, fdec; /* fire_params[0..4] */
+    int nmin;
+    double mass, fcut;
+    int max_steps;
+    int criterion; /* OR_CRIT_RMS: |F|/sqrt(2N) < fcut (reference); OR_CRIT_MAX: max_i |F_i| < fcut */
+} or_fire_params;
+
+typedef struct {
+    double rms_force, max_force, e_stretch, e_bend;
+    int steps;
+    int converged;
+} or_report;
+
+/* IO / topology (bit-exact restatements). */
+int or_read_network(const char *path, or_net *net);           /* returns 1 iff the reference's read_network returns true */
+void or_get_triples(or_net *net);                             /* fills tri_* (frees old) */
+void or_free_net(or_net *net);
+void or_fcodes(const or_net *net, const double *points, unsigned char *fcodes); /* :895-901 */
+void or_affine_displace(int n_points, double *pos, double miny, double yrange, double xdisp, double ydisp);
+
+/* Canonical math. */
+double or_atan2(double y, double x);
+double or_canon_sum(const double *terms, long n);
+
+/* Physics. */
+void or_forces(const or_model *m, const double *pos, double *forces);
+void or_energies(const or_model *m, const double *pos, double *e_stretch, double *e_bend);
+int or_fire(const or_model *m, double *pos, double *vel, double *forces, const or_fire_params *p, or_report *rep);
+
+/* Strain protocol of do_relaxation_run (large_strain_relax.cu:917-999),
+ * strain mode.  compr / shear = {min, max, inc} in strain units.  For every
+ * relaxation it appends one record {curr_disp, max_comp, E_s, E_b, rms, maxF,
+ * steps, is_shear} to records (capacity max_records) and, for shear steps,
+ * copies the relaxed positions into shear_pos (2*n_points each, capacity
+ * max_records).  Returns the number of records. */
+int or_sweep(const or_model *m, double *pos, double miny, double yrange, const or_fire_params *p,
+             const double compr[3], const double shear[3], double *records, int max_records,
+             double *shear_pos);
+
+/* Relaxes n independent models in parallel on n_threads host threads (one
+ * network per thread at a time).  Each network uses or_fire. */
+void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_params *params, or_report *reps,
+                   int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
