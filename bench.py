@@ -1,0 +1,408 @@
+#!/usr/bin/env python
+"""Benchmark: relaxed networks/s on the 512-network uneven batch.
+
+Workload (config C4): 512 independent diluted triangular lattices, side
+L ~ U{16..96}, bond probability p ~ U[0.55, 0.75], bending stiffness
+kappa ~ logU[1e-5, 1e-2], each sheared affinely to its own gamma ~ U[0, 0.1]
+and relaxed by FIRE to max|F| < 1e-10 (k = 1, Bitzek et al. FIRE
+parameters).  Synthetic, seeded (network_relaxation_gb300.workloads).
+
+One step = every network of the batch relaxed from its affinely sheared
+start (positions reset from a device-resident copy), through the batched
+persistent kernel (default precision: mixed FP32/FP64 with FP64
+certification).  Inputs are ~0.5 GB of device data, larger than L2.
+
+Also reported in the same JSON line:
+  e2e           the same step through the public C ABI with host buffers:
+                H2D of the start positions from pinned memory, relaxation,
+                D2H of the relaxed positions and of the per-network reports
+  roofline      the batch kernel's algorithmic bytes / its event-timed
+                duration vs the measured HBM copy bandwidth
+  fp64          plain FP64 path, network by network (grid kernel), on a
+                stratified sample, extrapolated by FP64 work to the batch
+  cpu_baseline  the CPU oracle (FP64 restatement of run_fire_md) on all host
+                threads, on a bounded sample, extrapolated by FP64 work
+  clocks        nvidia-smi samples during the timed region
+--impl reference times the CPU restatement alone (the reference's own GPU
+code cannot run on this machine; its CPU path sparse_relax needs SuiteSparse).
+
+Multi-GPU (torchrun): every rank relaxes its own 512-network batch (seeds
+offset by rank), no collective on the data path; value = all networks /
+max-over-ranks time ("scaling": "weak").
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "relaxed networks/s to max|F|<1e-10 (512-network uneven batch)"
+UNIT = "networks/s"
+
+
+def fire_params(nr, precision):
+    return nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=0.1, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
+                          max_steps=10_000_000, criterion="max", precision=precision)
+
+
+def load_c4_oracle():
+    path = os.path.join(ROOT, "tests", "golden", "c4_oracle.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
+def mixed_bytes_per_launch(reps, hosts):
+    """Algorithmic bytes of one batch launch: per node-iteration
+    73 + 24 e + 12 t bytes (FP32 u, v, F read+write, fcode, bond index +
+    rest vector, triple data) with e = E/N, t = T/N, times FIRE steps."""
+    total = 0.0
+    for r, h in zip(reps, hosts):
+        i = h.info()
+        total += r.steps * (73.0 * i.n_points + 24.0 * i.n_edges + 12.0 * i.n_triples)
+    return total
+
+
+def fp64_bytes_per_launch(reps, hosts):
+    """FP64 algorithmic bytes: 145 + 17 e + 14 t per node-iteration."""
+    total = 0.0
+    for r, h in zip(reps, hosts):
+        i = h.info()
+        total += r.steps * (145.0 * i.n_points + 17.0 * i.n_edges + 14.0 * i.n_triples)
+    return total
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(c4, n_threads, budget_s, rate_guess=8e6):
+    """Stratified bounded sample of the batch for the CPU oracle: networks
+    in index order, skipping any whose FP64 work alone exceeds the budget,
+    until the total work fills budget_s on n_threads."""
+    cap = budget_s * rate_guess
+    target = budget_s * rate_guess * n_threads * 0.8
+    pick, work = [], 0.0
+    for i, r in enumerate(c4["networks"]):
+        w = r["steps"] * r["n_points"]
+        if w > cap:
+            continue
+        pick.append(i)
+        work += w
+        if work >= target:
+            break
+    return pick
+
+
+def run_cpu_baseline(c4, n_threads, budget_s):
+    """Times the oracle on the sample; returns (networks/s extrapolated to
+    the batch, node-iterations/s, description)."""
+    import oracle
+    import network_relaxation_gb300 as nr
+
+    pick = cpu_sample(c4, n_threads, budget_s)
+    rows = [c4["networks"][i] for i in pick]
+    models, starts = [], []
+    for r in rows:
+        a = nr.HostNetwork.lattice(r["L"], r["L"], r["p"], 0.0, r["seed"]).get_triples().arrays()
+        H = a["maxy"] - a["miny"]
+        models.append(oracle.Model(a, 1.0, r["kappa"]))
+        starts.append(oracle.affine_displace(a["points"], a["miny"], H, r["gamma"] * H, 0.0))
+    prm = oracle.params(fcut=1e-10, criterion="max", max_steps=10**7)
+    t = time.perf_counter()
+    _, reps = oracle.fire_batch(models, starts, prm, n_threads)
+    wall = time.perf_counter() - t
+    work = sum(rep.steps * m.n for rep, m in zip(reps, models))
+    rate = work / wall
+    per_net = c4["node_iterations"] / len(c4["networks"])
+    return rate / per_net, rate, wall, ("%d of the 512 networks (indices %d..%d, FP64 work %.2e node-iterations), "
+                                        "extrapolated by FP64 node-iterations to the full batch"
+                                        % (len(pick), pick[0], pick[-1], work))
+
+
+def reference_arm(args):
+    """--impl reference: the CPU restatement of the reference's FIRE path on
+    all host threads; each step a bounded sample of the batch."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    c4 = load_c4_oracle()
+    n_threads = os.cpu_count() or 1
+    vals, walls = [], []
+    desc = ""
+    for s in range(args.warmup + args.steps):
+        v, rate, wall, desc = run_cpu_baseline(c4, n_threads, budget_s=args.cpu_budget)
+        if s >= args.warmup:
+            vals.append(v)
+            walls.append(wall)
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(walls)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "C4: 512 uneven diluted triangular lattices L~U{16..96}, p~U[0.55,0.75], "
+                                   "kappa~logU[1e-5,1e-2], gamma~U[0,0.1], FIRE to max|F|<1e-10",
+                       "parallelism": "host threads x%d" % n_threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n_threads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work per CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+
+    import network_relaxation_gb300 as nr
+    from network_relaxation_gb300 import workloads
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    prm_list = workloads.c4_params(seed=workloads.C4_SEED + 512 * rank)
+    hosts = workloads.c4_networks(prm_list)
+    kappa = np.array([q["kappa"] for q in prm_list])
+    gamma = np.array([q["gamma"] for q in prm_list])
+    batch = nr.Batch(hosts, 1.0, kappa, stream=sp)
+    batch.affine_displace(gamma * (batch.maxy - batch.miny), 0.0, stream=sp)
+    n_nodes = int(batch.offsets[-1])
+    start_dev = torch.empty((n_nodes, 2), dtype=torch.float64, device="cuda")
+    check = nr._capi.check
+    lib = nr.lib()
+    check(lib.nr_batch_get_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "snapshot")
+    start_host = torch.empty((n_nodes, 2), dtype=torch.float64, pin_memory=True)
+    start_host.copy_(start_dev)
+    out_host = torch.empty_like(start_host).pin_memory()
+    prm = fire_params(nr, args.precision)
+    reps_arr = (nr.Report * batch.n)()
+
+    def step_device():
+        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "reset")
+        return lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        check(step_device(), "warmup relax")
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kernel_ms = []
+    barrier()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "reset")
+        k0.record(stream)
+        check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
+        k1.record(stream)
+        k1.synchronize()
+        kernel_ms.append(k0.elapsed_time(k1))
+    ev1.record(stream)
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    reps = [reps_arr[i] for i in range(batch.n)]
+    value = world * batch.n / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    e2e_ms = []
+    for _ in range(args.steps):
+        barrier()
+        t = time.perf_counter()
+        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_host.data_ptr()), C.c_void_p(sp)), "h2d")
+        check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
+        check(lib.nr_batch_get_positions(batch._h, C.c_void_p(out_host.data_ptr()), C.c_void_p(sp)), "d2h")
+        e2e_ms.append(1e3 * (time.perf_counter() - t))
+    e2e_step_ms = float(np.mean(e2e_ms))
+    if dist is not None:
+        t = torch.tensor([e2e_step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_step_ms = float(t.item())
+    h2d = n_nodes * 16
+    d2h = n_nodes * 16 + batch.n * C.sizeof(nr.Report)
+
+    steps = np.array([r.steps for r in reps])
+    status = [r.status for r in reps]
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm = peaks.get("hbm_gbs")
+    peak_kind = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    bytes_launch = (mixed_bytes_per_launch if args.precision == "mixed" else fp64_bytes_per_launch)(reps, hosts)
+    kern_ms = float(np.mean(kernel_ms))
+    achieved = bytes_launch / (kern_ms / 1e3) / 1e9
+    c4 = load_c4_oracle() if rank == 0 else None
+    line = None
+    if rank == 0:
+        node_iters = float(sum(r.steps * h.n_points for r, h in zip(reps, hosts)))
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": "C4: 512 uneven diluted triangular lattices L~U{16..96}, p~U[0.55,0.75], "
+                                   "kappa~logU[1e-5,1e-2], gamma~U[0,0.1], FIRE to max|F|<1e-10",
+                       "precision": args.precision, "networks_per_gpu": batch.n, "nodes_per_gpu": n_nodes,
+                       "l2": "inputs larger than L2 (%.0f MB device data)" % (batch_bytes(batch) / 1e6),
+                       "parallelism": "one batch per GPU" if world > 1 else "single GPU"},
+            "e2e": {"value": world * batch.n / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps,
+            "node_iter_per_s": world * node_iters / (ms / 1e3),
+            "iterations": {"p50": float(np.median(steps)), "p99": float(np.percentile(steps, 99)),
+                           "max": int(steps.max())},
+            "all_converged": all(s == 0 for s in status),
+            "fp64_anchor_evals_median": float(np.median([r.fp64_steps for r in reps])),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "peak_source": peak_kind,
+                         "kernel": "k_fire_batch_mixed" if args.precision == "mixed" else "k_fire_batch"},
+            "clocks": clk,
+            "wall_s_timed_region": wall,
+        }
+        if c4 is not None and rank == 0:
+            e_or = np.array([float.fromhex(r["e_stretch"]) + float.fromhex(r["e_bend"]) for r in c4["networks"]])
+            e_gpu = np.array([r.e_stretch + r.e_bend for r in reps])
+            rel = np.abs(e_gpu - e_or) / np.abs(e_or)
+            line["energy_rel_err_vs_fp64_oracle"] = {"max": float(rel.max()), "median": float(np.median(rel))}
+            line["fp64_node_iterations"] = c4["node_iterations"]
+    if rank == 0 and not args.no_fp64 and c4 is not None:
+        line["fp64"] = fp64_network_by_network(nr, hosts, prm_list, c4, sp)
+        line["batched_vs_fp64_network_by_network"] = value / line["fp64"]["value"]
+    if rank == 0 and not args.no_cpu and c4 is not None:
+        n_threads = os.cpu_count() or 1
+        v, rate, wall_cpu, desc = run_cpu_baseline(c4, n_threads, args.cpu_budget)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": n_threads, "kind": "port", "sample": desc,
+                                "node_iter_per_s": rate, "wall_s": wall_cpu}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def batch_bytes(batch):
+    return batch.offsets[-1] * 200.0
+
+
+def fp64_network_by_network(nr, hosts, prm_list, c4, sp, budget_s=20.0):
+    """Plain FP64 path (nr_relax, one network at a time on the whole GPU) on
+    a stratified sample (every 16th network, capped by time), extrapolated
+    to the batch by its FP64 node-iterations."""
+    import torch
+
+    idx = list(range(0, len(hosts), 16))
+    done, work, t_total = [], 0.0, 0.0
+    prm = fire_params(nr, "fp64")
+    for i in idx:
+        q = prm_list[i]
+        net = nr.Network(hosts[i], 1.0, q["kappa"], stream=sp)
+        H = net.maxy - net.miny
+        net.affine_displace(net.miny, H, q["gamma"] * H, 0.0, stream=sp)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        rep = net.relax(prm, stream=sp)
+        t_total += time.perf_counter() - t
+        work += rep.steps * net.n
+        done.append(i)
+        net.close()
+        if t_total > budget_s:
+            break
+    rate = work / t_total
+    per_net = c4["node_iterations"] / len(c4["networks"])
+    return {"value": rate / per_net, "unit": UNIT, "node_iter_per_s": rate,
+            "sample": "%d networks (every 16th, indices %s), %.1f s" % (len(done), done[:8], t_total)}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

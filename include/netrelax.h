@@ -166,6 +166,7 @@ typedef struct nr_network nr_network;
 int nr_network_create(const nr_host_network *net, double ks, double kb, void *stream, nr_network **out);
 int nr_network_destroy(nr_network *dnet);
 int nr_network_n_points(const nr_network *dnet);
+/* Position copies accept host (pageable or pinned) or device pointers. */
 int nr_network_set_positions(nr_network *dnet, const double *host_xy, void *stream);
 int nr_network_get_positions(const nr_network *dnet, double *host_xy, void *stream);
 /* Device pointer to the 2*N positions (valid until destroy). */
@@ -238,7 +239,8 @@ int nr_batch_create(int n, const nr_host_network *const *nets, const double *ks,
 int nr_batch_destroy(nr_batch *b);
 int nr_batch_size(const nr_batch *b);
 int nr_batch_total_points(const nr_batch *b);
-/* Positions of all networks, concatenated in network order (host). */
+/* Positions of all networks, concatenated in network order (host or
+ * device pointer). */
 int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream);
 int nr_batch_get_positions(const nr_batch *b, double *host_xy, void *stream);
 /* Device pointer to the concatenated positions. */

@@ -28,7 +28,7 @@ CXX = os.environ.get("CXX", "g++")
 # (source, extra flags)
 CUDA_UNITS = [
     ("fire_fp64.cu", ["--fmad=false"]),
-    ("fire_mixed.cu", []),
+    ("fire_mixed.cu", ["--fmad=false"]),
     ("api.cu", []),
 ]
 HOST_UNITS = ["host_network.cpp", "generators.cpp", "driver.cpp"]
@@ -82,7 +82,7 @@ def build(verbose=False, force=False):
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    if force or jobs or not os.path.exists(LIB):
+    if force or jobs or not _newer(LIB, objs):
         tmp = LIB + ".tmp"
         _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)

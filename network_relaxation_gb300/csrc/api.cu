@@ -53,6 +53,7 @@ struct Image {
 };
 
 struct NetOff {
+    size_t mb_other, mb_data, mb_sk, mt_nodes, mt_arms, mt_pk;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
 };
@@ -71,6 +72,10 @@ struct DeviceSet {
     int *queue = nullptr;
     double4 *affine_prm = nullptr;
     double2 *x_all = nullptr, *v_all = nullptr, *f_all = nullptr;
+    float2 *u_hi_all = nullptr, *u_lo_all = nullptr, *vf_all = nullptr, *ff_all = nullptr;
+    float2 *fa_hi_all = nullptr, *fa_lo_all = nullptr;
+    int max_nodes = 0;
+    int *order = nullptr; /* networks by decreasing size (largest start first) */
     ~DeviceSet() {
         if (arena) cudaFree(arena);
     }
@@ -90,6 +95,17 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     const size_t x_off = img.add(sizeof(double2) * S.total_nodes);
     const size_t v_off = img.add(sizeof(double2) * S.total_nodes);
     const size_t f_off = img.add(sizeof(double2) * S.total_nodes);
+    const size_t uh_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t ul_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t vf_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t ff_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t fah_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t fal_off = img.add(sizeof(float2) * S.total_nodes);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return nets[a]->n_points > nets[b]->n_points; });
+    const size_t order_off = img.put(order.data(), order.size());
     const size_t st_off = img.add(sizeof(FireState) * n);
     const size_t q_off = img.add(256);
     const size_t aff_off = img.add(sizeof(double4) * n);
@@ -126,6 +142,28 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.bent = img.put(inc.bent.data(), inc.bent.size());
         o.tptr = img.put(inc.tptr.data(), inc.tptr.size());
         o.tent = img.put(inc.tent.data(), inc.tent.size());
+        /* mixed-precision entry records: the other node(s) of every entry */
+        std::vector<int> mb_other(inc.bent.size());
+        for (int v = 0; v < h.n_points; ++v)
+            for (int e = inc.bptr[v]; e < inc.bptr[v + 1]; ++e) {
+                const int b = inc.bent[e] >> 1;
+                mb_other[e] = (inc.bent[e] & 1) ? h.edge_ij[2 * b] : h.edge_ij[2 * b + 1];
+            }
+        std::vector<int2> mt_nodes(inc.tent.size());
+        for (int v = 0; v < h.n_points; ++v)
+            for (int e = inc.tptr[v]; e < inc.tptr[v + 1]; ++e) {
+                const int t = inc.tent[e] >> 2, role = inc.tent[e] & 3;
+                const int hh = h.tri_hjk[3 * t], jj = h.tri_hjk[3 * t + 1], kk = h.tri_hjk[3 * t + 2];
+                const int n1 = role == 0 ? jj : hh, n2 = role == 2 ? jj : kk;
+                mt_nodes[e] = make_int2(n1 | (role << 30), n2);
+            }
+        o.mb_other = img.put(mb_other.data(), mb_other.size());
+        o.mb_data = img.add(sizeof(float4) * mb_other.size());
+        o.mb_sk = img.add(sizeof(float2) * mb_other.size());
+        o.mt_nodes = img.put(mt_nodes.data(), mt_nodes.size());
+        o.mt_arms = img.add(sizeof(float4) * mt_nodes.size());
+        o.mt_pk = img.add(sizeof(float2) * mt_nodes.size());
+        S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
         o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
         const int tb = (ne + kTile - 1) / kTile, tt = (nt + kTile - 1) / kTile;
@@ -144,6 +182,13 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     S.x_all = (double2 *)(base + x_off);
     S.v_all = (double2 *)(base + v_off);
     S.f_all = (double2 *)(base + f_off);
+    S.u_hi_all = (float2 *)(base + uh_off);
+    S.u_lo_all = (float2 *)(base + ul_off);
+    S.vf_all = (float2 *)(base + vf_off);
+    S.ff_all = (float2 *)(base + ff_off);
+    S.fa_hi_all = (float2 *)(base + fah_off);
+    S.fa_lo_all = (float2 *)(base + fal_off);
+    S.order = (int *)(base + order_off);
     S.st = (FireState *)(base + st_off);
     S.queue = (int *)(base + q_off);
     S.affine_prm = (double4 *)(base + aff_off);
@@ -169,6 +214,18 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.x = S.x_all + S.node_off[i];
         d.v = S.v_all + S.node_off[i];
         d.f = S.f_all + S.node_off[i];
+        d.u_hi = S.u_hi_all + S.node_off[i];
+        d.u_lo = S.u_lo_all + S.node_off[i];
+        d.vf = S.vf_all + S.node_off[i];
+        d.ff = S.ff_all + S.node_off[i];
+        d.fa_hi = S.fa_hi_all + S.node_off[i];
+        d.fa_lo = S.fa_lo_all + S.node_off[i];
+        d.mb_other = (int *)(base + o.mb_other);
+        d.mb_data = (float4 *)(base + o.mb_data);
+        d.mb_sk = (float2 *)(base + o.mb_sk);
+        d.mt_nodes = (int2 *)(base + o.mt_nodes);
+        d.mt_arms = (float4 *)(base + o.mt_arms);
+        d.mt_pk = (float2 *)(base + o.mt_pk);
         d.fcode = (const unsigned char *)(base + o.fcode);
         d.bond = (const int4 *)(base + o.bond);
         d.bond_l0 = (const double *)(base + o.bond_l0);
@@ -258,12 +315,42 @@ static int relax_single_fp64(DeviceSet &S, int i, const nr_fire_params &prm, cud
     return rep->status;
 }
 
-static int relax_set_fp64_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
-    int max_blocks = 0;
-    NR_CUDA_TRY(fp64_batch_max_blocks(&max_blocks));
-    const int blocks = std::max(1, std::min(S.n_nets, max_blocks));
+static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps);
+
+/* Mixed precision, one network: up to kMixedCtaNodes nodes the whole
+ * relaxation runs in one CTA with u in shared memory (no grid barriers);
+ * larger networks use the cooperative kernel over the whole GPU. */
+static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
+    constexpr int kMixedCtaNodes = 4096;
+    NetDev d = S.dev[0];
+    if (d.n <= kMixedCtaNodes) return relax_set_batch(S, prm, stream, rep);
+    const int blocks = mixed_grid_blocks(d.n);
+    if (blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
+    if ((size_t)5 * blocks > (size_t)4 * d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
+    NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
+    NR_CUDA_TRY(launch_mixed_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
+    const int sms = sm_count();
+    const int eblocks = std::max(1, std::min(2 * sms, (std::max(d.n_edges, d.n_triples) + kTile - 1) / kTile * 2));
+    NR_CUDA_TRY(launch_energies(d, eblocks, stream));
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    fill_report(st, d, rep);
+    if (rep->status == NR_ERR_TIMEOUT) return fail(NR_ERR_TIMEOUT, "grid barrier wait budget exceeded");
+    if (rep->status < 0) return fail(rep->status, "relaxation produced non-finite forces");
+    return rep->status;
+}
+
+static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
-    NR_CUDA_TRY(launch_fp64_batch(S.dev_array, S.n_nets, to_dev(prm), S.queue, blocks, stream));
+    if (prm.precision == NR_MIXED) {
+        NR_CUDA_TRY(launch_mixed_batch(S.dev_array, S.n_nets, S.max_nodes, to_dev(prm), S.queue, S.order, stream));
+    } else {
+        int max_blocks = 0;
+        NR_CUDA_TRY(fp64_batch_max_blocks(&max_blocks));
+        const int blocks = std::max(1, std::min(S.n_nets, max_blocks));
+        NR_CUDA_TRY(launch_fp64_batch(S.dev_array, S.n_nets, to_dev(prm), S.queue, blocks, stream));
+    }
     std::vector<FireState> st(S.n_nets);
     NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -315,7 +402,7 @@ int nr_network_n_points(const nr_network *d) { return d ? d->set.dev[0].n : 0; }
 
 int nr_network_set_positions(nr_network *d, const double *host_xy, void *stream) {
     if (!d || !host_xy) return fail(NR_ERR_INVALID, "nr_network_set_positions: null argument");
-    NR_CUDA_TRY(cudaMemcpyAsync(d->set.x_all, host_xy, sizeof(double2) * d->set.total_nodes, cudaMemcpyHostToDevice,
+    NR_CUDA_TRY(cudaMemcpyAsync(d->set.x_all, host_xy, sizeof(double2) * d->set.total_nodes, cudaMemcpyDefault,
                                 as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     return NR_OK;
@@ -323,7 +410,7 @@ int nr_network_set_positions(nr_network *d, const double *host_xy, void *stream)
 
 int nr_network_get_positions(const nr_network *d, double *host_xy, void *stream) {
     if (!d || !host_xy) return fail(NR_ERR_INVALID, "nr_network_get_positions: null argument");
-    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, d->set.x_all, sizeof(double2) * d->set.total_nodes, cudaMemcpyDeviceToHost,
+    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, d->set.x_all, sizeof(double2) * d->set.total_nodes, cudaMemcpyDefault,
                                 as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     return NR_OK;
@@ -342,7 +429,7 @@ int nr_relax(nr_network *d, const nr_fire_params *params, nr_report *report, voi
     int rc = check_params(params);
     if (rc != NR_OK) return rc;
     clear_error();
-    if (params->precision == NR_MIXED) return fail(NR_ERR_INVALID, "mixed precision is not available in this build");
+    if (params->precision == NR_MIXED) return relax_single_mixed(d->set, *params, as_stream(stream), report);
     return relax_single_fp64(d->set, 0, *params, as_stream(stream), report);
 }
 
@@ -525,7 +612,7 @@ int nr_batch_total_points(const nr_batch *b) { return b ? (int)b->set.total_node
 
 int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream) {
     if (!b || !host_xy) return fail(NR_ERR_INVALID, "nr_batch_set_positions: null argument");
-    NR_CUDA_TRY(cudaMemcpyAsync(b->set.x_all, host_xy, sizeof(double2) * b->set.total_nodes, cudaMemcpyHostToDevice,
+    NR_CUDA_TRY(cudaMemcpyAsync(b->set.x_all, host_xy, sizeof(double2) * b->set.total_nodes, cudaMemcpyDefault,
                                 as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     return NR_OK;
@@ -533,7 +620,7 @@ int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream) {
 
 int nr_batch_get_positions(const nr_batch *b, double *host_xy, void *stream) {
     if (!b || !host_xy) return fail(NR_ERR_INVALID, "nr_batch_get_positions: null argument");
-    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, b->set.x_all, sizeof(double2) * b->set.total_nodes, cudaMemcpyDeviceToHost,
+    NR_CUDA_TRY(cudaMemcpyAsync(host_xy, b->set.x_all, sizeof(double2) * b->set.total_nodes, cudaMemcpyDefault,
                                 as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     return NR_OK;
@@ -558,8 +645,7 @@ int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports
     int rc = check_params(params);
     if (rc != NR_OK) return rc;
     clear_error();
-    if (params->precision == NR_MIXED) return fail(NR_ERR_INVALID, "mixed precision is not available in this build");
-    return relax_set_fp64_batch(b->set, *params, as_stream(stream), reports);
+    return relax_set_batch(b->set, *params, as_stream(stream), reports);
 }
 
 }  // extern "C"

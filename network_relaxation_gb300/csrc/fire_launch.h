@@ -21,6 +21,13 @@ cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double 
                           cudaStream_t stream);
 cudaError_t launch_affine_batch(const NetDev *nets_dev, const double4 *prm_dev, int n_nets, cudaStream_t stream);
 
+cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
+                               int *queue_dev, const int *order_dev, cudaStream_t stream);
+
+int mixed_grid_blocks(int n);
+cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
+                              cudaStream_t stream);
+
 }  // namespace nr
 
 #endif

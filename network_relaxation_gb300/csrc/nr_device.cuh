@@ -46,7 +46,9 @@ struct __align__(128) FireState {
     double e_stretch, e_bend;
     int mix_pending, zero_v, since, step;
     int done, converged, status, fp64_steps;
-    int pad[8];
+    double m2_anchor; /* mixed precision: max|F|^2 at the current anchor */
+    int anchor_now;   /* mixed precision: the team re-anchors before the next pass */
+    int pad[5];
     unsigned int bar_count, bar_gen, abort_flag, timeout_site;
     unsigned int pad2[28];
 };
@@ -62,6 +64,17 @@ struct NetDev {
     const int4 *tri;
     const double *tri_kb, *tri_phi0;
     const int *bptr, *bent, *tptr, *tent;
+    /* mixed precision (fire_mixed.cu): double-float displacement from the
+     * anchor x (global copy, used when it does not fit shared memory), FP32
+     * velocity and force, double-float anchor force; per incidence entry the
+     * other node(s) and the FP32 anchor record */
+    float2 *u_hi, *u_lo, *vf, *ff, *fa_hi, *fa_lo;
+    int *mb_other;
+    float4 *mb_data; /* anchor vector self -> other, {hi.x, hi.y, lo.x, lo.y} */
+    float2 *mb_sk;   /* {|r_anchor| - l0, k} */
+    int2 *mt_nodes;
+    float4 *mt_arms;
+    float2 *mt_pk;
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
     double *epart;  /* 2 * max(bond tiles, triple tiles) energy partials */
     FireState *st;

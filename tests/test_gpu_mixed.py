@@ -1,0 +1,94 @@
+"""Mixed-precision path (FP32 bulk, FP64 anchors + certification) vs the
+FP64 oracle.  The trajectory differs from the FP64 one, so the bar is the
+physics, not the bits: every returned state is certified by the canonical
+FP64 force (checked here independently with the oracle), and energies agree
+with the FP64 oracle's relaxed energies to a small relative tolerance."""
+import numpy as np
+import pytest
+
+import network_relaxation_gb300 as nr
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+FIRE = dict(alpha0=0.1, falpha=0.99, dt_max=0.1, finc=1.1, fdec=0.5, nmin=5, mass=1.0)
+# Both runs stop at max|F| < 1e-10 from different trajectories; their
+# energies differ by O(|F|^2 / lambda_min).
+ENERGY_RTOL = 1e-8
+
+
+def batch_case(n_nets, seed, L_range=(8, 40), jitter=0.0):
+    rng = np.random.default_rng(seed)
+    hosts, arrs, kb, gam = [], [], [], []
+    for i in range(n_nets):
+        L = int(rng.integers(*L_range))
+        h = nr.HostNetwork.lattice(L, L, float(rng.uniform(0.6, 0.8)), jitter, seed + i,
+                                   line_triples=jitter > 0)
+        if jitter == 0:
+            h.get_triples()
+        hosts.append(h)
+        arrs.append(h.arrays())
+        kb.append(float(10 ** rng.uniform(-4, -2)))
+        gam.append(float(rng.uniform(0.005, 0.08)))
+    return hosts, arrs, np.array(kb), np.array(gam)
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.05])
+def test_mixed_batch_certified_and_matches_fp64_oracle(cuda, jitter):
+    hosts, arrs, kb, gam = batch_case(10, 77, jitter=jitter)
+    b = nr.Batch(hosts, 1.0, kb)
+    b.affine_displace(gam * (b.maxy - b.miny), 0.0)
+    reps = b.relax(nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **FIRE))
+    X = b.positions()
+    for i, a in enumerate(arrs):
+        r = reps[i]
+        assert r.status == nr.NR_OK
+        assert r.max_force < 1e-10 and r.fp64_steps >= 1
+        x = X[b.offsets[i]:b.offsets[i + 1]]
+        m = oracle.Model(a, 1.0, kb[i])
+        # independent certification with the oracle's force
+        assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+        es, eb = m.energies(x)
+        assert es == r.e_stretch and eb == r.e_bend
+        H = a["maxy"] - a["miny"]
+        x0 = oracle.affine_displace(a["points"], a["miny"], H, gam[i] * H, 0.0)
+        _, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
+        e_or = orep.e_stretch + orep.e_bend
+        assert abs(es + eb - e_or) <= ENERGY_RTOL * e_or
+        # the anchor is re-taken rarely: FP64 evaluations are a small
+        # fraction of the iterations
+        assert r.fp64_steps <= max(20, r.steps // 50)
+
+
+def test_mixed_single_network_grid_kernel(cuda):
+    """A network above the one-CTA size runs on the cooperative kernel."""
+    h = nr.HostNetwork.lattice(80, 80, 0.8, 0.0, 5).get_triples()
+    a = h.arrays()
+    H = a["maxy"] - a["miny"]
+    net = nr.Network(h, 1.0, 1e-2)
+    net.affine_displace(a["miny"], H, 0.02 * H, 0.0)
+    rep = net.relax(nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **FIRE))
+    assert rep.status == nr.NR_OK and rep.max_force < 1e-10
+    x = net.positions()
+    m = oracle.Model(a, 1.0, 1e-2)
+    assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+    x0 = oracle.affine_displace(a["points"], a["miny"], H, 0.02 * H, 0.0)
+    _, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
+    e_or = orep.e_stretch + orep.e_bend
+    assert abs(rep.e_stretch + rep.e_bend - e_or) <= ENERGY_RTOL * e_or
+
+
+def test_mixed_step_cap_reports_fp64_state(cuda):
+    h = nr.HostNetwork.lattice(20, 20, 0.7, 0.0, 3).get_triples()
+    a = h.arrays()
+    H = a["maxy"] - a["miny"]
+    net = nr.Network(h, 1.0, 1e-3)
+    net.affine_displace(a["miny"], H, 0.05 * H, 0.0)
+    rep = net.relax(nr.fire_params(fcut=1e-12, criterion="max", precision="mixed", max_steps=50, **FIRE))
+    assert rep.status == nr.NR_NOT_CONVERGED and rep.steps == 50
+    # the reported force and energies are the FP64 ones at the returned positions
+    x = net.positions()
+    m = oracle.Model(a, 1.0, 1e-3)
+    assert abs(rep.max_force - np.sqrt((m.forces(x) ** 2).sum(1)).max()) <= 1e-14 * rep.max_force
+    es, eb = m.energies(x)
+    assert (es, eb) == (rep.e_stretch, rep.e_bend)
