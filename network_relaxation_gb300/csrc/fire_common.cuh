@@ -154,17 +154,20 @@ __device__ __forceinline__ void scal_load(Scal &s, const FireState *st_) {
     s.done = st->done; s.converged = st->converged; s.status = st->status;
 }
 
-/* Energy partials of bond tiles [t0, ...) and triple tiles, sub = 8 (256
- * threads), tiles of 256 items. */
+/* Energy partials of bond tiles [t0, ...) and triple tiles, tiles of 256
+ * items reduced by the CTA's first 256 threads (8 warps; s_red holds 8
+ * doubles).  The CTA must have at least 256 threads; threads beyond the
+ * first 256 only take part in the barriers. */
 __device__ inline void energy_tiles(const NetDev &d, int t0, int tstride, double *s_red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool in_tile = threadIdx.x < kTile;
     const double W = d.width;
     const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
     const int total = (d.use_bonds ? tb : 0) + (d.use_triples ? tt : 0);
     for (int t = t0; t < total; t += tstride) {
         const bool is_bond = d.use_bonds && t < tb;
         const int tile = is_bond ? t : t - (d.use_bonds ? tb : 0);
-        const int item = tile * kTile + threadIdx.x;
+        const int item = in_tile ? tile * kTile + threadIdx.x : (is_bond ? d.n_edges : d.n_triples);
         double e = 0.0;
         if (is_bond) {
             if (item < d.n_edges) {
@@ -183,8 +186,10 @@ __device__ inline void energy_tiles(const NetDev &d, int t0, int tstride, double
             const double phi0 = d.tri_phi0 ? d.tri_phi0[item] : 0.0;
             e = bend_energy(ax, ay, bx, by, kb, phi0);
         }
-        e = warp_sum(e);
-        if (lane == 0) s_red[warp] = e;
+        if (in_tile) { /* warp-uniform: kTile is a multiple of 32 */
+            e = warp_sum(e);
+            if (lane == 0) s_red[warp] = e;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             const size_t off = is_bond ? 0 : (size_t)(tb > tt ? tb : tt);

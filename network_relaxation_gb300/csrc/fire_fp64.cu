@@ -119,7 +119,7 @@ __device__ void reduce_parts(const NetDev &d, double *s_red, double &P, double &
 
 __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget_ns) {
     extern __shared__ double s_units[];
-    __shared__ double s_red[8];
+    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     const unsigned G = gridDim.x;
     Scal s;
     bool last;
@@ -151,12 +151,12 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
 }
 
 __global__ void k_energy_tiles(NetDev d) {
-    __shared__ double s_red[8];
+    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     energy_tiles(d, blockIdx.x, gridDim.x, s_red);
 }
 
 __global__ void k_energy_final(NetDev d) {
-    __shared__ double s_red[8];
+    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     double es, eb;
     energy_final(d, s_red, es, eb);
     if (threadIdx.x == 0) {
@@ -168,7 +168,7 @@ __global__ void k_energy_final(NetDev d) {
 /* One CTA per network, networks taken from *queue until exhausted. */
 __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_nets, FireParamsDev p, int *queue) {
     extern __shared__ double s_units[];
-    __shared__ double s_red[8];
+    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     __shared__ int s_net;
     __shared__ NetDev s_d; /* descriptor staged once per network (hoistable loads) */
     for (;;) {

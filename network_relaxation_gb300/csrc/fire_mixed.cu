@@ -25,16 +25,19 @@
  * kErr * sum_b |df_b|, exceeds a tenth of the force still to be resolved
  * (on soft modes bond-force changes can exceed the net force by 10^6), when
  * max|F| has dropped below kAnchorF * max|F(X)|, and whenever the FP32
- * force meets the stop criterion or the step cap is reached: the run stops as converged only
- * when the FP64 force at the anchor meets the criterion, so the returned
- * positions are certified by the same FP64 force as the plain path.
+ * force meets the stop criterion or the step cap is reached.  The run stops
+ * as converged only when the FP64 force at the anchor meets the criterion,
+ * so the returned positions are certified by the same FP64 force as the
+ * plain path.
  *
  * Layout per network: u (hi, lo) lives in shared memory for the whole
  * relaxation when it fits (16 B/node), else in global memory; v, F and the
  * anchor force stream from global memory, coalesced (thread t owns nodes
  * t, t + blockDim, ...).  Every incidence entry carries its own oriented
  * FP32 anchor record, so the gather issues no dependent global loads:
- *   bond entry    mb_other (int), mb_data {ra.x, ra.y, l0, k}, ra from self
+ *   bond entry    mb_other (int), mb_data {ra hi.x, hi.y, lo.x, lo.y} (the
+ *                 anchor vector self -> other as a double-float),
+ *                 mb_sk {|ra| - l0, k}
  *   triple entry  mt_nodes {n1 | role << 30, n2}, mt_arms {a_a, b_a},
  *                 mt_pk {phi_a, kb}; role 0: self = hinge (n1 = j, n2 = k),
  *                 1: self = j (n1 = h, n2 = k), 2: self = k (n1 = h, n2 = j)
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_batch_mixed(const NetDe
                                                                      int *queue, const int *order, int smem_nodes) {
     extern __shared__ float2 s_u[];
     __shared__ double smem[5 * 32];
-    __shared__ double s_red[8];
+    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     __shared__ int s_net;
     /* The network's descriptor is staged in shared memory: its pointer
      * fields are then loop-invariant loads the compiler can hoist (a copy

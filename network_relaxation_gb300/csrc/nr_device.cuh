@@ -115,7 +115,8 @@ __device__ __forceinline__ double tile_from_units(const double *p, int sub) {
 
 /* Final stage of the canonical sum for the calling CTA: units[] holds
  * n_units unit partials (sub chunks each) of n_tiles tiles.  Every thread of
- * the CTA returns the same value.  smem: >= 8 doubles. */
+ * the CTA returns the same value.  smem: >= 8 doubles (one per warp of the
+ * first 8 warps). */
 __device__ inline double final_sum(const double *units, int n_tiles, int sub, double *smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int upt = 8 / sub; /* units per tile */
@@ -134,6 +135,7 @@ __device__ inline double final_sum(const double *units, int n_tiles, int sub, do
     __syncthreads();
     return r;
 }
+/* Maximum of n_units partials; smem: one double per warp of the CTA. */
 __device__ inline double final_max(const double *units, int n_units, double *smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     double m = 0.0;
