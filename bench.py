@@ -208,7 +208,7 @@ def reference_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -224,7 +224,7 @@ def main():
     import torch
 
     import network_relaxation_gb300 as nr
-    from network_relaxation_gb300 import workloads
+    from network_relaxation_gb300 import sharding, workloads
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -238,7 +238,7 @@ def main():
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
 
-    prm_list = workloads.c4_params(seed=workloads.C4_SEED + 512 * rank)
+    prm_list = sharding.rank_c4_params(rank)
     hosts = workloads.c4_networks(prm_list)
     kappa = np.array([q["kappa"] for q in prm_list])
     gamma = np.array([q["gamma"] for q in prm_list])
@@ -286,13 +286,9 @@ def main():
     barrier()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, total_nets = sharding.reduce_timing(dist, ev0.elapsed_time(ev1) / args.steps, batch.n, device="cuda")
     reps = [reps_arr[i] for i in range(batch.n)]
-    value = world * batch.n / (ms / 1e3)
+    value = total_nets / (ms / 1e3)
 
     # end to end through the C ABI with host buffers
     e2e_ms = []
@@ -303,11 +299,9 @@ def main():
         check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
         check(lib.nr_batch_get_positions(batch._h, C.c_void_p(out_host.data_ptr()), C.c_void_p(sp)), "d2h")
         e2e_ms.append(1e3 * (time.perf_counter() - t))
-    e2e_step_ms = float(np.mean(e2e_ms))
-    if dist is not None:
-        t = torch.tensor([e2e_step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step_ms = float(t.item())
+        if not all(reps_arr[i].status == 0 for i in range(batch.n)):
+            raise RuntimeError("end-to-end step: a network did not converge")
+    e2e_step_ms, _ = sharding.reduce_timing(dist, float(np.mean(e2e_ms)), batch.n, device="cuda")
     h2d = n_nodes * 16
     d2h = n_nodes * 16 + batch.n * C.sizeof(nr.Report)
 
@@ -336,7 +330,7 @@ def main():
                        "precision": args.precision, "networks_per_gpu": batch.n, "nodes_per_gpu": n_nodes,
                        "l2": "inputs larger than L2 (%.0f MB device data)" % (batch_bytes(batch) / 1e6),
                        "parallelism": "one batch per GPU" if world > 1 else "single GPU"},
-            "e2e": {"value": world * batch.n / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": total_nets / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps,
             "node_iter_per_s": world * node_iters / (ms / 1e3),

@@ -53,7 +53,7 @@ struct Image {
 };
 
 struct NetOff {
-    size_t mb_other, mb_data, mb_sk, mt_nodes, mt_arms, mt_pk;
+    size_t mb_other, mb_data, mb_sk, mt_nodes, mt_arms, mt_pk, bfrc, tfrc;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
 };
@@ -163,6 +163,8 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.mt_nodes = img.put(mt_nodes.data(), mt_nodes.size());
         o.mt_arms = img.add(sizeof(float4) * mt_nodes.size());
         o.mt_pk = img.add(sizeof(float2) * mt_nodes.size());
+        o.bfrc = img.add(sizeof(double2) * (size_t)ne);
+        o.tfrc = img.add(sizeof(double4) * (size_t)nt);
         S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
         o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
@@ -226,6 +228,8 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.mt_nodes = (int2 *)(base + o.mt_nodes);
         d.mt_arms = (float4 *)(base + o.mt_arms);
         d.mt_pk = (float2 *)(base + o.mt_pk);
+        d.bfrc = (double2 *)(base + o.bfrc);
+        d.tfrc = (double4 *)(base + o.tfrc);
         d.fcode = (const unsigned char *)(base + o.fcode);
         d.bond = (const int4 *)(base + o.bond);
         d.bond_l0 = (const double *)(base + o.bond_l0);
@@ -344,7 +348,13 @@ static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStrea
 static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     if (prm.precision == NR_MIXED) {
-        NR_CUDA_TRY(launch_mixed_batch(S.dev_array, S.n_nets, S.max_nodes, to_dev(prm), S.queue, S.order, stream));
+        const char *env = getenv("NR_CLUSTER");
+        const int cluster = env ? std::max(1, std::min(8, atoi(env))) : mixed_cluster_size(S.max_nodes);
+        if (cluster > 1)
+            NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
+        else
+            NR_CUDA_TRY(
+                launch_mixed_batch(S.dev_array, S.n_nets, S.max_nodes, to_dev(prm), S.queue, S.order, stream));
     } else {
         int max_blocks = 0;
         NR_CUDA_TRY(fp64_batch_max_blocks(&max_blocks));

@@ -72,6 +72,80 @@ __device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &
     if (!(c & 2)) fy = 0.0;
 }
 
+/* Item pass of the FP64 force: every bond force (the value its first
+ * endpoint receives) and every triple's (F_j, F_k) computed ONCE into
+ * scratch, items b = first, first + stride, ...  GB300's FP64 pipe is the
+ * bound of the plain path, and the per-node gather below would otherwise
+ * evaluate each bond twice and each triple three times. */
+__device__ inline void items_pass(const NetDev &d, int first, int stride) {
+    const double W = d.width;
+    if (d.use_bonds)
+        for (int b = first; b < d.n_edges; b += stride) {
+            const int4 r = d.bond[b];
+            const double2 p1 = d.x[r.x], p2 = d.x[r.y];
+            const double k = d.bond_k ? d.bond_k[b] : d.ks;
+            double fx, fy;
+            bond_force(p1.x, p1.y, p2.x, p2.y, wrap_shift(r.z, W), d.bond_l0[b], k, fx, fy);
+            d.bfrc[b] = make_double2(fx, fy);
+        }
+    if (d.use_triples)
+        for (int t = first; t < d.n_triples; t += stride) {
+            const int4 r = d.tri[t];
+            const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
+            const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+            const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+            const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
+            const double kb = d.tri_kb ? d.tri_kb[t] : d.kb;
+            const double phi0 = d.tri_phi0 ? d.tri_phi0[t] : 0.0;
+            double fjx, fjy, fkx, fky;
+            bend_force(ax, ay, bx, by, kb, phi0, fjx, fjy, fkx, fky);
+            d.tfrc[t] = make_double4(fjx, fjy, fkx, fky);
+        }
+}
+
+/* Per-node gather of the item forces in the canonical order; the same bits
+ * as node_force_fp64 (the same values summed in the same order). */
+__device__ __forceinline__ void node_force_items(const NetDev &d, int i, double &fx, double &fy) {
+    fx = 0.0;
+    fy = 0.0;
+    const unsigned c = d.fcode[i];
+    if (c == 0) return;
+    if (d.use_bonds) {
+        const int e1 = d.bptr[i + 1];
+        for (int e = d.bptr[i]; e < e1; ++e) {
+            const int code = d.bent[e];
+            const double2 f = d.bfrc[code >> 1];
+            if (code & 1) {
+                fx = fx + (-f.x);
+                fy = fy + (-f.y);
+            } else {
+                fx = fx + f.x;
+                fy = fy + f.y;
+            }
+        }
+    }
+    if (d.use_triples) {
+        const int e1 = d.tptr[i + 1];
+        for (int e = d.tptr[i]; e < e1; ++e) {
+            const int code = d.tent[e];
+            const double4 f = d.tfrc[code >> 2];
+            const int role = code & 3;
+            if (role == 0) {
+                fx = fx + ((-f.x) - f.z);
+                fy = fy + ((-f.y) - f.w);
+            } else if (role == 1) {
+                fx = fx + f.x;
+                fy = fy + f.y;
+            } else {
+                fx = fx + f.z;
+                fy = fy + f.w;
+            }
+        }
+    }
+    if (!(c & 1)) fx = 0.0;
+    if (!(c & 2)) fy = 0.0;
+}
+
 /* FIRE scalars, advanced identically by whoever holds them. */
 struct Scal {
     double dt, dtm, dtsq, alpha, mix_na, mix_a, fmag, maxf, power, vmag;

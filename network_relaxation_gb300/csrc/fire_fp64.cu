@@ -6,11 +6,13 @@
  * Compiled with --fmad=false: every fused multiply-add is an explicit fma()
  * in canon_math.h or below, so results are bit-identical to the CPU oracle.
  *
- * One FIRE iteration is two passes over the nodes:
- *   pass A  v mixing / zeroing from the previous step's scalars, then drift
- *           x += dt v; x += dt^2/2m F; half kick v += dt/2m F
- *   pass B  force gather at the new x, half kick, per-node terms of
- *           P = v.F, |v|^2, |F|^2, max|F|^2 -> canonical unit partials
+ * One FIRE iteration is three passes:
+ *   pass A  (nodes) v mixing / zeroing from the previous step's scalars,
+ *           then drift x += dt v; x += dt^2/2m F; half kick v += dt/2m F
+ *   items   (bonds, triples) each force computed once into scratch
+ *   pass B  (nodes) canonical-order gather of the item forces, half kick,
+ *           per-node terms of P = v.F, |v|^2, |F|^2, max|F|^2 -> canonical
+ *           unit partials
  * separated by barriers; after pass B one CTA finishes the reductions and
  * advances the FIRE scalars (dt, alpha, N+, convergence).  Two kernels share
  * this code:
@@ -65,7 +67,7 @@ __device__ void pass_b(const NetDev &d, double dtm, bool init, int u0, int ustri
             double tP = 0.0, tV = 0.0, tF = 0.0;
             if (i < d.n) {
                 double fx, fy;
-                node_force_fp64(d, i, fx, fy);
+                node_force_items(d, i, fx, fy);
                 double2 vi;
                 if (init) {
                     vi = make_double2(0.0, 0.0);
@@ -123,13 +125,19 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
     const unsigned G = gridDim.x;
     Scal s;
     bool last;
+    const int item0 = blockIdx.x * blockDim.x + threadIdx.x, istride = G * blockDim.x;
+    items_pass(d, item0, istride);
+    if (!barrier_arrive(d.st, G, budget_ns, last, 4)) return;
+    if (last) barrier_release(d.st);
     pass_b(d, 0.0, true, blockIdx.x, G, s_units);
     if (!barrier_arrive(d.st, G, budget_ns, last, 1)) return;
     if (last) {
         double P, V2, F2, M2;
         reduce_parts(d, s_red, P, V2, F2, M2);
-        scal_init(s, p, F2, M2, d.sqrt_dof);
-        if (threadIdx.x == 0) scal_store(d.st, s);
+        if (threadIdx.x == 0) { /* FP64 scalars: one thread (GB300 FP64 is scarce) */
+            scal_init(s, p, F2, M2, d.sqrt_dof);
+            scal_store(d.st, s);
+        }
         barrier_release(d.st);
     }
     for (;;) {
@@ -138,13 +146,18 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
         if (s.done) break;
         if (!barrier_arrive(d.st, G, budget_ns, last, 2)) return;
         if (last) barrier_release(d.st);
+        items_pass(d, item0, istride);
+        if (!barrier_arrive(d.st, G, budget_ns, last, 5)) return;
+        if (last) barrier_release(d.st);
         pass_b(d, s.dtm, false, blockIdx.x, G, s_units);
         if (!barrier_arrive(d.st, G, budget_ns, last, 3)) return;
         if (last) {
             double P, V2, F2, M2;
             reduce_parts(d, s_red, P, V2, F2, M2);
-            scal_step(s, p, P, V2, F2, M2, d.sqrt_dof);
-            if (threadIdx.x == 0) scal_store(d.st, s);
+            if (threadIdx.x == 0) {
+                scal_step(s, p, P, V2, F2, M2, d.sqrt_dof);
+                scal_store(d.st, s);
+            }
             barrier_release(d.st);
         }
     }
@@ -171,6 +184,7 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
     __shared__ int s_net;
     __shared__ NetDev s_d; /* descriptor staged once per network (hoistable loads) */
+    __shared__ Scal s_sc;  /* FIRE scalars, advanced by thread 0 (GB300 FP64 is scarce) */
     for (;;) {
         if (threadIdx.x == 0) {
             s_net = atomicAdd(queue, 1);
@@ -180,25 +194,30 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
         const int net = s_net;
         if (net >= n_nets) return;
         const NetDev &d = s_d;
-        Scal s;
         double P, V2, F2, M2;
+        items_pass(d, threadIdx.x, blockDim.x);
+        __syncthreads();
         pass_b(d, 0.0, true, 0, 1, s_units);
         reduce_parts(d, s_red, P, V2, F2, M2);
-        scal_init(s, p, F2, M2, d.sqrt_dof);
+        if (threadIdx.x == 0) scal_init(s_sc, p, F2, M2, d.sqrt_dof);
+        __syncthreads();
         for (;;) {
-            pass_a(d, s, 0, 1);
-            if (s.done) break;
+            pass_a(d, s_sc, 0, 1);
+            if (s_sc.done) break;
             __syncthreads();
-            pass_b(d, s.dtm, false, 0, 1, s_units);
+            items_pass(d, threadIdx.x, blockDim.x);
+            __syncthreads();
+            pass_b(d, s_sc.dtm, false, 0, 1, s_units);
             reduce_parts(d, s_red, P, V2, F2, M2);
-            scal_step(s, p, P, V2, F2, M2, d.sqrt_dof);
+            if (threadIdx.x == 0) scal_step(s_sc, p, P, V2, F2, M2, d.sqrt_dof);
+            __syncthreads();
         }
         __syncthreads();
         energy_tiles(d, 0, 1, s_red);
         double es, eb;
         energy_final(d, s_red, es, eb);
         if (threadIdx.x == 0) {
-            scal_store(d.st, s);
+            scal_store(d.st, s_sc);
             d.st->e_stretch = es;
             d.st->e_bend = eb;
         }

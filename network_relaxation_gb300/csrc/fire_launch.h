@@ -24,6 +24,9 @@ cudaError_t launch_affine_batch(const NetDev *nets_dev, const double4 *prm_dev, 
 cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
                                int *queue_dev, const int *order_dev, cudaStream_t stream);
 
+int mixed_cluster_size(int max_nodes);
+cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
+                                 int *queue_dev, const int *order_dev, cudaStream_t stream);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                               cudaStream_t stream);

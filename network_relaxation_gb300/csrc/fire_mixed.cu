@@ -45,6 +45,8 @@
  * Compiled with --fmad=false (the FP64 anchor code stays canonical); FP32
  * expressions use explicit fmaf().
  */
+#include <cooperative_groups.h>
+
 #include "fire_common.cuh"
 #include "fire_launch.h"
 
@@ -72,21 +74,33 @@ __device__ __forceinline__ float df_diff(float ah, float al, float bh, float bl)
  * On soft modes bonds mostly ROTATE: |d| is dominated by the component
  * perpendicular to the bond while the stretch |r| - |ra| that k multiplies
  * is tiny.  FP32 rounding of d or ra would leak ~6e-8 |d| of the
- * perpendicular part into the stretch, so the projection ra.d is formed
- * with exact products from the double-float pairs:
- *   |r| - |ra| = (2 ra.d + d.d) / (|r| + |ra|),  1 - l0/|r| = (|r| - |ra| + s_a) / |r|
+ * perpendicular part into the stretch, so |r|^2 - |ra|^2 = d.(2 ra + d) is
+ * formed with exact products from the double-float pairs:
+ *   |r| - |ra| = d.(2 ra + d) / (|r| + |ra|),  1 - l0/|r| = (|r| - |ra| + s_a) / |r|
  * and every remaining FP32 rounding is relative to the force change. */
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
 __device__ __forceinline__ float2 bond_dforce(float4 ra, float2 sk, float2 dh, float2 dlo) {
     const float rax = ra.x, ray = ra.y;
-    /* ra.d as hi + lo: exact products of the hi parts, then the cross terms */
-    const float p1 = rax * dh.x, p2 = ray * dh.y;
-    const float e1 = fmaf(rax, dh.x, -p1), e2 = fmaf(ray, dh.y, -p2);
-    const float s = p1 + p2;
-    const float bb = s - p1;
-    const float es = (p1 - (s - bb)) + (p2 - bb);
-    const float lo = ((e1 + e2) + es) + (fmaf(rax, dlo.x, ray * dlo.y) + fmaf(ra.z, dh.x, ra.w * dh.y));
+    /* |r|^2 - |ra|^2 = d.(2 ra + d).  Large rotations (floppy parts turn by
+     * O(1) radians) make 2 ra.d and d.d cancel down to the stretch, so the
+     * whole product is a double-float: w = 2 ra + d by two-sums, then exact
+     * products of the hi parts and the cross terms. */
+    float wxh, wxe, wyh, wye;
+    two_sum(2.0f * rax, dh.x, wxh, wxe);
+    two_sum(2.0f * ray, dh.y, wyh, wye);
+    const float wxl = wxe + fmaf(2.0f, ra.z, dlo.x), wyl = wye + fmaf(2.0f, ra.w, dlo.y);
+    const float p1 = dh.x * wxh, p2 = dh.y * wyh;
+    const float e1 = fmaf(dh.x, wxh, -p1), e2 = fmaf(dh.y, wyh, -p2);
+    float s, es;
+    two_sum(p1, p2, s, es);
+    const float lo = ((e1 + e2) + es) + (fmaf(dh.x, wxl, dh.y * wyl) + fmaf(dlo.x, wxh, dlo.y * wyh));
+    const float dd = s + lo;
     const float dx = dh.x + dlo.x, dy = dh.y + dlo.y;
-    const float dd = fmaf(2.0f, s, fmaf(dx, dx, dy * dy)) + 2.0f * lo;
     const float rx = rax + dx, ry = ray + dy;
     const float rl = sqrtf(fmaf(rx, rx, ry * ry));
     const float ral = sqrtf(fmaf(rax, rax, ray * ray));
@@ -146,6 +160,7 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, const UView &u, i
     mag = 0.f;
     if (d.use_bonds) {
         const int e1 = d.bptr[i + 1];
+#pragma unroll 2
         for (int e = d.bptr[i]; e < e1; ++e) {
             float2 dh, dlo;
             u.diff2(d.mb_other[e], i, dh, dlo);
@@ -157,6 +172,7 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, const UView &u, i
     }
     if (d.use_triples) {
         const int e1 = d.tptr[i + 1];
+#pragma unroll 2
         for (int e = d.tptr[i]; e < e1; ++e) {
             const int2 nn = d.mt_nodes[e];
             const int role = (unsigned)nn.x >> 30, n1 = nn.x & 0x3fffffff, n2 = nn.y;
@@ -188,28 +204,84 @@ struct Team {
     __device__ int stride() const { return size * blockDim.x; }
 };
 
-/* CTA reduction: sums for q < nsum, maxima after; every thread gets the
- * CTA totals.  smem: NQ * 32 doubles. */
-template <int NQ>
-__device__ void block_reduce(const double (&v)[NQ], int nsum, double (&out)[NQ], double *smem) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+/* FP32 coefficients of the FIRE scalars the passes need; one thread owns
+ * the FP64 scalars (Scal) and broadcasts these through shared memory, so
+ * the CTA's other threads issue no FP64 work outside anchors. */
+struct Coef {
+    float na, a, dt, dtsq, dtm;
+    int mix_pending, zero_v, done, anchor;
+};
+__device__ __forceinline__ void coef_from(Coef &c, const Scal &s, int anchor) {
+    c.na = (float)s.mix_na;
+    c.a = (float)s.mix_a;
+    c.dt = (float)s.dt;
+    c.dtsq = (float)s.dtsq;
+    c.dtm = (float)s.dtm;
+    c.mix_pending = s.mix_pending;
+    c.zero_v = s.zero_v;
+    c.done = s.done;
+    c.anchor = anchor;
+}
+
+/* Per-thread FP32 partials of pass B: sums of P = v.F, |v|^2, |F|^2 and
+ * maxima of |F|^2 and of sum_b |df_b| (the FP32 error bound). */
+struct Part {
+    float P, V2, F2, M2, A;
+};
+
+/* Warp reduction of a Part in FP32; lane 0 stores it in slots[q * 32 + warp]. */
+__device__ __forceinline__ void warp_part(Part t, float *slots) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        double x = v[q];
-        for (int off = 16; off >= 1; off >>= 1) {
-            const double o = __shfl_xor_sync(kFull, x, off);
-            x = q < nsum ? x + o : fmax(x, o);
+    for (int off = 16; off >= 1; off >>= 1) {
+        t.P += __shfl_xor_sync(kFull, t.P, off);
+        t.V2 += __shfl_xor_sync(kFull, t.V2, off);
+        t.F2 += __shfl_xor_sync(kFull, t.F2, off);
+        t.M2 = fmaxf(t.M2, __shfl_xor_sync(kFull, t.M2, off));
+        t.A = fmaxf(t.A, __shfl_xor_sync(kFull, t.A, off));
+    }
+    if (lane == 0) {
+        slots[0 * 32 + warp] = t.P;
+        slots[1 * 32 + warp] = t.V2;
+        slots[2 * 32 + warp] = t.F2;
+        slots[3 * 32 + warp] = t.M2;
+        slots[4 * 32 + warp] = t.A;
+    }
+}
+
+/* CTA totals of the warp slots, in FP64, by the calling thread. */
+__device__ __forceinline__ void slots_total(const float *slots, double (&t)[5]) {
+    const int nw = blockDim.x >> 5;
+    for (int q = 0; q < 5; ++q) {
+        double acc = slots[q * 32];
+        for (int w = 1; w < nw; ++w) {
+            const double v = slots[q * 32 + w];
+            acc = q < 3 ? acc + v : fmax(acc, v);
         }
-        if (lane == 0) smem[q * 32 + warp] = x;
+        t[q] = acc;
+    }
+}
+
+/* CTA totals of per-thread FP64 anchor partials (sum of F2, max of M2);
+ * valid in thread 0 after the call.  dslots: 64 doubles. */
+__device__ __forceinline__ void anchor_reduce(double F2, double M2, double *dslots, double &tF2, double &tM2) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int off = 16; off >= 1; off >>= 1) {
+        F2 += __shfl_xor_sync(kFull, F2, off);
+        M2 = fmax(M2, __shfl_xor_sync(kFull, M2, off));
+    }
+    if (lane == 0) {
+        dslots[warp] = F2;
+        dslots[32 + warp] = M2;
     }
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        double acc = smem[q * 32];
-        for (int w = 1; w < nw; ++w) acc = q < nsum ? acc + smem[q * 32 + w] : fmax(acc, smem[q * 32 + w]);
-        out[q] = acc;
-    }
-    __syncthreads();
+    tF2 = 0.0;
+    tM2 = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; ++w) {
+            tF2 += dslots[w];
+            tM2 = fmax(tM2, dslots[32 + w]);
+        }
 }
 
 /* Anchor step 1: X += u (exactly, in FP64), u = 0. */
@@ -277,27 +349,25 @@ __device__ void anchor_eval(const NetDev &d, const Team &tm, double &F2, double 
 }
 
 /* Pass A (FP32): mixing / zeroing from the previous step, then drift. */
-__device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Scal &s, const UView &u) {
-    const float na = (float)s.mix_na, a = (float)s.mix_a;
-    const float dt = (float)s.dt, dtsq = (float)s.dtsq, dtm = (float)s.dtm;
+__device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Coef &c, const UView &u) {
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         float2 v = d.vf[i];
         const float2 F = d.ff[i];
-        if (s.mix_pending) {
-            v.x = fmaf(na, v.x, v.x);
-            v.y = fmaf(na, v.y, v.y);
-            v.x = fmaf(a, F.x, v.x);
-            v.y = fmaf(a, F.y, v.y);
-            if (s.zero_v) v = make_float2(0.f, 0.f);
+        if (c.mix_pending) {
+            v.x = fmaf(c.na, v.x, v.x);
+            v.y = fmaf(c.na, v.y, v.y);
+            v.x = fmaf(c.a, F.x, v.x);
+            v.y = fmaf(c.a, F.y, v.y);
+            if (c.zero_v) v = make_float2(0.f, 0.f);
         }
-        if (!s.done) {
+        if (!c.done) {
             float2 h = u.hi[i], l = u.lo[i];
-            df_add(h.x, l.x, fmaf(dt, v.x, dtsq * F.x));
-            df_add(h.y, l.y, fmaf(dt, v.y, dtsq * F.y));
+            df_add(h.x, l.x, fmaf(c.dt, v.x, c.dtsq * F.x));
+            df_add(h.y, l.y, fmaf(c.dt, v.y, c.dtsq * F.y));
             u.hi[i] = h;
             u.lo[i] = l;
-            v.x = fmaf(dtm, F.x, v.x);
-            v.y = fmaf(dtm, F.y, v.y);
+            v.x = fmaf(c.dtm, F.x, v.x);
+            v.y = fmaf(c.dtm, F.y, v.y);
         }
         d.vf[i] = v;
     }
@@ -305,7 +375,7 @@ __device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Scal &s, con
 
 /* Pass B (FP32): F = F(X) + dF, half kick, partials {P, V2, F2 | maxF2,
  * max_i sum |df|} (the last bounds the FP32 error of the difference sum). */
-__device__ void mixed_pass_b(const NetDev &d, const Team &tm, float dtm, const UView &u, double (&acc)[5]) {
+__device__ Part mixed_pass_b(const NetDev &d, const Team &tm, float dtm, const UView &u) {
     float P = 0.f, V2 = 0.f, F2 = 0.f, M2 = 0.f, A = 0.f;
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         const unsigned c = d.fcode[i];
@@ -331,11 +401,7 @@ __device__ void mixed_pass_b(const NetDev &d, const Team &tm, float dtm, const U
         F2 += f2;
         M2 = fmaxf(M2, f2);
     }
-    acc[0] = P;
-    acc[1] = V2;
-    acc[2] = F2;
-    acc[3] = M2;
-    acc[4] = A;
+    return Part{P, V2, F2, M2, A};
 }
 
 __device__ void mixed_finish(const NetDev &d, const Team &tm) {
@@ -370,8 +436,15 @@ __device__ __forceinline__ void certify(Scal &s, const FireParamsDev &p, double 
 /* One CTA per network (batched)                                        */
 /* ------------------------------------------------------------------ */
 
+struct MixShared {
+    float slots[5 * 32];
+    double dslots[64];
+    double red[32];
+    Coef coef;
+};
+
 __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p, float2 *s_u, int smem_nodes,
-                                        double *smem, double *s_red) {
+                                        MixShared &sh) {
     const Team tm{0, 1};
     UView u;
     if (d.n <= smem_nodes) {
@@ -386,36 +459,50 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
         u.lo[i] = make_float2(0.f, 0.f);
         d.vf[i] = make_float2(0.f, 0.f);
     }
-    Scal s;
+    Scal s; /* meaningful in thread 0 only */
     int n_anchor = 1;
-    double r2[2], o2[2];
-    anchor_eval(d, tm, r2[0], r2[1]);
-    block_reduce<2>(r2, 1, o2, smem);
-    scal_init(s, p, o2[0], o2[1], d.sqrt_dof);
-    double M2_anchor = o2[1];
+    double M2_anchor = 0.0, F2, M2, tF2, tM2;
+    anchor_eval(d, tm, F2, M2);
+    anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
+    if (threadIdx.x == 0) {
+        scal_init(s, p, tF2, tM2, d.sqrt_dof);
+        M2_anchor = tM2;
+        coef_from(sh.coef, s, 0);
+    }
+    __syncthreads();
     for (;;) {
-        mixed_pass_a(d, tm, s, u);
-        if (s.done) break;
+        const Coef c = sh.coef;
+        mixed_pass_a(d, tm, c, u);
+        if (c.done) break;
         __syncthreads();
-        double acc[5], tot[5];
-        mixed_pass_b(d, tm, (float)s.dtm, u, acc);
-        block_reduce<5>(acc, 3, tot, smem);
-        scal_step(s, p, tot[0], tot[1], tot[2], tot[3], d.sqrt_dof);
-        if (need_anchor(s, p, tot[3], tot[4], M2_anchor)) {
+        warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t[5];
+            slots_total(sh.slots, t);
+            scal_step(s, p, t[0], t[1], t[2], t[3], d.sqrt_dof);
+            coef_from(sh.coef, s, need_anchor(s, p, t[3], t[4], M2_anchor));
+        }
+        __syncthreads();
+        if (sh.coef.anchor) {
             anchor_move(d, tm, u);
             __syncthreads();
-            anchor_eval(d, tm, r2[0], r2[1]);
-            block_reduce<2>(r2, 1, o2, smem);
-            M2_anchor = o2[1];
-            n_anchor++;
-            certify(s, p, o2[0], o2[1], d.sqrt_dof);
+            anchor_eval(d, tm, F2, M2);
+            anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
+            if (threadIdx.x == 0) {
+                M2_anchor = tM2;
+                n_anchor++;
+                certify(s, p, tF2, tM2, d.sqrt_dof);
+                coef_from(sh.coef, s, 0);
+            }
+            __syncthreads();
         }
     }
     mixed_finish(d, tm);
     __syncthreads();
-    energy_tiles(d, 0, 1, s_red);
+    energy_tiles(d, 0, 1, sh.red);
     double es, eb;
-    energy_final(d, s_red, es, eb);
+    energy_final(d, sh.red, es, eb);
     if (threadIdx.x == 0) {
         scal_store(d.st, s);
         d.st->fp64_steps = n_anchor;
@@ -428,8 +515,7 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
 __global__ void __launch_bounds__(kMixThreads, 1) k_fire_batch_mixed(const NetDev *nets, int n_nets, FireParamsDev p,
                                                                      int *queue, const int *order, int smem_nodes) {
     extern __shared__ float2 s_u[];
-    __shared__ double smem[5 * 32];
-    __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
+    __shared__ MixShared sh;
     __shared__ int s_net;
     /* The network's descriptor is staged in shared memory: its pointer
      * fields are then loop-invariant loads the compiler can hoist (a copy
@@ -444,9 +530,171 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_batch_mixed(const NetDe
         __syncthreads();
         const int slot = s_net;
         if (slot >= n_nets) return;
-        relax_network_cta_mixed(s_d, p, s_u, smem_nodes, smem, s_red);
+        relax_network_cta_mixed(s_d, p, s_u, smem_nodes, sh);
         __syncthreads();
     }
+}
+
+/* ------------------------------------------------------------------ */
+/* One thread-block cluster per network (batched, multi-SM teams)       */
+/* ------------------------------------------------------------------ */
+
+/* A network relaxed by the C CTAs of one cluster (C SMs): nodes are split
+ * over the CTAs (interleaved), u lives in global memory (L2-resident), the
+ * hardware cluster barrier orders the passes, and each CTA's partial sums
+ * are read by every other CTA through distributed shared memory.  Thread 0
+ * of every CTA advances an identical copy of the FP64 FIRE scalars from the
+ * same totals taken in the same rank order, so no broadcast is needed. */
+__device__ void cluster_totals(cooperative_groups::cluster_group &cl, double *s_part, int nq, int nsum, double *t) {
+    const int C = (int)cl.num_blocks();
+    for (int q = 0; q < nq; ++q) t[q] = 0.0;
+    for (int r = 0; r < C; ++r) {
+        const double *rp = cl.map_shared_rank(s_part, r);
+        for (int q = 0; q < nq; ++q) t[q] = q < nsum ? t[q] + rp[q] : fmax(t[q], rp[q]);
+    }
+}
+
+__global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const NetDev *nets, int n_nets,
+                                                                       FireParamsDev p, int *queue,
+                                                                       const int *order) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ MixShared sh;
+    __shared__ NetDev s_d;
+    __shared__ int s_slot;
+    __shared__ double s_part[5];
+    const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
+    for (;;) {
+        if (rank == 0 && threadIdx.x == 0) s_slot = atomicAdd(queue, 1);
+        cl.sync();
+        const int slot = *cl.map_shared_rank(&s_slot, 0);
+        /* every CTA has read rank 0's slot before any CTA may exit (a CTA's
+         * shared memory must not be read remotely after it exits) or rank 0
+         * overwrites it for the next network */
+        cl.sync();
+        if (slot >= n_nets) return;
+        if (threadIdx.x == 0) s_d = nets[order ? order[slot] : slot];
+        __syncthreads();
+        const NetDev &d = s_d;
+        const Team tm{rank, C};
+        const UView u{d.u_hi, d.u_lo};
+        for (int i = tm.first(); i < d.n; i += tm.stride()) {
+            u.hi[i] = make_float2(0.f, 0.f);
+            u.lo[i] = make_float2(0.f, 0.f);
+            d.vf[i] = make_float2(0.f, 0.f);
+        }
+        Scal s; /* replicated in thread 0 of every CTA */
+        int n_anchor = 1;
+        double M2_anchor = 0.0, F2, M2, tF2, tM2;
+        anchor_eval(d, tm, F2, M2);
+        anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
+        if (threadIdx.x == 0) {
+            s_part[0] = tF2;
+            s_part[1] = tM2;
+        }
+        cl.sync();
+        if (threadIdx.x == 0) {
+            double t[2];
+            cluster_totals(cl, s_part, 2, 1, t);
+            scal_init(s, p, t[0], t[1], d.sqrt_dof);
+            M2_anchor = t[1];
+            coef_from(sh.coef, s, 0);
+        }
+        __syncthreads();
+        for (;;) {
+            const Coef c = sh.coef;
+            mixed_pass_a(d, tm, c, u);
+            if (c.done) break;
+            cl.sync();
+            warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double t[5];
+                slots_total(sh.slots, t);
+                for (int q = 0; q < 5; ++q) s_part[q] = t[q];
+            }
+            cl.sync();
+            if (threadIdx.x == 0) {
+                double t[5];
+                cluster_totals(cl, s_part, 5, 3, t);
+                scal_step(s, p, t[0], t[1], t[2], t[3], d.sqrt_dof);
+                coef_from(sh.coef, s, need_anchor(s, p, t[3], t[4], M2_anchor));
+            }
+            __syncthreads();
+            if (sh.coef.anchor) {
+                anchor_move(d, tm, u);
+                cl.sync();
+                anchor_eval(d, tm, F2, M2);
+                anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
+                if (threadIdx.x == 0) {
+                    s_part[0] = tF2;
+                    s_part[1] = tM2;
+                }
+                cl.sync();
+                if (threadIdx.x == 0) {
+                    double t[2];
+                    cluster_totals(cl, s_part, 2, 1, t);
+                    M2_anchor = t[1];
+                    n_anchor++;
+                    certify(s, p, t[0], t[1], d.sqrt_dof);
+                    coef_from(sh.coef, s, 0);
+                }
+                __syncthreads();
+            }
+        }
+        mixed_finish(d, tm);
+        cl.sync();
+        if (rank == 0) {
+            energy_tiles(d, 0, 1, sh.red);
+            double es, eb;
+            energy_final(d, sh.red, es, eb);
+            if (threadIdx.x == 0) {
+                scal_store(d.st, s);
+                d.st->fp64_steps = n_anchor;
+                d.st->e_stretch = es;
+                d.st->e_bend = eb;
+            }
+        }
+        cl.sync();
+    }
+}
+
+/* CTAs per network for a batch: enough that the largest network has about
+ * kNodesPerCta nodes per CTA, a power of two up to the portable cluster
+ * size 8. */
+constexpr int kNodesPerCta = 1536;
+int mixed_cluster_size(int max_nodes) {
+    int c = 1;
+    while (c < 8 && c * kNodesPerCta < max_nodes) c *= 2;
+    return c;
+}
+
+cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
+                                 int *queue_dev, const int *order_dev, cudaStream_t stream) {
+    cudaError_t e;
+    int dev, sms;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kMixThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3((sms / cluster) * cluster);
+    int max_clusters = 0;
+    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, (void *)k_fire_cluster_mixed, &cfg)) != cudaSuccess)
+        return e;
+    if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
+    const int clusters = std::max(1, std::min(n_nets, max_clusters));
+    cfg.gridDim = dim3(clusters * cluster);
+    if ((e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream)) != cudaSuccess) return e;
+    return cudaLaunchKernelEx(&cfg, k_fire_cluster_mixed, nets_dev, n_nets, p, queue_dev, order_dev);
 }
 
 /* Shared memory for u: the largest network of the batch, capped so one CTA
@@ -497,24 +745,24 @@ __device__ void team_totals(const double *part, int G, int nq, int nsum, double 
 
 __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, FireParamsDev p,
                                                                     unsigned long long budget_ns) {
-    __shared__ double smem[5 * 32];
+    __shared__ MixShared sh;
     const Team tm{(int)blockIdx.x, (int)gridDim.x};
     const unsigned G = gridDim.x;
     FireState *st = d.st;
     const UView u{d.u_hi, d.u_lo};
     bool last;
-    Scal s;
+    Scal s; /* meaningful in thread 0 only */
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         u.hi[i] = make_float2(0.f, 0.f);
         u.lo[i] = make_float2(0.f, 0.f);
         d.vf[i] = make_float2(0.f, 0.f);
     }
-    double r2[2], o2[2];
-    anchor_eval(d, tm, r2[0], r2[1]);
-    block_reduce<2>(r2, 1, o2, smem);
+    double F2, M2, tF2, tM2;
+    anchor_eval(d, tm, F2, M2);
+    anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
     if (threadIdx.x == 0) {
-        d.part[blockIdx.x] = o2[0];
-        d.part[G + blockIdx.x] = o2[1];
+        d.part[blockIdx.x] = tF2;
+        d.part[G + blockIdx.x] = tM2;
     }
     if (!barrier_arrive(st, G, budget_ns, last, 11)) return;
     if (last) {
@@ -530,16 +778,23 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
         barrier_release(st);
     }
     for (;;) {
-        scal_load(s, st);
-        mixed_pass_a(d, tm, s, u);
-        if (s.done) break;
+        if (threadIdx.x == 0) {
+            scal_load(s, st);
+            coef_from(sh.coef, s, 0);
+        }
+        __syncthreads();
+        const Coef c = sh.coef;
+        mixed_pass_a(d, tm, c, u);
+        if (c.done) break;
         if (!barrier_arrive(st, G, budget_ns, last, 12)) return;
         if (last) barrier_release(st);
-        double acc[5], tot[5];
-        mixed_pass_b(d, tm, (float)s.dtm, u, acc);
-        block_reduce<5>(acc, 3, tot, smem);
-        if (threadIdx.x == 0)
-            for (int q = 0; q < 5; ++q) d.part[(size_t)q * G + blockIdx.x] = tot[q];
+        warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t[5];
+            slots_total(sh.slots, t);
+            for (int q = 0; q < 5; ++q) d.part[(size_t)q * G + blockIdx.x] = t[q];
+        }
         if (!barrier_arrive(st, G, budget_ns, last, 13)) return;
         if (last) {
             if (threadIdx.x == 0) {
@@ -553,16 +808,20 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
             }
             barrier_release(st);
         }
-        const volatile FireState *vs = st;
-        if (vs->anchor_now) {
+        if (threadIdx.x == 0) {
+            const volatile FireState *vs = st;
+            sh.coef.anchor = vs->anchor_now;
+        }
+        __syncthreads();
+        if (sh.coef.anchor) {
             anchor_move(d, tm, u);
             if (!barrier_arrive(st, G, budget_ns, last, 14)) return;
             if (last) barrier_release(st);
-            anchor_eval(d, tm, r2[0], r2[1]);
-            block_reduce<2>(r2, 1, o2, smem);
+            anchor_eval(d, tm, F2, M2);
+            anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
             if (threadIdx.x == 0) {
-                d.part[blockIdx.x] = o2[0];
-                d.part[G + blockIdx.x] = o2[1];
+                d.part[blockIdx.x] = tF2;
+                d.part[G + blockIdx.x] = tM2;
             }
             if (!barrier_arrive(st, G, budget_ns, last, 15)) return;
             if (last) {

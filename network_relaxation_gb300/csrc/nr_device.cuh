@@ -75,6 +75,8 @@ struct NetDev {
     int2 *mt_nodes;
     float4 *mt_arms;
     float2 *mt_pk;
+    double2 *bfrc;  /* FP64 path: force of every bond on its first endpoint */
+    double4 *tfrc;  /* FP64 path: (F_j, F_k) of every triple */
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
     double *epart;  /* 2 * max(bond tiles, triple tiles) energy partials */
     FireState *st;

@@ -92,3 +92,32 @@ def test_mixed_step_cap_reports_fp64_state(cuda):
     assert abs(rep.max_force - np.sqrt((m.forces(x) ** 2).sum(1)).max()) <= 1e-14 * rep.max_force
     es, eb = m.energies(x)
     assert (es, eb) == (rep.e_stretch, rep.e_bend)
+
+
+@pytest.mark.parametrize("cluster", [None, "4"])
+def test_mixed_cluster_teams(cuda, cluster, monkeypatch):
+    """Networks above the one-CTA size class run on a thread-block cluster
+    (CTAs of one cluster share a network through distributed shared
+    memory); results certified by the oracle's FP64 force."""
+    if cluster:
+        monkeypatch.setenv("NR_CLUSTER", cluster)
+    rng = np.random.default_rng(5)
+    hosts, arrs, kb, gam = [], [], [], []
+    for i, L in enumerate([50, 12, 44, 20]):
+        h = nr.HostNetwork.lattice(L, L, 0.75, 0.0, 900 + i).get_triples()
+        hosts.append(h)
+        arrs.append(h.arrays())
+        kb.append(1e-2)
+        gam.append(float(rng.uniform(0.01, 0.03)))
+    kb, gam = np.array(kb), np.array(gam)
+    b = nr.Batch(hosts, 1.0, kb)
+    b.affine_displace(gam * (b.maxy - b.miny), 0.0)
+    reps = b.relax(nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **FIRE))
+    X = b.positions()
+    for i, a in enumerate(arrs):
+        assert reps[i].status == nr.NR_OK
+        x = X[b.offsets[i]:b.offsets[i + 1]]
+        m = oracle.Model(a, 1.0, kb[i])
+        assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+        es, eb = m.energies(x)
+        assert (es, eb) == (reps[i].e_stretch, reps[i].e_bend)
