@@ -53,7 +53,7 @@ struct Image {
 };
 
 struct NetOff {
-    size_t mb_other, mb_data, mb_sk, mt_nodes, mt_arms, mt_pk, bfrc, tfrc;
+    size_t mb_data, mb_sk, bdf, mt_arms, mt_pk, tdf, bfrc, tfrc;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
 };
@@ -142,27 +142,13 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.bent = img.put(inc.bent.data(), inc.bent.size());
         o.tptr = img.put(inc.tptr.data(), inc.tptr.size());
         o.tent = img.put(inc.tent.data(), inc.tent.size());
-        /* mixed-precision entry records: the other node(s) of every entry */
-        std::vector<int> mb_other(inc.bent.size());
-        for (int v = 0; v < h.n_points; ++v)
-            for (int e = inc.bptr[v]; e < inc.bptr[v + 1]; ++e) {
-                const int b = inc.bent[e] >> 1;
-                mb_other[e] = (inc.bent[e] & 1) ? h.edge_ij[2 * b] : h.edge_ij[2 * b + 1];
-            }
-        std::vector<int2> mt_nodes(inc.tent.size());
-        for (int v = 0; v < h.n_points; ++v)
-            for (int e = inc.tptr[v]; e < inc.tptr[v + 1]; ++e) {
-                const int t = inc.tent[e] >> 2, role = inc.tent[e] & 3;
-                const int hh = h.tri_hjk[3 * t], jj = h.tri_hjk[3 * t + 1], kk = h.tri_hjk[3 * t + 2];
-                const int n1 = role == 0 ? jj : hh, n2 = role == 2 ? jj : kk;
-                mt_nodes[e] = make_int2(n1 | (role << 30), n2);
-            }
-        o.mb_other = img.put(mb_other.data(), mb_other.size());
-        o.mb_data = img.add(sizeof(float4) * mb_other.size());
-        o.mb_sk = img.add(sizeof(float2) * mb_other.size());
-        o.mt_nodes = img.put(mt_nodes.data(), mt_nodes.size());
-        o.mt_arms = img.add(sizeof(float4) * mt_nodes.size());
-        o.mt_pk = img.add(sizeof(float2) * mt_nodes.size());
+        /* mixed precision: per-item anchor records and force changes */
+        o.mb_data = img.add(sizeof(float4) * (size_t)ne);
+        o.mb_sk = img.add(sizeof(float2) * (size_t)ne);
+        o.bdf = img.add(sizeof(float2) * (size_t)ne);
+        o.mt_arms = img.add(sizeof(float4) * (size_t)nt);
+        o.mt_pk = img.add(sizeof(float2) * (size_t)nt);
+        o.tdf = img.add(sizeof(float4) * (size_t)nt);
         o.bfrc = img.add(sizeof(double2) * (size_t)ne);
         o.tfrc = img.add(sizeof(double4) * (size_t)nt);
         S.max_nodes = std::max(S.max_nodes, h.n_points);
@@ -222,12 +208,12 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.ff = S.ff_all + S.node_off[i];
         d.fa_hi = S.fa_hi_all + S.node_off[i];
         d.fa_lo = S.fa_lo_all + S.node_off[i];
-        d.mb_other = (int *)(base + o.mb_other);
         d.mb_data = (float4 *)(base + o.mb_data);
         d.mb_sk = (float2 *)(base + o.mb_sk);
-        d.mt_nodes = (int2 *)(base + o.mt_nodes);
+        d.bdf = (float2 *)(base + o.bdf);
         d.mt_arms = (float4 *)(base + o.mt_arms);
         d.mt_pk = (float2 *)(base + o.mt_pk);
+        d.tdf = (float4 *)(base + o.tdf);
         d.bfrc = (double2 *)(base + o.bfrc);
         d.tfrc = (double4 *)(base + o.tfrc);
         d.fcode = (const unsigned char *)(base + o.fcode);

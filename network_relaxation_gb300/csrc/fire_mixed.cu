@@ -33,14 +33,18 @@
  * Layout per network: u (hi, lo) lives in shared memory for the whole
  * relaxation when it fits (16 B/node), else in global memory; v, F and the
  * anchor force stream from global memory, coalesced (thread t owns nodes
- * t, t + blockDim, ...).  Every incidence entry carries its own oriented
- * FP32 anchor record, so the gather issues no dependent global loads:
- *   bond entry    mb_other (int), mb_data {ra hi.x, hi.y, lo.x, lo.y} (the
- *                 anchor vector self -> other as a double-float),
- *                 mb_sk {|ra| - l0, k}
- *   triple entry  mt_nodes {n1 | role << 30, n2}, mt_arms {a_a, b_a},
- *                 mt_pk {phi_a, kb}; role 0: self = hinge (n1 = j, n2 = k),
- *                 1: self = j (n1 = h, n2 = k), 2: self = k (n1 = h, n2 = j)
+ * t, t + blockDim, ...).  Pass B is item-centric: every bond and every
+ * triple computes its force change ONCE, from its FP32 anchor record,
+ *   bond    mb_data {ra hi.x, hi.y, lo.x, lo.y} (the anchor vector i -> j as
+ *           a double-float), mb_sk {|ra| - l0, k}     -> bdf (change on i)
+ *   triple  mt_arms {a_a, b_a}, mt_pk {phi_a, kb}     -> tdf (changes on j, k)
+ * and after a team sync every node gathers its entries in incidence order
+ * (bonds, then triples; a bond's second node takes -bdf, a hinge
+ * -(dF_j + dF_k)).  Computing a bond from either end gives exactly opposite
+ * FP32 results (round-to-nearest is odd-symmetric and every step of
+ * bond_dforce is sign-covariant), so the gather reproduces a node-centric
+ * evaluation bit for bit while doing a third of its arithmetic, free of the
+ * warp divergence of per-entry roles.
  *
  * Compiled with --fmad=false (the FP64 anchor code stays canonical); FP32
  * expressions use explicit fmaf().
@@ -154,17 +158,18 @@ struct UView {
     }
 };
 
-/* FP32 force change since the anchor for node i. */
-__device__ __forceinline__ float2 node_dforce(const NetDev &d, const UView &u, int i, float &mag) {
+/* FP32 force change since the anchor for node i, gathered from the item
+ * results bdf/tdf in incidence order; mag = sum of the entries' |df|. */
+__device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag) {
     float2 F = make_float2(0.f, 0.f);
     mag = 0.f;
     if (d.use_bonds) {
         const int e1 = d.bptr[i + 1];
-#pragma unroll 2
+#pragma unroll 4
         for (int e = d.bptr[i]; e < e1; ++e) {
-            float2 dh, dlo;
-            u.diff2(d.mb_other[e], i, dh, dlo);
-            const float2 df = bond_dforce(d.mb_data[e], d.mb_sk[e], dh, dlo);
+            const int code = d.bent[e];
+            float2 df = d.bdf[code >> 1];
+            if (code & 1) df = make_float2(-df.x, -df.y);
             F.x += df.x;
             F.y += df.y;
             mag += fabsf(df.x) + fabsf(df.y);
@@ -172,30 +177,47 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, const UView &u, i
     }
     if (d.use_triples) {
         const int e1 = d.tptr[i + 1];
-#pragma unroll 2
+#pragma unroll 4
         for (int e = d.tptr[i]; e < e1; ++e) {
-            const int2 nn = d.mt_nodes[e];
-            const int role = (unsigned)nn.x >> 30, n1 = nn.x & 0x3fffffff, n2 = nn.y;
-            float2 dFj, dFk;
+            const int code = d.tent[e];
+            const int role = code & 3;
+            const float4 q = d.tdf[code >> 2];
+            float gx, gy, m;
             if (role == 0) {
-                tri_dforce(d.mt_arms[e], d.mt_pk[e], u.diff(n1, i), u.diff(n2, i), dFj, dFk);
-                F.x -= dFj.x + dFk.x;
-                F.y -= dFj.y + dFk.y;
-                mag += fabsf(dFj.x) + fabsf(dFj.y) + fabsf(dFk.x) + fabsf(dFk.y);
-            } else if (role == 1) {
-                tri_dforce(d.mt_arms[e], d.mt_pk[e], u.diff(i, n1), u.diff(n2, n1), dFj, dFk);
-                F.x += dFj.x;
-                F.y += dFj.y;
-                mag += fabsf(dFj.x) + fabsf(dFj.y);
+                gx = -(q.x + q.z);
+                gy = -(q.y + q.w);
+                m = fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(q.w);
             } else {
-                tri_dforce(d.mt_arms[e], d.mt_pk[e], u.diff(n2, n1), u.diff(i, n1), dFj, dFk);
-                F.x += dFk.x;
-                F.y += dFk.y;
-                mag += fabsf(dFk.x) + fabsf(dFk.y);
+                gx = role == 1 ? q.x : q.z;
+                gy = role == 1 ? q.y : q.w;
+                m = fabsf(gx) + fabsf(gy);
             }
+            F.x += gx;
+            F.y += gy;
+            mag += m;
         }
     }
     return F;
+}
+
+/* Item pass (FP32): the force change of every bond on its node i and of
+ * every triple on its nodes j and k, each computed once, by the team's
+ * threads in item order. */
+__device__ void mixed_items(const NetDev &d, int first, int stride, const UView &u) {
+    if (d.use_bonds)
+        for (int b = first; b < d.n_edges; b += stride) {
+            const int4 r = d.bond[b];
+            float2 dh, dlo;
+            u.diff2(r.y, r.x, dh, dlo);
+            d.bdf[b] = bond_dforce(d.mb_data[b], d.mb_sk[b], dh, dlo);
+        }
+    if (d.use_triples)
+        for (int t = first; t < d.n_triples; t += stride) {
+            const int4 r = d.tri[t];
+            float2 dFj, dFk;
+            tri_dforce(d.mt_arms[t], d.mt_pk[t], u.diff(r.y, r.x), u.diff(r.z, r.x), dFj, dFk);
+            d.tdf[t] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+        }
 }
 
 struct Team {
@@ -297,44 +319,36 @@ __device__ void anchor_move(const NetDev &d, const Team &tm, const UView &u) {
     }
 }
 
-/* Anchor step 2 (after a team sync): the FP32 anchor records of every
- * incidence entry of the team's nodes from FP64 geometry, the FP64 forces
- * into f and the double-float anchor force, ff = F; CTA partials of |F|^2
- * and max|F|^2. */
+/* Anchor step 2 (after a team sync): the FP32 anchor record of every bond
+ * and triple from FP64 geometry, the FP64 forces into f and the
+ * double-float anchor force, ff = F; CTA partials of |F|^2 and max|F|^2. */
 __device__ void anchor_eval(const NetDev &d, const Team &tm, double &F2, double &M2) {
     const double W = d.width;
     F2 = 0.0;
     M2 = 0.0;
+    if (d.use_bonds)
+        for (int b = tm.first(); b < d.n_edges; b += tm.stride()) {
+            const int4 r = d.bond[b];
+            const double2 p1 = d.x[r.x], p2 = d.x[r.y];
+            const double rx = (p2.x + wrap_shift(r.z, W)) - p1.x, ry = p2.y - p1.y;
+            const double k = d.bond_k ? d.bond_k[b] : d.ks;
+            const float hx = (float)rx, hy = (float)ry;
+            d.mb_data[b] = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
+            d.mb_sk[b] = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)k);
+        }
+    if (d.use_triples)
+        for (int t = tm.first(); t < d.n_triples; t += tm.stride()) {
+            const int4 r = d.tri[t];
+            const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
+            const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+            const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+            const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
+            const double kb = d.tri_kb ? d.tri_kb[t] : d.kb;
+            const double phi0 = d.tri_phi0 ? d.tri_phi0[t] : 0.0;
+            d.mt_arms[t] = make_float4((float)ax, (float)ay, (float)bx, (float)by);
+            d.mt_pk[t] = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
+        }
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
-        if (d.use_bonds)
-            for (int e = d.bptr[i]; e < d.bptr[i + 1]; ++e) {
-                const int code = d.bent[e];
-                const int b = code >> 1;
-                const int4 r = d.bond[b];
-                const double2 p1 = d.x[r.x], p2 = d.x[r.y];
-                double rx = (p2.x + wrap_shift(r.z, W)) - p1.x, ry = p2.y - p1.y;
-                if (code & 1) {
-                    rx = -rx;
-                    ry = -ry;
-                }
-                const double k = d.bond_k ? d.bond_k[b] : d.ks;
-                const float hx = (float)rx, hy = (float)ry;
-                d.mb_data[e] = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
-                d.mb_sk[e] = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)k);
-            }
-        if (d.use_triples)
-            for (int e = d.tptr[i]; e < d.tptr[i + 1]; ++e) {
-                const int t = d.tent[e] >> 2;
-                const int4 r = d.tri[t];
-                const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
-                const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
-                const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
-                const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
-                const double kb = d.tri_kb ? d.tri_kb[t] : d.kb;
-                const double phi0 = d.tri_phi0 ? d.tri_phi0[t] : 0.0;
-                d.mt_arms[e] = make_float4((float)ax, (float)ay, (float)bx, (float)by);
-                d.mt_pk[e] = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
-            }
         double fx, fy;
         node_force_fp64(d, i, fx, fy);
         d.f[i] = make_double2(fx, fy);
@@ -373,16 +387,17 @@ __device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Coef &c, con
     }
 }
 
-/* Pass B (FP32): F = F(X) + dF, half kick, partials {P, V2, F2 | maxF2,
- * max_i sum |df|} (the last bounds the FP32 error of the difference sum). */
-__device__ Part mixed_pass_b(const NetDev &d, const Team &tm, float dtm, const UView &u) {
+/* Pass B, gather (FP32, after the item pass and a team sync): F = F(X) + dF,
+ * half kick, partials {P, V2, F2 | maxF2, max_i sum |df|} (the last bounds
+ * the FP32 error of the difference sum). */
+__device__ Part mixed_pass_b(const NetDev &d, const Team &tm, float dtm) {
     float P = 0.f, V2 = 0.f, F2 = 0.f, M2 = 0.f, A = 0.f;
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         const unsigned c = d.fcode[i];
         float2 F = make_float2(0.f, 0.f);
         if (c != 0) {
             float mag;
-            const float2 dF = node_dforce(d, u, i, mag);
+            const float2 dF = node_dforce(d, i, mag);
             A = fmaxf(A, mag);
             const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
             F.x = ah.x + (al.x + dF.x);
@@ -475,7 +490,9 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
         mixed_pass_a(d, tm, c, u);
         if (c.done) break;
         __syncthreads();
-        warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+        mixed_items(d, tm.first(), tm.stride(), u);
+        __syncthreads();
+        warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
         __syncthreads();
         if (threadIdx.x == 0) {
             double t[5];
@@ -606,7 +623,9 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
             mixed_pass_a(d, tm, c, u);
             if (c.done) break;
             cl.sync();
-            warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+            mixed_items(d, tm.first(), tm.stride(), u);
+            cl.sync();
+            warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
             __syncthreads();
             if (threadIdx.x == 0) {
                 double t[5];
@@ -788,7 +807,10 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
         if (c.done) break;
         if (!barrier_arrive(st, G, budget_ns, last, 12)) return;
         if (last) barrier_release(st);
-        warp_part(mixed_pass_b(d, tm, c.dtm, u), sh.slots);
+        mixed_items(d, tm.first(), tm.stride(), u);
+        if (!barrier_arrive(st, G, budget_ns, last, 16)) return;
+        if (last) barrier_release(st);
+        warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
         __syncthreads();
         if (threadIdx.x == 0) {
             double t[5];

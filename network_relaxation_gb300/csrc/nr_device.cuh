@@ -66,15 +66,15 @@ struct NetDev {
     const int *bptr, *bent, *tptr, *tent;
     /* mixed precision (fire_mixed.cu): double-float displacement from the
      * anchor x (global copy, used when it does not fit shared memory), FP32
-     * velocity and force, double-float anchor force; per incidence entry the
-     * other node(s) and the FP32 anchor record */
+     * velocity and force, double-float anchor force; per bond and per triple
+     * the FP32 anchor record and the FP32 force change of the current pass */
     float2 *u_hi, *u_lo, *vf, *ff, *fa_hi, *fa_lo;
-    int *mb_other;
-    float4 *mb_data; /* anchor vector self -> other, {hi.x, hi.y, lo.x, lo.y} */
+    float4 *mb_data; /* anchor vector i -> j, {hi.x, hi.y, lo.x, lo.y} */
     float2 *mb_sk;   /* {|r_anchor| - l0, k} */
-    int2 *mt_nodes;
-    float4 *mt_arms;
-    float2 *mt_pk;
+    float4 *mt_arms; /* anchor arms {a.x, a.y, b.x, b.y} (hinge -> j, hinge -> k) */
+    float2 *mt_pk;   /* {theta_anchor - pi, kb} */
+    float2 *bdf;     /* force change of the bond on node i */
+    float4 *tdf;     /* force changes of the triple on j and k */
     double2 *bfrc;  /* FP64 path: force of every bond on its first endpoint */
     double4 *tfrc;  /* FP64 path: (F_j, F_k) of every triple */
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
