@@ -164,10 +164,10 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
     float2 F = make_float2(0.f, 0.f);
     mag = 0.f;
     if (d.use_bonds) {
-        const int e1 = d.bptr[i + 1];
+        const int e1 = __ldg(d.bptr + i + 1);
 #pragma unroll 4
-        for (int e = d.bptr[i]; e < e1; ++e) {
-            const int code = d.bent[e];
+        for (int e = __ldg(d.bptr + i); e < e1; ++e) {
+            const int code = __ldg(d.bent + e);
             float2 df = d.bdf[code >> 1];
             if (code & 1) df = make_float2(-df.x, -df.y);
             F.x += df.x;
@@ -176,10 +176,10 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
         }
     }
     if (d.use_triples) {
-        const int e1 = d.tptr[i + 1];
+        const int e1 = __ldg(d.tptr + i + 1);
 #pragma unroll 4
-        for (int e = d.tptr[i]; e < e1; ++e) {
-            const int code = d.tent[e];
+        for (int e = __ldg(d.tptr + i); e < e1; ++e) {
+            const int code = __ldg(d.tent + e);
             const int role = code & 3;
             const float4 q = d.tdf[code >> 2];
             float gx, gy, m;
@@ -202,18 +202,20 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
 
 /* Item pass (FP32): the force change of every bond on its node i and of
  * every triple on its nodes j and k, each computed once, by the team's
- * threads in item order. */
+ * threads in item order.  Topology (bond, tri, the incidence lists, fcode)
+ * never changes during a relaxation and is read through the read-only
+ * cache; anchor records and u are rewritten in the kernel and are not. */
 __device__ void mixed_items(const NetDev &d, int first, int stride, const UView &u) {
     if (d.use_bonds)
         for (int b = first; b < d.n_edges; b += stride) {
-            const int4 r = d.bond[b];
+            const int4 r = __ldg(d.bond + b);
             float2 dh, dlo;
             u.diff2(r.y, r.x, dh, dlo);
             d.bdf[b] = bond_dforce(d.mb_data[b], d.mb_sk[b], dh, dlo);
         }
     if (d.use_triples)
         for (int t = first; t < d.n_triples; t += stride) {
-            const int4 r = d.tri[t];
+            const int4 r = __ldg(d.tri + t);
             float2 dFj, dFk;
             tri_dforce(d.mt_arms[t], d.mt_pk[t], u.diff(r.y, r.x), u.diff(r.z, r.x), dFj, dFk);
             d.tdf[t] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
@@ -226,34 +228,15 @@ struct Team {
     __device__ int stride() const { return size * blockDim.x; }
 };
 
-/* FP32 coefficients of the FIRE scalars the passes need; one thread owns
- * the FP64 scalars (Scal) and broadcasts these through shared memory, so
- * the CTA's other threads issue no FP64 work outside anchors. */
-struct Coef {
-    float na, a, dt, dtsq, dtm;
-    int mix_pending, zero_v, done, anchor;
-};
-__device__ __forceinline__ void coef_from(Coef &c, const Scal &s, int anchor) {
-    c.na = (float)s.mix_na;
-    c.a = (float)s.mix_a;
-    c.dt = (float)s.dt;
-    c.dtsq = (float)s.dtsq;
-    c.dtm = (float)s.dtm;
-    c.mix_pending = s.mix_pending;
-    c.zero_v = s.zero_v;
-    c.done = s.done;
-    c.anchor = anchor;
-}
-
 /* Per-thread FP32 partials of pass B: sums of P = v.F, |v|^2, |F|^2 and
  * maxima of |F|^2 and of sum_b |df_b| (the FP32 error bound). */
 struct Part {
     float P, V2, F2, M2, A;
 };
 
-/* Warp reduction of a Part in FP32; lane 0 stores it in slots[q * 32 + warp]. */
-__device__ __forceinline__ void warp_part(Part t, float *slots) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+/* Xor butterfly over the warp (fixed order: every lane ends with the same
+ * totals, and equal inputs give equal totals in every CTA). */
+__device__ __forceinline__ Part warp_reduce(Part t) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         t.P += __shfl_xor_sync(kFull, t.P, off);
@@ -262,6 +245,13 @@ __device__ __forceinline__ void warp_part(Part t, float *slots) {
         t.M2 = fmaxf(t.M2, __shfl_xor_sync(kFull, t.M2, off));
         t.A = fmaxf(t.A, __shfl_xor_sync(kFull, t.A, off));
     }
+    return t;
+}
+
+/* Warp totals of a Part; lane 0 stores them in slots[q * 32 + warp]. */
+__device__ __forceinline__ void warp_part(Part t, float *slots) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    t = warp_reduce(t);
     if (lane == 0) {
         slots[0 * 32 + warp] = t.P;
         slots[1 * 32 + warp] = t.V2;
@@ -271,17 +261,154 @@ __device__ __forceinline__ void warp_part(Part t, float *slots) {
     }
 }
 
-/* CTA totals of the warp slots, in FP64, by the calling thread. */
-__device__ __forceinline__ void slots_total(const float *slots, double (&t)[5]) {
-    const int nw = blockDim.x >> 5;
-    for (int q = 0; q < 5; ++q) {
-        double acc = slots[q * 32];
-        for (int w = 1; w < nw; ++w) {
-            const double v = slots[q * 32 + w];
-            acc = q < 3 ? acc + v : fmax(acc, v);
+/* CTA totals of the warp slots, computed by warp 0 (lane w takes warp w's
+ * slot); every lane of warp 0 returns them. */
+__device__ __forceinline__ Part block_totals(const float *slots) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    Part t{0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lane < nw) t = Part{slots[lane], slots[32 + lane], slots[64 + lane], slots[96 + lane], slots[128 + lane]};
+    return warp_reduce(t);
+}
+
+/* ----- FIRE scalars (large_strain_relax.cu:683-718) in FP32 -----
+ *
+ * The scalar update after each reduction is a serial chain that the whole
+ * team waits for, and FP64 issues at 1/64 of the FP32 rate on this GPU: in
+ * FP64 it took several microseconds per step.  The mixed path therefore
+ * runs it in FP32 on the FP32 totals (the forces it acts on are FP32
+ * already).  FP64 stays where the result is certified: |F| and max|F| from
+ * the anchors, and the stop decision. */
+struct MixParams {
+    float alpha0, falpha, dt_max, finc, fdec, half_inv_m;
+    float thr2;      /* stop threshold on the |F|^2 total (RMS) or on max |F|^2 */
+    float half_fcut;
+    int nmin, max_steps, crit_max;
+};
+
+__device__ __forceinline__ MixParams mix_params(const FireParamsDev &p, double sqrt_dof) {
+    MixParams q;
+    q.alpha0 = (float)p.alpha0;
+    q.falpha = (float)p.falpha;
+    q.dt_max = (float)p.dt_max;
+    q.finc = (float)p.finc;
+    q.fdec = (float)p.fdec;
+    q.half_inv_m = (float)(0.5 / p.mass);
+    const double thr = p.criterion == 1 ? p.fcut : p.fcut * sqrt_dof;
+    q.thr2 = (float)(thr * thr);
+    q.half_fcut = (float)(0.5 * p.fcut);
+    q.nmin = p.nmin;
+    q.max_steps = p.max_steps;
+    q.crit_max = p.criterion == 1;
+    return q;
+}
+
+/* State at the top of run_fire_md (large_strain_relax.cu:616-643); the
+ * first anchor's certification follows. */
+__device__ __forceinline__ void mix_init(MixScal &s, const MixParams &q) {
+    s.dt = q.dt_max;
+    s.dtm = s.dt * q.half_inv_m;
+    s.dtsq = s.dt * s.dtm;
+    s.alpha = q.alpha0;
+    s.na = 0.f;
+    s.a = 0.f;
+    s.m2_anchor = 0.f;
+    s.pad0 = 0.f;
+    s.since = 0;
+    s.step = 0;
+    s.mix_pending = 0;
+    s.zero_v = 0;
+    s.done = 0;
+    s.converged = 0;
+    s.status = 0;
+    s.n_anchor = 0;
+    s.fmag = 0.0;
+    s.maxf = 0.0;
+}
+
+/* End of one loop iteration: mixing coefficients with the current alpha,
+ * dt / alpha adaption, the (FP32) stop test that claims convergence. */
+__device__ __forceinline__ void mix_step(MixScal &s, const MixParams &q, const Part &t) {
+    s.step++;
+    s.a = s.alpha * sqrtf(t.V2) / sqrtf(t.F2);
+    s.na = -s.alpha;
+    s.mix_pending = 1;
+    if (t.P > 0.f) {
+        if (++s.since > q.nmin) {
+            s.dt = fminf(s.dt * q.finc, q.dt_max);
+            s.alpha *= q.falpha;
         }
-        t[q] = acc;
+        s.zero_v = 0;
+    } else {
+        s.since = 0;
+        s.dt *= q.fdec;
+        s.alpha = q.alpha0;
+        s.zero_v = 1;
     }
+    s.dtm = s.dt * q.half_inv_m;
+    s.dtsq = s.dt * s.dtm;
+    s.converged = (q.crit_max ? t.M2 : t.F2) < q.thr2;
+    if (!isfinite(t.F2) || !isfinite(t.P)) s.status = NR_ERR_NONFINITE;
+    s.done = s.converged || s.step >= q.max_steps || s.status != 0;
+}
+
+/* The anchor must move when the FP32 rounding of the difference sum,
+ * about kErr * max_i sum_b |df_b|, is no longer small against the force the
+ * run still has to resolve (the larger of max|F| and half the stop
+ * threshold), when max|F| has dropped far below the anchor force, and
+ * whenever the FP32 step claims convergence or ends the run. */
+constexpr float kErr = 2.0e-7f;
+__device__ __forceinline__ bool need_anchor(const MixScal &s, const MixParams &q, const Part &t) {
+    const float f = fmaxf(sqrtf(t.M2), q.half_fcut);
+    return s.converged || s.done || kErr * t.A > 0.1f * f || t.M2 < kAnchorF * kAnchorF * s.m2_anchor;
+}
+
+/* After an anchor: the FP64 totals at the anchor decide convergence (at
+ * step 0 only the step cap and a non-finite force stop the run: the
+ * reference always takes a first step). */
+__device__ __forceinline__ void mix_certify(MixScal &s, const FireParamsDev &p, double sqrt_dof, double F2,
+                                            double M2) {
+    s.fmag = sqrt(F2);
+    s.maxf = sqrt(M2);
+    s.m2_anchor = (float)M2;
+    s.n_anchor++;
+    s.converged = crit_met(p, s.fmag, s.maxf, sqrt_dof);
+    if (!isfinite(s.fmag)) s.status = NR_ERR_NONFINITE;
+    s.done = (s.step > 0 && s.converged) || s.step >= p.max_steps || s.status != 0;
+}
+
+/* Report fields of the network's FireState. */
+__device__ __forceinline__ void mix_report(FireState *st, const MixScal &s) {
+    st->fmag = s.fmag;
+    st->maxf = s.maxf;
+    st->step = s.step;
+    st->status = s.status;
+    st->converged = s.converged;
+    st->done = s.done;
+    st->fp64_steps = s.n_anchor;
+    st->dt = s.dt;
+    st->alpha = s.alpha;
+}
+
+/* MixScal of a multi-CTA team, read from L2 after a grid barrier. */
+__device__ __forceinline__ MixScal mix_load(const FireState *st) {
+    static_assert(sizeof(MixScal) == 80, "MixScal is five 16-byte words");
+    union {
+        MixScal s;
+        int4 w[5];
+    } u;
+    const int4 *src = reinterpret_cast<const int4 *>(&st->mix);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) u.w[k] = __ldcg(src + k);
+    return u.s;
+}
+
+/* FP32 coefficients of the next pass A, broadcast through shared memory. */
+struct Coef {
+    float na, a, dt, dtsq, dtm;
+    int mix_pending, zero_v, done, anchor;
+};
+__device__ __forceinline__ Coef coef_of(const MixScal &s, int anchor) {
+    return Coef{s.na, s.a, s.dt, s.dtsq, s.dtm, s.mix_pending, s.zero_v, s.done, anchor};
 }
 
 /* CTA totals of per-thread FP64 anchor partials (sum of F2, max of M2);
@@ -393,7 +520,7 @@ __device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Coef &c, con
 __device__ Part mixed_pass_b(const NetDev &d, const Team &tm, float dtm) {
     float P = 0.f, V2 = 0.f, F2 = 0.f, M2 = 0.f, A = 0.f;
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
-        const unsigned c = d.fcode[i];
+        const unsigned c = __ldg(d.fcode + i);
         float2 F = make_float2(0.f, 0.f);
         if (c != 0) {
             float mag;
@@ -426,27 +553,6 @@ __device__ void mixed_finish(const NetDev &d, const Team &tm) {
     }
 }
 
-/* The anchor must move when the FP32 rounding of the difference sum,
- * about kErr * max_i sum_b |df_b|, is no longer small against the force the
- * run still has to resolve (the larger of max|F| and half the stop
- * threshold), or when max|F| has dropped far below the anchor force. */
-constexpr double kErr = 2.0e-7;
-__device__ __forceinline__ bool need_anchor(const Scal &s, const FireParamsDev &p, double M2, double Amax,
-                                            double M2_anchor) {
-    const double f = fmax(sqrt(M2), 0.5 * p.fcut);
-    return s.converged || s.done || kErr * Amax > 0.1 * f ||
-           M2 < (double)kAnchorF * (double)kAnchorF * M2_anchor;
-}
-
-/* After an anchor: the FP64 force decides convergence. */
-__device__ __forceinline__ void certify(Scal &s, const FireParamsDev &p, double F2, double M2, double sqrt_dof) {
-    s.fmag = sqrt(F2);
-    s.maxf = sqrt(M2);
-    s.converged = crit_met(p, s.fmag, s.maxf, sqrt_dof);
-    if (!isfinite(s.fmag)) s.status = NR_ERR_NONFINITE;
-    s.done = s.converged || s.step >= p.max_steps || s.status != 0;
-}
-
 /* ------------------------------------------------------------------ */
 /* One CTA per network (batched)                                        */
 /* ------------------------------------------------------------------ */
@@ -474,15 +580,16 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
         u.lo[i] = make_float2(0.f, 0.f);
         d.vf[i] = make_float2(0.f, 0.f);
     }
-    Scal s; /* meaningful in thread 0 only */
-    int n_anchor = 1;
-    double M2_anchor = 0.0, F2, M2, tF2, tM2;
+    MixScal s; /* meaningful in thread 0 only */
+    MixParams q;
+    double F2, M2, tF2, tM2;
     anchor_eval(d, tm, F2, M2);
     anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
     if (threadIdx.x == 0) {
-        scal_init(s, p, tF2, tM2, d.sqrt_dof);
-        M2_anchor = tM2;
-        coef_from(sh.coef, s, 0);
+        q = mix_params(p, d.sqrt_dof);
+        mix_init(s, q);
+        mix_certify(s, p, d.sqrt_dof, tF2, tM2);
+        sh.coef = coef_of(s, 0);
     }
     __syncthreads();
     for (;;) {
@@ -494,11 +601,12 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
         __syncthreads();
         warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t[5];
-            slots_total(sh.slots, t);
-            scal_step(s, p, t[0], t[1], t[2], t[3], d.sqrt_dof);
-            coef_from(sh.coef, s, need_anchor(s, p, t[3], t[4], M2_anchor));
+        if (threadIdx.x < 32) {
+            const Part t = block_totals(sh.slots);
+            if (threadIdx.x == 0) {
+                mix_step(s, q, t);
+                sh.coef = coef_of(s, need_anchor(s, q, t));
+            }
         }
         __syncthreads();
         if (sh.coef.anchor) {
@@ -507,10 +615,8 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
             anchor_eval(d, tm, F2, M2);
             anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
             if (threadIdx.x == 0) {
-                M2_anchor = tM2;
-                n_anchor++;
-                certify(s, p, tF2, tM2, d.sqrt_dof);
-                coef_from(sh.coef, s, 0);
+                mix_certify(s, p, d.sqrt_dof, tF2, tM2);
+                sh.coef = coef_of(s, 0);
             }
             __syncthreads();
         }
@@ -521,8 +627,7 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
     double es, eb;
     energy_final(d, sh.red, es, eb);
     if (threadIdx.x == 0) {
-        scal_store(d.st, s);
-        d.st->fp64_steps = n_anchor;
+        mix_report(d.st, s);
         d.st->e_stretch = es;
         d.st->e_bend = eb;
     }
@@ -556,18 +661,23 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_batch_mixed(const NetDe
 /* One thread-block cluster per network (batched, multi-SM teams)       */
 /* ------------------------------------------------------------------ */
 
-/* A network relaxed by the C CTAs of one cluster (C SMs): nodes are split
- * over the CTAs (interleaved), u lives in global memory (L2-resident), the
- * hardware cluster barrier orders the passes, and each CTA's partial sums
- * are read by every other CTA through distributed shared memory.  Thread 0
- * of every CTA advances an identical copy of the FP64 FIRE scalars from the
- * same totals taken in the same rank order, so no broadcast is needed. */
-__device__ void cluster_totals(cooperative_groups::cluster_group &cl, double *s_part, int nq, int nsum, double *t) {
+/* A network relaxed by the C CTAs of one cluster (C SMs): nodes and items
+ * are split over the CTAs (interleaved), u lives in global memory
+ * (L2-resident), the hardware cluster barrier orders the passes, and each
+ * CTA's totals are read by every other CTA through distributed shared
+ * memory.  Thread 0 of every CTA advances an identical copy of the FIRE
+ * scalars from the same totals combined in the same order, so no broadcast
+ * is needed. */
+
+/* FP64 anchor totals (sum of F2, max of M2) over the ranks, in rank order. */
+__device__ void anchor_totals(cooperative_groups::cluster_group &cl, double *s_anc, double *t) {
     const int C = (int)cl.num_blocks();
-    for (int q = 0; q < nq; ++q) t[q] = 0.0;
+    t[0] = 0.0;
+    t[1] = 0.0;
     for (int r = 0; r < C; ++r) {
-        const double *rp = cl.map_shared_rank(s_part, r);
-        for (int q = 0; q < nq; ++q) t[q] = q < nsum ? t[q] + rp[q] : fmax(t[q], rp[q]);
+        const double *rp = cl.map_shared_rank(s_anc, r);
+        t[0] = t[0] + rp[0];
+        t[1] = fmax(t[1], rp[1]);
     }
 }
 
@@ -579,7 +689,8 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
     __shared__ MixShared sh;
     __shared__ NetDev s_d;
     __shared__ int s_slot;
-    __shared__ double s_part[5];
+    __shared__ Part s_part;   /* this CTA's step totals */
+    __shared__ double s_anc[2]; /* this CTA's FP64 anchor totals */
     const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
     for (;;) {
         if (rank == 0 && threadIdx.x == 0) s_slot = atomicAdd(queue, 1);
@@ -600,22 +711,23 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
             u.lo[i] = make_float2(0.f, 0.f);
             d.vf[i] = make_float2(0.f, 0.f);
         }
-        Scal s; /* replicated in thread 0 of every CTA */
-        int n_anchor = 1;
-        double M2_anchor = 0.0, F2, M2, tF2, tM2;
+        MixScal s; /* replicated in thread 0 of every CTA */
+        MixParams q;
+        double F2, M2, tF2, tM2;
         anchor_eval(d, tm, F2, M2);
         anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
         if (threadIdx.x == 0) {
-            s_part[0] = tF2;
-            s_part[1] = tM2;
+            s_anc[0] = tF2;
+            s_anc[1] = tM2;
         }
         cl.sync();
         if (threadIdx.x == 0) {
             double t[2];
-            cluster_totals(cl, s_part, 2, 1, t);
-            scal_init(s, p, t[0], t[1], d.sqrt_dof);
-            M2_anchor = t[1];
-            coef_from(sh.coef, s, 0);
+            anchor_totals(cl, s_anc, t);
+            q = mix_params(p, d.sqrt_dof);
+            mix_init(s, q);
+            mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
+            sh.coef = coef_of(s, 0);
         }
         __syncthreads();
         for (;;) {
@@ -627,17 +739,20 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
             cl.sync();
             warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
             __syncthreads();
-            if (threadIdx.x == 0) {
-                double t[5];
-                slots_total(sh.slots, t);
-                for (int q = 0; q < 5; ++q) s_part[q] = t[q];
+            if (threadIdx.x < 32) {
+                const Part t = block_totals(sh.slots);
+                if (threadIdx.x == 0) s_part = t;
             }
             cl.sync();
-            if (threadIdx.x == 0) {
-                double t[5];
-                cluster_totals(cl, s_part, 5, 3, t);
-                scal_step(s, p, t[0], t[1], t[2], t[3], d.sqrt_dof);
-                coef_from(sh.coef, s, need_anchor(s, p, t[3], t[4], M2_anchor));
+            if (threadIdx.x < 32) {
+                /* lane r takes rank r's totals: the same butterfly in every CTA */
+                Part t{0.f, 0.f, 0.f, 0.f, 0.f};
+                if ((int)threadIdx.x < C) t = *cl.map_shared_rank(&s_part, (int)threadIdx.x);
+                t = warp_reduce(t);
+                if (threadIdx.x == 0) {
+                    mix_step(s, q, t);
+                    sh.coef = coef_of(s, need_anchor(s, q, t));
+                }
             }
             __syncthreads();
             if (sh.coef.anchor) {
@@ -646,17 +761,15 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
                 anchor_eval(d, tm, F2, M2);
                 anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
                 if (threadIdx.x == 0) {
-                    s_part[0] = tF2;
-                    s_part[1] = tM2;
+                    s_anc[0] = tF2;
+                    s_anc[1] = tM2;
                 }
                 cl.sync();
                 if (threadIdx.x == 0) {
                     double t[2];
-                    cluster_totals(cl, s_part, 2, 1, t);
-                    M2_anchor = t[1];
-                    n_anchor++;
-                    certify(s, p, t[0], t[1], d.sqrt_dof);
-                    coef_from(sh.coef, s, 0);
+                    anchor_totals(cl, s_anc, t);
+                    mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
+                    sh.coef = coef_of(s, 0);
                 }
                 __syncthreads();
             }
@@ -668,8 +781,7 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
             double es, eb;
             energy_final(d, sh.red, es, eb);
             if (threadIdx.x == 0) {
-                scal_store(d.st, s);
-                d.st->fp64_steps = n_anchor;
+                mix_report(d.st, s);
                 d.st->e_stretch = es;
                 d.st->e_bend = eb;
             }
@@ -749,17 +861,32 @@ cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes
 /* One network over the whole GPU (cooperative team of CTAs)            */
 /* ------------------------------------------------------------------ */
 
-/* Combines the CTA partials part[q * G + c] (q < nq) of all G CTAs in CTA
- * order: sums for q < nsum, maxima after.  Called by the last-arriving CTA. */
-__device__ void team_totals(const double *part, int G, int nq, int nsum, double *out) {
-    for (int q = 0; q < nq; ++q) {
-        double acc = q < nsum ? 0.0 : 0.0;
-        for (int c = 0; c < G; ++c) {
-            const double v = __ldcg(part + (size_t)q * G + c);
-            acc = q < nsum ? acc + v : fmax(acc, v);
-        }
-        out[q] = acc;
+/* Combines the FP64 CTA partials part[q * G + c] (q < 2: sum, then max) of
+ * all G CTAs in CTA order.  Called by one thread of the last-arriving CTA. */
+__device__ void anchor_team_totals(const double *part, int G, double *out) {
+    double s = 0.0, m = 0.0;
+    for (int c = 0; c < G; ++c) {
+        s = s + __ldcg(part + c);
+        m = fmax(m, __ldcg(part + G + c));
     }
+    out[0] = s;
+    out[1] = m;
+}
+
+/* Step totals of the G CTAs' FP32 totals fpart[q * G + c], by warp 0 of the
+ * last-arriving CTA: lane l accumulates CTAs l, l + 32, ... in order, then
+ * the butterfly combines the lanes. */
+__device__ __forceinline__ Part team_step_totals(const float *fpart, int G) {
+    const int lane = threadIdx.x & 31;
+    Part t{0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c = lane; c < G; c += 32) {
+        t.P += __ldcg(fpart + c);
+        t.V2 += __ldcg(fpart + G + c);
+        t.F2 += __ldcg(fpart + 2 * G + c);
+        t.M2 = fmaxf(t.M2, __ldcg(fpart + 3 * G + c));
+        t.A = fmaxf(t.A, __ldcg(fpart + 4 * G + c));
+    }
+    return warp_reduce(t);
 }
 
 __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, FireParamsDev p,
@@ -769,8 +896,11 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
     const unsigned G = gridDim.x;
     FireState *st = d.st;
     const UView u{d.u_hi, d.u_lo};
+    /* d.part: FP64 anchor partials in [0, 2G), FP32 step totals after them */
+    float *fpart = reinterpret_cast<float *>(d.part + 2 * (size_t)G);
     bool last;
-    Scal s; /* meaningful in thread 0 only */
+    MixParams q; /* thread 0 of the last-arriving CTA uses it */
+    if (threadIdx.x == 0) q = mix_params(p, d.sqrt_dof);
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         u.hi[i] = make_float2(0.f, 0.f);
         u.lo[i] = make_float2(0.f, 0.f);
@@ -787,20 +917,17 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
     if (last) {
         if (threadIdx.x == 0) {
             double t[2];
-            team_totals(d.part, G, 2, 1, t);
-            scal_init(s, p, t[0], t[1], d.sqrt_dof);
-            scal_store(st, s);
-            st->m2_anchor = t[1];
-            st->fp64_steps = 1;
+            anchor_team_totals(d.part, G, t);
+            MixScal s;
+            mix_init(s, q);
+            mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
+            st->mix = s;
             st->anchor_now = 0;
         }
         barrier_release(st);
     }
     for (;;) {
-        if (threadIdx.x == 0) {
-            scal_load(s, st);
-            coef_from(sh.coef, s, 0);
-        }
+        if (threadIdx.x == 0) sh.coef = coef_of(mix_load(st), 0);
         __syncthreads();
         const Coef c = sh.coef;
         mixed_pass_a(d, tm, c, u);
@@ -812,21 +939,26 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
         if (last) barrier_release(st);
         warp_part(mixed_pass_b(d, tm, c.dtm), sh.slots);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t[5];
-            slots_total(sh.slots, t);
-            for (int q = 0; q < 5; ++q) d.part[(size_t)q * G + blockIdx.x] = t[q];
+        if (threadIdx.x < 32) {
+            const Part t = block_totals(sh.slots);
+            if (threadIdx.x == 0) {
+                fpart[blockIdx.x] = t.P;
+                fpart[G + blockIdx.x] = t.V2;
+                fpart[2 * G + blockIdx.x] = t.F2;
+                fpart[3 * G + blockIdx.x] = t.M2;
+                fpart[4 * G + blockIdx.x] = t.A;
+            }
         }
         if (!barrier_arrive(st, G, budget_ns, last, 13)) return;
         if (last) {
-            if (threadIdx.x == 0) {
-                double t[5];
-                team_totals(d.part, G, 5, 3, t);
-                scal_step(s, p, t[0], t[1], t[2], t[3], d.sqrt_dof);
-                const volatile FireState *vs = st;
-                const double m2a = vs->m2_anchor;
-                scal_store(st, s);
-                st->anchor_now = need_anchor(s, p, t[3], t[4], m2a);
+            if (threadIdx.x < 32) {
+                const Part t = team_step_totals(fpart, G);
+                if (threadIdx.x == 0) {
+                    MixScal s = mix_load(st);
+                    mix_step(s, q, t);
+                    st->anchor_now = need_anchor(s, q, t);
+                    st->mix = s;
+                }
             }
             barrier_release(st);
         }
@@ -849,12 +981,10 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
             if (last) {
                 if (threadIdx.x == 0) {
                     double t[2];
-                    team_totals(d.part, G, 2, 1, t);
-                    scal_load(s, st);
-                    certify(s, p, t[0], t[1], d.sqrt_dof);
-                    scal_store(st, s);
-                    st->m2_anchor = t[1];
-                    st->fp64_steps = st->fp64_steps + 1;
+                    anchor_team_totals(d.part, G, t);
+                    MixScal s = mix_load(st);
+                    mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
+                    st->mix = s;
                     st->anchor_now = 0;
                 }
                 barrier_release(st);
@@ -862,6 +992,7 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_grid_mixed(NetDev d, Fi
         }
     }
     mixed_finish(d, tm);
+    if (blockIdx.x == 0 && threadIdx.x == 0) mix_report(st, mix_load(st));
 }
 
 int mixed_grid_blocks(int n) {

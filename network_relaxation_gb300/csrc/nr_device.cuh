@@ -37,6 +37,17 @@ struct FireParamsDev {
     int nmin, max_steps, criterion, precision;
 };
 
+/* FIRE scalars of the mixed-precision path (fire_mixed.cu): the per-step
+ * update runs in FP32, |F| and max|F| are the FP64 values certified at the
+ * last anchor. */
+struct MixScal {
+    float dt, dtm, dtsq, alpha, na, a; /* na, a: mixing pending for the next pass A */
+    float m2_anchor;                   /* max|F|^2 at the current anchor */
+    float pad0;
+    int since, step, mix_pending, zero_v, done, converged, status, n_anchor;
+    double fmag, maxf;
+};
+
 /* Per-network FIRE state, written by one CTA after each reduction and read by
  * all CTAs of the network.  The barrier words sit on their own 128-byte line. */
 struct __align__(128) FireState {
@@ -46,9 +57,9 @@ struct __align__(128) FireState {
     double e_stretch, e_bend;
     int mix_pending, zero_v, since, step;
     int done, converged, status, fp64_steps;
-    double m2_anchor; /* mixed precision: max|F|^2 at the current anchor */
-    int anchor_now;   /* mixed precision: the team re-anchors before the next pass */
-    int pad[5];
+    MixScal mix;    /* mixed precision, multi-CTA teams */
+    int anchor_now; /* mixed precision: the team re-anchors before the next pass */
+    int pad[11];
     unsigned int bar_count, bar_gen, abort_flag, timeout_site;
     unsigned int pad2[28];
 };
