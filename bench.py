@@ -17,7 +17,8 @@ Also reported in the same JSON line:
                 H2D of the start positions from pinned memory, relaxation,
                 D2H of the relaxed positions and of the per-network reports
   roofline      the batch kernel's algorithmic bytes / its event-timed
-                duration vs the measured HBM copy bandwidth
+                duration vs the measured HBM copy bandwidth; traffic = DRAM
+                bytes per launch from the committed ncu summary
   fp64          plain FP64 path, network by network (grid kernel), on a
                 stratified sample, extrapolated by FP64 work to the batch
   cpu_baseline  the CPU oracle (FP64 restatement of run_fire_md) on all host
@@ -70,6 +71,34 @@ def mixed_bytes_per_launch(reps, hosts):
         i = h.info()
         total += r.steps * (73.0 * i.n_points + 24.0 * i.n_edges + 12.0 * i.n_triples)
     return total
+
+
+def batch_kernel(precision, max_nodes):
+    """Name of the kernel nr_batch_relax launches, by the library's policy:
+    mixed precision runs one thread-block cluster of C CTAs per network, C
+    the smallest power of two (at most 8) leaving at most 2304 nodes per CTA
+    (NR_CLUSTER overrides), and C = 1 runs one CTA per network."""
+    if precision != "mixed":
+        return "k_fire_batch", 1
+    env = os.environ.get("NR_CLUSTER")
+    c = max(1, min(16, int(env))) if env else 1
+    if not env:
+        while c < 8 and c * 2304 < max_nodes:
+            c *= 2
+    return ("k_fire_cluster_mixed" if c > 1 else "k_fire_batch_mixed"), c
+
+
+def committed_traffic(kernel):
+    """DRAM bytes per launch of `kernel` on this workload from the committed
+    ncu summary (profiles/c4_<kernel>_dram.txt, a line 'bytes_per_launch: X'),
+    or None."""
+    path = os.path.join(ROOT, "profiles", "c4_%s_dram.txt" % kernel)
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("bytes_per_launch:"):
+            return float(ln.split(":", 1)[1])
+    return None
 
 
 def fp64_bytes_per_launch(reps, hosts):
@@ -316,6 +345,8 @@ def main():
     peak_kind = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
     bytes_launch = (mixed_bytes_per_launch if args.precision == "mixed" else fp64_bytes_per_launch)(reps, hosts)
+    kname, kcl = batch_kernel(args.precision, max(h.n_points for h in hosts))
+    traffic = committed_traffic(kname)
     kern_ms = float(np.mean(kernel_ms))
     achieved = bytes_launch / (kern_ms / 1e3) / 1e9
     c4 = load_c4_oracle() if rank == 0 else None
@@ -340,8 +371,8 @@ def main():
             "all_converged": all(s == 0 for s in status),
             "fp64_anchor_evals_median": float(np.median([r.fp64_steps for r in reps])),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "peak_source": peak_kind,
-                         "kernel": "k_fire_batch_mixed" if args.precision == "mixed" else "k_fire_batch"},
+                         "traffic": traffic, "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
+                         "kernel": kname, "cluster_ctas": kcl},
             "clocks": clk,
             "wall_s_timed_region": wall,
         }

@@ -335,7 +335,7 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     if (prm.precision == NR_MIXED) {
         const char *env = getenv("NR_CLUSTER");
-        const int cluster = env ? std::max(1, std::min(8, atoi(env))) : mixed_cluster_size(S.max_nodes);
+        const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
         if (cluster > 1)
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
         else

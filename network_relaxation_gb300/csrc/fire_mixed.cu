@@ -57,7 +57,7 @@
 namespace nr {
 
 constexpr float kAnchorF = 1.0e-4f;
-constexpr int kMixThreads = 512;
+constexpr int kMixThreads = 512; /* grid kernel; batch and cluster kernels: 512 or 1024 */
 
 /* Double-float helpers (Knuth two-sum). */
 __device__ __forceinline__ void df_add(float &hi, float &lo, float x) {
@@ -449,7 +449,7 @@ __device__ void anchor_move(const NetDev &d, const Team &tm, const UView &u) {
 /* Anchor step 2 (after a team sync): the FP32 anchor record of every bond
  * and triple from FP64 geometry, the FP64 forces into f and the
  * double-float anchor force, ff = F; CTA partials of |F|^2 and max|F|^2. */
-__device__ void anchor_eval(const NetDev &d, const Team &tm, double &F2, double &M2) {
+__device__ __noinline__ void anchor_eval(const NetDev &d, const Team &tm, double &F2, double &M2) {
     const double W = d.width;
     F2 = 0.0;
     M2 = 0.0;
@@ -564,6 +564,19 @@ struct MixShared {
     Coef coef;
 };
 
+/* Canonical FP64 energies of the network into st (one CTA).  Kept out of
+ * line, like anchor_eval: the FP64 code's register demand stays out of the
+ * FP32 loop. */
+__device__ __noinline__ void mixed_energies(const NetDev &d, double *s_red) {
+    energy_tiles(d, 0, 1, s_red);
+    double es, eb;
+    energy_final(d, s_red, es, eb);
+    if (threadIdx.x == 0) {
+        d.st->e_stretch = es;
+        d.st->e_bend = eb;
+    }
+}
+
 __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p, float2 *s_u, int smem_nodes,
                                         MixShared &sh) {
     const Team tm{0, 1};
@@ -623,19 +636,14 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
     }
     mixed_finish(d, tm);
     __syncthreads();
-    energy_tiles(d, 0, 1, sh.red);
-    double es, eb;
-    energy_final(d, sh.red, es, eb);
-    if (threadIdx.x == 0) {
-        mix_report(d.st, s);
-        d.st->e_stretch = es;
-        d.st->e_bend = eb;
-    }
+    mixed_energies(d, sh.red);
+    if (threadIdx.x == 0) mix_report(d.st, s);
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kMixThreads, 1) k_fire_batch_mixed(const NetDev *nets, int n_nets, FireParamsDev p,
-                                                                     int *queue, const int *order, int smem_nodes) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_fire_batch_mixed(const NetDev *nets, int n_nets, FireParamsDev p,
+                                                            int *queue, const int *order, int smem_nodes) {
     extern __shared__ float2 s_u[];
     __shared__ MixShared sh;
     __shared__ int s_net;
@@ -681,9 +689,9 @@ __device__ void anchor_totals(cooperative_groups::cluster_group &cl, double *s_a
     }
 }
 
-__global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const NetDev *nets, int n_nets,
-                                                                       FireParamsDev p, int *queue,
-                                                                       const int *order) {
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets, int n_nets, FireParamsDev p,
+                                                              int *queue, const int *order) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     __shared__ MixShared sh;
@@ -777,55 +785,71 @@ __global__ void __launch_bounds__(kMixThreads, 1) k_fire_cluster_mixed(const Net
         mixed_finish(d, tm);
         cl.sync();
         if (rank == 0) {
-            energy_tiles(d, 0, 1, sh.red);
-            double es, eb;
-            energy_final(d, sh.red, es, eb);
-            if (threadIdx.x == 0) {
-                mix_report(d.st, s);
-                d.st->e_stretch = es;
-                d.st->e_bend = eb;
-            }
+            mixed_energies(d, sh.red);
+            if (threadIdx.x == 0) mix_report(d.st, s);
         }
         cl.sync();
     }
 }
 
-/* CTAs per network for a batch: enough that the largest network has about
- * kNodesPerCta nodes per CTA, a power of two up to the portable cluster
- * size 8. */
-constexpr int kNodesPerCta = 1536;
+/* CTAs per network for a batch: enough that the largest network has at
+ * most kNodesPerCta nodes per CTA, a power of two up to the portable
+ * cluster size 8. */
+constexpr int kNodesPerCta = 2304;
 int mixed_cluster_size(int max_nodes) {
     int c = 1;
     while (c < 8 && c * kNodesPerCta < max_nodes) c *= 2;
     return c;
 }
 
-cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
-                                 int *queue_dev, const int *order_dev, cudaStream_t stream) {
+/* Threads per CTA of the batch and cluster kernels: NR_MIX_THREADS (512 or
+ * 1024), default 1024.  A step is a chain of dependent passes, so more
+ * warps per SM hide more of its latency: 1024 threads (64 registers, the
+ * FP64 anchor code out of line) ran C4-sized networks 1.3-1.6x faster per
+ * step than 512. */
+static int mixed_threads() {
+    const char *env = getenv("NR_MIX_THREADS");
+    return env && atoi(env) == 512 ? 512 : 1024;
+}
+
+template <int NT>
+static cudaError_t launch_cluster_nt(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
+                                     int *queue_dev, const int *order_dev, cudaStream_t stream) {
     cudaError_t e;
     int dev, sms;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if (cluster > 8 &&
+        (e = cudaFuncSetAttribute(k_fire_cluster_mixed<NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) !=
+            cudaSuccess)
+        return e;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(kMixThreads);
+    cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3((sms / cluster) * cluster);
     int max_clusters = 0;
-    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, (void *)k_fire_cluster_mixed, &cfg)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, (void *)k_fire_cluster_mixed<NT>, &cfg)) != cudaSuccess)
         return e;
     if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
     const int clusters = std::max(1, std::min(n_nets, max_clusters));
     cfg.gridDim = dim3(clusters * cluster);
     if ((e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream)) != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_fire_cluster_mixed, nets_dev, n_nets, p, queue_dev, order_dev);
+    return cudaLaunchKernelEx(&cfg, k_fire_cluster_mixed<NT>, nets_dev, n_nets, p, queue_dev, order_dev);
+}
+
+cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
+                                 int *queue_dev, const int *order_dev, cudaStream_t stream) {
+    return mixed_threads() == 1024
+               ? launch_cluster_nt<1024>(nets_dev, n_nets, cluster, p, queue_dev, order_dev, stream)
+               : launch_cluster_nt<512>(nets_dev, n_nets, cluster, p, queue_dev, order_dev, stream);
 }
 
 /* Shared memory for u: the largest network of the batch, capped so one CTA
@@ -839,22 +863,30 @@ static int mixed_smem_nodes(int max_nodes) {
     return max_nodes < cap ? max_nodes : cap;
 }
 
-cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
-                               int *queue_dev, const int *order_dev, cudaStream_t stream) {
+template <int NT>
+static cudaError_t launch_batch_nt(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
+                                   int *queue_dev, const int *order_dev, cudaStream_t stream) {
     const int smem_nodes = mixed_smem_nodes(max_nodes);
     const size_t smem = (size_t)smem_nodes * 16;
-    cudaError_t e = cudaFuncSetAttribute(k_fire_batch_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_fire_batch_mixed<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int dev, sms, per_sm = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_batch_mixed, kMixThreads, smem)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_batch_mixed<NT>, NT, smem)) !=
         cudaSuccess)
         return e;
     const int blocks = std::max(1, std::min(n_nets, std::max(1, per_sm) * sms));
     if ((e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream)) != cudaSuccess) return e;
-    k_fire_batch_mixed<<<blocks, kMixThreads, smem, stream>>>(nets_dev, n_nets, p, queue_dev, order_dev, smem_nodes);
+    k_fire_batch_mixed<NT><<<blocks, NT, smem, stream>>>(nets_dev, n_nets, p, queue_dev, order_dev, smem_nodes);
     return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
+                               int *queue_dev, const int *order_dev, cudaStream_t stream) {
+    return mixed_threads() == 1024 ? launch_batch_nt<1024>(nets_dev, n_nets, max_nodes, p, queue_dev, order_dev, stream)
+                                   : launch_batch_nt<512>(nets_dev, n_nets, max_nodes, p, queue_dev, order_dev, stream);
 }
 
 /* ------------------------------------------------------------------ */
