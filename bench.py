@@ -49,6 +49,11 @@ METRIC = "relaxed networks/s to max|F|<1e-10 (512-network uneven batch)"
 UNIT = "networks/s"
 
 
+def dptr(t):
+    """double* of a torch tensor's storage (host or device)."""
+    return C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+
+
 def fire_params(nr, precision):
     return nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=0.1, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
                           max_steps=10_000_000, criterion="max", precision=precision)
@@ -277,7 +282,7 @@ def main():
     start_dev = torch.empty((n_nodes, 2), dtype=torch.float64, device="cuda")
     check = nr._capi.check
     lib = nr.lib()
-    check(lib.nr_batch_get_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "snapshot")
+    check(lib.nr_batch_get_positions(batch._h, dptr(start_dev), C.c_void_p(sp)), "snapshot")
     start_host = torch.empty((n_nodes, 2), dtype=torch.float64, pin_memory=True)
     start_host.copy_(start_dev)
     out_host = torch.empty_like(start_host).pin_memory()
@@ -285,7 +290,7 @@ def main():
     reps_arr = (nr.Report * batch.n)()
 
     def step_device():
-        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "reset")
+        check(lib.nr_batch_set_positions(batch._h, dptr(start_dev), C.c_void_p(sp)), "reset")
         return lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp))
 
     def barrier():
@@ -305,7 +310,7 @@ def main():
     ev0.record(stream)
     for _ in range(args.steps):
         k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_dev.data_ptr()), C.c_void_p(sp)), "reset")
+        check(lib.nr_batch_set_positions(batch._h, dptr(start_dev), C.c_void_p(sp)), "reset")
         k0.record(stream)
         check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
         k1.record(stream)
@@ -325,9 +330,9 @@ def main():
     for _ in range(e2e_steps):
         barrier()
         t = time.perf_counter()
-        check(lib.nr_batch_set_positions(batch._h, C.c_void_p(start_host.data_ptr()), C.c_void_p(sp)), "h2d")
+        check(lib.nr_batch_set_positions(batch._h, dptr(start_host), C.c_void_p(sp)), "h2d")
         check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
-        check(lib.nr_batch_get_positions(batch._h, C.c_void_p(out_host.data_ptr()), C.c_void_p(sp)), "d2h")
+        check(lib.nr_batch_get_positions(batch._h, dptr(out_host), C.c_void_p(sp)), "d2h")
         e2e_ms.append(1e3 * (time.perf_counter() - t))
         if not all(reps_arr[i].status == 0 for i in range(batch.n)):
             raise RuntimeError("end-to-end step: a network did not converge")
