@@ -227,6 +227,40 @@ int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double k
                    int max_steps, int nmin, double report_data[3], int *step_count, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Energies without allocating                                         */
+/* ------------------------------------------------------------------ */
+
+/* No counterpart in the reference: its energy step cudaMallocs a per-bond
+ * and a per-triple array for every call (large_strain_relax.cu:738-758).
+ *
+ * Stretch and bend energies of a network held in the reference's device
+ * layout (the arrays nr_run_fire_md takes; wrap codes as signed chars), with
+ * the canonical FP64 sums of nr_energies (bit-identical results), for
+ * callers that cannot allocate device memory: a host framework that hands
+ * out all device memory from its own pool and forbids other allocations, or
+ * a loop that must not pay for cudaMalloc / cudaFree, which can synchronize
+ * the whole device.  It allocates nothing.  Its only scratch, the per-tile
+ * partial sums, is a fixed array in the library's device memory: 2 x
+ * NR_NOALLOC_MAX_ITEMS / 256 doubles (256 KiB), held on every GPU that
+ * loads the library until the process exits.
+ *
+ * d_energies: device pointer to 2 doubles; receives {E_stretch, E_bend}
+ * (a term is 0 when its stiffness is not positive).  npairs or ntriples
+ * above NR_NOALLOC_MAX_ITEMS is rejected with NR_ERR_CAPACITY and a message
+ * in nr_last_error.  A node index outside [0, n_points) makes the energy
+ * NaN.  The first call on each device looks up the scratch array's device
+ * address (this can load the library's device code): make that first call
+ * before any stream capture.  Every call uses the same scratch array, so
+ * calls that overlap on the GPU (other streams or host threads) race: the
+ * caller must order them.  Nothing in the array needs clearing between
+ * calls.  Asynchronous on `stream`. */
+#define NR_NOALLOC_MAX_ITEMS 4194304
+int nr_energies_noalloc(int n_points, int npairs, int ntriples, double width, double ks, double kb,
+                        const double *d_pos, const int *d_pair_list, const double *d_lengths,
+                        const signed char *d_e_offsets, const int *d_triples, const signed char *d_t_offsets,
+                        double *d_energies, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Batched relaxation of many independent networks in one launch       */
 /* ------------------------------------------------------------------ */
 

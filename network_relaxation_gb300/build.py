@@ -30,6 +30,7 @@ CUDA_UNITS = [
     ("fire_fp64.cu", ["--fmad=false"]),
     ("fire_mixed.cu", ["--fmad=false"]),
     ("api.cu", []),
+    ("noalloc.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["host_network.cpp", "generators.cpp", "driver.cpp"]
 
