@@ -249,7 +249,14 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work per CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--largest", type=int, default=0,
+                    help="profiling case: only the K largest networks of the batch (not a bench line)")
+    ap.add_argument("--max-steps", type=int, default=10_000_000,
+                    help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
+    profiling_case = args.largest > 0 or args.max_steps != 10_000_000
+    if profiling_case:
+        args.no_cpu = args.no_fp64 = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -273,6 +280,8 @@ def main():
     sp = stream.cuda_stream
 
     prm_list = sharding.rank_c4_params(rank)
+    if args.largest > 0:
+        prm_list = sorted(prm_list, key=lambda q: -q["L"])[:args.largest]
     hosts = workloads.c4_networks(prm_list)
     kappa = np.array([q["kappa"] for q in prm_list])
     gamma = np.array([q["gamma"] for q in prm_list])
@@ -287,6 +296,7 @@ def main():
     start_host.copy_(start_dev)
     out_host = torch.empty_like(start_host).pin_memory()
     prm = fire_params(nr, args.precision)
+    prm.max_steps = args.max_steps
     reps_arr = (nr.Report * batch.n)()
 
     def step_device():
@@ -334,7 +344,7 @@ def main():
         check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
         check(lib.nr_batch_get_positions(batch._h, dptr(out_host), C.c_void_p(sp)), "d2h")
         e2e_ms.append(1e3 * (time.perf_counter() - t))
-        if not all(reps_arr[i].status == 0 for i in range(batch.n)):
+        if not profiling_case and not all(reps_arr[i].status == 0 for i in range(batch.n)):
             raise RuntimeError("end-to-end step: a network did not converge")
     e2e_step_ms, _ = sharding.reduce_timing(dist, float(np.mean(e2e_ms)), batch.n, device="cuda")
     h2d = n_nodes * 16
@@ -354,7 +364,7 @@ def main():
     traffic = committed_traffic(kname)
     kern_ms = float(np.mean(kernel_ms))
     achieved = bytes_launch / (kern_ms / 1e3) / 1e9
-    c4 = load_c4_oracle() if rank == 0 else None
+    c4 = load_c4_oracle() if rank == 0 and not profiling_case else None
     line = None
     if rank == 0:
         node_iters = float(sum(r.steps * h.n_points for r, h in zip(reps, hosts)))
@@ -370,6 +380,7 @@ def main():
             "e2e": {"value": total_nets / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps, "ms_per_step": e2e_step_ms},
             "gpu_launches": args.steps,
+            "profiling_case": ({"largest": args.largest, "max_steps": args.max_steps} if profiling_case else None),
             "node_iter_per_s": world * node_iters / (ms / 1e3),
             "iterations": {"p50": float(np.median(steps)), "p99": float(np.percentile(steps, 99)),
                            "max": int(steps.max())},
