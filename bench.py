@@ -82,7 +82,9 @@ def batch_kernel(precision, max_nodes):
     """Name of the kernel nr_batch_relax launches, by the library's policy:
     mixed precision runs one thread-block cluster of C CTAs per network, C
     the smallest power of two (at most 8) leaving at most 2304 nodes per CTA
-    (NR_CLUSTER overrides), and C = 1 runs one CTA per network."""
+    (NR_CLUSTER overrides), with the step's state in distributed shared
+    memory (k_fire_dsm_mixed, when it fits; C4 does) or, with
+    NR_MIX_KERNEL=l2, in global memory."""
     if precision != "mixed":
         return "k_fire_batch", 1
     env = os.environ.get("NR_CLUSTER")
@@ -90,6 +92,8 @@ def batch_kernel(precision, max_nodes):
     if not env:
         while c < 8 and c * 2304 < max_nodes:
             c *= 2
+    if os.environ.get("NR_MIX_KERNEL") != "l2":
+        return "k_fire_dsm_mixed", c
     return ("k_fire_cluster_mixed" if c > 1 else "k_fire_batch_mixed"), c
 
 

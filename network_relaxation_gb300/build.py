@@ -29,6 +29,7 @@ CXX = os.environ.get("CXX", "g++")
 CUDA_UNITS = [
     ("fire_fp64.cu", ["--fmad=false"]),
     ("fire_mixed.cu", ["--fmad=false"]),
+    ("fire_dsm.cu", ["--fmad=false"]),
     ("api.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
 ]

@@ -54,6 +54,7 @@ struct Image {
 
 struct NetOff {
     size_t mb_data, mb_sk, bdf, mt_arms, mt_pk, tdf, bfrc, tfrc;
+    size_t dsm_bref, dsm_bidx, dsm_tref, dsm_bent, dsm_tent;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
 };
@@ -76,10 +77,72 @@ struct DeviceSet {
     float2 *fa_hi_all = nullptr, *fa_lo_all = nullptr;
     int max_nodes = 0;
     int *order = nullptr; /* networks by decreasing size (largest start first) */
+    /* sub-block layouts for the distributed-shared-memory kernel (host copy
+     * for sizing, device array for the kernel); dsm_ok: every network has one */
+    std::vector<NetDsm> dsm;
+    NetDsm *dsm_array = nullptr;
+    bool dsm_ok = true;
     ~DeviceSet() {
         if (arena) cudaFree(arena);
     }
 };
+
+/* Sub-block layout of one network for the distributed-shared-memory kernel
+ * (NetDsm, nr_device.cuh): item slots grouped by the sub-block of the
+ * bond's node i / the triple's hinge, in index order within a group; node
+ * references and resolved incidence entries.  m.bsub = 0 when the network
+ * is too large for the encoding (more than 2^20 nodes). */
+static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Image &img, NetOff &o, NetDsm &m) {
+    const int n = h.n_points, ne = h.n_edges(), nt = h.n_triples();
+    memset(&m, 0, sizeof(m));
+    const int bsub = (n + kDsmParts - 1) / kDsmParts;
+    const bool fits = n <= (1 << 20) && bsub <= 0xffff;
+    auto part = [&](int v) { return v / bsub; };
+    auto ref = [&](int v) { return (part(v) << 16) | (v % bsub); };
+    std::vector<int2> bref(fits ? ne : 0);
+    std::vector<int> bidx(fits ? ne : 0), bslot(fits ? ne : 0), dbent(fits ? inc.bent.size() : 0);
+    std::vector<int4> tref(fits ? nt : 0);
+    std::vector<int> tslot(fits ? nt : 0), dtent(fits ? inc.tent.size() : 0);
+    if (fits) {
+        int cnt[kDsmParts + 1] = {0};
+        for (int b = 0; b < ne; ++b) cnt[part(h.edge_ij[2 * b]) + 1]++;
+        for (int g = 0; g < kDsmParts; ++g) cnt[g + 1] += cnt[g];
+        for (int g = 0; g <= kDsmParts; ++g) m.bo[g] = cnt[g];
+        for (int b = 0; b < ne; ++b) {
+            const int i = h.edge_ij[2 * b], j = h.edge_ij[2 * b + 1];
+            const int sl = cnt[part(i)]++;
+            bslot[b] = sl;
+            bref[sl] = make_int2(ref(i), ref(j));
+            bidx[sl] = b;
+        }
+        int tc[kDsmParts + 1] = {0};
+        for (int t = 0; t < nt; ++t) tc[part(h.tri_hjk[3 * t]) + 1]++;
+        for (int g = 0; g < kDsmParts; ++g) tc[g + 1] += tc[g];
+        for (int g = 0; g <= kDsmParts; ++g) m.to[g] = tc[g];
+        for (int t = 0; t < nt; ++t) {
+            const int hh = h.tri_hjk[3 * t], jj = h.tri_hjk[3 * t + 1], kk = h.tri_hjk[3 * t + 2];
+            const int sl = tc[part(hh)]++;
+            tslot[t] = sl;
+            tref[sl] = make_int4(ref(hh), ref(jj), ref(kk), t);
+        }
+        for (size_t e = 0; e < inc.bent.size(); ++e) {
+            const int b = inc.bent[e] >> 1, role = inc.bent[e] & 1;
+            const unsigned g = (unsigned)part(h.edge_ij[2 * b]);
+            dbent[e] = (int)((g << 28) | ((unsigned)bslot[b] << 1) | (unsigned)role);
+        }
+        for (size_t e = 0; e < inc.tent.size(); ++e) {
+            const int t = inc.tent[e] >> 2, role = inc.tent[e] & 3;
+            const unsigned g = (unsigned)part(h.tri_hjk[3 * t]);
+            dtent[e] = (int)((g << 28) | ((unsigned)tslot[t] << 2) | (unsigned)role);
+        }
+        m.bsub = bsub;
+    }
+    o.dsm_bref = img.put(bref.data(), bref.size());
+    o.dsm_bidx = img.put(bidx.data(), bidx.size());
+    o.dsm_tref = img.put(tref.data(), tref.size());
+    o.dsm_bent = img.put(dbent.data(), dbent.size());
+    o.dsm_tent = img.put(dtent.data(), dtent.size());
+}
 
 static int build_set(int n, const nr_host_network *const *nets, const double *ks, const double *kb,
                      const unsigned char *const *fcodes_in, cudaStream_t stream, DeviceSet &S) {
@@ -110,6 +173,8 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     const size_t q_off = img.add(256);
     const size_t aff_off = img.add(sizeof(double4) * n);
     const size_t dev_off = img.add(sizeof(NetDev) * n);
+    const size_t dsm_off = img.add(sizeof(NetDsm) * n);
+    S.dsm.assign(n, NetDsm{});
     std::vector<NetOff> off(n);
     for (int i = 0; i < n; ++i) {
         const nr_host_network &h = *nets[i];
@@ -151,6 +216,8 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.tdf = img.add(sizeof(float4) * (size_t)nt);
         o.bfrc = img.add(sizeof(double2) * (size_t)ne);
         o.tfrc = img.add(sizeof(double4) * (size_t)nt);
+        build_dsm_layout(h, inc, img, o, S.dsm[i]);
+        if (S.dsm[i].bsub <= 0) S.dsm_ok = false;
         S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
         o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
@@ -231,6 +298,17 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.epart = (double *)(base + o.epart);
         d.st = S.st + i;
     }
+    for (int i = 0; i < n; ++i) {
+        const NetOff &o = off[i];
+        NetDsm &m = S.dsm[i];
+        m.bref = (const int2 *)(base + o.dsm_bref);
+        m.bidx = (const int *)(base + o.dsm_bidx);
+        m.tref = (const int4 *)(base + o.dsm_tref);
+        m.bent = (const int *)(base + o.dsm_bent);
+        m.tent = (const int *)(base + o.dsm_tent);
+    }
+    S.dsm_array = (NetDsm *)(base + dsm_off);
+    memcpy(img.bytes.data() + dsm_off, S.dsm.data(), sizeof(NetDsm) * n);
     memcpy(img.bytes.data() + dev_off, S.dev.data(), sizeof(NetDev) * n);
     NR_CUDA_TRY(cudaMemcpyAsync(S.arena, img.bytes.data(), S.arena_bytes, cudaMemcpyHostToDevice, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -331,12 +409,49 @@ static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStrea
     return rep->status;
 }
 
+/* Cluster size and shared-memory maxima for the distributed-shared-memory
+ * kernel: `forced` C if nonzero, else the smallest C >= `least` (a power of
+ * two dividing 16) whose per-CTA state fits.  False when the batch has no
+ * layout, NR_MIX_KERNEL=l2 asks for the global-memory kernels, or nothing
+ * fits. */
+static bool dsm_plan(const DeviceSet &S, int forced, int least, int *C_out, int *bmax, int *emax, int *tmax) {
+    const char *k = getenv("NR_MIX_KERNEL");
+    if (!S.dsm_ok || (k && strcmp(k, "l2") == 0)) return false;
+    const size_t limit = dsm_smem_limit();
+    for (int C = 1; C <= kDsmParts; C *= 2) {
+        if (forced ? C != forced : C < least) continue;
+        const int spr = kDsmParts / C;
+        int bm = 0, em = 0, tm = 0;
+        for (int i = 0; i < S.n_nets; ++i) {
+            const NetDsm &m = S.dsm[i];
+            const NetDev &d = S.dev[i];
+            bm = std::max(bm, spr * m.bsub);
+            for (int r = 0; r < C; ++r) {
+                if (d.use_bonds) em = std::max(em, m.bo[(r + 1) * spr] - m.bo[r * spr]);
+                if (d.use_triples) tm = std::max(tm, m.to[(r + 1) * spr] - m.to[r * spr]);
+            }
+        }
+        if (dsm_smem_bytes(bm, em, tm) <= limit) {
+            *C_out = C;
+            *bmax = bm;
+            *emax = em;
+            *tmax = tm;
+            return true;
+        }
+    }
+    return false;
+}
+
 static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     if (prm.precision == NR_MIXED) {
         const char *env = getenv("NR_CLUSTER");
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
-        if (cluster > 1)
+        int dc = 0, bmax = 0, emax = 0, tmax = 0;
+        if (dsm_plan(S, env ? cluster : 0, cluster, &dc, &bmax, &emax, &tmax))
+            NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, S.n_nets, dc, bmax, emax, tmax, to_dev(prm),
+                                         S.queue, S.order, stream));
+        else if (cluster > 1)
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
         else
             NR_CUDA_TRY(

@@ -1,5 +1,5 @@
-/* Host-side launchers of the FIRE kernels (defined in fire_fp64.cu and
- * fire_mixed.cu). */
+/* Host-side launchers of the FIRE kernels (defined in fire_fp64.cu,
+ * fire_mixed.cu and fire_dsm.cu). */
 #ifndef NR_FIRE_LAUNCH_H
 #define NR_FIRE_LAUNCH_H
 
@@ -27,6 +27,11 @@ cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes
 int mixed_cluster_size(int max_nodes);
 cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
                                  int *queue_dev, const int *order_dev, cudaStream_t stream);
+size_t dsm_smem_bytes(int bmax, int emax, int tmax);
+size_t dsm_smem_limit();
+cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
+                             int emax, int tmax, const FireParamsDev &p, int *queue_dev, const int *order_dev,
+                             cudaStream_t stream);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                               cudaStream_t stream);

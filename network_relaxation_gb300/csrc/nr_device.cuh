@@ -80,6 +80,8 @@ struct NetDev {
      * velocity and force, double-float anchor force; per bond and per triple
      * the FP32 anchor record and the FP32 force change of the current pass */
     float2 *u_hi, *u_lo, *vf, *ff, *fa_hi, *fa_lo;
+    /* anchor records are indexed by bond / triple, or by item slot in the
+     * distributed-shared-memory kernel */
     float4 *mb_data; /* anchor vector i -> j, {hi.x, hi.y, lo.x, lo.y} */
     float2 *mb_sk;   /* {|r_anchor| - l0, k} */
     float4 *mt_arms; /* anchor arms {a.x, a.y, b.x, b.y} (hinge -> j, hinge -> k) */
@@ -91,6 +93,27 @@ struct NetDev {
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
     double *epart;  /* 2 * max(bond tiles, triple tiles) energy partials */
     FireState *st;
+};
+
+/* Layout of a network for the distributed-shared-memory cluster kernel
+ * (fire_dsm.cu).  Nodes are cut into 16 sub-blocks of bsub consecutive
+ * nodes; a cluster of C CTAs gives CTA r the 16/C sub-blocks
+ * [r 16/C, (r+1) 16/C), so one layout serves C = 1, 2, 4, 8, 16.  A bond
+ * belongs to the sub-block of its node i, a triple to that of its hinge;
+ * item slots list each sub-block's items in index order, so every CTA's
+ * items are one contiguous slot range.
+ *   node reference   sub-block << 16 | index within the sub-block
+ *   bond entry       sub-block << 28 | slot << 1 | role
+ *   triple entry     sub-block << 28 | slot << 2 | role
+ * (entries parallel to NetDev bent / tent, in the same canonical order). */
+constexpr int kDsmParts = 16;
+struct NetDsm {
+    int bsub;
+    int bo[kDsmParts + 1], to[kDsmParts + 1]; /* first bond / triple slot of each sub-block */
+    const int2 *bref;                         /* per bond slot: references of i, j */
+    const int *bidx;                          /* per bond slot: bond index */
+    const int4 *tref;                         /* per triple slot: references of h, j, k; triple index */
+    const int *bent, *tent;
 };
 
 /* ----- reductions ----- */

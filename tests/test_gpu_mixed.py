@@ -94,13 +94,20 @@ def test_mixed_step_cap_reports_fp64_state(cuda):
     assert (es, eb) == (rep.e_stretch, rep.e_bend)
 
 
-@pytest.mark.parametrize("cluster", [None, "4"])
-def test_mixed_cluster_teams(cuda, cluster, monkeypatch):
-    """Networks above the one-CTA size class run on a thread-block cluster
-    (CTAs of one cluster share a network through distributed shared
-    memory); results certified by the oracle's FP64 force."""
+@pytest.mark.parametrize("kernel,cluster,threads", [
+    ("dsm", None, None), ("dsm", "1", None), ("dsm", "2", None), ("dsm", "4", "512"), ("dsm", "16", None),
+    ("l2", None, None), ("l2", "4", None), ("l2", "1", "512"),
+])
+def test_mixed_cluster_teams(cuda, kernel, cluster, threads, monkeypatch):
+    """Batches run one thread-block cluster per network: the state of a step
+    in distributed shared memory ("dsm", the default when it fits) or in
+    global memory ("l2"), for several cluster sizes and CTA widths; results
+    certified by the oracle's FP64 force."""
+    monkeypatch.setenv("NR_MIX_KERNEL", kernel)
     if cluster:
         monkeypatch.setenv("NR_CLUSTER", cluster)
+    if threads:
+        monkeypatch.setenv("NR_MIX_THREADS", threads)
     rng = np.random.default_rng(5)
     hosts, arrs, kb, gam = [], [], [], []
     for i, L in enumerate([50, 12, 44, 20]):
