@@ -77,6 +77,7 @@ struct DeviceSet {
     float2 *fa_hi_all = nullptr, *fa_lo_all = nullptr;
     int max_nodes = 0;
     int *order = nullptr; /* networks by decreasing size (largest start first) */
+    int *order2 = nullptr; /* networks of a later escalation phase */
     /* sub-block layouts for the distributed-shared-memory kernel (host copy
      * for sizing, device array for the kernel); dsm_ok: every network has one */
     std::vector<NetDsm> dsm;
@@ -169,6 +170,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return nets[a]->n_points > nets[b]->n_points; });
     const size_t order_off = img.put(order.data(), order.size());
+    const size_t order2_off = img.add(sizeof(int) * n);
     const size_t st_off = img.add(sizeof(FireState) * n);
     const size_t q_off = img.add(256);
     const size_t aff_off = img.add(sizeof(double4) * n);
@@ -244,6 +246,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     S.fa_hi_all = (float2 *)(base + fah_off);
     S.fa_lo_all = (float2 *)(base + fal_off);
     S.order = (int *)(base + order_off);
+    S.order2 = (int *)(base + order2_off);
     S.st = (FireState *)(base + st_off);
     S.queue = (int *)(base + q_off);
     S.affine_prm = (double4 *)(base + aff_off);
@@ -442,16 +445,61 @@ static bool dsm_plan(const DeviceSet &S, int forced, int least, int *C_out, int 
     return false;
 }
 
+/* Fraction of idle clusters at which running networks escalate to clusters
+ * twice as large: NR_ESCALATE (default 0.5; 0 disables). */
+static double escalate_fraction() {
+    const char *env = getenv("NR_ESCALATE");
+    const double f = env ? atof(env) : 0.5;
+    return f > 0 && f <= 1 ? f : 0.0;
+}
+
+/* The distributed-shared-memory kernel in phases: all networks on clusters
+ * of C CTAs; when a fraction of the clusters has gone idle (the queue is
+ * empty), the networks still running stop at an anchor and the next phase
+ * resumes them on clusters twice as large, up to 16 CTAs.  The soft
+ * networks that need 10^5-10^6 steps thus end on the widest clusters
+ * instead of holding the whole batch on 4 SMs each. */
+static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, int C, int bmax, int emax, int tmax,
+                            cudaStream_t stream) {
+    const double frac = escalate_fraction();
+    int n_run = S.n_nets;
+    const int *order_dev = S.order;
+    std::vector<FireState> st;
+    std::vector<int> next;
+    for (;;) {
+        const bool last = C >= kDsmParts || frac <= 0;
+        NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, C, bmax, emax, tmax, last ? 0.0 : frac,
+                                     to_dev(prm), S.queue, order_dev, stream));
+        if (last) return NR_OK;
+        st.resize(S.n_nets);
+        NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
+        NR_CUDA_TRY(cudaStreamSynchronize(stream));
+        next.clear();
+        for (int i = 0; i < S.n_nets; ++i)
+            if (st[i].yielded) next.push_back(i);
+        if (next.empty()) return NR_OK;
+        int C2 = 0, b2 = 0, e2 = 0, t2 = 0;
+        if (!dsm_plan(S, 2 * C, 0, &C2, &b2, &e2, &t2)) return fail(NR_ERR_CUDA, "escalation: no cluster plan");
+        NR_CUDA_TRY(cudaMemcpyAsync(S.order2, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice, stream));
+        n_run = (int)next.size();
+        order_dev = S.order2;
+        C = C2;
+        bmax = b2;
+        emax = e2;
+        tmax = t2;
+    }
+}
+
 static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     if (prm.precision == NR_MIXED) {
         const char *env = getenv("NR_CLUSTER");
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
         int dc = 0, bmax = 0, emax = 0, tmax = 0;
-        if (dsm_plan(S, env ? cluster : 0, cluster, &dc, &bmax, &emax, &tmax))
-            NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, S.n_nets, dc, bmax, emax, tmax, to_dev(prm),
-                                         S.queue, S.order, stream));
-        else if (cluster > 1)
+        if (dsm_plan(S, env ? cluster : 0, cluster, &dc, &bmax, &emax, &tmax)) {
+            const int st = relax_dsm_phases(S, prm, dc, bmax, emax, tmax, stream);
+            if (st != NR_OK) return st;
+        } else if (cluster > 1)
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
         else
             NR_CUDA_TRY(

@@ -106,7 +106,7 @@ static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDs
 template <int NT>
 __global__ void __launch_bounds__(NT, 1)
     k_fire_dsm_mixed(const NetDev *nets, const NetDsm *dsms, int n_nets, FireParamsDev p, int *queue,
-                     const int *order, int bmax, int emax, int tmax) {
+                     const int *order, int bmax, int emax, int tmax, int yield_at) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ float4 s_dyn[];
@@ -121,6 +121,8 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ int s_slot;
     __shared__ Part s_part;
     __shared__ double s_anc[2];
+    __shared__ int s_yield; /* rank 0: half the clusters are idle, escalate */
+    __shared__ int s_flag;  /* network start: resume a yielded network; in the loop: leave after this anchor */
     __shared__ unsigned s_au[kDsmParts], s_ab[kDsmParts], s_at[kDsmParts];
     const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
     const int spr = kDsmParts / C, lg = __ffs(spr) - 1; /* sub-blocks per CTA, log2 */
@@ -137,7 +139,10 @@ __global__ void __launch_bounds__(NT, 1)
          * shared memory must not be read remotely after it exits) or rank 0
          * overwrites it for the next network */
         cl.sync();
-        if (slot >= n_nets) return;
+        if (slot >= n_nets) {
+            if (rank == 0 && threadIdx.x == 0) atomicAdd(queue + 1, 1); /* one more idle cluster */
+            return;
+        }
         if (threadIdx.x == 0) {
             const int idx = order ? order[slot] : slot;
             s_d = nets[idx];
@@ -150,29 +155,49 @@ __global__ void __launch_bounds__(NT, 1)
         const int n0 = rank * spr * bsub, nloc = max(0, min(spr * bsub, d.n - n0));
         const int b0 = m.bo[rank * spr], b1 = m.bo[(rank + 1) * spr];
         const int t0 = m.to[rank * spr], t1 = m.to[(rank + 1) * spr];
-        for (int li = threadIdx.x; li < nloc; li += NT) {
-            s_u[li] = make_float4(0.f, 0.f, 0.f, 0.f);
-            s_v[li] = make_float2(0.f, 0.f);
-        }
+        if (threadIdx.x == 0) s_flag = ((volatile FireState *)d.st)->yielded;
+        __syncthreads();
         MixScal s; /* replicated in thread 0 of every CTA */
         MixParams q;
         double F2, M2, tF2, tM2;
-        anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, F2, M2);
-        anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
-        if (threadIdx.x == 0) {
-            s_anc[0] = tF2;
-            s_anc[1] = tM2;
+        if (s_flag) {
+            /* resume a network a smaller cluster left at an anchor: u = 0,
+             * v and the FIRE scalars saved, F = F(X) and the anchor records
+             * in global memory (slot-indexed: the layout does not depend on
+             * the cluster size) */
+            for (int li = threadIdx.x; li < nloc; li += NT) {
+                s_u[li] = make_float4(0.f, 0.f, 0.f, 0.f);
+                s_v[li] = d.vf[n0 + li];
+                s_f[li] = d.fa_hi[n0 + li];
+            }
+            if (threadIdx.x == 0) {
+                s = mix_load(d.st);
+                q = mix_params(p, d.sqrt_dof);
+                sh.coef = coef_of(s, 0);
+            }
+            __syncthreads();
+        } else {
+            for (int li = threadIdx.x; li < nloc; li += NT) {
+                s_u[li] = make_float4(0.f, 0.f, 0.f, 0.f);
+                s_v[li] = make_float2(0.f, 0.f);
+            }
+            anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, F2, M2);
+            anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
+            if (threadIdx.x == 0) {
+                s_anc[0] = tF2;
+                s_anc[1] = tM2;
+            }
+            cl.sync();
+            if (threadIdx.x == 0) {
+                double t[2];
+                anchor_totals(cl, s_anc, t);
+                q = mix_params(p, d.sqrt_dof);
+                mix_init(s, q);
+                mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
+                sh.coef = coef_of(s, 0);
+            }
+            __syncthreads();
         }
-        cl.sync();
-        if (threadIdx.x == 0) {
-            double t[2];
-            anchor_totals(cl, s_anc, t);
-            q = mix_params(p, d.sqrt_dof);
-            mix_init(s, q);
-            mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
-            sh.coef = coef_of(s, 0);
-        }
-        __syncthreads();
         for (;;) {
             const Coef c = sh.coef;
             /* pass A: mixing, drift, half kick of the owned nodes */
@@ -198,40 +223,88 @@ __global__ void __launch_bounds__(NT, 1)
             }
             if (c.done) break;
             cl.sync();
-            /* item pass: owned bonds and triples, u of any CTA */
-            if (d.use_bonds)
-                for (int sl = b0 + threadIdx.x; sl < b1; sl += NT) {
-                    const int2 r = __ldg(m.bref + sl);
-                    const float4 ui = dsm_ld4(u_addr(s_au, r.x, lg, bsub)), uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub));
-                    float2 dh, dlo;
-                    u_diff2(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), make_float2(ui.x, ui.y),
-                            make_float2(ui.z, ui.w), dh, dlo);
-                    s_bdf[sl - b0] = bond_dforce(d.mb_data[sl], d.mb_sk[sl], dh, dlo);
+            /* item pass: owned bonds and triples, u of any CTA.  Software
+             * pipelined: the next item's reference and anchor record (read
+             * only, mostly from L2) are loaded while the current one computes */
+            if (d.use_bonds) {
+                int sl = b0 + threadIdx.x;
+                if (sl < b1) {
+                    int2 r = __ldg(m.bref + sl);
+                    float4 ra = d.mb_data[sl];
+                    float2 sk = d.mb_sk[sl];
+                    for (;;) {
+                        const float4 ui = dsm_ld4(u_addr(s_au, r.x, lg, bsub));
+                        const float4 uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub));
+                        const int nx = sl + NT;
+                        int2 rn = r;
+                        float4 ran = ra;
+                        float2 skn = sk;
+                        if (nx < b1) {
+                            rn = __ldg(m.bref + nx);
+                            ran = d.mb_data[nx];
+                            skn = d.mb_sk[nx];
+                        }
+                        float2 dh, dlo;
+                        u_diff2(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), make_float2(ui.x, ui.y),
+                                make_float2(ui.z, ui.w), dh, dlo);
+                        s_bdf[sl - b0] = bond_dforce(ra, sk, dh, dlo);
+                        if (nx >= b1) break;
+                        sl = nx;
+                        r = rn;
+                        ra = ran;
+                        sk = skn;
+                    }
                 }
-            if (d.use_triples)
-                for (int sl = t0 + threadIdx.x; sl < t1; sl += NT) {
-                    const int4 r = __ldg(m.tref + sl);
-                    const float4 uh = dsm_ld4(u_addr(s_au, r.x, lg, bsub)), uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub)), uk = dsm_ld4(u_addr(s_au, r.z, lg, bsub));
-                    const float2 hh = make_float2(uh.x, uh.y), hl = make_float2(uh.z, uh.w);
-                    float2 dFj, dFk;
-                    tri_dforce(d.mt_arms[sl], d.mt_pk[sl], u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
-                               u_diff(make_float2(uk.x, uk.y), make_float2(uk.z, uk.w), hh, hl), dFj, dFk);
-                    s_tdf[sl - t0] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+            }
+            if (d.use_triples) {
+                int sl = t0 + threadIdx.x;
+                if (sl < t1) {
+                    int4 r = __ldg(m.tref + sl);
+                    float4 arms = d.mt_arms[sl];
+                    float2 pk = d.mt_pk[sl];
+                    for (;;) {
+                        const float4 uh = dsm_ld4(u_addr(s_au, r.x, lg, bsub));
+                        const float4 uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub));
+                        const float4 uk = dsm_ld4(u_addr(s_au, r.z, lg, bsub));
+                        const int nx = sl + NT;
+                        int4 rn = r;
+                        float4 armsn = arms;
+                        float2 pkn = pk;
+                        if (nx < t1) {
+                            rn = __ldg(m.tref + nx);
+                            armsn = d.mt_arms[nx];
+                            pkn = d.mt_pk[nx];
+                        }
+                        const float2 hh = make_float2(uh.x, uh.y), hl = make_float2(uh.z, uh.w);
+                        float2 dFj, dFk;
+                        tri_dforce(arms, pk, u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
+                                   u_diff(make_float2(uk.x, uk.y), make_float2(uk.z, uk.w), hh, hl), dFj, dFk);
+                        s_tdf[sl - t0] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+                        if (nx >= t1) break;
+                        sl = nx;
+                        r = rn;
+                        arms = armsn;
+                        pk = pkn;
+                    }
                 }
+            }
             cl.sync();
             /* gather: F = F(X) + the node's entries in incidence order, half kick */
             float P = 0.f, V2 = 0.f, Fs = 0.f, M2f = 0.f, A = 0.f;
             for (int li = threadIdx.x; li < nloc; li += NT) {
                 const int i = n0 + li;
+                /* the node's independent global loads first: one round trip */
                 const unsigned fc = __ldg(d.fcode + i);
+                const int be0 = __ldg(d.bptr + i), be1 = __ldg(d.bptr + i + 1);
+                const int te0 = __ldg(d.tptr + i), te1 = __ldg(d.tptr + i + 1);
+                const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
                     float2 dF = make_float2(0.f, 0.f);
                     float mag = 0.f;
                     if (d.use_bonds) {
-                        const int e1 = __ldg(d.bptr + i + 1);
 #pragma unroll 4
-                        for (int e = __ldg(d.bptr + i); e < e1; ++e) {
+                        for (int e = be0; e < be1; ++e) {
                             const unsigned code = (unsigned)__ldg(m.bent + e);
                             const int r = (int)(code >> 28) >> lg;
                             const int ls = (int)((code >> 1) & 0x7ffffffu) - s_m.bo[r * spr];
@@ -243,9 +316,8 @@ __global__ void __launch_bounds__(NT, 1)
                         }
                     }
                     if (d.use_triples) {
-                        const int e1 = __ldg(d.tptr + i + 1);
 #pragma unroll 4
-                        for (int e = __ldg(d.tptr + i); e < e1; ++e) {
+                        for (int e = te0; e < te1; ++e) {
                             const unsigned code = (unsigned)__ldg(m.tent + e);
                             const int r = (int)(code >> 28) >> lg;
                             const int role = code & 3;
@@ -267,7 +339,6 @@ __global__ void __launch_bounds__(NT, 1)
                         }
                     }
                     A = fmaxf(A, mag);
-                    const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
                     F.x = ah.x + (al.x + dF.x);
                     F.y = ah.y + (al.y + dF.y);
                     if (!(fc & 1)) F.x = 0.f;
@@ -288,7 +359,10 @@ __global__ void __launch_bounds__(NT, 1)
             __syncthreads();
             if (threadIdx.x < 32) {
                 const Part t = block_totals(sh.slots);
-                if (threadIdx.x == 0) s_part = t;
+                if (threadIdx.x == 0) {
+                    s_part = t;
+                    if (rank == 0) s_yield = yield_at > 0 && *(volatile int *)(queue + 1) >= yield_at;
+                }
             }
             cl.sync();
             if (threadIdx.x < 32) {
@@ -297,8 +371,11 @@ __global__ void __launch_bounds__(NT, 1)
                 if ((int)threadIdx.x < C) t = *cl.map_shared_rank(&s_part, (int)threadIdx.x);
                 t = warp_reduce(t);
                 if (threadIdx.x == 0) {
+                    /* rank 0's escalation flag, the same in every CTA */
+                    const int y = *cl.map_shared_rank(&s_yield, 0);
                     mix_step(s, q, t);
-                    sh.coef = coef_of(s, need_anchor(s, q, t));
+                    sh.coef = coef_of(s, need_anchor(s, q, t) || y);
+                    s_flag = y;
                 }
             }
             __syncthreads();
@@ -326,9 +403,20 @@ __global__ void __launch_bounds__(NT, 1)
                     anchor_totals(cl, s_anc, t);
                     mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
                     sh.coef = coef_of(s, 0);
+                    s_flag = s_flag && !s.done;
                 }
                 __syncthreads();
+                if (s_flag) break;
             }
+        }
+        if (s_flag) {
+            /* escalate: keep v and the FIRE scalars for the relaunch */
+            for (int li = threadIdx.x; li < nloc; li += NT) d.vf[n0 + li] = s_v[li];
+            if (rank == 0 && threadIdx.x == 0) {
+                d.st->mix = s;
+                d.st->yielded = 1;
+            }
+            continue;
         }
         for (int li = threadIdx.x; li < nloc; li += NT) {
             const float2 v = s_v[li];
@@ -337,7 +425,10 @@ __global__ void __launch_bounds__(NT, 1)
         cl.sync();
         if (rank == 0) {
             mixed_energies(d, sh.red);
-            if (threadIdx.x == 0) mix_report(d.st, s);
+            if (threadIdx.x == 0) {
+                mix_report(d.st, s);
+                d.st->yielded = 0;
+            }
         }
         cl.sync();
     }
@@ -359,9 +450,8 @@ size_t dsm_smem_limit() {
 }
 
 template <int NT>
-static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                                 int emax, int tmax, const FireParamsDev &p, int *queue_dev, const int *order_dev,
-                                 cudaStream_t stream) {
+static cudaError_t dsm_config(int cluster, int bmax, int emax, int tmax, cudaLaunchConfig_t &cfg,
+                              cudaLaunchAttribute *attr, int *max_clusters) {
     cudaError_t e;
     int dev, sms;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
@@ -374,39 +464,60 @@ static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, 
         (e = cudaFuncSetAttribute(k_fire_dsm_mixed<NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) !=
             cudaSuccess)
         return e;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = cluster;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    cfg = cudaLaunchConfig_t{};
     cfg.blockDim = dim3(NT);
     cfg.dynamicSmemBytes = smem;
-    cfg.stream = stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cfg.gridDim = dim3((sms / cluster) * cluster);
+    *max_clusters = 0;
+    return cudaOccupancyMaxActiveClusters(max_clusters, (void *)k_fire_dsm_mixed<NT>, &cfg);
+}
+
+template <int NT>
+static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
+                                 int emax, int tmax, double escalate, const FireParamsDev &p, int *queue_dev,
+                                 const int *order_dev, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
     int max_clusters = 0;
-    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, (void *)k_fire_dsm_mixed<NT>, &cfg)) != cudaSuccess)
-        return e;
+    cudaError_t e = dsm_config<NT>(cluster, bmax, emax, tmax, cfg, attr, &max_clusters);
+    if (e != cudaSuccess) return e;
     if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
     const int clusters = std::max(1, std::min(n_nets, max_clusters));
     cfg.gridDim = dim3(clusters * cluster);
-    if ((e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream)) != cudaSuccess) return e;
+    cfg.stream = stream;
+    const int yield_at = escalate > 0 ? std::max(1, (int)(escalate * clusters)) : 0;
+    if ((e = cudaMemsetAsync(queue_dev, 0, 2 * sizeof(int), stream)) != cudaSuccess) return e;
     return cudaLaunchKernelEx(&cfg, k_fire_dsm_mixed<NT>, nets_dev, dsm_dev, n_nets, p, queue_dev, order_dev, bmax,
-                              emax, tmax);
+                              emax, tmax, yield_at);
+}
+
+static bool dsm_wide() {
+    const char *env = getenv("NR_MIX_THREADS");
+    return !(env && atoi(env) == 512);
 }
 
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                             int emax, int tmax, const FireParamsDev &p, int *queue_dev, const int *order_dev,
-                             cudaStream_t stream) {
+                             int emax, int tmax, double escalate, const FireParamsDev &p, int *queue_dev,
+                             const int *order_dev, cudaStream_t stream) {
     if (cluster < 1 || cluster > kDsmParts || (kDsmParts % cluster) != 0) return cudaErrorInvalidValue;
-    const char *env = getenv("NR_MIX_THREADS");
-    if (env && atoi(env) == 512)
-        return launch_dsm_nt<512>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, p, queue_dev, order_dev,
-                                  stream);
-    return launch_dsm_nt<1024>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, p, queue_dev, order_dev,
-                               stream);
+    if (dsm_wide())
+        return launch_dsm_nt<1024>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, escalate, p, queue_dev,
+                                   order_dev, stream);
+    return launch_dsm_nt<512>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, escalate, p, queue_dev,
+                              order_dev, stream);
+}
+
+cudaError_t dsm_max_clusters(int cluster, int bmax, int emax, int tmax, int *out) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    return dsm_wide() ? dsm_config<1024>(cluster, bmax, emax, tmax, cfg, attr, out)
+                      : dsm_config<512>(cluster, bmax, emax, tmax, cfg, attr, out);
 }
 
 }  // namespace nr

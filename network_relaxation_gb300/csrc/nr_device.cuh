@@ -59,7 +59,8 @@ struct __align__(128) FireState {
     int done, converged, status, fp64_steps;
     MixScal mix;    /* mixed precision, multi-CTA teams */
     int anchor_now; /* mixed precision: the team re-anchors before the next pass */
-    int pad[11];
+    int yielded;    /* mixed precision: left at an anchor for a larger cluster (fire_dsm.cu) */
+    int pad[10];
     unsigned int bar_count, bar_gen, abort_flag, timeout_site;
     unsigned int pad2[28];
 };

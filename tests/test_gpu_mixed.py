@@ -128,3 +128,33 @@ def test_mixed_cluster_teams(cuda, kernel, cluster, threads, monkeypatch):
         assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
         es, eb = m.energies(x)
         assert (es, eb) == (reps[i].e_stretch, reps[i].e_bend)
+
+
+@pytest.mark.parametrize("escalate", ["0", "0.5", "0.25"])
+def test_mixed_escalation(cuda, escalate, monkeypatch):
+    """When part of the clusters has gone idle, networks still running stop
+    at an anchor and resume on clusters twice as large (NR_ESCALATE: idle
+    fraction, 0 = never).  One soft network among quick stiff ones runs
+    through every phase; results stay certified by the oracle's FP64 force
+    and its energies."""
+    monkeypatch.setenv("NR_ESCALATE", escalate)
+    monkeypatch.delenv("NR_CLUSTER", raising=False)
+    specs = [(30, 0.6, 1e-5, 0.05)] + [(20, 0.75, 1e-2, 0.02)] * 7
+    hosts, arrs = [], []
+    for i, (L, p, _, _) in enumerate(specs):
+        h = nr.HostNetwork.lattice(L, L, p, 0.0, 700 + i).get_triples()
+        hosts.append(h)
+        arrs.append(h.arrays())
+    kb = np.array([s[2] for s in specs])
+    gam = np.array([s[3] for s in specs])
+    b = nr.Batch(hosts, 1.0, kb)
+    b.affine_displace(gam * (b.maxy - b.miny), 0.0)
+    reps = b.relax(nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **FIRE))
+    X = b.positions()
+    assert reps[0].steps > 5 * max(r.steps for r in reps[1:])
+    for i, a in enumerate(arrs):
+        assert reps[i].status == nr.NR_OK
+        x = X[b.offsets[i]:b.offsets[i + 1]]
+        m = oracle.Model(a, 1.0, kb[i])
+        assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+        assert m.energies(x) == (reps[i].e_stretch, reps[i].e_bend)
