@@ -136,6 +136,11 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
             const unsigned g = (unsigned)part(h.tri_hjk[3 * t]);
             dtent[e] = (int)((g << 28) | ((unsigned)tslot[t] << 2) | (unsigned)role);
         }
+        for (int g = 0; g <= kDsmParts; ++g) {
+            const int v = std::min(n, g * bsub);
+            m.be[g] = inc.bptr[v];
+            m.te[g] = inc.tptr[v];
+        }
         m.bsub = bsub;
     }
     o.dsm_bref = img.put(bref.data(), bref.size());
@@ -412,33 +417,47 @@ static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStrea
     return rep->status;
 }
 
-/* Cluster size and shared-memory maxima for the distributed-shared-memory
- * kernel: `forced` C if nonzero, else the smallest C >= `least` (a power of
- * two dividing 16) whose per-CTA state fits.  False when the batch has no
- * layout, NR_MIX_KERNEL=l2 asks for the global-memory kernels, or nothing
- * fits. */
-static bool dsm_plan(const DeviceSet &S, int forced, int least, int *C_out, int *bmax, int *emax, int *tmax) {
+/* Launch plan of the distributed-shared-memory kernel: cluster size and
+ * per-CTA maxima (nodes, bonds, triples, incidence entries). */
+struct DsmPlan {
+    int C, bmax, emax, tmax, ebmax, etmax, resident;
+};
+
+/* `forced` C if nonzero, else the smallest C >= `least` (a power of two
+ * dividing 16) whose per-CTA state fits in shared memory; the read-only
+ * slices go to shared memory as well when they fit too (NR_DSM_RESIDENT=0
+ * keeps them in global memory).  False when the batch has no layout,
+ * NR_MIX_KERNEL=l2 asks for the global-memory kernels, or nothing fits. */
+static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl) {
     const char *k = getenv("NR_MIX_KERNEL");
     if (!S.dsm_ok || (k && strcmp(k, "l2") == 0)) return false;
+    const char *rk = getenv("NR_DSM_RESIDENT");
+    const bool allow_res = !(rk && atoi(rk) == 0);
     const size_t limit = dsm_smem_limit();
     for (int C = 1; C <= kDsmParts; C *= 2) {
         if (forced ? C != forced : C < least) continue;
         const int spr = kDsmParts / C;
-        int bm = 0, em = 0, tm = 0;
+        int bm = 0, em = 0, tm = 0, ebm = 0, etm = 0;
         for (int i = 0; i < S.n_nets; ++i) {
             const NetDsm &m = S.dsm[i];
             const NetDev &d = S.dev[i];
             bm = std::max(bm, spr * m.bsub);
             for (int r = 0; r < C; ++r) {
-                if (d.use_bonds) em = std::max(em, m.bo[(r + 1) * spr] - m.bo[r * spr]);
-                if (d.use_triples) tm = std::max(tm, m.to[(r + 1) * spr] - m.to[r * spr]);
+                if (d.use_bonds) {
+                    em = std::max(em, m.bo[(r + 1) * spr] - m.bo[r * spr]);
+                    ebm = std::max(ebm, m.be[(r + 1) * spr] - m.be[r * spr]);
+                }
+                if (d.use_triples) {
+                    tm = std::max(tm, m.to[(r + 1) * spr] - m.to[r * spr]);
+                    etm = std::max(etm, m.te[(r + 1) * spr] - m.te[r * spr]);
+                }
             }
         }
-        if (dsm_smem_bytes(bm, em, tm) <= limit) {
-            *C_out = C;
-            *bmax = bm;
-            *emax = em;
-            *tmax = tm;
+        int res = -1;
+        if (allow_res && dsm_smem_bytes(bm, em, tm, ebm, etm, 1) <= limit) res = 1;
+        else if (dsm_smem_bytes(bm, em, tm, ebm, etm, 0) <= limit) res = 0;
+        if (res >= 0) {
+            pl = DsmPlan{C, bm, em, tm, ebm, etm, res};
             return true;
         }
     }
@@ -446,10 +465,10 @@ static bool dsm_plan(const DeviceSet &S, int forced, int least, int *C_out, int 
 }
 
 /* Fraction of idle clusters at which running networks escalate to clusters
- * twice as large: NR_ESCALATE (default 0.5; 0 disables). */
+ * twice as large: NR_ESCALATE (default 0.25; 0 disables). */
 static double escalate_fraction() {
     const char *env = getenv("NR_ESCALATE");
-    const double f = env ? atof(env) : 0.5;
+    const double f = env ? atof(env) : 0.25;
     return f > 0 && f <= 1 ? f : 0.0;
 }
 
@@ -459,17 +478,17 @@ static double escalate_fraction() {
  * resumes them on clusters twice as large, up to 16 CTAs.  The soft
  * networks that need 10^5-10^6 steps thus end on the widest clusters
  * instead of holding the whole batch on 4 SMs each. */
-static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, int C, int bmax, int emax, int tmax,
-                            cudaStream_t stream) {
+static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl, cudaStream_t stream) {
     const double frac = escalate_fraction();
     int n_run = S.n_nets;
     const int *order_dev = S.order;
     std::vector<FireState> st;
     std::vector<int> next;
     for (;;) {
-        const bool last = C >= kDsmParts || frac <= 0;
-        NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, C, bmax, emax, tmax, last ? 0.0 : frac,
-                                     to_dev(prm), S.queue, order_dev, stream));
+        const bool last = pl.C >= kDsmParts || frac <= 0;
+        NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, pl.C, pl.bmax, pl.emax, pl.tmax, pl.ebmax,
+                                     pl.etmax, pl.resident, last ? 0.0 : frac, to_dev(prm), S.queue, order_dev,
+                                     stream));
         if (last) return NR_OK;
         st.resize(S.n_nets);
         NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
@@ -478,15 +497,12 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, int C, int 
         for (int i = 0; i < S.n_nets; ++i)
             if (st[i].yielded) next.push_back(i);
         if (next.empty()) return NR_OK;
-        int C2 = 0, b2 = 0, e2 = 0, t2 = 0;
-        if (!dsm_plan(S, 2 * C, 0, &C2, &b2, &e2, &t2)) return fail(NR_ERR_CUDA, "escalation: no cluster plan");
+        DsmPlan p2;
+        if (!dsm_plan(S, 2 * pl.C, 0, p2)) return fail(NR_ERR_CUDA, "escalation: no cluster plan");
         NR_CUDA_TRY(cudaMemcpyAsync(S.order2, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice, stream));
         n_run = (int)next.size();
         order_dev = S.order2;
-        C = C2;
-        bmax = b2;
-        emax = e2;
-        tmax = t2;
+        pl = p2;
     }
 }
 
@@ -495,9 +511,9 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
     if (prm.precision == NR_MIXED) {
         const char *env = getenv("NR_CLUSTER");
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
-        int dc = 0, bmax = 0, emax = 0, tmax = 0;
-        if (dsm_plan(S, env ? cluster : 0, cluster, &dc, &bmax, &emax, &tmax)) {
-            const int st = relax_dsm_phases(S, prm, dc, bmax, emax, tmax, stream);
+        DsmPlan pl;
+        if (dsm_plan(S, env ? cluster : 0, cluster, pl)) {
+            const int st = relax_dsm_phases(S, prm, pl, stream);
             if (st != NR_OK) return st;
         } else if (cluster > 1)
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));

@@ -56,11 +56,55 @@ __device__ __forceinline__ unsigned u_addr(const unsigned *au, int ref, int lg, 
     return au[r] + 16u * (unsigned)local;
 }
 
+/* Per-CTA dynamic shared memory: the step's state and, when `resident`,
+ * copies of the CTA's read-only slices (item references and anchor
+ * records, node pointers and incidence entries, anchor force).  Segments
+ * of 16-byte elements first, then 8-byte, then 4-byte ones. */
+struct DsmSizes {
+    int bmax, emax, tmax;   /* nodes, bonds, triples per CTA */
+    int ebmax, etmax;       /* bond / triple incidence entries per CTA */
+    int resident;
+};
+struct DsmLayout {
+    size_t u, tdf, mb, arms, tref, v, f, bdf, fahi, falo, sk, pk, bref, bptr, tptr, bent, tent, total;
+};
+__host__ __device__ inline DsmLayout dsm_layout(const DsmSizes &z) {
+    const size_t R = z.resident ? 1 : 0, bm = (size_t)z.bmax, em = (size_t)z.emax, tm = (size_t)z.tmax;
+    DsmLayout L;
+    size_t o = 0;
+    L.u = o;    o += 16 * bm;
+    L.tdf = o;  o += 16 * tm;
+    L.mb = o;   o += R * 16 * em;
+    L.arms = o; o += R * 16 * tm;
+    L.tref = o; o += R * 16 * tm;
+    L.v = o;    o += 8 * bm;
+    L.f = o;    o += 8 * bm;
+    L.bdf = o;  o += 8 * em;
+    L.fahi = o; o += R * 8 * bm;
+    L.falo = o; o += R * 8 * bm;
+    L.sk = o;   o += R * 8 * em;
+    L.pk = o;   o += R * 8 * tm;
+    L.bref = o; o += R * 8 * em;
+    L.bptr = o; o += R * 4 * (bm + 1);
+    L.tptr = o; o += R * 4 * (bm + 1);
+    L.bent = o; o += R * 4 * (size_t)z.ebmax;
+    L.tent = o; o += R * 4 * (size_t)z.etmax;
+    L.total = o;
+    return L;
+}
+
+/* Shared-memory copies the anchor writes besides global memory (null when
+ * the CTA is not resident). */
+struct DsmRes {
+    float4 *mb, *arms;
+    float2 *sk, *pk, *fahi, *falo;
+};
+
 /* Anchor step 2 for the CTA's own items and nodes: FP32 anchor records by
  * slot, FP64 forces into f, the double-float anchor force, F = F(X) in
  * shared memory; CTA partials of |F|^2 and max|F|^2 in F2, M2. */
 static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDsm &m, int n0, int nloc, int b0, int b1,
-                                                    int t0, int t1, float2 *s_f, double &F2, double &M2) {
+                                                    int t0, int t1, float2 *s_f, DsmRes res, double &F2, double &M2) {
     const double W = d.width;
     F2 = 0.0;
     M2 = 0.0;
@@ -72,8 +116,14 @@ static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDs
             const double rx = (p2.x + wrap_shift(r.z, W)) - p1.x, ry = p2.y - p1.y;
             const double k = d.bond_k ? d.bond_k[b] : d.ks;
             const float hx = (float)rx, hy = (float)ry;
-            d.mb_data[sl] = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
-            d.mb_sk[sl] = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)k);
+            const float4 rec = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
+            const float2 sk = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)k);
+            d.mb_data[sl] = rec;
+            d.mb_sk[sl] = sk;
+            if (res.mb) {
+                res.mb[sl - b0] = rec;
+                res.sk[sl - b0] = sk;
+            }
         }
     if (d.use_triples)
         for (int sl = t0 + threadIdx.x; sl < t1; sl += blockDim.x) {
@@ -85,8 +135,14 @@ static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDs
             const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
             const double kb = d.tri_kb ? d.tri_kb[t] : d.kb;
             const double phi0 = d.tri_phi0 ? d.tri_phi0[t] : 0.0;
-            d.mt_arms[sl] = make_float4((float)ax, (float)ay, (float)bx, (float)by);
-            d.mt_pk[sl] = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
+            const float4 arms = make_float4((float)ax, (float)ay, (float)bx, (float)by);
+            const float2 pkv = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
+            d.mt_arms[sl] = arms;
+            d.mt_pk[sl] = pkv;
+            if (res.arms) {
+                res.arms[sl - t0] = arms;
+                res.pk[sl - t0] = pkv;
+            }
         }
     for (int li = threadIdx.x; li < nloc; li += blockDim.x) {
         const int i = n0 + li;
@@ -94,27 +150,54 @@ static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDs
         node_force_fp64(d, i, fx, fy);
         d.f[i] = make_double2(fx, fy);
         const float hx = (float)fx, hy = (float)fy;
-        d.fa_hi[i] = make_float2(hx, hy);
-        d.fa_lo[i] = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));
-        s_f[li] = make_float2(hx, hy);
+        const float2 fh = make_float2(hx, hy), fl = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));
+        d.fa_hi[i] = fh;
+        d.fa_lo[i] = fl;
+        if (res.fahi) {
+            res.fahi[li] = fh;
+            res.falo[li] = fl;
+        }
+        s_f[li] = fh;
         const double t = dot2(fx, fy, fx, fy);
         F2 += t;
         M2 = fmax(M2, t);
     }
 }
 
-template <int NT>
+/* Read-only load: through the read-only cache from global memory, or a
+ * plain load of a shared-memory copy. */
+template <bool RES, class T>
+__device__ __forceinline__ T ldro(const T *p) {
+    if constexpr (RES) return *p;
+    else return __ldg(p);
+}
+
+template <int NT, bool RES>
 __global__ void __launch_bounds__(NT, 1)
     k_fire_dsm_mixed(const NetDev *nets, const NetDsm *dsms, int n_nets, FireParamsDev p, int *queue,
-                     const int *order, int bmax, int emax, int tmax, int yield_at) {
+                     const int *order, DsmSizes z, int yield_at) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ float4 s_dyn[];
-    float4 *s_u = s_dyn;                       /* [bmax] {hi.x, hi.y, lo.x, lo.y} */
-    float4 *s_tdf = s_u + bmax;                /* [tmax] */
-    float2 *s_v = reinterpret_cast<float2 *>(s_tdf + tmax); /* [bmax] */
-    float2 *s_f = s_v + bmax;                  /* [bmax] */
-    float2 *s_bdf = s_f + bmax;                /* [emax] */
+    unsigned char *dyn = reinterpret_cast<unsigned char *>(s_dyn);
+    const DsmLayout L = dsm_layout(z);
+    constexpr bool R = RES;
+    float4 *s_u = reinterpret_cast<float4 *>(dyn + L.u); /* {hi.x, hi.y, lo.x, lo.y} */
+    float4 *s_tdf = reinterpret_cast<float4 *>(dyn + L.tdf);
+    float2 *s_v = reinterpret_cast<float2 *>(dyn + L.v);
+    float2 *s_f = reinterpret_cast<float2 *>(dyn + L.f);
+    float2 *s_bdf = reinterpret_cast<float2 *>(dyn + L.bdf);
+    DsmRes res{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (R)
+        res = DsmRes{reinterpret_cast<float4 *>(dyn + L.mb), reinterpret_cast<float4 *>(dyn + L.arms),
+                     reinterpret_cast<float2 *>(dyn + L.sk), reinterpret_cast<float2 *>(dyn + L.pk),
+                     reinterpret_cast<float2 *>(dyn + L.fahi), reinterpret_cast<float2 *>(dyn + L.falo)};
+    int4 *s_tref = reinterpret_cast<int4 *>(dyn + L.tref);
+    int2 *s_bref = reinterpret_cast<int2 *>(dyn + L.bref);
+    int *s_bptr = reinterpret_cast<int *>(dyn + L.bptr);
+    int *s_tptr = reinterpret_cast<int *>(dyn + L.tptr);
+    int *s_bent = reinterpret_cast<int *>(dyn + L.bent);
+    int *s_tent = reinterpret_cast<int *>(dyn + L.tent);
     __shared__ MixShared sh;
     __shared__ NetDev s_d;
     __shared__ NetDsm s_m;
@@ -155,6 +238,34 @@ __global__ void __launch_bounds__(NT, 1)
         const int n0 = rank * spr * bsub, nloc = max(0, min(spr * bsub, d.n - n0));
         const int b0 = m.bo[rank * spr], b1 = m.bo[(rank + 1) * spr];
         const int t0 = m.to[rank * spr], t1 = m.to[(rank + 1) * spr];
+        const int eb0 = m.be[rank * spr], eb1 = m.be[(rank + 1) * spr];
+        const int et0 = m.te[rank * spr], et1 = m.te[(rank + 1) * spr];
+        if (R) { /* the CTA's read-only slices into shared memory */
+            if (nloc > 0)
+                for (int k = threadIdx.x; k <= nloc; k += NT) {
+                    s_bptr[k] = d.bptr[n0 + k];
+                    s_tptr[k] = d.tptr[n0 + k];
+                }
+            for (int k = threadIdx.x; k < eb1 - eb0; k += NT) s_bent[k] = m.bent[eb0 + k];
+            for (int k = threadIdx.x; k < et1 - et0; k += NT) s_tent[k] = m.tent[et0 + k];
+            if (d.use_bonds)
+                for (int k = threadIdx.x; k < b1 - b0; k += NT) s_bref[k] = m.bref[b0 + k];
+            if (d.use_triples)
+                for (int k = threadIdx.x; k < t1 - t0; k += NT) s_tref[k] = m.tref[t0 + k];
+        }
+        /* item and node data for the step loops: shared copies or global */
+        const int2 *Bref = R ? s_bref : m.bref + b0;
+        const float4 *Mb = R ? res.mb : d.mb_data + b0;
+        const float2 *Sk = R ? res.sk : d.mb_sk + b0;
+        const int4 *Tref = R ? s_tref : m.tref + t0;
+        const float4 *Arms = R ? res.arms : d.mt_arms + t0;
+        const float2 *Pk = R ? res.pk : d.mt_pk + t0;
+        const int *Bp = R ? s_bptr : d.bptr + n0;
+        const int *Tp = R ? s_tptr : d.tptr + n0;
+        const int *Be = R ? s_bent : m.bent + eb0;
+        const int *Te = R ? s_tent : m.tent + et0;
+        const float2 *FaH = R ? res.fahi : d.fa_hi + n0;
+        const float2 *FaL = R ? res.falo : d.fa_lo + n0;
         if (threadIdx.x == 0) s_flag = ((volatile FireState *)d.st)->yielded;
         __syncthreads();
         MixScal s; /* replicated in thread 0 of every CTA */
@@ -170,6 +281,22 @@ __global__ void __launch_bounds__(NT, 1)
                 s_v[li] = d.vf[n0 + li];
                 s_f[li] = d.fa_hi[n0 + li];
             }
+            if (R) {
+                if (d.use_bonds)
+                    for (int k = threadIdx.x; k < b1 - b0; k += NT) {
+                        res.mb[k] = d.mb_data[b0 + k];
+                        res.sk[k] = d.mb_sk[b0 + k];
+                    }
+                if (d.use_triples)
+                    for (int k = threadIdx.x; k < t1 - t0; k += NT) {
+                        res.arms[k] = d.mt_arms[t0 + k];
+                        res.pk[k] = d.mt_pk[t0 + k];
+                    }
+                for (int li = threadIdx.x; li < nloc; li += NT) {
+                    res.fahi[li] = d.fa_hi[n0 + li];
+                    res.falo[li] = d.fa_lo[n0 + li];
+                }
+            }
             if (threadIdx.x == 0) {
                 s = mix_load(d.st);
                 q = mix_params(p, d.sqrt_dof);
@@ -181,7 +308,7 @@ __global__ void __launch_bounds__(NT, 1)
                 s_u[li] = make_float4(0.f, 0.f, 0.f, 0.f);
                 s_v[li] = make_float2(0.f, 0.f);
             }
-            anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, F2, M2);
+            anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, res, F2, M2);
             anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
             if (threadIdx.x == 0) {
                 s_anc[0] = tF2;
@@ -227,11 +354,12 @@ __global__ void __launch_bounds__(NT, 1)
              * pipelined: the next item's reference and anchor record (read
              * only, mostly from L2) are loaded while the current one computes */
             if (d.use_bonds) {
-                int sl = b0 + threadIdx.x;
-                if (sl < b1) {
-                    int2 r = __ldg(m.bref + sl);
-                    float4 ra = d.mb_data[sl];
-                    float2 sk = d.mb_sk[sl];
+                const int nb = b1 - b0;
+                int sl = threadIdx.x;
+                if (sl < nb) {
+                    int2 r = ldro<RES>(Bref + sl);
+                    float4 ra = Mb[sl];
+                    float2 sk = Sk[sl];
                     for (;;) {
                         const float4 ui = dsm_ld4(u_addr(s_au, r.x, lg, bsub));
                         const float4 uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub));
@@ -239,16 +367,16 @@ __global__ void __launch_bounds__(NT, 1)
                         int2 rn = r;
                         float4 ran = ra;
                         float2 skn = sk;
-                        if (nx < b1) {
-                            rn = __ldg(m.bref + nx);
-                            ran = d.mb_data[nx];
-                            skn = d.mb_sk[nx];
+                        if (nx < nb) {
+                            rn = ldro<RES>(Bref + nx);
+                            ran = Mb[nx];
+                            skn = Sk[nx];
                         }
                         float2 dh, dlo;
                         u_diff2(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), make_float2(ui.x, ui.y),
                                 make_float2(ui.z, ui.w), dh, dlo);
-                        s_bdf[sl - b0] = bond_dforce(ra, sk, dh, dlo);
-                        if (nx >= b1) break;
+                        s_bdf[sl] = bond_dforce(ra, sk, dh, dlo);
+                        if (nx >= nb) break;
                         sl = nx;
                         r = rn;
                         ra = ran;
@@ -257,11 +385,12 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
             if (d.use_triples) {
-                int sl = t0 + threadIdx.x;
-                if (sl < t1) {
-                    int4 r = __ldg(m.tref + sl);
-                    float4 arms = d.mt_arms[sl];
-                    float2 pk = d.mt_pk[sl];
+                const int nt = t1 - t0;
+                int sl = threadIdx.x;
+                if (sl < nt) {
+                    int4 r = ldro<RES>(Tref + sl);
+                    float4 arms = Arms[sl];
+                    float2 pk = Pk[sl];
                     for (;;) {
                         const float4 uh = dsm_ld4(u_addr(s_au, r.x, lg, bsub));
                         const float4 uj = dsm_ld4(u_addr(s_au, r.y, lg, bsub));
@@ -270,17 +399,17 @@ __global__ void __launch_bounds__(NT, 1)
                         int4 rn = r;
                         float4 armsn = arms;
                         float2 pkn = pk;
-                        if (nx < t1) {
-                            rn = __ldg(m.tref + nx);
-                            armsn = d.mt_arms[nx];
-                            pkn = d.mt_pk[nx];
+                        if (nx < nt) {
+                            rn = ldro<RES>(Tref + nx);
+                            armsn = Arms[nx];
+                            pkn = Pk[nx];
                         }
                         const float2 hh = make_float2(uh.x, uh.y), hl = make_float2(uh.z, uh.w);
                         float2 dFj, dFk;
                         tri_dforce(arms, pk, u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
                                    u_diff(make_float2(uk.x, uk.y), make_float2(uk.z, uk.w), hh, hl), dFj, dFk);
-                        s_tdf[sl - t0] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
-                        if (nx >= t1) break;
+                        s_tdf[sl] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+                        if (nx >= nt) break;
                         sl = nx;
                         r = rn;
                         arms = armsn;
@@ -295,17 +424,17 @@ __global__ void __launch_bounds__(NT, 1)
                 const int i = n0 + li;
                 /* the node's independent global loads first: one round trip */
                 const unsigned fc = __ldg(d.fcode + i);
-                const int be0 = __ldg(d.bptr + i), be1 = __ldg(d.bptr + i + 1);
-                const int te0 = __ldg(d.tptr + i), te1 = __ldg(d.tptr + i + 1);
-                const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
+                const int bq0 = ldro<RES>(Bp + li) - eb0, bq1 = ldro<RES>(Bp + li + 1) - eb0;
+                const int tq0 = ldro<RES>(Tp + li) - et0, tq1 = ldro<RES>(Tp + li + 1) - et0;
+                const float2 ah = FaH[li], al = FaL[li];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
                     float2 dF = make_float2(0.f, 0.f);
                     float mag = 0.f;
                     if (d.use_bonds) {
 #pragma unroll 4
-                        for (int e = be0; e < be1; ++e) {
-                            const unsigned code = (unsigned)__ldg(m.bent + e);
+                        for (int e = bq0; e < bq1; ++e) {
+                            const unsigned code = (unsigned)ldro<RES>(Be + e);
                             const int r = (int)(code >> 28) >> lg;
                             const int ls = (int)((code >> 1) & 0x7ffffffu) - s_m.bo[r * spr];
                             float2 df = dsm_ld2(s_ab[r] + 8u * (unsigned)ls);
@@ -317,8 +446,8 @@ __global__ void __launch_bounds__(NT, 1)
                     }
                     if (d.use_triples) {
 #pragma unroll 4
-                        for (int e = te0; e < te1; ++e) {
-                            const unsigned code = (unsigned)__ldg(m.tent + e);
+                        for (int e = tq0; e < tq1; ++e) {
+                            const unsigned code = (unsigned)ldro<RES>(Te + e);
                             const int r = (int)(code >> 28) >> lg;
                             const int role = code & 3;
                             const int ls = (int)((code >> 2) & 0x3ffffffu) - s_m.to[r * spr];
@@ -391,7 +520,7 @@ __global__ void __launch_bounds__(NT, 1)
                     s_u[li] = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
                 cl.sync();
-                anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, F2, M2);
+                anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, res, F2, M2);
                 anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
                 if (threadIdx.x == 0) {
                     s_anc[0] = tF2;
@@ -435,8 +564,8 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 /* Dynamic shared memory of k_fire_dsm_mixed for the given per-CTA maxima. */
-size_t dsm_smem_bytes(int bmax, int emax, int tmax) {
-    return (size_t)bmax * 16 + (size_t)tmax * 16 + (size_t)bmax * 16 + (size_t)emax * 8;
+size_t dsm_smem_bytes(int bmax, int emax, int tmax, int ebmax, int etmax, int resident) {
+    return dsm_layout(DsmSizes{bmax, emax, tmax, ebmax, etmax, resident}).total;
 }
 
 /* Largest dynamic shared memory the kernel may use on this device. */
@@ -445,23 +574,23 @@ size_t dsm_smem_limit() {
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
     cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, (const void *)k_fire_dsm_mixed<1024>) != cudaSuccess) return 0;
+    if (cudaFuncGetAttributes(&fa, (const void *)k_fire_dsm_mixed<512, true>) != cudaSuccess) return 0;
     return optin > (int)fa.sharedSizeBytes ? (size_t)(optin - (int)fa.sharedSizeBytes) : 0;
 }
 
-template <int NT>
-static cudaError_t dsm_config(int cluster, int bmax, int emax, int tmax, cudaLaunchConfig_t &cfg,
-                              cudaLaunchAttribute *attr, int *max_clusters) {
+template <int NT, bool RES>
+static cudaError_t dsm_config(int cluster, const DsmSizes &z, cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr,
+                              int *max_clusters) {
     cudaError_t e;
     int dev, sms;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    const size_t smem = dsm_smem_bytes(bmax, emax, tmax);
-    if ((e = cudaFuncSetAttribute(k_fire_dsm_mixed<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+    const size_t smem = dsm_layout(z).total;
+    if ((e = cudaFuncSetAttribute(k_fire_dsm_mixed<NT, RES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
         cudaSuccess)
         return e;
     if (cluster > 8 &&
-        (e = cudaFuncSetAttribute(k_fire_dsm_mixed<NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) !=
+        (e = cudaFuncSetAttribute(k_fire_dsm_mixed<NT, RES>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) !=
             cudaSuccess)
         return e;
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -475,17 +604,17 @@ static cudaError_t dsm_config(int cluster, int bmax, int emax, int tmax, cudaLau
     cfg.numAttrs = 1;
     cfg.gridDim = dim3((sms / cluster) * cluster);
     *max_clusters = 0;
-    return cudaOccupancyMaxActiveClusters(max_clusters, (void *)k_fire_dsm_mixed<NT>, &cfg);
+    return cudaOccupancyMaxActiveClusters(max_clusters, (void *)k_fire_dsm_mixed<NT, RES>, &cfg);
 }
 
-template <int NT>
-static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                                 int emax, int tmax, double escalate, const FireParamsDev &p, int *queue_dev,
+template <int NT, bool RES>
+static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster,
+                                 const DsmSizes &z, double escalate, const FireParamsDev &p, int *queue_dev,
                                  const int *order_dev, cudaStream_t stream) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
     int max_clusters = 0;
-    cudaError_t e = dsm_config<NT>(cluster, bmax, emax, tmax, cfg, attr, &max_clusters);
+    cudaError_t e = dsm_config<NT, RES>(cluster, z, cfg, attr, &max_clusters);
     if (e != cudaSuccess) return e;
     if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
     const int clusters = std::max(1, std::min(n_nets, max_clusters));
@@ -493,31 +622,35 @@ static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, 
     cfg.stream = stream;
     const int yield_at = escalate > 0 ? std::max(1, (int)(escalate * clusters)) : 0;
     if ((e = cudaMemsetAsync(queue_dev, 0, 2 * sizeof(int), stream)) != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_fire_dsm_mixed<NT>, nets_dev, dsm_dev, n_nets, p, queue_dev, order_dev, bmax,
-                              emax, tmax, yield_at);
+    return cudaLaunchKernelEx(&cfg, k_fire_dsm_mixed<NT, RES>, nets_dev, dsm_dev, n_nets, p, queue_dev, order_dev, z,
+                              yield_at);
 }
 
-static bool dsm_wide() {
+/* Threads per CTA: NR_MIX_THREADS (512 or 1024), else 1024 when the state
+ * fills shared memory (many items per thread: more warps hide more
+ * latency) and 512 when the CTA is resident (few items per thread: the
+ * 128-register budget keeps the step free of spills). */
+static int dsm_threads(bool resident) {
     const char *env = getenv("NR_MIX_THREADS");
-    return !(env && atoi(env) == 512);
+    if (env && (atoi(env) == 512 || atoi(env) == 1024)) return atoi(env);
+    return resident ? 512 : 1024;
 }
 
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                             int emax, int tmax, double escalate, const FireParamsDev &p, int *queue_dev,
-                             const int *order_dev, cudaStream_t stream) {
+                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate,
+                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream) {
     if (cluster < 1 || cluster > kDsmParts || (kDsmParts % cluster) != 0) return cudaErrorInvalidValue;
-    if (dsm_wide())
-        return launch_dsm_nt<1024>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, escalate, p, queue_dev,
-                                   order_dev, stream);
-    return launch_dsm_nt<512>(nets_dev, dsm_dev, n_nets, cluster, bmax, emax, tmax, escalate, p, queue_dev,
-                              order_dev, stream);
-}
-
-cudaError_t dsm_max_clusters(int cluster, int bmax, int emax, int tmax, int *out) {
-    cudaLaunchConfig_t cfg;
-    cudaLaunchAttribute attr[1];
-    return dsm_wide() ? dsm_config<1024>(cluster, bmax, emax, tmax, cfg, attr, out)
-                      : dsm_config<512>(cluster, bmax, emax, tmax, cfg, attr, out);
+    const DsmSizes z{bmax, emax, tmax, ebmax, etmax, resident};
+    const bool wide = dsm_threads(resident != 0) == 1024;
+    if (resident)
+        return wide ? launch_dsm_nt<1024, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev,
+                                                order_dev, stream)
+                    : launch_dsm_nt<512, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev,
+                                               order_dev, stream);
+    return wide ? launch_dsm_nt<1024, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev, order_dev,
+                                             stream)
+                : launch_dsm_nt<512, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev, order_dev,
+                                            stream);
 }
 
 }  // namespace nr

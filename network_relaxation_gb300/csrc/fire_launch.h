@@ -27,17 +27,18 @@ cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes
 int mixed_cluster_size(int max_nodes);
 cudaError_t launch_mixed_cluster(const NetDev *nets_dev, int n_nets, int cluster, const FireParamsDev &p,
                                  int *queue_dev, const int *order_dev, cudaStream_t stream);
-size_t dsm_smem_bytes(int bmax, int emax, int tmax);
+size_t dsm_smem_bytes(int bmax, int emax, int tmax, int ebmax, int etmax, int resident);
 size_t dsm_smem_limit();
 /* One launch of the distributed-shared-memory kernel over n_nets networks
- * (order_dev[0..n_nets)).  escalate > 0: once that fraction of the launched
+ * (order_dev[0..n_nets)); per-CTA maxima of nodes, bonds, triples and
+ * incidence entries; resident: the CTAs keep their read-only slices in
+ * shared memory too.  escalate > 0: once that fraction of the launched
  * clusters is idle, running networks stop at an anchor with their state
  * saved (FireState.yielded) for a relaunch on larger clusters.  queue_dev:
  * 2 ints (next slot, idle clusters). */
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                             int emax, int tmax, double escalate, const FireParamsDev &p, int *queue_dev,
-                             const int *order_dev, cudaStream_t stream);
-cudaError_t dsm_max_clusters(int cluster, int bmax, int emax, int tmax, int *out);
+                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate,
+                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                               cudaStream_t stream);

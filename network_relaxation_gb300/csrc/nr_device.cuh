@@ -111,6 +111,7 @@ constexpr int kDsmParts = 16;
 struct NetDsm {
     int bsub;
     int bo[kDsmParts + 1], to[kDsmParts + 1]; /* first bond / triple slot of each sub-block */
+    int be[kDsmParts + 1], te[kDsmParts + 1]; /* first bond / triple incidence entry of each sub-block */
     const int2 *bref;                         /* per bond slot: references of i, j */
     const int *bidx;                          /* per bond slot: bond index */
     const int4 *tref;                         /* per triple slot: references of h, j, k; triple index */
