@@ -98,9 +98,9 @@ def batch_kernel(precision, max_nodes):
 
 
 def committed_traffic(kernel):
-    """DRAM bytes per launch of `kernel` on this workload from the committed
-    ncu summary (profiles/c4_<kernel>_dram.txt, a line 'bytes_per_launch: X'),
-    or None."""
+    """DRAM bytes of one batch relaxation (all launches of `kernel` in it:
+    escalation relaunches included) from the committed ncu summary
+    (profiles/c4_<kernel>_dram.txt, a line 'bytes_per_launch: X'), or None."""
     path = os.path.join(ROOT, "profiles", "c4_%s_dram.txt" % kernel)
     if not os.path.exists(path):
         return None
@@ -319,6 +319,7 @@ def main():
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     kernel_ms = []
+    launches = 0
     barrier()
     t0 = time.perf_counter()
     ev0.record(stream)
@@ -327,6 +328,7 @@ def main():
         check(lib.nr_batch_set_positions(batch._h, dptr(start_dev), C.c_void_p(sp)), "reset")
         k0.record(stream)
         check(lib.nr_batch_relax(batch._h, C.byref(prm), reps_arr, C.c_void_p(sp)), "relax")
+        launches += lib.nr_batch_last_launches(batch._h)
         k1.record(stream)
         k1.synchronize()
         kernel_ms.append(k0.elapsed_time(k1))
@@ -383,7 +385,7 @@ def main():
                        "parallelism": "one batch per GPU" if world > 1 else "single GPU"},
             "e2e": {"value": total_nets / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e2e_steps, "ms_per_step": e2e_step_ms},
-            "gpu_launches": args.steps,
+            "gpu_launches": launches,
             "profiling_case": ({"largest": args.largest, "max_steps": args.max_steps} if profiling_case else None),
             "node_iter_per_s": world * node_iters / (ms / 1e3),
             "iterations": {"p50": float(np.median(steps)), "p99": float(np.percentile(steps, 99)),

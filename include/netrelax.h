@@ -272,6 +272,10 @@ int nr_batch_create(int n, const nr_host_network *const *nets, const double *ks,
                     nr_batch **out);
 int nr_batch_destroy(nr_batch *b);
 int nr_batch_size(const nr_batch *b);
+/* Kernel launches the last nr_batch_relax made on this batch (one, plus one
+ * per escalation of long-running networks to larger thread-block clusters).
+ * No counterpart in the reference, which relaxes one network at a time. */
+int nr_batch_last_launches(const nr_batch *b);
 int nr_batch_total_points(const nr_batch *b);
 /* Positions of all networks, concatenated in network order (host or
  * device pointer). */

@@ -99,6 +99,7 @@ SIGNATURES = {
     "nr_batch_create": (C.c_int, [C.c_int, C.POINTER(P), c_double_p, c_double_p, P, C.POINTER(P)]),
     "nr_batch_destroy": (C.c_int, [P]),
     "nr_batch_size": (C.c_int, [P]),
+    "nr_batch_last_launches": (C.c_int, [P]),
     "nr_batch_total_points": (C.c_int, [P]),
     "nr_batch_set_positions": (C.c_int, [P, c_double_p, P]),
     "nr_batch_get_positions": (C.c_int, [P, c_double_p, P]),

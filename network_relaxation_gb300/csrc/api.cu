@@ -83,6 +83,7 @@ struct DeviceSet {
     std::vector<NetDsm> dsm;
     NetDsm *dsm_array = nullptr;
     bool dsm_ok = true;
+    int launches = 0; /* kernel launches of the last batch relaxation */
     ~DeviceSet() {
         if (arena) cudaFree(arena);
     }
@@ -428,7 +429,7 @@ struct DsmPlan {
  * slices go to shared memory as well when they fit too (NR_DSM_RESIDENT=0
  * keeps them in global memory).  False when the batch has no layout,
  * NR_MIX_KERNEL=l2 asks for the global-memory kernels, or nothing fits. */
-static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl) {
+static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl, const std::vector<int> *subset = nullptr) {
     const char *k = getenv("NR_MIX_KERNEL");
     if (!S.dsm_ok || (k && strcmp(k, "l2") == 0)) return false;
     const char *rk = getenv("NR_DSM_RESIDENT");
@@ -438,7 +439,9 @@ static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl) {
         if (forced ? C != forced : C < least) continue;
         const int spr = kDsmParts / C;
         int bm = 0, em = 0, tm = 0, ebm = 0, etm = 0;
-        for (int i = 0; i < S.n_nets; ++i) {
+        const int count = subset ? (int)subset->size() : S.n_nets;
+        for (int j = 0; j < count; ++j) {
+            const int i = subset ? (*subset)[j] : j;
             const NetDsm &m = S.dsm[i];
             const NetDev &d = S.dev[i];
             bm = std::max(bm, spr * m.bsub);
@@ -489,6 +492,7 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
         NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, pl.C, pl.bmax, pl.emax, pl.tmax, pl.ebmax,
                                      pl.etmax, pl.resident, last ? 0.0 : frac, to_dev(prm), S.queue, order_dev,
                                      stream));
+        S.launches++;
         if (last) return NR_OK;
         st.resize(S.n_nets);
         NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
@@ -498,7 +502,7 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
             if (st[i].yielded) next.push_back(i);
         if (next.empty()) return NR_OK;
         DsmPlan p2;
-        if (!dsm_plan(S, 2 * pl.C, 0, p2)) return fail(NR_ERR_CUDA, "escalation: no cluster plan");
+        if (!dsm_plan(S, 2 * pl.C, 0, p2, &next)) return fail(NR_ERR_CUDA, "escalation: no cluster plan");
         NR_CUDA_TRY(cudaMemcpyAsync(S.order2, next.data(), sizeof(int) * next.size(), cudaMemcpyHostToDevice, stream));
         n_run = (int)next.size();
         order_dev = S.order2;
@@ -508,6 +512,7 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
 
 static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
+    S.launches = 0;
     if (prm.precision == NR_MIXED) {
         const char *env = getenv("NR_CLUSTER");
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
@@ -515,16 +520,20 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
         if (dsm_plan(S, env ? cluster : 0, cluster, pl)) {
             const int st = relax_dsm_phases(S, prm, pl, stream);
             if (st != NR_OK) return st;
-        } else if (cluster > 1)
+        } else if (cluster > 1) {
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
-        else
+            S.launches++;
+        } else {
             NR_CUDA_TRY(
                 launch_mixed_batch(S.dev_array, S.n_nets, S.max_nodes, to_dev(prm), S.queue, S.order, stream));
+            S.launches++;
+        }
     } else {
         int max_blocks = 0;
         NR_CUDA_TRY(fp64_batch_max_blocks(&max_blocks));
         const int blocks = std::max(1, std::min(S.n_nets, max_blocks));
         NR_CUDA_TRY(launch_fp64_batch(S.dev_array, S.n_nets, to_dev(prm), S.queue, blocks, stream));
+        S.launches++;
     }
     std::vector<FireState> st(S.n_nets);
     NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
@@ -783,6 +792,7 @@ int nr_batch_destroy(nr_batch *b) {
     return NR_OK;
 }
 int nr_batch_size(const nr_batch *b) { return b ? b->set.n_nets : 0; }
+int nr_batch_last_launches(const nr_batch *b) { return b ? b->set.launches : 0; }
 int nr_batch_total_points(const nr_batch *b) { return b ? (int)b->set.total_nodes : 0; }
 
 int nr_batch_set_positions(nr_batch *b, const double *host_xy, void *stream) {
