@@ -378,9 +378,5 @@ int nr_lsrelax_main(int argc, char **argv) {
     return rc < 0 ? 1 : 0;
 }
 
-int nr_gen_mikado(int, double, double, double, uint64_t, nr_host_network **out) {
-    if (out) *out = nullptr;
-    return fail(NR_ERR_INVALID, "nr_gen_mikado is not available in this build");
-}
 
 }  // extern "C"

@@ -138,3 +138,213 @@ extern "C" int nr_gen_lattice(int nx, int ny, double p, double jitter, uint64_t 
     *out = net;
     return NR_OK;
 }
+
+namespace {
+
+/* One straight fiber after the cut at y = 0 and y = 1: endpoints in an
+ * unwrapped x frame (the periodic box is [0, 1) in x). */
+struct Fiber {
+    double ax, ay, bx, by;
+    bool cut_a, cut_b; /* end lies on y = 0 or y = 1 (a clamped boundary node) */
+};
+
+/* Crossing of segments p + t r and q + s w (t, s in [0, 1]); false when
+ * parallel or disjoint. */
+bool crossing(double px, double py, double rx, double ry, double qx, double qy, double wx, double wy, double &t,
+              double &s) {
+    const double den = rx * wy - ry * wx;
+    if (den == 0.0) return false;
+    const double dx = qx - px, dy = qy - py;
+    t = (dx * wy - dy * wx) / den;
+    s = (dx * ry - dy * rx) / den;
+    return t >= 0.0 && t <= 1.0 && s >= 0.0 && s <= 1.0;
+}
+
+double wrap01(double x) {
+    double v = x - std::floor(x);
+    return v >= 1.0 ? 0.0 : v;
+}
+
+}  // namespace
+
+extern "C" int nr_gen_mikado(int n_fibers, double fiber_len, double k0, double kappa0, uint64_t seed,
+                             nr_host_network **out) {
+    if (!out || n_fibers <= 0 || n_fibers > (1 << 24) || !(fiber_len > 0 && fiber_len < 0.5) || !(k0 > 0) ||
+        !(kappa0 >= 0))
+        return fail(NR_ERR_INVALID, "nr_gen_mikado: bad arguments");
+    *out = nullptr;
+    SplitMix64 rng(seed);
+    const double pi = 3.14159265358979323846;
+    std::vector<Fiber> fib;
+    fib.reserve(n_fibers);
+    for (int f = 0; f < n_fibers; ++f) {
+        const double cx = rng.uniform(), cy = rng.uniform(), th = pi * rng.uniform();
+        const double hx = 0.5 * fiber_len * std::cos(th), hy = 0.5 * fiber_len * std::sin(th);
+        Fiber g{cx - hx, cy - hy, cx + hx, cy + hy, false, false};
+        /* cut at y = 0 and y = 1 */
+        double t0 = 0.0, t1 = 1.0;
+        const double dy = g.by - g.ay;
+        if (dy != 0.0) {
+            const double ta = (0.0 - g.ay) / dy, tb = (1.0 - g.ay) / dy;
+            const double lo = std::min(ta, tb), hi = std::max(ta, tb);
+            t0 = std::max(t0, lo);
+            t1 = std::min(t1, hi);
+        } else if (g.ay < 0.0 || g.ay > 1.0) {
+            continue;
+        }
+        if (!(t1 > t0)) continue;
+        const double dx = g.bx - g.ax;
+        Fiber c{g.ax + t0 * dx, g.ay + t0 * dy, g.ax + t1 * dx, g.ay + t1 * dy, t0 > 0.0, t1 < 1.0};
+        if (c.cut_a) c.ay = (c.ay < 0.5) ? 0.0 : 1.0;
+        if (c.cut_b) c.by = (c.by < 0.5) ? 0.0 : 1.0;
+        fib.push_back(c);
+    }
+    const int nf = (int)fib.size();
+    /* nodes: position in the box and whether clamped; per fiber its nodes
+     * as (t, node, unwrapped x) */
+    std::vector<double> nx, ny;
+    std::vector<char> boundary;
+    struct Stop {
+        double t;
+        int node;
+        double xu;
+    };
+    std::vector<std::vector<Stop>> stops(nf);
+    auto add_node = [&](double x, double y, bool bnd) {
+        nx.push_back(wrap01(x));
+        ny.push_back(y);
+        boundary.push_back(bnd ? 1 : 0);
+        return (int)nx.size() - 1;
+    };
+    for (int f = 0; f < nf; ++f) {
+        const Fiber &c = fib[f];
+        if (c.cut_a) stops[f].push_back({0.0, add_node(c.ax, c.ay, true), c.ax});
+        if (c.cut_b) stops[f].push_back({1.0, add_node(c.bx, c.by, true), c.bx});
+    }
+    /* crossings: a uniform grid of cells at least one fiber long; a pair is
+     * tested in every cell both touch and kept only in the cell holding the
+     * crossing point */
+    const int ncx = std::max(1, (int)std::floor(1.0 / fiber_len)), ncy = ncx;
+    std::vector<std::vector<int>> cell((size_t)ncx * ncy);
+    auto cx_of = [&](double x) { return std::min(ncx - 1, (int)(wrap01(x) * ncx)); };
+    auto cy_of = [&](double y) { return std::min(ncy - 1, std::max(0, (int)(y * ncy))); };
+    for (int f = 0; f < nf; ++f) {
+        const Fiber &c = fib[f];
+        const double x0 = std::min(c.ax, c.bx), x1 = std::max(c.ax, c.bx);
+        const double y0 = std::min(c.ay, c.by), y1 = std::max(c.ay, c.by);
+        const int i0 = (int)std::floor(x0 * ncx), i1 = (int)std::floor(x1 * ncx);
+        const int j0 = cy_of(y0), j1 = cy_of(y1);
+        for (int i = i0; i <= i1; ++i)
+            for (int j = j0; j <= j1; ++j) cell[(size_t)(((i % ncx) + ncx) % ncx) * ncy + j].push_back(f);
+    }
+    for (int ci = 0; ci < ncx; ++ci)
+        for (int cj = 0; cj < ncy; ++cj) {
+            const std::vector<int> &lst = cell[(size_t)ci * ncy + cj];
+            for (size_t a = 0; a < lst.size(); ++a)
+                for (size_t b = a + 1; b < lst.size(); ++b) {
+                    const int f = std::min(lst[a], lst[b]), g = std::max(lst[a], lst[b]);
+                    if (f == g) continue;
+                    const Fiber &F = fib[f], &G = fib[g];
+                    for (int sh = -1; sh <= 1; ++sh) {
+                        double t, s;
+                        if (!crossing(F.ax, F.ay, F.bx - F.ax, F.by - F.ay, G.ax + sh, G.ay, G.bx - G.ax, G.by - G.ay,
+                                      t, s))
+                            continue;
+                        const double px = F.ax + t * (F.bx - F.ax), py = F.ay + t * (F.by - F.ay);
+                        if (cx_of(px) != ci || cy_of(py) != cj) break;
+                        const int node = add_node(px, py, false);
+                        stops[f].push_back({t, node, px});
+                        stops[g].push_back({s, node, px - sh});
+                        break;
+                    }
+                }
+        }
+    /* segments between consecutive stops; dangling ends pruned repeatedly */
+    struct Seg {
+        int a, b, fiber;
+        double dxu, dyu; /* b - a in the fiber's unwrapped frame */
+    };
+    std::vector<Seg> seg;
+    for (int f = 0; f < nf; ++f) {
+        std::vector<Stop> &st = stops[f];
+        std::sort(st.begin(), st.end(), [](const Stop &x, const Stop &y) { return x.t < y.t; });
+        for (size_t k = 1; k < st.size(); ++k)
+            seg.push_back({st[k - 1].node, st[k].node, f, st[k].xu - st[k - 1].xu, ny[st[k].node] - ny[st[k - 1].node]});
+    }
+    const int nn = (int)nx.size();
+    std::vector<std::vector<int>> adj(nn);
+    for (int e = 0; e < (int)seg.size(); ++e) {
+        adj[seg[e].a].push_back(e);
+        adj[seg[e].b].push_back(e);
+    }
+    std::vector<char> seg_alive(seg.size(), 1), node_alive(nn, 1);
+    std::vector<int> deg(nn);
+    std::vector<int> work;
+    for (int v = 0; v < nn; ++v) {
+        deg[v] = (int)adj[v].size();
+        if (deg[v] == 0 || (deg[v] == 1 && !boundary[v])) work.push_back(v);
+    }
+    while (!work.empty()) {
+        const int v = work.back();
+        work.pop_back();
+        if (!node_alive[v]) continue;
+        node_alive[v] = 0;
+        for (int e : adj[v]) {
+            if (!seg_alive[e]) continue;
+            seg_alive[e] = 0;
+            const int o = seg[e].a == v ? seg[e].b : seg[e].a;
+            if (--deg[o] == 0 || (deg[o] == 1 && !boundary[o])) work.push_back(o);
+        }
+    }
+    /* renumber the surviving nodes by y (then x): consecutive node blocks are
+     * horizontal bands */
+    std::vector<int> keep;
+    for (int v = 0; v < nn; ++v)
+        if (node_alive[v]) keep.push_back(v);
+    std::stable_sort(keep.begin(), keep.end(), [&](int a, int b) { return ny[a] < ny[b] || (ny[a] == ny[b] && nx[a] < nx[b]); });
+    if (keep.empty()) return fail(NR_ERR_INVALID, "nr_gen_mikado: no connected network (too few fibers)");
+    std::vector<int> id(nn, -1);
+    auto *net = new nr_host_network();
+    net->n_points = (int)keep.size();
+    net->offset = 1.0;
+    net->points.resize(2 * keep.size());
+    for (size_t k = 0; k < keep.size(); ++k) {
+        id[keep[k]] = (int)k;
+        net->points[2 * k] = nx[keep[k]];
+        net->points[2 * k + 1] = ny[keep[k]];
+    }
+    auto wrap_of = [&](int i1, int i2, double dxu) {
+        return (int)std::lround(dxu - (net->points[2 * i2] - net->points[2 * i1]));
+    };
+    std::vector<int> seg_bond(seg.size(), -1);
+    for (size_t e = 0; e < seg.size(); ++e) {
+        if (!seg_alive[e]) continue;
+        const int i1 = id[seg[e].a], i2 = id[seg[e].b];
+        const int w = wrap_of(i1, i2, seg[e].dxu);
+        seg_bond[e] = net->n_edges();
+        net->edge_ij.push_back(i1);
+        net->edge_ij.push_back(i2);
+        net->edge_wrap.push_back((signed char)w);
+        const double l0 = rest_length(net->points, i1, i2, w, 1.0);
+        net->edge_l0.push_back(l0);
+        net->bond_k.push_back(k0 / l0);
+    }
+    /* triples: consecutive surviving segments of a fiber */
+    for (size_t e = 1; e < seg.size(); ++e) {
+        const Seg &s1 = seg[e - 1], &s2 = seg[e];
+        if (s1.fiber != s2.fiber || !seg_alive[e - 1] || !seg_alive[e] || s1.b != s2.a) continue;
+        const int h = id[s1.b], j = id[s1.a], k = id[s2.b];
+        const int wj = wrap_of(h, j, -s1.dxu), wk = wrap_of(h, k, s2.dxu);
+        net->tri_hjk.push_back(h);
+        net->tri_hjk.push_back(j);
+        net->tri_hjk.push_back(k);
+        net->tri_wrap.push_back((signed char)wj);
+        net->tri_wrap.push_back((signed char)wk);
+        const double lbar = 0.5 * (net->edge_l0[seg_bond[e - 1]] + net->edge_l0[seg_bond[e]]);
+        net->tri_kb.push_back(kappa0 / lbar);
+        net->tri_phi0.push_back(rest_phi0(net->points, h, j, k, wj, wk, 1.0));
+    }
+    nr::y_range(net->points, net->miny, net->maxy);
+    *out = net;
+    return NR_OK;
+}

@@ -167,3 +167,21 @@ def test_run_fire_md_dropin(cuda):
     assert np.array_equal(d_pos.cpu().numpy().reshape(-1, 2), xo)
     assert np.array_equal(d_f.cpu().numpy().reshape(-1, 2), Fo)
     assert report == [orep.rms_force, orep.e_stretch, orep.e_bend]
+
+
+def test_relax_bitwise_mikado(cuda):
+    """C3-type network (Mikado fibres: per-bond k = 1/l0, per-triple kb and
+    rest angles, x-periodic wraps): one shear increment, FP64 relaxation
+    identical to the oracle.  dt_max follows the stiffest bond."""
+    h = nr.HostNetwork.mikado(300, 0.1, 1.0, 1e-3, 7)
+    a = h.arrays()
+    prm = dict(FIRE, dt_max=0.1 * float(np.sqrt(a["edge_l0"].min())))
+    H = a["maxy"] - a["miny"]
+    net = nr.Network(h, ks=1.0, kb=1.0)
+    net.affine_displace(a["miny"], H, 0.01 * H, 0.0)
+    rep = net.relax(nr.fire_params(fcut=1e-10, criterion="max", **prm))
+    x0 = oracle.affine_displace(a["points"], a["miny"], H, 0.01 * H, 0.0)
+    xo, vo, Fo, orep = oracle.Model(a, 1.0, 1.0).fire(x0, oracle.params(fcut=1e-10, criterion="max", **prm))
+    assert rep.status == nr.NR_OK and rep.steps == orep.steps
+    assert np.array_equal(net.positions(), xo)
+    assert rep.e_stretch == orep.e_stretch and rep.e_bend == orep.e_bend

@@ -158,3 +158,24 @@ def test_mixed_escalation(cuda, escalate, monkeypatch):
         m = oracle.Model(a, 1.0, kb[i])
         assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
         assert m.energies(x) == (reps[i].e_stretch, reps[i].e_bend)
+
+
+def test_mixed_mikado_certified(cuda):
+    """Mixed precision on Mikado networks (per-item stiffness, wraps, very
+    short segments): a batch of two, certified by the oracle's FP64 force.
+    (Mikado networks whose shortest segments are stiffer than dt_max resolves
+    diverge in FP64 as well; with dt_max = 0.05 sqrt(l0_min) these two
+    relax in the oracle in 78K and 134K steps.)"""
+    hosts = [nr.HostNetwork.mikado(300, 0.1, 1.0, 1e-3, s) for s in (7, 8)]
+    arrs = [h.arrays() for h in hosts]
+    dt_max = 0.05 * float(np.sqrt(min(a["edge_l0"].min() for a in arrs)))
+    b = nr.Batch(hosts, 1.0, np.ones(2))
+    b.affine_displace(0.01 * (b.maxy - b.miny), 0.0)
+    reps = b.relax(nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **dict(FIRE, dt_max=dt_max)))
+    X = b.positions()
+    for i, a in enumerate(arrs):
+        assert reps[i].status == nr.NR_OK
+        x = X[b.offsets[i]:b.offsets[i + 1]]
+        m = oracle.Model(a, 1.0, 1.0)
+        assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+        assert m.energies(x) == (reps[i].e_stretch, reps[i].e_bend)
