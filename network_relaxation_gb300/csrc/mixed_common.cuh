@@ -218,20 +218,59 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
  * never changes during a relaxation and is read through the read-only
  * cache; anchor records and u are rewritten in the kernel and are not. */
 static __device__ void mixed_items(const NetDev &d, int first, int stride, const UView &u) {
-    if (d.use_bonds)
-        for (int b = first; b < d.n_edges; b += stride) {
-            const int4 r = __ldg(d.bond + b);
+    /* software pipelined: the next item's nodes and anchor record load
+     * while the current item computes */
+    if (d.use_bonds && first < d.n_edges) {
+        int b = first;
+        int4 r = __ldg(d.bond + b);
+        float4 ra = d.mb_data[b];
+        float2 sk = d.mb_sk[b];
+        for (;;) {
             float2 dh, dlo;
             u.diff2(r.y, r.x, dh, dlo);
-            d.bdf[b] = bond_dforce(d.mb_data[b], d.mb_sk[b], dh, dlo);
+            const int nb = b + stride;
+            int4 rn = r;
+            float4 ran = ra;
+            float2 skn = sk;
+            if (nb < d.n_edges) {
+                rn = __ldg(d.bond + nb);
+                ran = d.mb_data[nb];
+                skn = d.mb_sk[nb];
+            }
+            d.bdf[b] = bond_dforce(ra, sk, dh, dlo);
+            if (nb >= d.n_edges) break;
+            b = nb;
+            r = rn;
+            ra = ran;
+            sk = skn;
         }
-    if (d.use_triples)
-        for (int t = first; t < d.n_triples; t += stride) {
-            const int4 r = __ldg(d.tri + t);
+    }
+    if (d.use_triples && first < d.n_triples) {
+        int t = first;
+        int4 r = __ldg(d.tri + t);
+        float4 arms = d.mt_arms[t];
+        float2 pk = d.mt_pk[t];
+        for (;;) {
+            const float2 dj = u.diff(r.y, r.x), dk = u.diff(r.z, r.x);
+            const int nt = t + stride;
+            int4 rn = r;
+            float4 armsn = arms;
+            float2 pkn = pk;
+            if (nt < d.n_triples) {
+                rn = __ldg(d.tri + nt);
+                armsn = d.mt_arms[nt];
+                pkn = d.mt_pk[nt];
+            }
             float2 dFj, dFk;
-            tri_dforce(d.mt_arms[t], d.mt_pk[t], u.diff(r.y, r.x), u.diff(r.z, r.x), dFj, dFk);
+            tri_dforce(arms, pk, dj, dk, dFj, dFk);
             d.tdf[t] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+            if (nt >= d.n_triples) break;
+            t = nt;
+            r = rn;
+            arms = armsn;
+            pk = pkn;
         }
+    }
 }
 
 struct Team {
@@ -532,19 +571,20 @@ static __device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Coef 
 static __device__ Part mixed_pass_b(const NetDev &d, const Team &tm, float dtm) {
     float P = 0.f, V2 = 0.f, F2 = 0.f, M2 = 0.f, A = 0.f;
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
+        /* the node's independent loads first: one round trip */
         const unsigned c = __ldg(d.fcode + i);
+        const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
+        float2 v = d.vf[i];
         float2 F = make_float2(0.f, 0.f);
         if (c != 0) {
             float mag;
             const float2 dF = node_dforce(d, i, mag);
             A = fmaxf(A, mag);
-            const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
             F.x = ah.x + (al.x + dF.x);
             F.y = ah.y + (al.y + dF.y);
             if (!(c & 1)) F.x = 0.f;
             if (!(c & 2)) F.y = 0.f;
         }
-        float2 v = d.vf[i];
         v.x = fmaf(dtm, F.x, v.x);
         v.y = fmaf(dtm, F.y, v.y);
         d.vf[i] = v;
