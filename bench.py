@@ -255,6 +255,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
+    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5"],
+                    help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
+                         "first strain increment of its protocol, FIRE steps capped by --max-steps")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
@@ -265,6 +268,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "C4":
+        return single_network_arm(args)
 
     import torch
 
@@ -416,6 +421,79 @@ def main():
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+    return 0
+
+
+SINGLE = {
+    # name: (generator, kappa, strain increment (shear x, compression y) of the protocol's first step)
+    "C2": ("lattice 256x256, p=0.65, jitter 0.05, generator triples, seed 2", 1e-4, (0.01, 0.0)),
+    "C5": ("lattice 1024x1024, p=0.65, jitter 0.05, generator triples, seed 5", 1e-4, (0.0025, 0.0)),
+    "C3": ("Mikado, 15850 fibres of length 0.05, k = 1/l0, kb = kappa0/mean l0, seed 3", 1e-5, (0.0, -0.01)),
+}
+
+
+def single_network(nr, name):
+    if name == "C2":
+        return nr.HostNetwork.lattice(256, 256, 0.65, 0.05, 2, line_triples=True), 1e-4, 0.1
+    if name == "C5":
+        return nr.HostNetwork.lattice(1024, 1024, 0.65, 0.05, 5, line_triples=True), 1e-4, 0.1
+    h = nr.HostNetwork.mikado(15850, 0.05, 1.0, 1e-5, 3)
+    return h, 1.0, 0.05 * float(np.sqrt(h.arrays()["edge_l0"].min()))
+
+
+def single_network_arm(args):
+    """--workload C2|C3|C5: one large network relaxed by the cooperative
+    grid kernel (the whole GPU), FIRE steps capped: node-iterations/s."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    h, kb, dt_max = single_network(nr, args.workload)
+    info = h.info()
+    net = nr.Network(h, 1.0, kb)
+    H = net.maxy - net.miny
+    sx, sy = SINGLE[args.workload][2]
+    net.affine_displace(net.miny, H, sx * H, sy * H)
+    x0 = net.positions()
+    cap = min(args.max_steps, 2000)
+    prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
+                         max_steps=cap, criterion="max", precision=args.precision)
+    stream = torch.cuda.current_stream()
+    times, steps = [], 0
+    for s in range(args.warmup + args.steps):
+        net.set_positions(x0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rep = net.relax(prm)
+        e1.record(stream)
+        e1.synchronize()
+        if s >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+            steps = rep.steps
+    ms = float(np.mean(times))
+    n, e, t = info.n_points, info.n_edges / info.n_points, info.n_triples / info.n_points
+    bpn = (145 + 17 * e + 14 * t) if args.precision == "fp64" else (73 + 24 * e + 12 * t)
+    hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+           if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
+    rate = n * steps / (ms / 1e3)
+    achieved = bpn * rate / 1e9
+    if rank == 0:
+        print(json.dumps({
+            "metric": "node-iterations/s, one network (%s), first strain step, FIRE capped at %d steps"
+                      % (args.workload, cap),
+            "value": rate, "unit": "node-iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "us_per_fire_step": 1e3 * ms / steps, "higher_is_better": True, "scaling": "replicas",
+            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": {"workload": "%s: %s, N=%d E=%d T=%d" % (args.workload, SINGLE[args.workload][0], n,
+                                                                info.n_edges, info.n_triples),
+                       "precision": args.precision},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "kernel": "k_fire_grid_mixed" if args.precision == "mixed" else "k_fire_grid"},
+        }))
     return 0
 
 

@@ -73,7 +73,8 @@ struct DeviceSet {
     int *queue = nullptr;
     double4 *affine_prm = nullptr;
     double2 *x_all = nullptr, *v_all = nullptr, *f_all = nullptr;
-    float2 *u_hi_all = nullptr, *u_lo_all = nullptr, *vf_all = nullptr, *ff_all = nullptr;
+    float4 *u_all = nullptr;
+    float2 *vf_all = nullptr, *ff_all = nullptr;
     float2 *fa_hi_all = nullptr, *fa_lo_all = nullptr;
     int max_nodes = 0;
     int *order = nullptr; /* networks by decreasing size (largest start first) */
@@ -165,8 +166,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     const size_t x_off = img.add(sizeof(double2) * S.total_nodes);
     const size_t v_off = img.add(sizeof(double2) * S.total_nodes);
     const size_t f_off = img.add(sizeof(double2) * S.total_nodes);
-    const size_t uh_off = img.add(sizeof(float2) * S.total_nodes);
-    const size_t ul_off = img.add(sizeof(float2) * S.total_nodes);
+    const size_t u_off = img.add(sizeof(float4) * S.total_nodes);
     const size_t vf_off = img.add(sizeof(float2) * S.total_nodes);
     const size_t ff_off = img.add(sizeof(float2) * S.total_nodes);
     const size_t fah_off = img.add(sizeof(float2) * S.total_nodes);
@@ -245,8 +245,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     S.x_all = (double2 *)(base + x_off);
     S.v_all = (double2 *)(base + v_off);
     S.f_all = (double2 *)(base + f_off);
-    S.u_hi_all = (float2 *)(base + uh_off);
-    S.u_lo_all = (float2 *)(base + ul_off);
+    S.u_all = (float4 *)(base + u_off);
     S.vf_all = (float2 *)(base + vf_off);
     S.ff_all = (float2 *)(base + ff_off);
     S.fa_hi_all = (float2 *)(base + fah_off);
@@ -278,8 +277,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.x = S.x_all + S.node_off[i];
         d.v = S.v_all + S.node_off[i];
         d.f = S.f_all + S.node_off[i];
-        d.u_hi = S.u_hi_all + S.node_off[i];
-        d.u_lo = S.u_lo_all + S.node_off[i];
+        d.u = S.u_all + S.node_off[i];
         d.vf = S.vf_all + S.node_off[i];
         d.ff = S.ff_all + S.node_off[i];
         d.fa_hi = S.fa_hi_all + S.node_off[i];

@@ -11,20 +11,12 @@
 
 namespace nr {
 
-__device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p, float2 *s_u, int smem_nodes,
+__device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p, float4 *s_u, int smem_nodes,
                                         MixShared &sh) {
     const Team tm{0, 1};
-    UView u;
-    if (d.n <= smem_nodes) {
-        u.hi = s_u;
-        u.lo = s_u + smem_nodes;
-    } else {
-        u.hi = d.u_hi;
-        u.lo = d.u_lo;
-    }
+    const UView u{d.n <= smem_nodes ? s_u : d.u};
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
-        u.hi[i] = make_float2(0.f, 0.f);
-        u.lo[i] = make_float2(0.f, 0.f);
+        u.u[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         d.vf[i] = make_float2(0.f, 0.f);
     }
     MixScal s; /* meaningful in thread 0 only */
@@ -78,7 +70,7 @@ __device__ void relax_network_cta_mixed(const NetDev &d, const FireParamsDev &p,
 template <int NT>
 __global__ void __launch_bounds__(NT, 1) k_fire_batch_mixed(const NetDev *nets, int n_nets, FireParamsDev p,
                                                             int *queue, const int *order, int smem_nodes) {
-    extern __shared__ float2 s_u[];
+    extern __shared__ float4 s_u[];
     __shared__ MixShared sh;
     __shared__ int s_net;
     /* The network's descriptor is staged in shared memory: its pointer
@@ -135,10 +127,9 @@ __global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets
         __syncthreads();
         const NetDev &d = s_d;
         const Team tm{rank, C};
-        const UView u{d.u_hi, d.u_lo};
+        const UView u{d.u};
         for (int i = tm.first(); i < d.n; i += tm.stride()) {
-            u.hi[i] = make_float2(0.f, 0.f);
-            u.lo[i] = make_float2(0.f, 0.f);
+            u.u[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             d.vf[i] = make_float2(0.f, 0.f);
         }
         MixScal s; /* replicated in thread 0 of every CTA */
@@ -349,15 +340,14 @@ __global__ void __launch_bounds__(NT, 1) k_fire_grid_mixed(NetDev d, FireParamsD
     const Team tm{(int)blockIdx.x, (int)gridDim.x};
     const unsigned G = gridDim.x;
     FireState *st = d.st;
-    const UView u{d.u_hi, d.u_lo};
+    const UView u{d.u};
     /* d.part: FP64 anchor partials in [0, 2G), FP32 step totals after them */
     float *fpart = reinterpret_cast<float *>(d.part + 2 * (size_t)G);
     bool last;
     MixParams q; /* thread 0 of the last-arriving CTA uses it */
     if (threadIdx.x == 0) q = mix_params(p, d.sqrt_dof);
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
-        u.hi[i] = make_float2(0.f, 0.f);
-        u.lo[i] = make_float2(0.f, 0.f);
+        u.u[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         d.vf[i] = make_float2(0.f, 0.f);
     }
     double F2, M2, tF2, tM2;

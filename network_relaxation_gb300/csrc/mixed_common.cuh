@@ -159,14 +159,19 @@ __device__ __forceinline__ void u_diff2(float2 ah, float2 al, float2 bh, float2 
     dl = make_float2(ex + (al.x - bl.x), ey + (al.y - bl.y));
 }
 
-/* Displacement store: double-float xy per node, in shared or global memory. */
+/* Displacement store: double-float xy per node, {hi.x, hi.y, lo.x, lo.y},
+ * in shared or global memory (one 16-byte access per node). */
 struct UView {
-    float2 *hi, *lo;
+    float4 *u;
     __device__ __forceinline__ float2 diff(int a, int b) const { /* u_a - u_b */
-        return u_diff(hi[a], lo[a], hi[b], lo[b]);
+        const float4 ua = u[a], ub = u[b];
+        return u_diff(make_float2(ua.x, ua.y), make_float2(ua.z, ua.w), make_float2(ub.x, ub.y),
+                      make_float2(ub.z, ub.w));
     }
     __device__ __forceinline__ void diff2(int a, int b, float2 &dh, float2 &dl) const {
-        u_diff2(hi[a], lo[a], hi[b], lo[b], dh, dl);
+        const float4 ua = u[a], ub = u[b];
+        u_diff2(make_float2(ua.x, ua.y), make_float2(ua.z, ua.w), make_float2(ub.x, ub.y), make_float2(ub.z, ub.w),
+                dh, dl);
     }
 };
 
@@ -487,13 +492,13 @@ __device__ __forceinline__ void anchor_reduce(double F2, double M2, double *dslo
 /* Anchor step 1: X += u (exactly, in FP64), u = 0. */
 static __device__ void anchor_move(const NetDev &d, const Team &tm, const UView &u) {
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
-        const float2 h = u.hi[i], l = u.lo[i];
+        const float4 w = u.u[i];
+        const float2 h = make_float2(w.x, w.y), l = make_float2(w.z, w.w);
         double2 x = d.x[i];
         x.x = x.x + ((double)h.x + (double)l.x);
         x.y = x.y + ((double)h.y + (double)l.y);
         d.x[i] = x;
-        u.hi[i] = make_float2(0.f, 0.f);
-        u.lo[i] = make_float2(0.f, 0.f);
+        u.u[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
@@ -553,11 +558,10 @@ static __device__ void mixed_pass_a(const NetDev &d, const Team &tm, const Coef 
             if (c.zero_v) v = make_float2(0.f, 0.f);
         }
         if (!c.done) {
-            float2 h = u.hi[i], l = u.lo[i];
-            df_add(h.x, l.x, fmaf(c.dt, v.x, c.dtsq * F.x));
-            df_add(h.y, l.y, fmaf(c.dt, v.y, c.dtsq * F.y));
-            u.hi[i] = h;
-            u.lo[i] = l;
+            float4 w = u.u[i];
+            df_add(w.x, w.z, fmaf(c.dt, v.x, c.dtsq * F.x));
+            df_add(w.y, w.w, fmaf(c.dt, v.y, c.dtsq * F.y));
+            u.u[i] = w;
             v.x = fmaf(c.dtm, F.x, v.x);
             v.y = fmaf(c.dtm, F.y, v.y);
         }

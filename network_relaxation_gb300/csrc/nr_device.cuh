@@ -80,7 +80,8 @@ struct NetDev {
      * anchor x (global copy, used when it does not fit shared memory), FP32
      * velocity and force, double-float anchor force; per bond and per triple
      * the FP32 anchor record and the FP32 force change of the current pass */
-    float2 *u_hi, *u_lo, *vf, *ff, *fa_hi, *fa_lo;
+    float4 *u; /* {hi.x, hi.y, lo.x, lo.y}: one 16-byte load per node */
+    float2 *vf, *ff, *fa_hi, *fa_lo;
     /* anchor records are indexed by bond / triple, or by item slot in the
      * distributed-shared-memory kernel */
     float4 *mb_data; /* anchor vector i -> j, {hi.x, hi.y, lo.x, lo.y} */
