@@ -227,6 +227,33 @@ int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double k
                    int max_steps, int nmin, double report_data[3], int *step_count, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Post-relaxation analyses                                            */
+/* ------------------------------------------------------------------ */
+
+/* The computations of the reference's analysis programs, on the GPU, for a
+ * network given by its reference positions pos0 (2N doubles, xy) and a
+ * displacement field disp (2N doubles), bonds as in nr_run_fire_md
+ * (pair_list 2E ints, e_offsets E wrap codes, width = x period).  Arrays
+ * may be host or device memory; the calls return when the results are
+ * written.  Totals use the library's fixed summation tree (reproducible;
+ * the reference sums sequentially, so they agree to rounding).
+ *
+ * strain_calc.cpp:96-120 (get_strains): strains[b] = (l_final - l_initial)
+ * / l_initial, l_final from pos0 + disp. */
+int nr_bond_strains(int n_points, int npairs, double width, const double *pos0, const double *disp,
+                    const int *pair_list, const signed char *e_offsets, double *strains, void *stream);
+/* axial_contribution.cpp:64-70, 176-190: *energy = k/2 sum_b ((u_j - u_i)
+ * . r_hat_b)^2 with r_hat_b the unit bond vector in pos0. */
+int nr_linear_axial_energy(int n_points, int npairs, double width, double k, const double *pos0,
+                           const double *disp, const int *pair_list, const signed char *e_offsets, double *energy,
+                           void *stream);
+/* na_calc.cpp:308-327 (calc_na_val): *na = mean over nodes of
+ * |u - u_affine|^2, u_affine = (y - miny) (shear_strain, axial_strain),
+ * y from pos0. */
+int nr_nonaffinity(int n_points, const double *pos0, const double *disp, double miny, double axial_strain,
+                   double shear_strain, double *na, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* Energies without allocating                                         */
 /* ------------------------------------------------------------------ */
 

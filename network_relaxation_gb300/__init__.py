@@ -21,7 +21,7 @@ from ._capi import (NR_CRIT_MAX, NR_CRIT_RMS, NR_ERR_CAPACITY, NR_ERR_CUDA, NR_E
 __all__ = [
     "HostNetwork", "Network", "Batch", "fire_params", "read_network", "get_triples", "run_fire_md",
     "parse_batch_file", "do_relaxation_run", "relaxation_batch", "lsrelax_main", "get_file_lists", "lib",
-    "NetRelaxError", "FireParams", "Report",
+    "NetRelaxError", "FireParams", "Report", "get_strains", "linear_axial_energy", "calc_na_val",
 ]
 
 
@@ -332,6 +332,51 @@ class Batch:
         st = self._lib.nr_batch_relax(self._h, C.byref(params), reps, _stream(stream))
         check(st, "nr_batch_relax")
         return [reps[i] for i in range(self.n)]
+
+
+def _analysis_arrays(pos0, disp, edges):
+    p0 = np.ascontiguousarray(pos0, np.float64).reshape(-1, 2)
+    u = np.ascontiguousarray(disp, np.float64).reshape(-1, 2)
+    if u.shape != p0.shape:
+        raise ValueError("point and displacement count mismatch")
+    ij = w = None
+    if edges is not None:
+        ij = np.ascontiguousarray(edges[0], np.int32).reshape(-1, 2)
+        w = np.ascontiguousarray(edges[1], np.int8).reshape(-1)
+    return p0, u, ij, w
+
+
+def get_strains(points, edges, offset, disps, stream=None):
+    """get_strains (strain_calc.cpp:96-120) on the GPU: per-bond
+    (l_final - l_initial) / l_initial.  edges = (ij[E, 2], wrap[E])."""
+    p0, u, ij, w = _analysis_arrays(points, disps, edges)
+    out = np.empty(len(ij), np.float64)
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(_capi.load().nr_bond_strains(len(p0), len(ij), float(offset), vp(p0), vp(u), vp(ij), vp(w), vp(out),
+                                       _stream(stream)), "nr_bond_strains")
+    return out
+
+
+def linear_axial_energy(points, edges, offset, disps, k, stream=None):
+    """axial_contribution.cpp:64-70, 176-190 on the GPU: k/2 sum over bonds of
+    the squared projection of the relative displacement on the bond."""
+    p0, u, ij, w = _analysis_arrays(points, disps, edges)
+    e = C.c_double()
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(_capi.load().nr_linear_axial_energy(len(p0), len(ij), float(offset), float(k), vp(p0), vp(u), vp(ij),
+                                              vp(w), C.byref(e), _stream(stream)), "nr_linear_axial_energy")
+    return e.value
+
+
+def calc_na_val(points, disps, miny, axial_strain, shear_strain, stream=None):
+    """calc_na_val (na_calc.cpp:308-327) on the GPU: mean square deviation of
+    the displacement field from the affine one."""
+    p0, u, _, _ = _analysis_arrays(points, disps, None)
+    na = C.c_double()
+    vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(_capi.load().nr_nonaffinity(len(p0), vp(p0), vp(u), float(miny), float(axial_strain), float(shear_strain),
+                                      C.byref(na), _stream(stream)), "nr_nonaffinity")
+    return na.value
 
 
 def run_fire_md(num_dof, npairs, ntriples, width, ks, kb, d_pos, d_vel, d_forces, d_pair_list, d_lengths,

@@ -94,6 +94,9 @@ SIGNATURES = {
                            C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
     "nr_run_fire_md": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P, P, P, P, P, P,
                                  P, P, c_double_p, C.c_double, C.c_double, C.c_int, C.c_int, c_double_p, c_int_p, P]),
+    "nr_bond_strains": (C.c_int, [C.c_int, C.c_int, C.c_double, P, P, P, P, P, P]),
+    "nr_linear_axial_energy": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, c_double_p, P]),
+    "nr_nonaffinity": (C.c_int, [C.c_int, P, P, C.c_double, C.c_double, C.c_double, c_double_p, P]),
     "nr_energies_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P, P, P, P,
                                       P, P, P]),
     "nr_batch_create": (C.c_int, [C.c_int, C.POINTER(P), c_double_p, c_double_p, P, C.POINTER(P)]),

@@ -32,6 +32,7 @@ CUDA_UNITS = [
     ("fire_dsm.cu", ["--fmad=false"]),
     ("api.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
+    ("analysis.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["host_network.cpp", "generators.cpp", "driver.cpp"]
 

@@ -77,6 +77,11 @@ def lib():
         L.or_atan2.argtypes = [C.c_double, C.c_double]
         L.or_canon_sum.restype = C.c_double
         L.or_canon_sum.argtypes = [dp, C.c_long]
+        L.or_bond_strains.argtypes = [C.c_int, ip, bp, C.c_double, dp, dp, dp]
+        L.or_linear_axial_energy.restype = C.c_double
+        L.or_linear_axial_energy.argtypes = [C.c_int, ip, bp, C.c_double, C.c_double, dp, dp]
+        L.or_nonaffinity.restype = C.c_double
+        L.or_nonaffinity.argtypes = [C.c_int, dp, dp, C.c_double, C.c_double, C.c_double]
         L.or_forces.argtypes = [C.POINTER(OrModel), dp, dp]
         L.or_energies.argtypes = [C.POINTER(OrModel), dp, dp, dp]
         L.or_fire.argtypes = [C.POINTER(OrModel), dp, dp, dp, C.POINTER(OrParams), C.POINTER(OrReport)]
@@ -91,6 +96,14 @@ def lib():
 
 def _d(a):
     return a.ctypes.data_as(dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(ip)
+
+
+def _b(a):
+    return a.ctypes.data_as(bp)
 
 
 def read_network(path, want_triples=True):
@@ -219,6 +232,37 @@ def affine_displace(pos, miny, yrange, xdisp, ydisp):
 
 def atan2(y, x):
     return lib().or_atan2(float(y), float(x))
+
+
+def _edges(a):
+    ij = np.ascontiguousarray(a["edge_ij"], np.int32).reshape(-1, 2)
+    w = np.ascontiguousarray(a["edge_wrap"], np.int8)
+    return ij, w
+
+
+def bond_strains(a, pos0, disp):
+    """strain_calc.cpp:96-120 on network arrays a (edge_ij, edge_wrap, offset)."""
+    ij, w = _edges(a)
+    p0 = np.ascontiguousarray(pos0, np.float64)
+    u = np.ascontiguousarray(disp, np.float64)
+    out = np.empty(len(ij), np.float64)
+    lib().or_bond_strains(len(ij), _i(ij), _b(w), float(a["offset"]), _d(p0), _d(u), _d(out))
+    return out
+
+
+def linear_axial_energy(a, k, pos0, disp):
+    """axial_contribution.cpp:64-70, 176-190 (canonical sum)."""
+    ij, w = _edges(a)
+    p0 = np.ascontiguousarray(pos0, np.float64)
+    u = np.ascontiguousarray(disp, np.float64)
+    return lib().or_linear_axial_energy(len(ij), _i(ij), _b(w), float(a["offset"]), float(k), _d(p0), _d(u))
+
+
+def nonaffinity(pos0, disp, miny, axial_strain, shear_strain):
+    """na_calc.cpp:308-327 (canonical sum)."""
+    p0 = np.ascontiguousarray(pos0, np.float64)
+    u = np.ascontiguousarray(disp, np.float64)
+    return lib().or_nonaffinity(len(p0), _d(p0), _d(u), float(miny), float(axial_strain), float(shear_strain))
 
 
 def canon_sum(terms):

@@ -33,3 +33,13 @@ sed -E -e 's/([A-Za-z_][A-Za-z0-9_]*)<<<([^>]*)>>>\(/nr_ref_launch(\2, \1, /g' \
 "$CXX" -std=c++17 -O2 -fPIC -I "$HERE/refshim/include" -c "$HERE/refshim/ref_api.cpp" -o "$OUT/ref_api.o"
 "$CXX" -shared -o "$OUT/liblsr_ref.so" "$OUT/lsr_ref.o" "$OUT/ref_api.o"
 echo "build_ref: built $OUT/liblsr_ref.so"
+# The analysis programs strain_calc.cpp and axial_contribution.cpp need only
+# the standard library: built unchanged as executables.  (na_calc.cpp needs
+# Boost, which is absent: not built.)
+for prog in strain_calc axial_contribution; do
+    if "$CXX" -std=c++17 -O2 -w "$REF/src/$prog.cpp" -o "$OUT/$prog"; then
+        echo "build_ref: built $OUT/$prog"
+    else
+        echo "build_ref: $prog not built"
+    fi
+done

@@ -583,3 +583,55 @@ void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_pa
     for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
     free(th);
 }
+
+/* ----- post-relaxation analyses (strain_calc, axial_contribution, na_calc) ----- */
+
+void or_bond_strains(int n_edges, const int *edge_ij, const signed char *wrap, double width, const double *pos0,
+                     const double *disp, double *strains) {
+    for (int b = 0; b < n_edges; ++b) {
+        const int i1 = edge_ij[2 * b], i2 = edge_ij[2 * b + 1];
+        /* strain_calc.cpp:108-116, operation for operation */
+        const double dxi = pos0[2 * i2] + wrap[b] * width - pos0[2 * i1];
+        const double dyi = pos0[2 * i2 + 1] - pos0[2 * i1 + 1];
+        const double dxf = dxi + disp[2 * i2] - disp[2 * i1];
+        const double dyf = dyi + disp[2 * i2 + 1] - disp[2 * i1 + 1];
+        const double li = sqrt(dxi * dxi + dyi * dyi);
+        const double lf = sqrt(dxf * dxf + dyf * dyf);
+        strains[b] = (lf - li) / li;
+    }
+}
+
+double or_linear_axial_energy(int n_edges, const int *edge_ij, const signed char *wrap, double width, double k,
+                              const double *pos0, const double *disp) {
+    double *terms = (double *)malloc(sizeof(double) * (size_t)(n_edges > 0 ? n_edges : 1));
+    for (int b = 0; b < n_edges; ++b) {
+        const int i1 = edge_ij[2 * b], i2 = edge_ij[2 * b + 1];
+        /* axial_contribution.cpp:64-70 */
+        double dx = pos0[2 * i2] + width * wrap[b] - pos0[2 * i1];
+        double dy = pos0[2 * i2 + 1] - pos0[2 * i1 + 1];
+        const double length = sqrt(dx * dx + dy * dy);
+        dx /= length;
+        dy /= length;
+        /* axial_contribution.cpp:178-188 */
+        const double proj = (disp[2 * i2] - disp[2 * i1]) * dx + (disp[2 * i2 + 1] - disp[2 * i1 + 1]) * dy;
+        terms[b] = .5 * proj * proj;
+    }
+    const double e = or_canon_sum(terms, n_edges);
+    free(terms);
+    return e * k;
+}
+
+double or_nonaffinity(int n_points, const double *pos0, const double *disp, double miny, double axial_strain,
+                      double shear_strain) {
+    double *terms = (double *)malloc(sizeof(double) * (size_t)(n_points > 0 ? n_points : 1));
+    for (int i = 0; i < n_points; ++i) {
+        /* na_calc.cpp:313-322 */
+        const double y = pos0[2 * i + 1];
+        const double ux_a = disp[2 * i], uy_a = disp[2 * i + 1];
+        const double ux_e = (y - miny) * shear_strain, uy_e = (y - miny) * axial_strain;
+        terms[i] = (ux_a - ux_e) * (ux_a - ux_e) + (uy_a - uy_e) * (uy_a - uy_e);
+    }
+    const double na = or_canon_sum(terms, n_points);
+    free(terms);
+    return na / n_points;
+}

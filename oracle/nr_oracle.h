@@ -105,6 +105,21 @@ int or_sweep(const or_model *m, double *pos, double miny, double yrange, const o
 
 /* Relaxes n independent models in parallel on n_threads host threads (one
  * network per thread at a time).  Each network uses or_fire. */
+/* Post-relaxation analyses on reference positions pos0 and displacements
+ * disp (2N each, xy interleaved); edges as (i, j) pairs with wrap codes.
+ * strain_calc.cpp:96-120: per-bond (l_final - l_initial) / l_initial. */
+void or_bond_strains(int n_edges, const int *edge_ij, const signed char *wrap, double width, const double *pos0,
+                     const double *disp, double *strains);
+/* axial_contribution.cpp:64-70 (unit bond vectors from pos0) and :176-190
+ * (k/2 sum of the squared projections of the relative displacements); the
+ * per-bond terms summed with or_canon_sum, then times k. */
+double or_linear_axial_energy(int n_edges, const int *edge_ij, const signed char *wrap, double width, double k,
+                              const double *pos0, const double *disp);
+/* na_calc.cpp:308-327 (calc_na_val): mean over nodes of |u - u_affine|^2,
+ * u_affine = (y - miny) (shear, axial); terms summed with or_canon_sum. */
+double or_nonaffinity(int n_points, const double *pos0, const double *disp, double miny, double axial_strain,
+                      double shear_strain);
+
 void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_params *params, or_report *reps,
                    int n_threads);
 
