@@ -85,8 +85,15 @@ struct DeviceSet {
     NetDsm *dsm_array = nullptr;
     bool dsm_ok = true;
     int launches = 0; /* kernel launches of the last batch relaxation */
+    std::vector<int> order_host;
+    /* second stream and events for the concurrent single-CTA launch */
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     ~DeviceSet() {
         if (arena) cudaFree(arena);
+        if (side) cudaStreamDestroy(side);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
     }
 };
 
@@ -176,6 +183,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return nets[a]->n_points > nets[b]->n_points; });
     const size_t order_off = img.put(order.data(), order.size());
+    S.order_host = order;
     const size_t order2_off = img.add(sizeof(int) * n);
     const size_t st_off = img.add(sizeof(FireState) * n);
     const size_t q_off = img.add(256);
@@ -479,18 +487,78 @@ static double escalate_fraction() {
  * resumes them on clusters twice as large, up to 16 CTAs.  The soft
  * networks that need 10^5-10^6 steps thus end on the widest clusters
  * instead of holding the whole batch on 4 SMs each. */
+/* Networks of at most this many nodes run one per CTA beside the clusters
+ * in the first phase (NR_SOLO_NODES; 0 disables). */
+static int solo_nodes() {
+    const char *env = getenv("NR_SOLO_NODES");
+    return env ? std::max(0, atoi(env)) : 2304;
+}
+
+/* First-phase split of a size-ordered batch: the small networks (a suffix
+ * of the order) relax one per CTA on a second stream while the others
+ * relax on clusters.  A CTA handles a small network with 1.3-1.6x the
+ * throughput per SM of a cluster (no cluster barriers), and the single
+ * CTAs also use the SMs that clusters of C cannot tile.  SMs are divided by
+ * node count, the single CTAs' share weighted by that throughput gain.
+ * Returns the number of small networks (0: no split) and their plan. */
+static int solo_split(const DeviceSet &S, const DsmPlan &pl, DsmPlan &ps, int &cap_clusters) {
+    const int limit = solo_nodes();
+    if (pl.C < 2 || limit <= 0 || S.n_nets < 2) return 0;
+    std::vector<int> small;
+    for (int k = S.n_nets - 1; k >= 0 && S.dev[S.order_host[k]].n <= limit; --k) small.push_back(S.order_host[k]);
+    if (small.empty() || (int)small.size() == S.n_nets) return 0;
+    if (!dsm_plan(S, 1, 0, ps, &small)) return 0;
+    int maxa = 0, dev = 0, sms = 0;
+    if (dsm_max_active(pl.C, pl.bmax, pl.emax, pl.tmax, pl.ebmax, pl.etmax, pl.resident, &maxa) != cudaSuccess ||
+        maxa < 2)
+        return 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    double n_small = 0, n_all = 0;
+    for (int i = 0; i < S.n_nets; ++i) n_all += S.dev[i].n;
+    for (int i : small) n_small += S.dev[i].n;
+    const int want = (int)std::lround(0.6 * sms * n_small / n_all);
+    cap_clusters = std::max(1, std::min(maxa, (sms - want) / pl.C));
+    return (int)small.size();
+}
+
 static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl, cudaStream_t stream) {
     const double frac = escalate_fraction();
     int n_run = S.n_nets;
     const int *order_dev = S.order;
     std::vector<FireState> st;
     std::vector<int> next;
-    for (;;) {
+    DsmPlan ps;
+    int cap = 0;
+    const int n_small = solo_split(S, pl, ps, cap);
+    if (n_small > 0) {
+        if (!S.side) {
+            NR_CUDA_TRY(cudaStreamCreateWithFlags(&S.side, cudaStreamNonBlocking));
+            NR_CUDA_TRY(cudaEventCreateWithFlags(&S.ev_fork, cudaEventDisableTiming));
+            NR_CUDA_TRY(cudaEventCreateWithFlags(&S.ev_join, cudaEventDisableTiming));
+        }
+        n_run = S.n_nets - n_small;
+    }
+    for (int phase = 0;; ++phase) {
         const bool last = pl.C >= kDsmParts || frac <= 0;
+        /* the side stream starts after the work queued so far, not after
+         * the cluster launch below: the two kernels run concurrently */
+        if (phase == 0 && n_small > 0) NR_CUDA_TRY(cudaEventRecord(S.ev_fork, stream));
         NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, pl.C, pl.bmax, pl.emax, pl.tmax, pl.ebmax,
-                                     pl.etmax, pl.resident, last ? 0.0 : frac, to_dev(prm), S.queue, order_dev,
-                                     stream));
+                                     pl.etmax, pl.resident, last ? 0.0 : frac, phase == 0 ? cap : 0, to_dev(prm),
+                                     S.queue, order_dev, stream));
         S.launches++;
+        if (phase == 0 && n_small > 0) {
+            /* the small networks (the order's suffix) on single CTAs, on
+             * the side stream, with their own queue counters */
+            NR_CUDA_TRY(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
+            NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_small, 1, ps.bmax, ps.emax, ps.tmax, ps.ebmax,
+                                         ps.etmax, ps.resident, last ? 0.0 : frac, 0, to_dev(prm), S.queue + 4,
+                                         S.order + (S.n_nets - n_small), S.side));
+            S.launches++;
+            NR_CUDA_TRY(cudaEventRecord(S.ev_join, S.side));
+            NR_CUDA_TRY(cudaStreamWaitEvent(stream, S.ev_join, 0));
+        }
         if (last) return NR_OK;
         st.resize(S.n_nets);
         NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));

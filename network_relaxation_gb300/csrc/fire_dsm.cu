@@ -609,7 +609,7 @@ static cudaError_t dsm_config(int cluster, const DsmSizes &z, cudaLaunchConfig_t
 
 template <int NT, bool RES>
 static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster,
-                                 const DsmSizes &z, double escalate, const FireParamsDev &p, int *queue_dev,
+                                 const DsmSizes &z, double escalate, int cap, const FireParamsDev &p, int *queue_dev,
                                  const int *order_dev, cudaStream_t stream) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
@@ -617,7 +617,8 @@ static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, 
     cudaError_t e = dsm_config<NT, RES>(cluster, z, cfg, attr, &max_clusters);
     if (e != cudaSuccess) return e;
     if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
-    const int clusters = std::max(1, std::min(n_nets, max_clusters));
+    int clusters = std::max(1, std::min(n_nets, max_clusters));
+    if (cap > 0) clusters = std::min(clusters, cap);
     cfg.gridDim = dim3(clusters * cluster);
     cfg.stream = stream;
     const int yield_at = escalate > 0 ? std::max(1, (int)(escalate * clusters)) : 0;
@@ -637,20 +638,30 @@ static int dsm_threads(bool resident) {
 }
 
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate,
+                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate, int cap,
                              const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream) {
     if (cluster < 1 || cluster > kDsmParts || (kDsmParts % cluster) != 0) return cudaErrorInvalidValue;
     const DsmSizes z{bmax, emax, tmax, ebmax, etmax, resident};
     const bool wide = dsm_threads(resident != 0) == 1024;
     if (resident)
-        return wide ? launch_dsm_nt<1024, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev,
+        return wide ? launch_dsm_nt<1024, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
                                                 order_dev, stream)
-                    : launch_dsm_nt<512, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev,
+                    : launch_dsm_nt<512, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
                                                order_dev, stream);
-    return wide ? launch_dsm_nt<1024, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev, order_dev,
-                                             stream)
-                : launch_dsm_nt<512, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, p, queue_dev, order_dev,
-                                            stream);
+    return wide ? launch_dsm_nt<1024, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
+                                             order_dev, stream)
+                : launch_dsm_nt<512, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
+                                            order_dev, stream);
+}
+
+cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out) {
+    const DsmSizes z{bmax, emax, tmax, ebmax, etmax, resident};
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr[1];
+    const bool wide = dsm_threads(resident != 0) == 1024;
+    if (resident)
+        return wide ? dsm_config<1024, true>(cluster, z, cfg, attr, out) : dsm_config<512, true>(cluster, z, cfg, attr, out);
+    return wide ? dsm_config<1024, false>(cluster, z, cfg, attr, out) : dsm_config<512, false>(cluster, z, cfg, attr, out);
 }
 
 }  // namespace nr

@@ -37,8 +37,11 @@ size_t dsm_smem_limit();
  * saved (FireState.yielded) for a relaunch on larger clusters.  queue_dev:
  * 2 ints (next slot, idle clusters). */
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
-                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate,
+                             int emax, int tmax, int ebmax, int etmax, int resident, double escalate, int cap,
                              const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream);
+/* (launch_mixed_dsm: cap > 0 limits the number of clusters launched.)
+ * Clusters of the given plan that fit the GPU at once. */
+cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                               cudaStream_t stream);
