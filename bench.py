@@ -417,6 +417,9 @@ def main():
         v, rate, wall_cpu, desc = run_cpu_baseline(c4, n_threads, args.cpu_budget)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": n_threads, "kind": "port", "sample": desc,
                                 "node_iter_per_s": rate, "wall_s": wall_cpu}
+        v1, rate1, wall1, desc1 = run_cpu_baseline(c4, 1, min(5.0, args.cpu_budget))
+        line["cpu_single_thread"] = {"value": v1, "unit": UNIT, "cores": 1, "kind": "port", "sample": desc1,
+                                     "node_iter_per_s": rate1, "wall_s": wall1}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
