@@ -151,6 +151,8 @@ typedef struct {
     int status;       /* nr_status of this relaxation */
     int fp64_steps;   /* iterations taken in FP64 (mixed precision only) */
     int reserved;
+    double e_gel;     /* report_data[3] of network_mesh_relax.cu's run_fire_md
+                         (0 without a gel) */
 } nr_report;
 
 /* ------------------------------------------------------------------ */
@@ -198,6 +200,7 @@ typedef struct {
     int is_shear;
     int status;
     int fp64_steps;
+    double e_gel; /* gel energy (nr_mesh_sweep; 0 without a gel) */
 } nr_step_record;
 
 /* The compression-then-shear loops of do_relaxation_run
@@ -225,6 +228,98 @@ int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double k
                    const signed char *d_e_offsets, const int *d_triples, const signed char *d_t_offsets,
                    const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
                    int max_steps, int nmin, double report_data[3], int *step_count, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Networks embedded in a gel (src/network_mesh_relax.cu)              */
+/* ------------------------------------------------------------------ */
+
+/* A network-mesh composite is an nr_host_network with FEM triangles
+ * ("facets"), their areas, and pairs of duplicate vertices on the mesh's
+ * left and right edges whose forces are summed (the periodic seam of the
+ * gel).  The gel's energy per triangle, with F the deformation gradient
+ * from the reference state, is
+ *   smod A (|F|^2 / det F - 2) / 2 + bmod A (det F - 1 - dilation)^2 / 2
+ * (network_mesh_relax.cu:674-699); it acts when bmod > 0 (:908). */
+typedef struct {
+    int n_facets, n_areas, n_mesh_pairs; /* n_areas < n_facets only in a partially read file */
+    double minx, maxx;                   /* as computed by the reader (max starts at FLT_MIN) */
+} nr_mesh_info;
+
+/* read_network_mesh (network_mesh_relax.cu:72-230): header "N E F offset",
+ * N points, E edges "i j wrap", F facets "i j k", F areas (> 0), same
+ * parsing rules and error cases; the duplicate pairs are found as the
+ * reader finds them (:219-227: points within 1e-10 of minx paired with the
+ * point at x + offset, same y, to 1e-10).  On NR_ERR_PARSE the partially
+ * read network is still returned in *out. */
+int nr_read_network_mesh(const char *path, nr_host_network **out);
+/* Writes the format nr_read_network_mesh reads (%.17g, round-trips). */
+int nr_write_network_mesh(const nr_host_network *net, const char *path);
+/* Attaches facets / areas / duplicate pairs to a network; n_pairs < 0
+ * finds the pairs from the points as the reader does. */
+int nr_host_network_set_mesh(nr_host_network *net, int n_facets, const int *facets, const double *areas, int n_pairs,
+                             const int *mesh_pairs);
+/* Changes the x period.  do_relaxation_run scales it by sqrt(1 + dilation)
+ * before get_triples and the relaxation (network_mesh_relax.cu:1141). */
+int nr_host_network_set_offset(nr_host_network *net, double offset);
+void nr_host_network_mesh_info(const nr_host_network *net, nr_mesh_info *info);
+void nr_host_network_mesh_arrays(const nr_host_network *net, int *facets, double *areas, int *mesh_pairs);
+/* Synthetic composite (no reference counterpart; the reference ships no
+ * inputs): nx x ny unit grid plus a copy of column 0 at x = nx (paired with
+ * column 0), every cell split along its up-right diagonal into two gel
+ * triangles; network bonds right (periodic), up and up-right on columns
+ * 0..nx-1, each kept with probability p (SplitMix64 from seed); jitter as in
+ * nr_gen_lattice (column 0 and its copy move in y only). */
+int nr_gen_lattice_mesh(int nx, int ny, double p, double jitter, uint64_t seed, nr_host_network **out);
+
+/* Device networks created from a composite carry its triangles; their
+ * reference inverse matrices are computed at nr_network_create from the
+ * positions then (get_inv_mats, network_mesh_relax.cu:503-531, which the
+ * reference runs before dilating).  The gel stays off until
+ * nr_network_set_gel gives bmod > 0; gel-coupled networks relax on the FP64
+ * path (nr_relax with NR_MIXED returns NR_ERR_INVALID). */
+int nr_network_set_gel(nr_network *dnet, double smod, double bmod, double dilation);
+/* get_inv_mats again, from the current positions. */
+int nr_network_gel_inv_mats(nr_network *dnet, void *stream);
+/* dilate (network_mesh_relax.cu:796-806): x = minx + factor (x - minx),
+ * y likewise, over the N nodes. */
+int nr_dilate(nr_network *dnet, double minx, double miny, double factor, void *stream);
+/* {E_stretch, E_bend, E_gel}: axial_energies, bending_energies and
+ * gel_energy summed (network_mesh_relax.cu:1030-1056; the gel term as
+ * cublasDasum sums it, absolute values). */
+int nr_mesh_energies(nr_network *dnet, double energies[3], void *stream);
+/* The set-up of do_relaxation_run (network_mesh_relax.cu:1254-1274) on a
+ * network created from the composite with its period already scaled:
+ * dilate by sqrt(1 + dilation) about (minx, miny), net_bmod = 2 E_stretch /
+ * area / dilation^2 (0 when ks <= 0), preferred dilation dilation (bmod +
+ * net_bmod) / bmod (returned), and the gel set with it. */
+int nr_mesh_prepare(nr_network *dnet, double smod, double bmod, double dilation, double area, double *pref_dilation,
+                    void *stream);
+/* The compression then shear loops of network_mesh_relax.cu's
+ * do_relaxation_run (:1276-1376), strain mode (height = the dilated
+ * height): the first displacement is min, later ones inc, and compression
+ * lowers the height affine_displace uses as it goes.  Records as nr_sweep
+ * (compression rows: curr_disp 0, max_comp the compression). */
+int nr_mesh_sweep(nr_network *dnet, double miny, double height, const nr_fire_params *params, const double compr[3],
+                  const double shear[3], nr_step_record *records, int max_records, int *n_records,
+                  double *shear_positions, void *stream);
+
+/* get_inv_mats (network_mesh_relax.cu:503) on the reference's device
+ * arrays: d_facets 3 ints per triangle (valid node indices of d_pos, as
+ * the reference's kernel assumes), d_inv_mats 6 doubles per triangle.
+ * Asynchronous on stream. */
+int nr_get_inv_mats(int n_facets, const double *d_pos, const int *d_facets, double *d_inv_mats, void *stream);
+/* bool run_fire_md(...) of network_mesh_relax.cu:865: same arguments in the
+ * same order and meaning, minus the dim3 launch shapes.  report_data =
+ * {RMS F, E_stretch, E_bend, E_gel}.  Gel arrays are read only when
+ * bmod > 0.  FP64 path, RMS criterion; NR_OK / NR_NOT_CONVERGED where the
+ * reference returns true. */
+int nr_mesh_run_fire_md(int num_dof, int npairs, int ntriples, int nelems, double width, double ks, double kb,
+                        double smod, double bmod, double dilation, double *d_pos, double *d_vel, double *d_forces,
+                        const int *d_pair_list, const double *d_lengths, const signed char *d_e_offsets,
+                        const int *d_triples, const signed char *d_t_offsets, const int *d_elems,
+                        const double *d_areas, const double *d_inv_mats, const int *d_mpairs, int n_mpairs,
+                        const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
+                        int max_steps, int nmin, double report_data[4], int *step_count, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Post-relaxation analyses                                            */
@@ -361,6 +456,28 @@ int nr_relaxation_batch(const char *batch_file, int precision, int criterion);
  * -b batch [-x bx] [-y by] [-a] [-i], plus --precision fp64|mixed and
  * --criterion rms|max. */
 int nr_lsrelax_main(int argc, char **argv);
+
+/* nmrelax (network_mesh_relax.cu): the same driver for networks embedded in
+ * a gel.  Its batch file's second line is "ks kb bmod smod dilation" (at
+ * least three values; missing ones are 0), the network files are *.nmc. */
+typedef struct {
+    nr_batch_spec net;
+    double bmod, smod, dilation;
+} nr_mesh_batch_spec;
+/* parse_batch_file (network_mesh_relax.cu:413-500). */
+int nr_parse_mesh_batch_file(const char *path, nr_mesh_batch_spec *spec);
+/* do_relaxation_run (network_mesh_relax.cu:1095-1390) on one .nmc file:
+ * period scaled by sqrt(1 + dilation), triples, inverse matrices, dilation,
+ * preferred dilation (printed), compression and shear loops with the gel,
+ * and the log, edata (gel column and total) and NNN.pos files in the
+ * reference's formats.  FP64 path. */
+int nr_do_mesh_relaxation_run(const char *net_file, const char *log_name, const char *edata_name,
+                              const char *disp_base, const nr_mesh_batch_spec *spec, int criterion);
+/* relaxation_batch (network_mesh_relax.cu:1393-1421). */
+int nr_mesh_relaxation_batch(const char *batch_file, int criterion);
+/* The nmrelax command line (network_mesh_relax.cu:1424-1503), options as
+ * nr_lsrelax_main (--precision is accepted; the gel runs in FP64). */
+int nr_nmrelax_main(int argc, char **argv);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,8 @@ import numpy as np
 from . import _capi
 from ._capi import (NR_CRIT_MAX, NR_CRIT_RMS, NR_ERR_CAPACITY, NR_ERR_CUDA, NR_ERR_INVALID, NR_ERR_IO,  # noqa: F401
                     NR_ERR_NONFINITE, NR_ERR_OOM, NR_ERR_PARSE, NR_ERR_TIMEOUT, NR_FP64, NR_MIXED,
-                    NR_NOT_CONVERGED, NR_OK, BatchSpec, FireParams, NetRelaxError, Report, StepRecord, check)
+                    NR_NOT_CONVERGED, NR_OK, BatchSpec, FireParams, MeshBatchSpec, MeshInfo, NetRelaxError, Report,
+                    StepRecord, check)
 
 __all__ = [
     "HostNetwork", "Network", "Batch", "fire_params", "read_network", "get_triples", "run_fire_md",
@@ -109,6 +110,48 @@ class HostNetwork:
         return cls(out)
 
     @classmethod
+    def read_mesh(cls, path, strict=True):
+        """read_network_mesh (network_mesh_relax.cu:72): a network with its
+        gel triangles, areas and duplicate pairs."""
+        out = C.c_void_p()
+        st = _capi.load().nr_read_network_mesh(str(path).encode(), C.byref(out))
+        if st != NR_OK and (strict or not out.value):
+            if out.value:
+                _capi.load().nr_host_network_free(out)
+            raise NetRelaxError(st, "read_network_mesh(%s)" % path)
+        return cls(out)
+
+    @classmethod
+    def lattice_mesh(cls, nx, ny, p, jitter=0.0, seed=1):
+        """Network embedded in a gel on an nx x ny grid (nr_gen_lattice_mesh)."""
+        out = C.c_void_p()
+        check(_capi.load().nr_gen_lattice_mesh(int(nx), int(ny), float(p), float(jitter), int(seed), C.byref(out)),
+              "nr_gen_lattice_mesh")
+        return cls(out)
+
+    def set_mesh(self, facets, areas, mesh_pairs=None):
+        """Attaches gel triangles and areas; mesh_pairs None finds the
+        duplicate pairs as the reader does."""
+        f = np.ascontiguousarray(facets, dtype=np.int32).reshape(-1, 3)
+        a = np.ascontiguousarray(areas, dtype=np.float64)
+        mp = None if mesh_pairs is None else np.ascontiguousarray(mesh_pairs, dtype=np.int32).reshape(-1, 2)
+        check(_capi.load().nr_host_network_set_mesh(self._h, len(f), _ip(f), _dp(a), -1 if mp is None else len(mp),
+                                                    _ip(mp)), "set_mesh")
+        return self
+
+    def set_offset(self, offset):
+        check(_capi.load().nr_host_network_set_offset(self._h, float(offset)), "set_offset")
+        return self
+
+    def mesh_info(self):
+        info = _capi.MeshInfo()
+        _capi.load().nr_host_network_mesh_info(self._h, C.byref(info))
+        return info
+
+    def write_mesh(self, path):
+        check(_capi.load().nr_write_network_mesh(self._h, str(path).encode()), "nr_write_network_mesh")
+
+    @classmethod
     def mikado(cls, n_fibers, fiber_len=0.05, k0=1.0, kappa0=1e-5, seed=3):
         out = C.c_void_p()
         check(_capi.load().nr_gen_mikado(int(n_fibers), float(fiber_len), float(k0), float(kappa0), int(seed),
@@ -163,6 +206,12 @@ class HostNetwork:
                                             _bp(a["edge_wrap"]), _ip(a["tri_hjk"]), _bp(a["tri_wrap"]),
                                             _dp(a["bond_k"]), _dp(a["tri_kb"]), _dp(a["tri_phi0"]))
         a.update(offset=i.offset, miny=i.miny, maxy=i.maxy)
+        m = self.mesh_info()
+        a["facets"] = np.empty((m.n_facets, 3), np.int32)
+        a["areas"] = np.empty(m.n_areas, np.float64)
+        a["mpairs"] = np.empty((m.n_mesh_pairs, 2), np.int32)
+        _capi.load().nr_host_network_mesh_arrays(self._h, _ip(a["facets"]), _dp(a["areas"]), _ip(a["mpairs"]))
+        a.update(minx=m.minx, maxx=m.maxx)
         return a
 
     def fcodes(self):
@@ -211,6 +260,8 @@ class Network:
         self.n = self._lib.nr_network_n_points(out)
         info = host.info()
         self.miny, self.maxy = info.miny, info.maxy
+        m = host.mesh_info()
+        self.minx, self.maxx = m.minx, m.maxx
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -253,10 +304,38 @@ class Network:
         check(self._lib.nr_energies(self._h, C.byref(es), C.byref(eb), _stream(stream)), "nr_energies")
         return es.value, eb.value
 
-    def sweep(self, compr, shear, params=None, miny=None, yrange=None, keep_positions=False, max_records=100000,
-              stream=None):
-        """The compression-then-shear protocol of do_relaxation_run.  Returns
+    # ---- gel coupling (network_mesh_relax.cu) ----
+
+    def set_gel(self, smod, bmod, dilation):
+        check(self._lib.nr_network_set_gel(self._h, float(smod), float(bmod), float(dilation)), "nr_network_set_gel")
+
+    def gel_inv_mats(self, stream=None):
+        check(self._lib.nr_network_gel_inv_mats(self._h, _stream(stream)), "nr_network_gel_inv_mats")
+
+    def dilate(self, minx, miny, factor, stream=None):
+        check(self._lib.nr_dilate(self._h, float(minx), float(miny), float(factor), _stream(stream)), "nr_dilate")
+
+    def mesh_energies(self, stream=None):
+        """(E_stretch, E_bend, E_gel)."""
+        e = (C.c_double * 3)()
+        check(self._lib.nr_mesh_energies(self._h, e, _stream(stream)), "nr_mesh_energies")
+        return e[0], e[1], e[2]
+
+    def mesh_prepare(self, smod, bmod, dilation, area, stream=None):
+        """Dilate, then set the gel with the preferred dilation (returned)."""
+        pref = C.c_double()
+        check(self._lib.nr_mesh_prepare(self._h, float(smod), float(bmod), float(dilation), float(area),
+                                        C.byref(pref), _stream(stream)), "nr_mesh_prepare")
+        return pref.value
+
+    def mesh_sweep(self, compr, shear, height, params=None, miny=None, keep_positions=False, max_records=100000,
+                   stream=None):
+        """network_mesh_relax.cu's compression then shear protocol.  Returns
         (records, shear_positions or None)."""
+        return self._sweep(self._lib.nr_mesh_sweep, "nr_mesh_sweep", compr, shear, params, miny, height,
+                           keep_positions, max_records, stream)
+
+    def _sweep(self, fn, name, compr, shear, params, miny, yrange, keep_positions, max_records, stream):
         params = params or fire_params()
         miny = self.miny if miny is None else miny
         yrange = (self.maxy - self.miny) if yrange is None else yrange
@@ -270,11 +349,18 @@ class Network:
         recs = (StepRecord * n_est)()
         nrec = C.c_int()
         pos = np.empty((n_est, self.n, 2), np.float64) if keep_positions else None
-        st = self._lib.nr_sweep(self._h, float(miny), float(yrange), C.byref(params), _dp(c), _dp(s), recs, n_est,
-                                C.byref(nrec), _dp(pos), _stream(stream))
-        check(st, "nr_sweep")
+        st = fn(self._h, float(miny), float(yrange), C.byref(params), _dp(c), _dp(s), recs, n_est, C.byref(nrec),
+                _dp(pos), _stream(stream))
+        check(st, name)
         recs = [recs[i] for i in range(nrec.value)]
         return recs, (pos[:nrec.value] if pos is not None else None)
+
+    def sweep(self, compr, shear, params=None, miny=None, yrange=None, keep_positions=False, max_records=100000,
+              stream=None):
+        """The compression-then-shear protocol of do_relaxation_run.  Returns
+        (records, shear_positions or None)."""
+        return self._sweep(self._lib.nr_sweep, "nr_sweep", compr, shear, params, miny, yrange, keep_positions,
+                           max_records, stream)
 
 
 class Batch:
@@ -395,6 +481,32 @@ def run_fire_md(num_dof, npairs, ntriples, width, ks, kb, d_pos, d_vel, d_forces
     return st, [rep[0], rep[1], rep[2]], steps.value
 
 
+def mesh_run_fire_md(num_dof, npairs, ntriples, nelems, width, ks, kb, smod, bmod, dilation, d_pos, d_vel, d_forces,
+                     d_pair_list, d_lengths, d_e_offsets, d_triples, d_t_offsets, d_elems, d_areas, d_inv_mats,
+                     d_mpairs, n_mpairs, d_fcodes, fire_params_, mass, fcut, max_steps, nmin, stream=None):
+    """run_fire_md (network_mesh_relax.cu:865) on device pointers.  Returns
+    (status, report_data[4], step_count)."""
+    fp = (C.c_double * 5)(*[float(v) for v in fire_params_])
+    rep = (C.c_double * 4)()
+    steps = C.c_int()
+    vp = lambda p: C.c_void_p(int(p)) if p else None  # noqa: E731
+    st = _capi.load().nr_mesh_run_fire_md(
+        int(num_dof), int(npairs), int(ntriples), int(nelems), float(width), float(ks), float(kb), float(smod),
+        float(bmod), float(dilation), vp(d_pos), vp(d_vel), vp(d_forces), vp(d_pair_list), vp(d_lengths),
+        vp(d_e_offsets), vp(d_triples), vp(d_t_offsets), vp(d_elems), vp(d_areas), vp(d_inv_mats), vp(d_mpairs),
+        int(n_mpairs), vp(d_fcodes), fp, float(mass), float(fcut), int(max_steps), int(nmin), rep, C.byref(steps),
+        _stream(stream))
+    check(st, "mesh_run_fire_md")
+    return st, [rep[i] for i in range(4)], steps.value
+
+
+def get_inv_mats(n_facets, d_pos, d_facets, d_inv_mats, stream=None):
+    """get_inv_mats (network_mesh_relax.cu:503) on device pointers."""
+    vp = lambda p: C.c_void_p(int(p)) if p else None  # noqa: E731
+    check(_capi.load().nr_get_inv_mats(int(n_facets), vp(d_pos), vp(d_facets), vp(d_inv_mats), _stream(stream)),
+          "get_inv_mats")
+
+
 def parse_batch_file(path):
     """parse_batch_file (large_strain_relax.cu:297): a BatchSpec."""
     spec = BatchSpec()
@@ -442,3 +554,32 @@ def lsrelax_main(argv):
     args = ["lsrelax"] + list(argv)
     arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
     return _capi.load().nr_lsrelax_main(len(args), arr)
+
+
+def parse_mesh_batch_file(path):
+    """parse_batch_file (network_mesh_relax.cu:413): a MeshBatchSpec."""
+    spec = MeshBatchSpec()
+    check(_capi.load().nr_parse_mesh_batch_file(str(path).encode(), C.byref(spec)), "parse_mesh_batch_file",
+          ok=(NR_OK,))
+    return spec
+
+
+def do_mesh_relaxation_run(net_file, log_name, edata_name, disp_base, spec, criterion="rms"):
+    """do_relaxation_run (network_mesh_relax.cu:1095) with a MeshBatchSpec."""
+    crit = {"rms": NR_CRIT_RMS, "max": NR_CRIT_MAX}[criterion]
+    return check(_capi.load().nr_do_mesh_relaxation_run(str(net_file).encode(), str(log_name).encode(),
+                                                        str(edata_name).encode(), str(disp_base).encode(),
+                                                        C.byref(spec), crit), "do_mesh_relaxation_run")
+
+
+def mesh_relaxation_batch(batch_file, criterion="rms"):
+    """relaxation_batch (network_mesh_relax.cu:1393)."""
+    crit = {"rms": NR_CRIT_RMS, "max": NR_CRIT_MAX}[criterion]
+    return check(_capi.load().nr_mesh_relaxation_batch(str(batch_file).encode(), crit), "mesh_relaxation_batch")
+
+
+def nmrelax_main(argv):
+    """The nmrelax command line (network_mesh_relax.cu:1424)."""
+    args = ["nmrelax"] + list(argv)
+    arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
+    return _capi.load().nr_nmrelax_main(len(args), arr)

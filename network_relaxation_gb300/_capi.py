@@ -45,19 +45,28 @@ class FireParams(C.Structure):
 class Report(C.Structure):
     _fields_ = [("rms_force", C.c_double), ("e_stretch", C.c_double), ("e_bend", C.c_double),
                 ("max_force", C.c_double), ("steps", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int),
-                ("reserved", C.c_int)]
+                ("reserved", C.c_int), ("e_gel", C.c_double)]
 
 
 class StepRecord(C.Structure):
     _fields_ = [("curr_disp", C.c_double), ("max_comp", C.c_double), ("e_stretch", C.c_double),
                 ("e_bend", C.c_double), ("rms_force", C.c_double), ("max_force", C.c_double), ("steps", C.c_int),
-                ("is_shear", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int)]
+                ("is_shear", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int), ("e_gel", C.c_double)]
+
+
+class MeshInfo(C.Structure):
+    _fields_ = [("n_facets", C.c_int), ("n_areas", C.c_int), ("n_mesh_pairs", C.c_int), ("minx", C.c_double),
+                ("maxx", C.c_double)]
 
 
 class BatchSpec(C.Structure):
     _fields_ = [("base", C.c_char * 1024), ("tag", C.c_char * 256), ("ks", C.c_double), ("kb", C.c_double),
                 ("fire_params", C.c_double * 5), ("nmin", C.c_int), ("mass", C.c_double), ("fcut", C.c_double),
                 ("nmax", C.c_int), ("compr", C.c_double * 3), ("shear", C.c_double * 3), ("absolute", C.c_int)]
+
+
+class MeshBatchSpec(C.Structure):
+    _fields_ = [("net", BatchSpec), ("bmod", C.c_double), ("smod", C.c_double), ("dilation", C.c_double)]
 
 
 P = C.c_void_p
@@ -94,6 +103,25 @@ SIGNATURES = {
                            C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
     "nr_run_fire_md": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P, P, P, P, P, P,
                                  P, P, c_double_p, C.c_double, C.c_double, C.c_int, C.c_int, c_double_p, c_int_p, P]),
+    "nr_read_network_mesh": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "nr_write_network_mesh": (C.c_int, [P, C.c_char_p]),
+    "nr_host_network_set_mesh": (C.c_int, [P, C.c_int, c_int_p, c_double_p, C.c_int, c_int_p]),
+    "nr_host_network_set_offset": (C.c_int, [P, C.c_double]),
+    "nr_host_network_mesh_info": (None, [P, C.POINTER(MeshInfo)]),
+    "nr_host_network_mesh_arrays": (None, [P, c_int_p, c_double_p, c_int_p]),
+    "nr_gen_lattice_mesh": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, C.POINTER(P)]),
+    "nr_network_set_gel": (C.c_int, [P, C.c_double, C.c_double, C.c_double]),
+    "nr_network_gel_inv_mats": (C.c_int, [P, P]),
+    "nr_dilate": (C.c_int, [P, C.c_double, C.c_double, C.c_double, P]),
+    "nr_mesh_energies": (C.c_int, [P, c_double_p, P]),
+    "nr_mesh_prepare": (C.c_int, [P, C.c_double, C.c_double, C.c_double, C.c_double, c_double_p, P]),
+    "nr_mesh_sweep": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,
+                                C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
+    "nr_get_inv_mats": (C.c_int, [C.c_int, P, P, P, P]),
+    "nr_mesh_run_fire_md": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                      C.c_double, C.c_double, C.c_double, P, P, P, P, P, P, P, P, P, P, P, P,
+                                      C.c_int, P, c_double_p, C.c_double, C.c_double, C.c_int, C.c_int, c_double_p,
+                                      c_int_p, P]),
     "nr_bond_strains": (C.c_int, [C.c_int, C.c_int, C.c_double, P, P, P, P, P, P]),
     "nr_linear_axial_energy": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, c_double_p, P]),
     "nr_nonaffinity": (C.c_int, [C.c_int, P, P, C.c_double, C.c_double, C.c_double, c_double_p, P]),
@@ -115,6 +143,11 @@ SIGNATURES = {
                                        C.c_int, C.c_int]),
     "nr_relaxation_batch": (C.c_int, [C.c_char_p, C.c_int, C.c_int]),
     "nr_lsrelax_main": (C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
+    "nr_parse_mesh_batch_file": (C.c_int, [C.c_char_p, C.POINTER(MeshBatchSpec)]),
+    "nr_do_mesh_relaxation_run": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                            C.POINTER(MeshBatchSpec), C.c_int]),
+    "nr_mesh_relaxation_batch": (C.c_int, [C.c_char_p, C.c_int]),
+    "nr_nmrelax_main": (C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
 }
 
 _lib = None

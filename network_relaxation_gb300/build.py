@@ -18,6 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnetrelax.so")
 CLI = os.path.join(HERE, "lsrelax")
+MESH_CLI = os.path.join(HERE, "nmrelax")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -34,7 +35,7 @@ CUDA_UNITS = [
     ("noalloc.cu", ["--fmad=false"]),
     ("analysis.cu", ["--fmad=false"]),
 ]
-HOST_UNITS = ["host_network.cpp", "generators.cpp", "driver.cpp"]
+HOST_UNITS = ["host_network.cpp", "mesh_host.cpp", "generators.cpp", "driver.cpp"]
 
 
 def _run(cmd):
@@ -89,16 +90,17 @@ def build(verbose=False, force=False):
         tmp = LIB + ".tmp"
         _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)
-    main_src = os.path.join(CSRC, "lsrelax_main.cpp")
-    if force or not _newer(CLI, [main_src, LIB]):
-        _run([CXX, "-std=c++17", "-O2", "-I", INCLUDE, main_src, "-o", CLI, "-L", HERE, "-lnetrelax",
-              "-Wl,-rpath,$ORIGIN"])
+    for cli, main in ((CLI, "lsrelax_main.cpp"), (MESH_CLI, "nmrelax_main.cpp")):
+        main_src = os.path.join(CSRC, main)
+        if force or not _newer(cli, [main_src, LIB]):
+            _run([CXX, "-std=c++17", "-O2", "-I", INCLUDE, main_src, "-o", cli, "-L", HERE, "-lnetrelax",
+                  "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 
 def clean():
     shutil.rmtree(BUILD, ignore_errors=True)
-    for p in (LIB, CLI):
+    for p in (LIB, CLI, MESH_CLI):
         if os.path.exists(p):
             os.remove(p)
 

@@ -56,6 +56,7 @@ struct NetOff {
     size_t mb_data, mb_sk, bdf, mt_arms, mt_pk, tdf, bfrc, tfrc;
     size_t dsm_bref, dsm_bidx, dsm_tref, dsm_bent, dsm_tent;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
+    size_t elem, elem_inv, elem_area, efrc, eptr, eent, partner;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
 };
 
@@ -65,7 +66,11 @@ struct DeviceSet {
     long total_nodes = 0;
     std::vector<long> node_off;
     std::vector<NetDev> dev;
-    std::vector<double> miny, maxy;
+    std::vector<double> miny, maxy, minx;
+    /* gel coupling possible: every node is in at most one duplicate pair */
+    std::vector<char> gel_ok;
+    std::vector<NetGel> gel; /* host copies of the device array gel_array */
+    NetGel *gel_array = nullptr;
     char *arena = nullptr;
     size_t arena_bytes = 0;
     NetDev *dev_array = nullptr;
@@ -190,7 +195,9 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     const size_t aff_off = img.add(sizeof(double4) * n);
     const size_t dev_off = img.add(sizeof(NetDev) * n);
     const size_t dsm_off = img.add(sizeof(NetDsm) * n);
+    const size_t gel_off = img.add(sizeof(NetGel) * n);
     S.dsm.assign(n, NetDsm{});
+    S.gel.assign(n, NetGel{});
     std::vector<NetOff> off(n);
     for (int i = 0; i < n; ++i) {
         const nr_host_network &h = *nets[i];
@@ -232,13 +239,46 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.tdf = img.add(sizeof(float4) * (size_t)nt);
         o.bfrc = img.add(sizeof(double2) * (size_t)ne);
         o.tfrc = img.add(sizeof(double4) * (size_t)nt);
+        /* gel: triangles, inverse matrices (computed on the device after the
+         * upload), element terms, per-node element incidence (3 e + role,
+         * elements in index order) and duplicate partners */
+        const int nf = h.n_facets();
+        std::vector<int4> elem(nf);
+        for (int f = 0; f < nf; ++f) elem[f] = make_int4(h.facets[3 * f], h.facets[3 * f + 1], h.facets[3 * f + 2], 0);
+        std::vector<int> eptr((size_t)h.n_points + 1, 0), eent(3 * (size_t)nf), partner(h.n_points, -1);
+        for (int v : h.facets) eptr[v + 1]++;
+        for (int v = 0; v < h.n_points; ++v) eptr[v + 1] += eptr[v];
+        {
+            std::vector<int> fill(eptr.begin(), eptr.end() - 1);
+            for (int f = 0; f < nf; ++f)
+                for (int r = 0; r < 3; ++r) eent[fill[h.facets[3 * f + r]]++] = 3 * f + r;
+        }
+        bool pairs_ok = true;
+        for (int q = 0; q < h.n_mesh_pairs(); ++q) {
+            const int a = h.mesh_pairs[2 * q], b = h.mesh_pairs[2 * q + 1];
+            if (a == b || partner[a] >= 0 || partner[b] >= 0) {
+                pairs_ok = false;
+                continue;
+            }
+            partner[a] = b;
+            partner[b] = a;
+        }
+        S.gel_ok.push_back(pairs_ok);
+        S.minx.push_back(h.minx);
+        o.elem = img.put(elem.data(), elem.size());
+        o.elem_inv = img.add(sizeof(double) * 6 * (size_t)nf);
+        o.elem_area = img.put(h.areas.data(), h.areas.size());
+        o.efrc = img.add(sizeof(double4) * 3 * (size_t)nf);
+        o.eptr = img.put(eptr.data(), eptr.size());
+        o.eent = img.put(eent.data(), eent.size());
+        o.partner = img.put(partner.data(), partner.size());
         build_dsm_layout(h, inc, img, o, S.dsm[i]);
         if (S.dsm[i].bsub <= 0) S.dsm_ok = false;
         S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
         o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
-        const int tb = (ne + kTile - 1) / kTile, tt = (nt + kTile - 1) / kTile;
-        o.epart = img.add(sizeof(double) * 2 * (size_t)std::max(1, std::max(tb, tt)));
+        const int tb = (ne + kTile - 1) / kTile, tt = (nt + kTile - 1) / kTile, tg = (nf + kTile - 1) / kTile;
+        o.epart = img.add(sizeof(double) * 3 * (size_t)std::max(1, std::max(tb, std::max(tt, tg))));
         S.miny.push_back(h.miny);
         S.maxy.push_back(h.maxy);
     }
@@ -312,7 +352,20 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.part = (double *)(base + o.part);
         d.epart = (double *)(base + o.epart);
         d.st = S.st + i;
+        d.n_elems = h.n_facets();
+        d.use_gel = 0;
+        d.gel = (const NetGel *)(base + gel_off) + i;
+        NetGel &g = S.gel[i];
+        g.elem = (const int4 *)(base + o.elem);
+        g.elem_inv = (double *)(base + o.elem_inv);
+        g.elem_area = (const double *)(base + o.elem_area);
+        g.efrc = (double4 *)(base + o.efrc);
+        g.eptr = (const int *)(base + o.eptr);
+        g.eent = (const int *)(base + o.eent);
+        g.partner = (const int *)(base + o.partner);
     }
+    S.gel_array = (NetGel *)(base + gel_off);
+    memcpy(img.bytes.data() + gel_off, S.gel.data(), sizeof(NetGel) * n);
     for (int i = 0; i < n; ++i) {
         const NetOff &o = off[i];
         NetDsm &m = S.dsm[i];
@@ -326,8 +379,19 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     memcpy(img.bytes.data() + dsm_off, S.dsm.data(), sizeof(NetDsm) * n);
     memcpy(img.bytes.data() + dev_off, S.dev.data(), sizeof(NetDev) * n);
     NR_CUDA_TRY(cudaMemcpyAsync(S.arena, img.bytes.data(), S.arena_bytes, cudaMemcpyHostToDevice, stream));
+    /* get_inv_mats on the positions as uploaded (network_mesh_relax.cu:1250
+     * runs it before dilate) */
+    for (int i = 0; i < n; ++i)
+        NR_CUDA_TRY(launch_inv_mats((const double *)S.dev[i].x, (const int *)S.gel[i].elem, 4, S.dev[i].n_elems,
+                                    S.gel[i].elem_inv, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
     return NR_OK;
+}
+
+/* Energy launch width for network d. */
+static int energy_blocks(const NetDev &d, int sms) {
+    const int items = std::max(d.n_edges, std::max(d.n_triples, d.n_elems));
+    return std::max(1, std::min(2 * sms, (items + kTile - 1) / kTile * 2));
 }
 
 static FireParamsDev to_dev(const nr_fire_params &p) {
@@ -358,6 +422,7 @@ static void fill_report(const FireState &st, const NetDev &d, nr_report *rep) {
     rep->rms_force = st.fmag / d.sqrt_dof;
     rep->e_stretch = st.e_stretch;
     rep->e_bend = st.e_bend;
+    rep->e_gel = d.use_gel ? st.e_gel : 0.0;
     rep->max_force = st.maxf;
     rep->steps = st.step;
     rep->fp64_steps = st.fp64_steps;
@@ -383,12 +448,11 @@ static int relax_single_fp64(DeviceSet &S, int i, const nr_fire_params &prm, cud
     d.sub = sub;
     d.n_units = d.n_tiles * (8 / sub);
     int max_blocks = 0;
-    NR_CUDA_TRY(fp64_grid_max_blocks(sub, &max_blocks));
+    NR_CUDA_TRY(fp64_grid_max_blocks(sub, d.use_gel != 0, &max_blocks));
     const int blocks = std::max(1, std::min(d.n_units, max_blocks));
     NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
     NR_CUDA_TRY(launch_fp64_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
-    const int eblocks = std::max(1, std::min(2 * sms, (std::max(d.n_edges, d.n_triples) + kTile - 1) / kTile * 2));
-    NR_CUDA_TRY(launch_energies(d, eblocks, stream));
+    NR_CUDA_TRY(launch_energies(d, energy_blocks(d, sms), stream));
     FireState st;
     NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -412,9 +476,7 @@ static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStrea
     if ((size_t)5 * blocks > (size_t)4 * d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
     NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
     NR_CUDA_TRY(launch_mixed_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
-    const int sms = sm_count();
-    const int eblocks = std::max(1, std::min(2 * sms, (std::max(d.n_edges, d.n_triples) + kTile - 1) / kTile * 2));
-    NR_CUDA_TRY(launch_energies(d, eblocks, stream));
+    NR_CUDA_TRY(launch_energies(d, energy_blocks(d, sm_count()), stream));
     FireState st;
     NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
@@ -614,6 +676,138 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
     return worst;
 }
 
+/* Gel arrays of network_mesh_relax.cu's run_fire_md (device pointers). */
+struct GelArgs {
+    int nelems, n_mpairs;
+    double smod, bmod, dilation;
+    const int *d_elems;
+    const double *d_areas, *d_inv_mats;
+    const int *d_mpairs;
+};
+
+/* Moduli and preferred dilation of network 0 of S; the gel acts when
+ * bmod > 0 (network_mesh_relax.cu:908). */
+static int set_gel(DeviceSet &S, double smod, double bmod, double dilation) {
+    NetDev &dv = S.dev[0];
+    NetGel &g = S.gel[0];
+    if (bmod > 0 && !S.gel_ok[0])
+        return fail(NR_ERR_INVALID, "gel coupling: a vertex is in more than one duplicate pair (or paired with itself)");
+    g.smod = smod;
+    g.bmod = bmod;
+    g.gdil = dilation;
+    dv.use_gel = bmod > 0;
+    NR_CUDA_TRY(cudaMemcpy(S.gel_array, &g, sizeof(NetGel), cudaMemcpyHostToDevice));
+    NR_CUDA_TRY(cudaMemcpy(S.dev_array, &dv, sizeof(NetDev), cudaMemcpyHostToDevice));
+    return NR_OK;
+}
+
+/* run_fire_md of large_strain_relax.cu:596 (gel == nullptr) or of
+ * network_mesh_relax.cu:865: the caller's device arrays are copied into a
+ * device image of the network, relaxed by the FP64 path with the RMS
+ * criterion, and positions, velocities and forces copied back.
+ * report_data: {RMS F, E_s, E_b, E_gel}. */
+static int run_fire_md_impl(const char *who, int num_dof, int npairs, int ntriples, double width, double ks, double kb,
+                            double *d_pos, double *d_vel, double *d_forces, const int *d_pair_list,
+                            const double *d_lengths, const signed char *d_e_offsets, const int *d_triples,
+                            const signed char *d_t_offsets, const unsigned char *d_fcodes,
+                            const double fire_params[5], double mass, double fcut, int max_steps, int nmin,
+                            const GelArgs *gel, double report_data[4], int *step_count, void *stream) {
+    const bool use_gel = gel && gel->bmod > 0;
+    if (num_dof <= 0 || (num_dof & 1) || npairs < 0 || ntriples < 0 || !d_pos || !d_fcodes || !fire_params ||
+        !report_data || !step_count || (npairs > 0 && ks > 0 && (!d_pair_list || !d_lengths || !d_e_offsets)) ||
+        (ntriples > 0 && kb > 0 && (!d_triples || !d_t_offsets)) ||
+        (use_gel && (gel->nelems < 0 || gel->n_mpairs < 0 ||
+                     (gel->nelems > 0 && (!gel->d_elems || !gel->d_areas || !gel->d_inv_mats)) ||
+                     (gel->n_mpairs > 0 && !gel->d_mpairs))))
+        return fail(NR_ERR_INVALID, std::string(who) + ": bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = num_dof / 2;
+    nr_host_network h;
+    h.n_points = n;
+    h.offset = width;
+    h.points.resize(num_dof);
+    NR_CUDA_TRY(cudaMemcpyAsync(h.points.data(), d_pos, sizeof(double) * num_dof, cudaMemcpyDeviceToHost, s));
+    std::vector<unsigned char> fc(n);
+    NR_CUDA_TRY(cudaMemcpyAsync(fc.data(), d_fcodes, n, cudaMemcpyDeviceToHost, s));
+    if (ks > 0 && npairs > 0) {
+        h.edge_ij.resize(2 * (size_t)npairs);
+        h.edge_l0.resize(npairs);
+        h.edge_wrap.resize(npairs);
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_ij.data(), d_pair_list, sizeof(int) * 2 * npairs, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_l0.data(), d_lengths, sizeof(double) * npairs, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_wrap.data(), d_e_offsets, npairs, cudaMemcpyDeviceToHost, s));
+    }
+    if (kb > 0 && ntriples > 0) {
+        h.tri_hjk.resize(3 * (size_t)ntriples);
+        h.tri_wrap.resize(2 * (size_t)ntriples);
+        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_hjk.data(), d_triples, sizeof(int) * 3 * ntriples, cudaMemcpyDeviceToHost, s));
+        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_wrap.data(), d_t_offsets, 2 * (size_t)ntriples, cudaMemcpyDeviceToHost, s));
+    }
+    if (use_gel) {
+        h.facets.resize(3 * (size_t)gel->nelems);
+        h.areas.resize(gel->nelems);
+        h.mesh_pairs.resize(2 * (size_t)gel->n_mpairs);
+        if (gel->nelems > 0) {
+            NR_CUDA_TRY(cudaMemcpyAsync(h.facets.data(), gel->d_elems, sizeof(int) * 3 * (size_t)gel->nelems,
+                                        cudaMemcpyDeviceToHost, s));
+            NR_CUDA_TRY(cudaMemcpyAsync(h.areas.data(), gel->d_areas, sizeof(double) * gel->nelems,
+                                        cudaMemcpyDeviceToHost, s));
+        }
+        if (gel->n_mpairs > 0)
+            NR_CUDA_TRY(cudaMemcpyAsync(h.mesh_pairs.data(), gel->d_mpairs, sizeof(int) * 2 * (size_t)gel->n_mpairs,
+                                        cudaMemcpyDeviceToHost, s));
+    }
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < h.edge_ij.size(); ++i)
+        if (h.edge_ij[i] < 0 || h.edge_ij[i] >= n) return fail(NR_ERR_INVALID, std::string(who) + ": bond index out of range");
+    for (size_t i = 0; i < h.tri_hjk.size(); ++i)
+        if (h.tri_hjk[i] < 0 || h.tri_hjk[i] >= n) return fail(NR_ERR_INVALID, std::string(who) + ": triple index out of range");
+    for (size_t i = 0; i < h.facets.size(); ++i)
+        if (h.facets[i] < 0 || h.facets[i] >= n) return fail(NR_ERR_INVALID, std::string(who) + ": element index out of range");
+    for (size_t i = 0; i < h.mesh_pairs.size(); ++i)
+        if (h.mesh_pairs[i] < 0 || h.mesh_pairs[i] >= n) return fail(NR_ERR_INVALID, std::string(who) + ": pair index out of range");
+    y_range(h.points, h.miny, h.maxy);
+    DeviceSet S;
+    const nr_host_network *nets[1] = {&h};
+    const unsigned char *fcs[1] = {fc.data()};
+    int rc = build_set(1, nets, &ks, &kb, fcs, s, S);
+    if (rc != NR_OK) return rc;
+    if (use_gel) {
+        if (gel->nelems > 0)
+            NR_CUDA_TRY(cudaMemcpyAsync(S.gel[0].elem_inv, gel->d_inv_mats,
+                                        sizeof(double) * 6 * (size_t)gel->nelems, cudaMemcpyDeviceToDevice, s));
+        rc = set_gel(S, gel->smod, gel->bmod, gel->dilation);
+        if (rc != NR_OK) return rc;
+    }
+    nr_fire_params p;
+    p.alpha0 = fire_params[0];
+    p.falpha = fire_params[1];
+    p.dt_max = fire_params[2];
+    p.finc = fire_params[3];
+    p.fdec = fire_params[4];
+    p.nmin = nmin;
+    p.mass = mass;
+    p.fcut = fcut;
+    p.max_steps = max_steps;
+    p.criterion = NR_CRIT_RMS;
+    p.precision = NR_FP64;
+    rc = check_params(&p);
+    if (rc != NR_OK) return rc;
+    nr_report rep;
+    rc = relax_single_fp64(S, 0, p, s, &rep);
+    if (rc < 0) return rc;
+    NR_CUDA_TRY(cudaMemcpyAsync(d_pos, S.x_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    if (d_vel) NR_CUDA_TRY(cudaMemcpyAsync(d_vel, S.v_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    if (d_forces) NR_CUDA_TRY(cudaMemcpyAsync(d_forces, S.f_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
+    NR_CUDA_TRY(cudaStreamSynchronize(s));
+    report_data[0] = rep.rms_force;
+    report_data[1] = rep.e_stretch;
+    report_data[2] = rep.e_bend;
+    report_data[3] = rep.e_gel;
+    *step_count = rep.steps;
+    return rc;
+}
+
 }  // namespace nr
 
 using namespace nr;
@@ -679,7 +873,10 @@ int nr_relax(nr_network *d, const nr_fire_params *params, nr_report *report, voi
     int rc = check_params(params);
     if (rc != NR_OK) return rc;
     clear_error();
-    if (params->precision == NR_MIXED) return relax_single_mixed(d->set, *params, as_stream(stream), report);
+    if (params->precision == NR_MIXED) {
+        if (d->set.dev[0].use_gel) return fail(NR_ERR_INVALID, "nr_relax: a gel-coupled network relaxes in FP64 only");
+        return relax_single_mixed(d->set, *params, as_stream(stream), report);
+    }
     return relax_single_fp64(d->set, 0, *params, as_stream(stream), report);
 }
 
@@ -695,9 +892,7 @@ int nr_forces(nr_network *d, double *host_f, void *stream) {
 int nr_energies(nr_network *d, double *e_stretch, double *e_bend, void *stream) {
     if (!d || !e_stretch || !e_bend) return fail(NR_ERR_INVALID, "nr_energies: null argument");
     const NetDev &dv = d->set.dev[0];
-    const int sms = sm_count();
-    const int eblocks = std::max(1, std::min(2 * sms, (std::max(dv.n_edges, dv.n_triples) + kTile - 1) / kTile * 2));
-    NR_CUDA_TRY(launch_energies(dv, eblocks, as_stream(stream)));
+    NR_CUDA_TRY(launch_energies(dv, energy_blocks(dv, sm_count()), as_stream(stream)));
     FireState st;
     NR_CUDA_TRY(cudaMemcpyAsync(&st, dv.st, sizeof(FireState), cudaMemcpyDeviceToHost, as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
@@ -731,6 +926,7 @@ int nr_sweep(nr_network *d, double miny, double yrange, const nr_fire_params *pa
             R.max_comp = maxc;
             R.e_stretch = rep.e_stretch;
             R.e_bend = rep.e_bend;
+            R.e_gel = rep.e_gel;
             R.rms_force = rep.rms_force;
             R.max_force = rep.max_force;
             R.steps = rep.steps;
@@ -773,70 +969,160 @@ int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double k
                    const signed char *d_e_offsets, const int *d_triples, const signed char *d_t_offsets,
                    const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
                    int max_steps, int nmin, double report_data[3], int *step_count, void *stream) {
-    if (num_dof <= 0 || (num_dof & 1) || npairs < 0 || ntriples < 0 || !d_pos || !d_fcodes || !fire_params ||
-        !report_data || !step_count || (npairs > 0 && ks > 0 && (!d_pair_list || !d_lengths || !d_e_offsets)) ||
-        (ntriples > 0 && kb > 0 && (!d_triples || !d_t_offsets)))
-        return fail(NR_ERR_INVALID, "nr_run_fire_md: bad arguments");
-    cudaStream_t s = as_stream(stream);
-    const int n = num_dof / 2;
-    nr_host_network h;
-    h.n_points = n;
-    h.offset = width;
-    h.points.resize(num_dof);
-    NR_CUDA_TRY(cudaMemcpyAsync(h.points.data(), d_pos, sizeof(double) * num_dof, cudaMemcpyDeviceToHost, s));
-    std::vector<unsigned char> fc(n);
-    NR_CUDA_TRY(cudaMemcpyAsync(fc.data(), d_fcodes, n, cudaMemcpyDeviceToHost, s));
-    if (ks > 0 && npairs > 0) {
-        h.edge_ij.resize(2 * (size_t)npairs);
-        h.edge_l0.resize(npairs);
-        h.edge_wrap.resize(npairs);
-        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_ij.data(), d_pair_list, sizeof(int) * 2 * npairs, cudaMemcpyDeviceToHost, s));
-        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_l0.data(), d_lengths, sizeof(double) * npairs, cudaMemcpyDeviceToHost, s));
-        NR_CUDA_TRY(cudaMemcpyAsync(h.edge_wrap.data(), d_e_offsets, npairs, cudaMemcpyDeviceToHost, s));
-    }
-    if (kb > 0 && ntriples > 0) {
-        h.tri_hjk.resize(3 * (size_t)ntriples);
-        h.tri_wrap.resize(2 * (size_t)ntriples);
-        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_hjk.data(), d_triples, sizeof(int) * 3 * ntriples, cudaMemcpyDeviceToHost, s));
-        NR_CUDA_TRY(cudaMemcpyAsync(h.tri_wrap.data(), d_t_offsets, 2 * (size_t)ntriples, cudaMemcpyDeviceToHost, s));
-    }
-    NR_CUDA_TRY(cudaStreamSynchronize(s));
-    for (size_t i = 0; i < h.edge_ij.size(); ++i)
-        if (h.edge_ij[i] < 0 || h.edge_ij[i] >= n) return fail(NR_ERR_INVALID, "nr_run_fire_md: bond index out of range");
-    for (size_t i = 0; i < h.tri_hjk.size(); ++i)
-        if (h.tri_hjk[i] < 0 || h.tri_hjk[i] >= n) return fail(NR_ERR_INVALID, "nr_run_fire_md: triple index out of range");
-    y_range(h.points, h.miny, h.maxy);
-    DeviceSet S;
-    const nr_host_network *nets[1] = {&h};
-    const unsigned char *fcs[1] = {fc.data()};
-    int rc = build_set(1, nets, &ks, &kb, fcs, s, S);
-    if (rc != NR_OK) return rc;
-    nr_fire_params p;
-    p.alpha0 = fire_params[0];
-    p.falpha = fire_params[1];
-    p.dt_max = fire_params[2];
-    p.finc = fire_params[3];
-    p.fdec = fire_params[4];
-    p.nmin = nmin;
-    p.mass = mass;
-    p.fcut = fcut;
-    p.max_steps = max_steps;
-    p.criterion = NR_CRIT_RMS;
-    p.precision = NR_FP64;
-    rc = check_params(&p);
-    if (rc != NR_OK) return rc;
-    nr_report rep;
-    rc = relax_single_fp64(S, 0, p, s, &rep);
-    if (rc < 0) return rc;
-    NR_CUDA_TRY(cudaMemcpyAsync(d_pos, S.x_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
-    if (d_vel) NR_CUDA_TRY(cudaMemcpyAsync(d_vel, S.v_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
-    if (d_forces) NR_CUDA_TRY(cudaMemcpyAsync(d_forces, S.f_all, sizeof(double) * num_dof, cudaMemcpyDeviceToDevice, s));
-    NR_CUDA_TRY(cudaStreamSynchronize(s));
-    report_data[0] = rep.rms_force;
-    report_data[1] = rep.e_stretch;
-    report_data[2] = rep.e_bend;
-    *step_count = rep.steps;
+    if (!report_data) return fail(NR_ERR_INVALID, "nr_run_fire_md: bad arguments");
+    double rep4[4];
+    const int rc = run_fire_md_impl("nr_run_fire_md", num_dof, npairs, ntriples, width, ks, kb, d_pos, d_vel, d_forces,
+                                    d_pair_list, d_lengths, d_e_offsets, d_triples, d_t_offsets, d_fcodes,
+                                    fire_params, mass, fcut, max_steps, nmin, nullptr, rep4, step_count, stream);
+    if (rc >= 0) memcpy(report_data, rep4, 3 * sizeof(double));
     return rc;
+}
+
+int nr_mesh_run_fire_md(int num_dof, int npairs, int ntriples, int nelems, double width, double ks, double kb,
+                        double smod, double bmod, double dilation, double *d_pos, double *d_vel, double *d_forces,
+                        const int *d_pair_list, const double *d_lengths, const signed char *d_e_offsets,
+                        const int *d_triples, const signed char *d_t_offsets, const int *d_elems,
+                        const double *d_areas, const double *d_inv_mats, const int *d_mpairs, int n_mpairs,
+                        const unsigned char *d_fcodes, const double fire_params[5], double mass, double fcut,
+                        int max_steps, int nmin, double report_data[4], int *step_count, void *stream) {
+    GelArgs g{nelems, n_mpairs, smod, bmod, dilation, d_elems, d_areas, d_inv_mats, d_mpairs};
+    return run_fire_md_impl("nr_mesh_run_fire_md", num_dof, npairs, ntriples, width, ks, kb, d_pos, d_vel, d_forces,
+                            d_pair_list, d_lengths, d_e_offsets, d_triples, d_t_offsets, d_fcodes, fire_params, mass,
+                            fcut, max_steps, nmin, &g, report_data, step_count, stream);
+}
+
+int nr_network_set_gel(nr_network *d, double smod, double bmod, double dilation) {
+    if (!d) return fail(NR_ERR_INVALID, "nr_network_set_gel: null network");
+    return set_gel(d->set, smod, bmod, dilation);
+}
+
+int nr_network_gel_inv_mats(nr_network *d, void *stream) {
+    if (!d) return fail(NR_ERR_INVALID, "nr_network_gel_inv_mats: null network");
+    const DeviceSet &S = d->set;
+    NR_CUDA_TRY(launch_inv_mats((const double *)S.dev[0].x, (const int *)S.gel[0].elem, 4, S.dev[0].n_elems,
+                                S.gel[0].elem_inv, as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_dilate(nr_network *d, double minx, double miny, double factor, void *stream) {
+    if (!d) return fail(NR_ERR_INVALID, "nr_dilate: null network");
+    NR_CUDA_TRY(launch_dilate(d->set.x_all, (int)d->set.total_nodes, minx, miny, factor, as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_mesh_energies(nr_network *d, double energies[3], void *stream) {
+    if (!d || !energies) return fail(NR_ERR_INVALID, "nr_mesh_energies: null argument");
+    const NetDev &dv = d->set.dev[0];
+    NR_CUDA_TRY(launch_energies(dv, energy_blocks(dv, sm_count()), as_stream(stream)));
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, dv.st, sizeof(FireState), cudaMemcpyDeviceToHost, as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    energies[0] = st.e_stretch;
+    energies[1] = st.e_bend;
+    energies[2] = dv.use_gel ? st.e_gel : 0.0;
+    return NR_OK;
+}
+
+int nr_get_inv_mats(int n_facets, const double *d_pos, const int *d_facets, double *d_inv_mats, void *stream) {
+    if (n_facets < 0 || (n_facets > 0 && (!d_pos || !d_facets || !d_inv_mats)))
+        return fail(NR_ERR_INVALID, "nr_get_inv_mats: bad arguments");
+    NR_CUDA_TRY(launch_inv_mats(d_pos, d_facets, 3, n_facets, d_inv_mats, as_stream(stream)));
+    return NR_OK;
+}
+
+int nr_mesh_prepare(nr_network *d, double smod, double bmod, double dilation, double area, double *pref_dilation,
+                    void *stream) {
+    if (!d || !pref_dilation) return fail(NR_ERR_INVALID, "nr_mesh_prepare: null argument");
+    DeviceSet &S = d->set;
+    int rc = nr_dilate(d, S.minx[0], S.miny[0], std::sqrt(1 + dilation), stream);
+    if (rc != NR_OK) return rc;
+    double net_bmod = 0;
+    if (S.dev[0].use_bonds) {
+        double es = 0, eb = 0;
+        rc = nr_energies(d, &es, &eb, stream);
+        if (rc != NR_OK) return rc;
+        net_bmod = es;
+        net_bmod *= 2 / area / (dilation * dilation);
+    }
+    const double pref_d = dilation * (bmod + net_bmod) / bmod;
+    *pref_dilation = pref_d;
+    return set_gel(S, smod, bmod, pref_d);
+}
+
+int nr_mesh_sweep(nr_network *d, double miny, double height, const nr_fire_params *params, const double compr[3],
+                  const double shear[3], nr_step_record *records, int max_records, int *n_records,
+                  double *shear_positions, void *stream) {
+    if (!d || !compr || !shear || !n_records || (max_records > 0 && !records))
+        return fail(NR_ERR_INVALID, "nr_mesh_sweep: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    if (!(height > 0)) return fail(NR_ERR_INVALID, "nr_mesh_sweep: height must be positive");
+    *n_records = 0;
+    const double smult = height;
+    double range = height;
+    const size_t n2 = 2 * (size_t)d->set.total_nodes;
+    int worst = NR_OK;
+    auto relax_record = [&](double curr, double maxc, int is_shear) -> int {
+        nr_report rep;
+        int r = nr_relax(d, params, &rep, stream);
+        if (r < 0) return r;
+        if (r == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+        if (*n_records < max_records) {
+            nr_step_record &R = records[*n_records];
+            R.curr_disp = curr;
+            R.max_comp = maxc;
+            R.e_stretch = rep.e_stretch;
+            R.e_bend = rep.e_bend;
+            R.e_gel = rep.e_gel;
+            R.rms_force = rep.rms_force;
+            R.max_force = rep.max_force;
+            R.steps = rep.steps;
+            R.is_shear = is_shear;
+            R.status = rep.status;
+            R.fp64_steps = rep.fp64_steps;
+            if (is_shear && shear_positions) {
+                r = nr_network_get_positions(d, shear_positions + n2 * (size_t)(*n_records), stream);
+                if (r != NR_OK) return r;
+            }
+            (*n_records)++;
+        }
+        return NR_OK;
+    };
+    double min_disp = compr[0] * smult, max_disp = compr[1] * smult, inc = compr[2] * smult;
+    double curr_disp = 0.0;
+    if (max_disp > 0) {
+        rc = nr_affine_displace(d, miny, range, 0, -min_disp, stream);
+        if (rc != NR_OK) return rc;
+        range -= min_disp;
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            rc = relax_record(0.0, curr_disp, 0);
+            if (rc < 0) return rc;
+            if (curr_disp < max_disp) {
+                rc = nr_affine_displace(d, miny, range, 0, -inc, stream);
+                if (rc != NR_OK) return rc;
+                range -= inc;
+            }
+            if (!(inc > 0)) break; /* the reference loops forever when inc == 0 */
+        }
+    }
+    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
+    min_disp = shear[0] * smult;
+    max_disp = shear[1] * smult;
+    inc = shear[2] * smult;
+    if (max_disp > 0) {
+        rc = nr_affine_displace(d, miny, range, min_disp, 0, stream);
+        if (rc != NR_OK) return rc;
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            rc = relax_record(curr_disp, max_comp, 1);
+            if (rc < 0) return rc;
+            if (curr_disp < max_disp) {
+                rc = nr_affine_displace(d, miny, range, inc, 0, stream);
+                if (rc != NR_OK) return rc;
+            }
+            if (!(inc > 0)) break;
+        }
+    }
+    return worst;
 }
 
 int nr_batch_create(int n, const nr_host_network *const *nets, const double *ks, const double *kb, void *stream,

@@ -1,9 +1,10 @@
 /*
- * The lsrelax-compatible driver: batch files (parse_batch_file,
- * large_strain_relax.cu:263-383), file lists (file_lists.cpp:11-138), the
- * per-network run with the reference's output files (do_relaxation_run,
- * large_strain_relax.cu:792-1010), relaxation_batch (:1016-1044) and the
- * command line (:1047-1126).
+ * The lsrelax- and nmrelax-compatible drivers: batch files (parse_batch_file,
+ * large_strain_relax.cu:263-383, network_mesh_relax.cu:413-500), file lists
+ * (file_lists.cpp:11-138), the per-network runs with the reference's output
+ * files (do_relaxation_run, large_strain_relax.cu:792-1010 and
+ * network_mesh_relax.cu:1095-1390), relaxation_batch and the command lines
+ * (large_strain_relax.cu:1016-1126, network_mesh_relax.cu:1393-1503).
  *
  * Output formats are the reference's, byte for byte:
  *   _log.txt    "Convergence [not ]reached: Steps: %d, RMS Force: %12.8le"
@@ -11,12 +12,16 @@
  *   _edata.txt  compression "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le"
  *               shear       "%12.10lf\t%12.10lf\t%12.10le\t%12.10le\t%12.10le"
  *   _NNN.pos    "%2.10le\t%2.10le" per node after each shear step
+ * nmrelax's _edata.txt has a gel column and a total:
+ *               compression "%12.0lf\t%12.10lf" then four "%12.8le"
+ *               shear       "%12.8lf\t%12.8lf" then four "%12.8le"
  * Deliberate differences: a network file that fails to parse is skipped
  * with an error instead of being relaxed half-read; an increment of 0 runs
  * one step instead of looping forever; -a selects absolute displacements
  * instead of falling through into -b with no argument.
  */
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -132,10 +137,9 @@ bool file_lists(const std::string &input, const std::string &ext, const std::str
 
 }  // namespace
 
-extern "C" {
-
-int nr_parse_batch_file(const char *path, nr_batch_spec *spec) {
-    if (!path || !spec) return fail(NR_ERR_INVALID, "nr_parse_batch_file: null argument");
+/* Both batch-file grammars: six non-comment lines; the second holds
+ * "ks kb" (lsrelax) or "ks kb bmod smod dilation" (nmrelax, mesh != null). */
+static int parse_batch(const char *path, nr_batch_spec *spec, nr_mesh_batch_spec *mesh) {
     memset(spec, 0, sizeof(*spec));
     std::ifstream input(path);
     if (!input.is_open()) {
@@ -148,7 +152,17 @@ int nr_parse_batch_file(const char *path, nr_batch_spec *spec) {
     snprintf(spec->base, sizeof(spec->base), "%s", tok.empty() ? "" : tok[0].c_str());
     if (tok.size() > 1) snprintf(spec->tag, sizeof(spec->tag), "%s", tok[1].c_str());
     if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing stiffness line");
-    if (sscanf(line.c_str(), "%lf %lf", &spec->ks, &spec->kb) < 2 || spec->ks < 0 || spec->kb < 0) {
+    if (mesh) {
+        /* network_mesh_relax.cu:440-446: "ks kb bmod smod dilation", at least
+         * three values (missing smod / dilation are 0 here; the reference
+         * leaves them uninitialised) */
+        if (sscanf(line.c_str(), "%lf %lf %lf %lf %lf", &spec->ks, &spec->kb, &mesh->bmod, &mesh->smod,
+                   &mesh->dilation) < 3 ||
+            spec->ks < 0 || spec->kb < 0 || mesh->bmod < 0 || mesh->smod < 0 || mesh->dilation < 0) {
+            fprintf(stderr, "Error: invalid format for mechanical attributes.");
+            return fail(NR_ERR_PARSE, "batch file: invalid mechanical attributes");
+        }
+    } else if (sscanf(line.c_str(), "%lf %lf", &spec->ks, &spec->kb) < 2 || spec->ks < 0 || spec->kb < 0) {
         fprintf(stderr, "Error: invalid format for mechanical attributes.");
         return fail(NR_ERR_PARSE, "batch file: invalid mechanical attributes");
     }
@@ -180,6 +194,19 @@ int nr_parse_batch_file(const char *path, nr_batch_spec *spec) {
         }
     }
     return NR_OK;
+}
+
+extern "C" {
+
+int nr_parse_batch_file(const char *path, nr_batch_spec *spec) {
+    if (!path || !spec) return fail(NR_ERR_INVALID, "nr_parse_batch_file: null argument");
+    return parse_batch(path, spec, nullptr);
+}
+
+int nr_parse_mesh_batch_file(const char *path, nr_mesh_batch_spec *spec) {
+    if (!path || !spec) return fail(NR_ERR_INVALID, "nr_parse_mesh_batch_file: null argument");
+    memset(spec, 0, sizeof(*spec));
+    return parse_batch(path, &spec->net, spec);
 }
 
 int nr_get_file_lists(const char *base, const char *ext, const char *tag, char *buf, size_t cap) {
@@ -303,38 +330,164 @@ int nr_do_relaxation_run(const char *net_file, const char *log_name, const char 
     return worst;
 }
 
+/* do_relaxation_run of network_mesh_relax.cu:1095-1390 on one .nmc file:
+ * the period scaled by sqrt(1 + dilation) before get_triples, the gel's
+ * inverse matrices from the undilated positions, dilation, the preferred
+ * dilation (printed as the reference prints it), then the compression and
+ * shear loops with the gel acting when bmod > 0.  FP64 path. */
+int nr_do_mesh_relaxation_run(const char *net_file, const char *log_name, const char *edata_name,
+                              const char *disp_base, const nr_mesh_batch_spec *mspec, int criterion) {
+    if (!net_file || !log_name || !edata_name || !disp_base || !mspec)
+        return fail(NR_ERR_INVALID, "nr_do_mesh_relaxation_run: null argument");
+    const nr_batch_spec *spec = &mspec->net;
+    const clock_t ct0 = clock();
+    nr_host_network *hn = nullptr;
+    int rc = nr_read_network_mesh(net_file, &hn);
+    if (rc != NR_OK) {
+        fprintf(stderr, "%s: %s\n", net_file, nr_last_error());
+        nr_host_network_free(hn);
+        return rc;
+    }
+    const double area = (hn->maxx - hn->minx) * (hn->maxy - hn->miny);
+    const double swell = std::sqrt(1 + mspec->dilation);
+    nr_host_network_set_offset(hn, hn->offset * swell);
+    if (spec->kb > 0) nr_get_triples(hn);
+    const double miny = hn->miny;
+    double range = (hn->maxy - hn->miny) * swell;
+    const double smult = spec->absolute ? 1.0 : range;
+    const double s_inc = spec->shear[2];
+    const int num_digits =
+        get_dec_digits(1 + (s_inc > 0 ? (int)((spec->shear[1] - spec->shear[0]) / s_inc) : 0));
+    nr_network *net = nullptr;
+    rc = nr_network_create(hn, spec->ks, spec->kb, nullptr, &net);
+    const int n_points = hn->n_points;
+    nr_host_network_free(hn);
+    if (rc != NR_OK) return rc;
+    double pref_d = 0;
+    rc = nr_mesh_prepare(net, mspec->smod, mspec->bmod, mspec->dilation, area, &pref_d, nullptr);
+    if (rc != NR_OK) {
+        nr_network_destroy(net);
+        return rc;
+    }
+    printf("Preferred dilation: %g\n", pref_d);
+    nr_fire_params p;
+    p.alpha0 = spec->fire_params[0];
+    p.falpha = spec->fire_params[1];
+    p.dt_max = spec->fire_params[2];
+    p.finc = spec->fire_params[3];
+    p.fdec = spec->fire_params[4];
+    p.nmin = spec->nmin;
+    p.mass = spec->mass;
+    p.fcut = spec->fcut;
+    p.max_steps = spec->nmax;
+    p.criterion = criterion;
+    p.precision = NR_FP64;
+    FILE *log_file = fopen(log_name, "w");
+    FILE *edata_file = fopen(edata_name, "w");
+    std::vector<double> pos(2 * (size_t)n_points);
+    int disp_count = 1;
+    int worst = NR_OK;
+    auto relax = [&](nr_report &rep) -> int {
+        int r = nr_relax(net, &p, &rep, nullptr);
+        if (r < 0) return r;
+        if (r == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+        const double measure = criterion == NR_CRIT_MAX ? rep.max_force : rep.rms_force;
+        if (log_file) {
+            fprintf(log_file, measure <= spec->fcut ? "Convergence reached: " : "Convergence not reached: ");
+            fprintf(log_file, "Steps: %d, RMS Force: %12.8le\n", rep.steps, rep.rms_force);
+        }
+        printf("Steps: %d, RMS Force: %12.8le\n", rep.steps, rep.rms_force);
+        return NR_OK;
+    };
+    double min_disp = spec->compr[0] * smult, max_disp = spec->compr[1] * smult, inc = spec->compr[2] * smult;
+    double curr_disp = 0.0;
+    if (max_disp > 0) {
+        rc = nr_affine_displace(net, miny, range, 0, -min_disp, nullptr);
+        range -= min_disp;
+        for (curr_disp = min_disp; rc >= 0 && curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            nr_report rep;
+            rc = relax(rep);
+            if (rc < 0) break;
+            if (edata_file)
+                fprintf(edata_file, "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le\t%12.8le\n", 0., curr_disp,
+                        rep.e_stretch, rep.e_bend, rep.e_gel, rep.e_stretch + rep.e_bend + rep.e_gel);
+            if (curr_disp < max_disp) {
+                rc = nr_affine_displace(net, miny, range, 0, -inc, nullptr);
+                range -= inc;
+            }
+            if (!(inc > 0)) break;
+        }
+    }
+    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
+    min_disp = spec->shear[0] * smult;
+    max_disp = spec->shear[1] * smult;
+    inc = spec->shear[2] * smult;
+    if (rc >= 0 && max_disp > 0) {
+        rc = nr_affine_displace(net, miny, range, min_disp, 0, nullptr);
+        for (curr_disp = min_disp; rc >= 0 && curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            nr_report rep;
+            rc = relax(rep);
+            if (rc < 0) break;
+            if (edata_file)
+                fprintf(edata_file, "%12.8lf\t%12.8lf\t%12.8le\t%12.8le\t%12.8le\t%12.8le\n", curr_disp, max_comp,
+                        rep.e_stretch, rep.e_bend, rep.e_gel, rep.e_stretch + rep.e_bend + rep.e_gel);
+            rc = nr_network_get_positions(net, pos.data(), nullptr);
+            if (rc != NR_OK) break;
+            const std::string name = report_name(disp_base, num_digits, disp_count++, "pos");
+            FILE *f = fopen(name.c_str(), "w");
+            if (f) {
+                for (int i = 0; i < n_points; ++i) fprintf(f, "%2.10le\t%2.10le\n", pos[2 * i], pos[2 * i + 1]);
+                fclose(f);
+            }
+            if (curr_disp < max_disp) rc = nr_affine_displace(net, miny, range, inc, 0, nullptr);
+            if (!(inc > 0)) break;
+        }
+    }
+    const clock_t ct = clock() - ct0;
+    if (log_file) {
+        fprintf(log_file, "Elapsed time: %f seconds\n", ((float)ct) / CLOCKS_PER_SEC);
+        fclose(log_file);
+    }
+    if (edata_file) fclose(edata_file);
+    nr_network_destroy(net);
+    if (rc < 0) {
+        fprintf(stderr, "Relaxation failed: %s\n", nr_last_error());
+        return rc;
+    }
+    return worst;
+}
+
 }  // extern "C"
 
-static int relaxation_batch(const char *batch_file, int precision, int criterion, int absolute) {
-    nr_batch_spec spec;
-    int rc = nr_parse_batch_file(batch_file, &spec);
+static int relaxation_batch(const char *batch_file, int precision, int criterion, int absolute, bool mesh) {
+    nr_mesh_batch_spec mspec;
+    int rc = mesh ? nr_parse_mesh_batch_file(batch_file, &mspec) : nr_parse_batch_file(batch_file, &mspec.net);
+    nr_batch_spec &spec = mspec.net;
     spec.absolute = absolute;
     if (rc != NR_OK) {
         fprintf(stderr, "Parsing of the batch file failed.\n");
         return rc;
     }
     FileLists fl;
-    if (!file_lists(spec.base, "dat", spec.tag, fl)) {
+    if (!file_lists(spec.base, mesh ? "nmc" : "dat", spec.tag, fl)) {
         fprintf(stderr, "File lists could not be read.\n");
         return fail(NR_ERR_IO, "file lists could not be read");
     }
     int worst = NR_OK;
     for (size_t i = 0; i < fl.dat.size(); ++i) {
-        rc = nr_do_relaxation_run(fl.dat[i].c_str(), fl.log[i].c_str(), fl.edat[i].c_str(), fl.disp[i].c_str(), &spec,
-                                  precision, criterion);
+        rc = mesh ? nr_do_mesh_relaxation_run(fl.dat[i].c_str(), fl.log[i].c_str(), fl.edat[i].c_str(),
+                                              fl.disp[i].c_str(), &mspec, criterion)
+                  : nr_do_relaxation_run(fl.dat[i].c_str(), fl.log[i].c_str(), fl.edat[i].c_str(), fl.disp[i].c_str(),
+                                         &spec, precision, criterion);
         if (rc < 0) worst = rc;
         else if (rc == NR_NOT_CONVERGED && worst == NR_OK) worst = rc;
     }
     return worst;
 }
 
-extern "C" {
-
-int nr_relaxation_batch(const char *batch_file, int precision, int criterion) {
-    return relaxation_batch(batch_file, precision, criterion, 0);
-}
-
-int nr_lsrelax_main(int argc, char **argv) {
+/* Both command lines: -b batch [-x bx] [-y by] [-a] [-i], --precision,
+ * --criterion. */
+static int cli_main(int argc, char **argv, bool mesh) {
     const char *batch_file = nullptr;
     int precision = NR_FP64, criterion = NR_CRIT_RMS, absolute = 0;
     for (int i = 1; i < argc; ++i) {
@@ -374,9 +527,22 @@ int nr_lsrelax_main(int argc, char **argv) {
         fprintf(stderr, "No batch file was specified.\n");
         return -1;
     }
-    const int rc = relaxation_batch(batch_file, precision, criterion, absolute);
+    const int rc = relaxation_batch(batch_file, precision, criterion, absolute, mesh);
     return rc < 0 ? 1 : 0;
 }
 
+extern "C" {
+
+int nr_relaxation_batch(const char *batch_file, int precision, int criterion) {
+    return relaxation_batch(batch_file, precision, criterion, 0, false);
+}
+
+int nr_mesh_relaxation_batch(const char *batch_file, int criterion) {
+    return relaxation_batch(batch_file, NR_FP64, criterion, 0, true);
+}
+
+int nr_lsrelax_main(int argc, char **argv) { return cli_main(argc, argv, false); }
+
+int nr_nmrelax_main(int argc, char **argv) { return cli_main(argc, argv, true); }
 
 }  // extern "C"

@@ -17,7 +17,71 @@ namespace nr {
 
 constexpr int kGroup = 16; /* reduction units buffered in shared memory per flush */
 
-__device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &fx, double &fy) {
+/* Deformation gradient of gel element e at the positions x
+ * (network_mesh_relax.cu:716-719, the reference's association). */
+__device__ __forceinline__ void gel_defgrad(const NetDev &d, int e, double &f11, double &f12, double &f21,
+                                            double &f22) {
+    const int4 el = d.gel->elem[e];
+    const double *M = d.gel->elem_inv + 6 * (size_t)e;
+    const double2 p1 = d.x[el.x], p2 = d.x[el.y], p3 = d.x[el.z];
+    f11 = p1.x * M[0] + p2.x * M[2] + p3.x * M[4];
+    f12 = p1.x * M[1] + p2.x * M[3] + p3.x * M[5];
+    f21 = p1.y * M[0] + p2.y * M[2] + p3.y * M[4];
+    f22 = p1.y * M[1] + p2.y * M[3] + p3.y * M[5];
+}
+
+/* gel_forces (network_mesh_relax.cu:702-751) of element e: for vertex r the
+ * two terms the reference adds to the x force (dU/dF11, dU/dF12 parts) and
+ * the two it adds to the y force, in its expression order. */
+__device__ __forceinline__ double4 gel_terms(const NetDev &d, int e, int r, double du11, double du12, double du21,
+                                             double du22) {
+    const double *M = d.gel->elem_inv + 6 * (size_t)e;
+    const double a = M[2 * r], b = M[2 * r + 1];
+    return make_double4(du11 * a, du12 * b, du21 * a, du22 * b);
+}
+__device__ __forceinline__ void gel_du(const NetDev &d, int e, double &du11, double &du12, double &du21,
+                                       double &du22) {
+    double f11, f12, f21, f22;
+    gel_defgrad(d, e, f11, f12, f21, f22);
+    const NetGel &g = *d.gel;
+    const double A = g.elem_area[e];
+    const double smod = g.smod, bmod = g.bmod, dil = g.gdil;
+    const double det = f11 * f22 - f12 * f21;
+    const double coeff1 = -smod * A / det;
+    double coeff2 = bmod * (dil + 1 - det) + smod * (f11 * f11 + f12 * f12 + f21 * f21 + f22 * f22) / (2 * det * det);
+    coeff2 *= A;
+    du11 = f11 * coeff1 + f22 * coeff2;
+    du12 = f12 * coeff1 - f21 * coeff2;
+    du21 = f21 * coeff1 - f12 * coeff2;
+    du22 = f22 * coeff1 + f11 * coeff2;
+}
+/* gel_energy (network_mesh_relax.cu:674-699) of element e, as |e| for the
+ * cublasDasum the reference sums it with. */
+__device__ __forceinline__ double gel_energy_abs(const NetDev &d, int e) {
+    double f11, f12, f21, f22;
+    gel_defgrad(d, e, f11, f12, f21, f22);
+    const NetGel &g = *d.gel;
+    const double A = g.elem_area[e];
+    const double smod = g.smod, bmod = g.bmod, dil = g.gdil;
+    const double det = f11 * f22 - f12 * f21;
+    double en = smod * A * ((f11 * f11 + f12 * f12 + f21 * f21 + f22 * f22) / det - 2) / 2;
+    en += bmod * A * (det - 1 - dil) * (det - 1 - dil) / 2;
+    return fabs(en);
+}
+/* Adds an element's terms to a node's force in the reference's atomicAdd
+ * order (x: term 1 then term 2; y likewise). */
+__device__ __forceinline__ void gel_add(double4 t, double &fx, double &fy) {
+    fx = fx + t.x;
+    fx = fx + t.y;
+    fy = fy + t.z;
+    fy = fy + t.w;
+}
+
+/* Masked force on node i from its bonds, triples and (kGel) gel elements,
+ * in the canonical order.  The mixed-precision kernels never carry a gel
+ * and instantiate kGel = false. */
+template <bool kGel = true>
+__device__ __forceinline__ void node_force_fp64_own(const NetDev &d, int i, double &fx, double &fy) {
     fx = 0.0;
     fy = 0.0;
     const unsigned c = d.fcode[i];
@@ -68,8 +132,35 @@ __device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &
             }
         }
     }
+    if (kGel && d.use_gel) {
+        const NetGel &g = *d.gel;
+        const int e1 = g.eptr[i + 1];
+        for (int e = g.eptr[i]; e < e1; ++e) {
+            const int code = g.eent[e];
+            const int el = code / 3, r = code - 3 * el;
+            double du11, du12, du21, du22;
+            gel_du(d, el, du11, du12, du21, du22);
+            gel_add(gel_terms(d, el, r, du11, du12, du21, du22), fx, fy);
+        }
+    }
     if (!(c & 1)) fx = 0.0;
     if (!(c & 2)) fy = 0.0;
+}
+
+/* Force on node i: its own masked sum plus, for a duplicate mesh vertex,
+ * its partner's (duplicate_forces, network_mesh_relax.cu:754-780, unmasked;
+ * a + b and b + a round alike, so both vertices get the same value). */
+__device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &fx, double &fy) {
+    node_force_fp64_own(d, i, fx, fy);
+    if (d.use_gel) {
+        const int q = d.gel->partner[i];
+        if (q >= 0) {
+            double gx, gy;
+            node_force_fp64_own(d, q, gx, gy);
+            fx = fx + gx;
+            fy = fy + gy;
+        }
+    }
 }
 
 /* Item pass of the FP64 force: every bond force (the value its first
@@ -77,6 +168,7 @@ __device__ __forceinline__ void node_force_fp64(const NetDev &d, int i, double &
  * scratch, items b = first, first + stride, ...  GB300's FP64 pipe is the
  * bound of the plain path, and the per-node gather below would otherwise
  * evaluate each bond twice and each triple three times. */
+template <bool kGel>
 __device__ inline void items_pass(const NetDev &d, int first, int stride) {
     const double W = d.width;
     if (d.use_bonds)
@@ -101,11 +193,18 @@ __device__ inline void items_pass(const NetDev &d, int first, int stride) {
             bend_force(ax, ay, bx, by, kb, phi0, fjx, fjy, fkx, fky);
             d.tfrc[t] = make_double4(fjx, fjy, fkx, fky);
         }
+    if (kGel && d.use_gel)
+        for (int e = first; e < d.n_elems; e += stride) {
+            double du11, du12, du21, du22;
+            gel_du(d, e, du11, du12, du21, du22);
+            for (int r = 0; r < 3; ++r) d.gel->efrc[3 * (size_t)e + r] = gel_terms(d, e, r, du11, du12, du21, du22);
+        }
 }
 
 /* Per-node gather of the item forces in the canonical order; the same bits
- * as node_force_fp64 (the same values summed in the same order). */
-__device__ __forceinline__ void node_force_items(const NetDev &d, int i, double &fx, double &fy) {
+ * as node_force_fp64_own (the same values summed in the same order). */
+template <bool kGel>
+__device__ __forceinline__ void node_force_items_own(const NetDev &d, int i, double &fx, double &fy) {
     fx = 0.0;
     fy = 0.0;
     const unsigned c = d.fcode[i];
@@ -142,8 +241,29 @@ __device__ __forceinline__ void node_force_items(const NetDev &d, int i, double 
             }
         }
     }
+    if (kGel && d.use_gel) {
+        const NetGel &g = *d.gel;
+        const int e1 = g.eptr[i + 1];
+        for (int e = g.eptr[i]; e < e1; ++e) gel_add(g.efrc[g.eent[e]], fx, fy);
+    }
     if (!(c & 1)) fx = 0.0;
     if (!(c & 2)) fy = 0.0;
+}
+
+/* node_force_fp64 from the item scratch.  kGel = false compiles the gel
+ * terms out (networks without a gel). */
+template <bool kGel>
+__device__ __forceinline__ void node_force_items(const NetDev &d, int i, double &fx, double &fy) {
+    node_force_items_own<kGel>(d, i, fx, fy);
+    if (kGel && d.use_gel) {
+        const int q = d.gel->partner[i];
+        if (q >= 0) {
+            double gx, gy;
+            node_force_items_own<kGel>(d, q, gx, gy);
+            fx = fx + gx;
+            fy = fy + gy;
+        }
+    }
 }
 
 /* FIRE scalars, advanced identically by whoever holds them. */
@@ -228,57 +348,73 @@ __device__ __forceinline__ void scal_load(Scal &s, const FireState *st_) {
     s.done = st->done; s.converged = st->converged; s.status = st->status;
 }
 
-/* Energy partials of bond tiles [t0, ...) and triple tiles, tiles of 256
- * items reduced by the CTA's first 256 threads (8 warps; s_red holds 8
- * doubles).  The CTA must have at least 256 threads; threads beyond the
- * first 256 only take part in the barriers. */
+/* Energy partials of bond, triple and gel-element tiles (t0, t0 + tstride,
+ * ... over the three lists in that order), tiles of 256 items reduced by the
+ * CTA's first 256 threads (8 warps; s_red holds 8 doubles).  The CTA must
+ * have at least 256 threads; threads beyond the first 256 only take part in
+ * the barriers.  Partials of list c go to epart[c * M + tile], M the largest
+ * tile count of the three. */
+__device__ __forceinline__ int energy_stride(const NetDev &d) {
+    const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
+    const int tg = (d.n_elems + kTile - 1) / kTile;
+    return max(tb, max(tt, tg));
+}
+
+template <bool kGel = true>
 __device__ inline void energy_tiles(const NetDev &d, int t0, int tstride, double *s_red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool in_tile = threadIdx.x < kTile;
     const double W = d.width;
-    const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
-    const int total = (d.use_bonds ? tb : 0) + (d.use_triples ? tt : 0);
+    const int nb = d.use_bonds ? (d.n_edges + kTile - 1) / kTile : 0;
+    const int nt = d.use_triples ? (d.n_triples + kTile - 1) / kTile : 0;
+    const int ng = kGel && d.use_gel ? (d.n_elems + kTile - 1) / kTile : 0;
+    const int total = nb + nt + ng;
+    const size_t M = (size_t)energy_stride(d);
     for (int t = t0; t < total; t += tstride) {
-        const bool is_bond = d.use_bonds && t < tb;
-        const int tile = is_bond ? t : t - (d.use_bonds ? tb : 0);
-        const int item = in_tile ? tile * kTile + threadIdx.x : (is_bond ? d.n_edges : d.n_triples);
+        const int cat = t < nb ? 0 : (t < nb + nt ? 1 : 2);
+        const int tile = cat == 0 ? t : (cat == 1 ? t - nb : t - nb - nt);
+        const int n_items = cat == 0 ? d.n_edges : (cat == 1 ? d.n_triples : d.n_elems);
+        const int item = in_tile ? tile * kTile + threadIdx.x : n_items;
         double e = 0.0;
-        if (is_bond) {
-            if (item < d.n_edges) {
+        if (item < n_items) {
+            if (cat == 0) {
                 const int4 r = d.bond[item];
                 const double2 p1 = d.x[r.x], p2 = d.x[r.y];
                 const double k = d.bond_k ? d.bond_k[item] : d.ks;
                 e = bond_energy(p1.x, p1.y, p2.x, p2.y, wrap_shift(r.z, W), d.bond_l0[item], k);
+            } else if (cat == 1) {
+                const int4 r = d.tri[item];
+                const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
+                const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+                const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+                const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
+                const double kb = d.tri_kb ? d.tri_kb[item] : d.kb;
+                const double phi0 = d.tri_phi0 ? d.tri_phi0[item] : 0.0;
+                e = bend_energy(ax, ay, bx, by, kb, phi0);
+            } else if (kGel) {
+                e = gel_energy_abs(d, item);
             }
-        } else if (item < d.n_triples) {
-            const int4 r = d.tri[item];
-            const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
-            const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
-            const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
-            const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
-            const double kb = d.tri_kb ? d.tri_kb[item] : d.kb;
-            const double phi0 = d.tri_phi0 ? d.tri_phi0[item] : 0.0;
-            e = bend_energy(ax, ay, bx, by, kb, phi0);
         }
         if (in_tile) { /* warp-uniform: kTile is a multiple of 32 */
             e = warp_sum(e);
             if (lane == 0) s_red[warp] = e;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            const size_t off = is_bond ? 0 : (size_t)(tb > tt ? tb : tt);
-            d.epart[off + tile] = tree8(s_red);
-        }
+        if (threadIdx.x == 0) d.epart[(size_t)cat * M + tile] = tree8(s_red);
         __syncthreads();
     }
 }
 
-__device__ inline void energy_final(const NetDev &d, double *s_red, double &es, double &eb) {
+__device__ inline void energy_final(const NetDev &d, double *s_red, double &es, double &eb, double &eg) {
     const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
+    const int tg = (d.n_elems + kTile - 1) / kTile;
+    const size_t M = (size_t)energy_stride(d);
     es = 0.0;
     eb = 0.0;
+    eg = 0.0;
     if (d.use_bonds && d.n_edges > 0) es = final_sum(d.epart, tb, 8, s_red);
-    if (d.use_triples && d.n_triples > 0) eb = final_sum(d.epart + (tb > tt ? tb : tt), tt, 8, s_red);
+    if (d.use_triples && d.n_triples > 0) eb = final_sum(d.epart + M, tt, 8, s_red);
+    if (d.use_gel && d.n_elems > 0) eg = final_sum(d.epart + 2 * M, tg, 8, s_red);
 }
 
 }  // namespace nr

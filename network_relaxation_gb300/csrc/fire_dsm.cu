@@ -147,7 +147,7 @@ static __device__ __noinline__ void anchor_eval_dsm(const NetDev &d, const NetDs
     for (int li = threadIdx.x; li < nloc; li += blockDim.x) {
         const int i = n0 + li;
         double fx, fy;
-        node_force_fp64(d, i, fx, fy);
+        node_force_fp64_own<false>(d, i, fx, fy);
         d.f[i] = make_double2(fx, fy);
         const float hx = (float)fx, hy = (float)fy;
         const float2 fh = make_float2(hx, hy), fl = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));

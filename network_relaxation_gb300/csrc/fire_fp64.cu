@@ -58,6 +58,7 @@ __device__ void pass_a(const NetDev &d, const Scal &s, int u0, int ustride) {
 
 /* Pass B: forces at the current x, half kick (or v = 0 when init), and the
  * canonical unit partials of P, |v|^2, |F|^2, max|F|^2 into d.part. */
+template <bool kGel>
 __device__ void pass_b(const NetDev &d, double dtm, bool init, int u0, int ustride, double *s_units) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, sub = d.sub;
     for (int ubase = u0; ubase < d.n_units; ubase += ustride * kGroup) {
@@ -67,7 +68,7 @@ __device__ void pass_b(const NetDev &d, double dtm, bool init, int u0, int ustri
             double tP = 0.0, tV = 0.0, tF = 0.0;
             if (i < d.n) {
                 double fx, fy;
-                node_force_items(d, i, fx, fy);
+                node_force_items<kGel>(d, i, fx, fy);
                 double2 vi;
                 if (init) {
                     vi = make_double2(0.0, 0.0);
@@ -119,6 +120,9 @@ __device__ void reduce_parts(const NetDev &d, double *s_red, double &P, double &
 
 /* ------------------------------------------------------------------ */
 
+/* kGel: the network carries a gel (network_mesh_relax.cu); the instance
+ * without it has no gel code. */
+template <bool kGel>
 __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget_ns) {
     extern __shared__ double s_units[];
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
@@ -126,10 +130,10 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
     Scal s;
     bool last;
     const int item0 = blockIdx.x * blockDim.x + threadIdx.x, istride = G * blockDim.x;
-    items_pass(d, item0, istride);
+    items_pass<kGel>(d, item0, istride);
     if (!barrier_arrive(d.st, G, budget_ns, last, 4)) return;
     if (last) barrier_release(d.st);
-    pass_b(d, 0.0, true, blockIdx.x, G, s_units);
+    pass_b<kGel>(d, 0.0, true, blockIdx.x, G, s_units);
     if (!barrier_arrive(d.st, G, budget_ns, last, 1)) return;
     if (last) {
         double P, V2, F2, M2;
@@ -146,10 +150,10 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
         if (s.done) break;
         if (!barrier_arrive(d.st, G, budget_ns, last, 2)) return;
         if (last) barrier_release(d.st);
-        items_pass(d, item0, istride);
+        items_pass<kGel>(d, item0, istride);
         if (!barrier_arrive(d.st, G, budget_ns, last, 5)) return;
         if (last) barrier_release(d.st);
-        pass_b(d, s.dtm, false, blockIdx.x, G, s_units);
+        pass_b<kGel>(d, s.dtm, false, blockIdx.x, G, s_units);
         if (!barrier_arrive(d.st, G, budget_ns, last, 3)) return;
         if (last) {
             double P, V2, F2, M2;
@@ -170,15 +174,17 @@ __global__ void k_energy_tiles(NetDev d) {
 
 __global__ void k_energy_final(NetDev d) {
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
-    double es, eb;
-    energy_final(d, s_red, es, eb);
+    double es, eb, eg;
+    energy_final(d, s_red, es, eb, eg);
     if (threadIdx.x == 0) {
         d.st->e_stretch = es;
         d.st->e_bend = eb;
+        d.st->e_gel = eg;
     }
 }
 
-/* One CTA per network, networks taken from *queue until exhausted. */
+/* One CTA per network, networks taken from *queue until exhausted
+ * (batches carry no gel). */
 __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_nets, FireParamsDev p, int *queue) {
     extern __shared__ double s_units[];
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
@@ -195,9 +201,9 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
         if (net >= n_nets) return;
         const NetDev &d = s_d;
         double P, V2, F2, M2;
-        items_pass(d, threadIdx.x, blockDim.x);
+        items_pass<false>(d, threadIdx.x, blockDim.x);
         __syncthreads();
-        pass_b(d, 0.0, true, 0, 1, s_units);
+        pass_b<false>(d, 0.0, true, 0, 1, s_units);
         reduce_parts(d, s_red, P, V2, F2, M2);
         if (threadIdx.x == 0) scal_init(s_sc, p, F2, M2, d.sqrt_dof);
         __syncthreads();
@@ -205,21 +211,22 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
             pass_a(d, s_sc, 0, 1);
             if (s_sc.done) break;
             __syncthreads();
-            items_pass(d, threadIdx.x, blockDim.x);
+            items_pass<false>(d, threadIdx.x, blockDim.x);
             __syncthreads();
-            pass_b(d, s_sc.dtm, false, 0, 1, s_units);
+            pass_b<false>(d, s_sc.dtm, false, 0, 1, s_units);
             reduce_parts(d, s_red, P, V2, F2, M2);
             if (threadIdx.x == 0) scal_step(s_sc, p, P, V2, F2, M2, d.sqrt_dof);
             __syncthreads();
         }
         __syncthreads();
-        energy_tiles(d, 0, 1, s_red);
-        double es, eb;
-        energy_final(d, s_red, es, eb);
+        energy_tiles<false>(d, 0, 1, s_red);
+        double es, eb, eg;
+        energy_final(d, s_red, es, eb, eg);
         if (threadIdx.x == 0) {
             scal_store(d.st, s_sc);
             d.st->e_stretch = es;
             d.st->e_bend = eb;
+            d.st->e_gel = eg;
         }
         __syncthreads();
     }
@@ -245,6 +252,38 @@ __global__ void k_affine(double2 *x, int n, double miny, double yrange, double x
     x[i] = p;
 }
 
+/* get_inv_mats (network_mesh_relax.cu:503-531): the inverse of each gel
+ * triangle's reference matrix from positions pos (2N doubles); vertex v of
+ * element e is facets[stride * e + v] (stride 3: the reference's list, 4:
+ * int4 records).  Plain IEEE operations in the reference's order
+ * (--fmad=false), as the oracle computes them. */
+__global__ void k_inv_mats(const double *pos, const int *facets, int stride, int n_elems, double *inv) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_elems) return;
+    const int i1 = facets[(size_t)stride * e], i2 = facets[(size_t)stride * e + 1], i3 = facets[(size_t)stride * e + 2];
+    const double x1 = pos[2 * (size_t)i1], y1 = pos[2 * (size_t)i1 + 1];
+    const double x2 = pos[2 * (size_t)i2], y2 = pos[2 * (size_t)i2 + 1];
+    const double x3 = pos[2 * (size_t)i3], y3 = pos[2 * (size_t)i3 + 1];
+    const double det = x1 * (y2 - y3) + x2 * (y3 - y1) + x3 * (y1 - y2);
+    double *M = inv + 6 * (size_t)e;
+    M[0] = (y2 - y3) / det;
+    M[1] = (x3 - x2) / det;
+    M[2] = (y3 - y1) / det;
+    M[3] = (x1 - x3) / det;
+    M[4] = (y1 - y2) / det;
+    M[5] = (x2 - x1) / det;
+}
+
+/* dilate (network_mesh_relax.cu:796-806) over N nodes. */
+__global__ void k_dilate(double2 *x, int n, double minx, double miny, double factor) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 p = x[i];
+    p.x = minx + factor * (p.x - minx);
+    p.y = miny + factor * (p.y - miny);
+    x[i] = p;
+}
+
 /* Per-network affine map for a batch: one CTA per network. */
 __global__ void k_affine_batch(const NetDev *nets, const double4 *prm) {
     const NetDev d = nets[blockIdx.x];
@@ -264,13 +303,14 @@ __global__ void k_affine_batch(const NetDev *nets, const double4 *prm) {
 
 static size_t grid_smem_bytes(int sub) { return (size_t)kGroup * 4 * sub * sizeof(double); }
 
-cudaError_t fp64_grid_max_blocks(int sub, int *max_blocks) {
+cudaError_t fp64_grid_max_blocks(int sub, bool gel, int *max_blocks) {
     int dev, sms, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_grid, 32 * sub, grid_smem_bytes(sub));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gel ? k_fire_grid<true> : k_fire_grid<false>, 32 * sub,
+                                                      grid_smem_bytes(sub));
     if (e != cudaSuccess) return e;
     *max_blocks = per_sm * sms;
     return cudaSuccess;
@@ -282,8 +322,8 @@ cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks
     FireParamsDev pp = p;
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &pp, &bb};
-    return cudaLaunchCooperativeKernel((const void *)k_fire_grid, dim3(blocks), dim3(32 * d.sub), args,
-                                       grid_smem_bytes(d.sub), stream);
+    const void *k = d.use_gel ? (const void *)k_fire_grid<true> : (const void *)k_fire_grid<false>;
+    return cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(32 * d.sub), args, grid_smem_bytes(d.sub), stream);
 }
 
 cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream) {
@@ -320,6 +360,18 @@ cudaError_t launch_forces(const NetDev &d, cudaStream_t stream) {
 cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
                           cudaStream_t stream) {
     k_affine<<<(n + 255) / 256, 256, 0, stream>>>(x, n, miny, yrange, xdisp, ydisp);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_inv_mats(const double *pos, const int *facets, int stride, int n_elems, double *inv,
+                            cudaStream_t stream) {
+    if (n_elems <= 0) return cudaSuccess;
+    k_inv_mats<<<(n_elems + 255) / 256, 256, 0, stream>>>(pos, facets, stride, n_elems, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dilate(double2 *x, int n, double minx, double miny, double factor, cudaStream_t stream) {
+    k_dilate<<<(n + 255) / 256, 256, 0, stream>>>(x, n, minx, miny, factor);
     return cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@
 
 namespace nr {
 
-cudaError_t fp64_grid_max_blocks(int sub, int *max_blocks);
+cudaError_t fp64_grid_max_blocks(int sub, bool gel, int *max_blocks);
 cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                              cudaStream_t stream);
 cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream);
@@ -20,6 +20,11 @@ cudaError_t launch_forces(const NetDev &d, cudaStream_t stream);
 cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
                           cudaStream_t stream);
 cudaError_t launch_affine_batch(const NetDev *nets_dev, const double4 *prm_dev, int n_nets, cudaStream_t stream);
+/* get_inv_mats over n_elems triangles (vertex v of element e at
+ * facets[stride * e + v]) and dilate over n nodes. */
+cudaError_t launch_inv_mats(const double *pos, const int *facets, int stride, int n_elems, double *inv,
+                            cudaStream_t stream);
+cudaError_t launch_dilate(double2 *x, int n, double minx, double miny, double factor, cudaStream_t stream);
 
 cudaError_t launch_mixed_batch(const NetDev *nets_dev, int n_nets, int max_nodes, const FireParamsDev &p,
                                int *queue_dev, const int *order_dev, cudaStream_t stream);

@@ -10,6 +10,7 @@
  * written to .dat and read back is bit-identical.
  */
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <map>
@@ -345,6 +346,82 @@ extern "C" int nr_gen_mikado(int n_fibers, double fiber_len, double k0, double k
         net->tri_phi0.push_back(rest_phi0(net->points, h, j, k, wj, wk, 1.0));
     }
     nr::y_range(net->points, net->miny, net->maxy);
+    *out = net;
+    return NR_OK;
+}
+
+/* Fiber network embedded in a gel, the input of network_mesh_relax.cu (the
+ * reference ships no such files).  Nodes on an nx x ny unit grid plus a copy
+ * of column 0 at x = nx, the mesh's right edge, which the reader's
+ * duplicate-vertex search pairs with column 0.  Every grid cell is split
+ * along its up-right diagonal into two gel triangles; their areas are
+ * computed from the positions.  The network lives on columns 0..nx-1: bonds
+ * right (wrapping from nx-1 to 0), up and up-right, each kept with
+ * probability p; the copied column carries gel only.  jitter moves interior
+ * nodes by U(-jitter, jitter) in x and y; column 0 (and its copy) moves in
+ * y only, and the top and bottom rows move in x only. */
+extern "C" int nr_gen_lattice_mesh(int nx, int ny, double p, double jitter, uint64_t seed, nr_host_network **out) {
+    if (!out || nx < 2 || ny < 2 || (long)(nx + 1) * ny > (1L << 28) || !(p >= 0 && p <= 1) ||
+        !(jitter >= 0 && jitter < 0.25))
+        return fail(NR_ERR_INVALID, "nr_gen_lattice_mesh: bad arguments");
+    SplitMix64 rng(seed);
+    const int W = nx + 1;
+    auto id = [W](int i, int j) { return j * W + i; };
+    auto *net = new nr_host_network();
+    net->n_points = W * ny;
+    net->offset = nx;
+    net->points.resize(2 * (size_t)net->n_points);
+    std::vector<double> &pt = net->points;
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const double dx = jitter * (2.0 * rng.uniform() - 1.0);
+            const double dy = jitter * (2.0 * rng.uniform() - 1.0);
+            pt[2 * id(i, j)] = i + (i == 0 ? 0.0 : dx);
+            pt[2 * id(i, j) + 1] = j + (j == 0 || j == ny - 1 ? 0.0 : dy);
+        }
+    for (int j = 0; j < ny; ++j) {
+        pt[2 * id(nx, j)] = pt[2 * id(0, j)] + nx;
+        pt[2 * id(nx, j) + 1] = pt[2 * id(0, j) + 1];
+    }
+    auto link = [&](int a, int b, int wrap) {
+        net->edge_ij.push_back(a);
+        net->edge_ij.push_back(b);
+        net->edge_wrap.push_back((signed char)wrap);
+        net->edge_l0.push_back(rest_length(pt, a, b, wrap, net->offset));
+    };
+    for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const bool last = i == nx - 1;
+            const int right = last ? 0 : i + 1;
+            if (rng.uniform() < p) link(id(i, j), id(right, j), last ? 1 : 0);
+            const double u_up = rng.uniform(), u_diag = rng.uniform();
+            if (j + 1 < ny) {
+                if (u_up < p) link(id(i, j), id(i, j + 1), 0);
+                if (u_diag < p) link(id(i, j), id(right, j + 1), last ? 1 : 0);
+            }
+        }
+    auto area = [&](int a, int b, int c) {
+        const double ux = pt[2 * b] - pt[2 * a], uy = pt[2 * b + 1] - pt[2 * a + 1];
+        const double vx = pt[2 * c] - pt[2 * a], vy = pt[2 * c + 1] - pt[2 * a + 1];
+        return 0.5 * std::fabs(ux * vy - uy * vx);
+    };
+    for (int j = 0; j + 1 < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+            const int a = id(i, j), b = id(i + 1, j), c = id(i, j + 1), d = id(i + 1, j + 1);
+            const int tris[2][3] = {{a, b, d}, {a, d, c}};
+            for (const auto &t : tris) {
+                net->facets.insert(net->facets.end(), t, t + 3);
+                net->areas.push_back(area(t[0], t[1], t[2]));
+            }
+        }
+    nr::y_range(pt, net->miny, net->maxy);
+    net->minx = FLT_MAX;
+    net->maxx = FLT_MIN;
+    for (int v = 0; v < net->n_points; ++v) {
+        net->minx = std::min(net->minx, pt[2 * v]);
+        net->maxx = std::max(net->maxx, pt[2 * v]);
+    }
+    nr::find_mesh_pairs(pt, net->offset, net->minx, net->mesh_pairs);
     *out = net;
     return NR_OK;
 }

@@ -533,7 +533,7 @@ static __device__ __noinline__ void anchor_eval(const NetDev &d, const Team &tm,
         }
     for (int i = tm.first(); i < d.n; i += tm.stride()) {
         double fx, fy;
-        node_force_fp64(d, i, fx, fy);
+        node_force_fp64_own<false>(d, i, fx, fy);
         d.f[i] = make_double2(fx, fy);
         const float hx = (float)fx, hy = (float)fy;
         d.fa_hi[i] = make_float2(hx, hy);
@@ -624,9 +624,9 @@ struct MixShared {
  * line, like anchor_eval: the FP64 code's register demand stays out of the
  * FP32 loop. */
 static __device__ __noinline__ void mixed_energies(const NetDev &d, double *s_red) {
-    energy_tiles(d, 0, 1, s_red);
-    double es, eb;
-    energy_final(d, s_red, es, eb);
+    energy_tiles<false>(d, 0, 1, s_red);
+    double es, eb, eg;
+    energy_final(d, s_red, es, eb, eg);
     if (threadIdx.x == 0) {
         d.st->e_stretch = es;
         d.st->e_bend = eb;

@@ -14,6 +14,13 @@
  *   bptr/bent      int[N+1]/int[2E]  incidence: (bond << 1) | role
  *   tptr/tent      int[N+1]/int[3T]  incidence: (triple << 2) | role
  *   part           double[4 * n_units]  reduction partials
+ * Networks embedded in a gel (network_mesh_relax.cu) add
+ *   elem           int4[F]      FEM triangle {v1, v2, v3, 0}
+ *   elem_inv       double[6F]   reference inverse matrix (get_inv_mats layout)
+ *   elem_area      double[F]
+ *   efrc           double4[3F]  per element and vertex the gel force terms
+ *   eptr/eent      int[N+1]/int[3F] incidence: 3 * element + role
+ *   partner        int[N]       duplicate vertex (-1: none)
  * Canonical reduction (identical to the oracle's or_canon_sum): items are
  * grouped in tiles of 256 (8 chunks of 32, one warp each); a chunk is reduced
  * by an xor butterfly (16, 8, 4, 2, 1), the 8 chunk sums of a tile by the tree
@@ -60,7 +67,8 @@ struct __align__(128) FireState {
     MixScal mix;    /* mixed precision, multi-CTA teams */
     int anchor_now; /* mixed precision: the team re-anchors before the next pass */
     int yielded;    /* mixed precision: left at an anchor for a larger cluster (fire_dsm.cu) */
-    int pad[10];
+    double e_gel;   /* gel energy (networks embedded in a gel) */
+    int pad[8];
     unsigned int bar_count, bar_gen, abort_flag, timeout_site;
     unsigned int pad2[28];
 };
@@ -93,8 +101,26 @@ struct NetDev {
     double2 *bfrc;  /* FP64 path: force of every bond on its first endpoint */
     double4 *tfrc;  /* FP64 path: (F_j, F_k) of every triple */
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
-    double *epart;  /* 2 * max(bond tiles, triple tiles) energy partials */
+    double *epart;  /* 3 * max(bond, triple, element tiles) energy partials */
     FireState *st;
+    /* gel coupling (network_mesh_relax.cu), read only when use_gel; kept
+     * behind one pointer so the descriptor the mixed-precision kernels
+     * stage in shared memory stays small */
+    int use_gel, n_elems;
+    const struct NetGel *gel;
+};
+
+/* Gel of a network embedded in a gel: shear and bulk moduli, preferred
+ * dilation (active when bmod > 0, network_mesh_relax.cu:908) and its FEM
+ * triangles. */
+struct NetGel {
+    double smod, bmod, gdil;
+    const int4 *elem;
+    double *elem_inv;
+    const double *elem_area;
+    double4 *efrc; /* per element and vertex {x term 1, x term 2, y term 1, y term 2} */
+    const int *eptr, *eent;
+    const int *partner;
 };
 
 /* Layout of a network for the distributed-shared-memory cluster kernel

@@ -20,8 +20,16 @@ struct nr_host_network {
     std::vector<double> bond_k;       // empty or E
     std::vector<double> tri_kb;       // empty or T
     std::vector<double> tri_phi0;     // empty or T
+    // network-mesh composites (network_mesh_relax.cu): FEM triangles, their
+    // areas, pairs of duplicate vertices on the left / right edges, x range
+    std::vector<int> facets;          // 3F
+    std::vector<double> areas;        // F
+    std::vector<int> mesh_pairs;      // 2P
+    double minx = 0, maxx = 0;
     int n_edges() const { return (int)edge_l0.size(); }
     int n_triples() const { return (int)(tri_hjk.size() / 3); }
+    int n_facets() const { return (int)(facets.size() / 3); }
+    int n_mesh_pairs() const { return (int)(mesh_pairs.size() / 2); }
 };
 
 namespace nr {
@@ -43,6 +51,10 @@ void build_incidence(int n_points, const int *edge_ij, int n_edges, const int *t
 /* Min/max y in the reader's convention (min starts at FLT_MAX, max at
  * FLT_MIN). */
 void y_range(const std::vector<double> &points, double &miny, double &maxy);
+
+/* The duplicate-vertex search of read_network_mesh
+ * (network_mesh_relax.cu:219-227): 2P indices. */
+void find_mesh_pairs(const std::vector<double> &points, double offset, double minx, std::vector<int> &pairs);
 
 }  // namespace nr
 

@@ -1,6 +1,6 @@
-"""Python bindings of the oracle (nr_oracle.c) and of the reference compiled
-for the host (oracle/_ref/liblsr_ref.so, present only where the reference
-checkout exists).
+"""Python bindings of the oracle (nr_oracle.c, nr_oracle_mesh.c) and of the
+reference compiled for the host (oracle/_ref/liblsr_ref.so and
+oracle/_ref/libnmr_ref.so, present only where the reference checkout exists).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg, never by the product package.
@@ -14,6 +14,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libnr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblsr_ref.so")
+REF_MESH_SO = os.path.join(HERE, "_ref", "libnmr_ref.so")
+SOURCES = ["nr_oracle.c", "nr_oracle_mesh.c", "nr_oracle.h", "nr_oracle_internal.h"]
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int)
@@ -31,7 +33,9 @@ class OrModel(C.Structure):
     _fields_ = [("n_points", C.c_int), ("n_edges", C.c_int), ("n_triples", C.c_int), ("width", C.c_double),
                 ("ks", C.c_double), ("kb", C.c_double), ("edge_ij", ip), ("edge_l0", dp), ("edge_wrap", bp),
                 ("tri_hjk", ip), ("tri_wrap", bp), ("fcodes", ubp), ("bond_k", dp), ("tri_kb", dp),
-                ("tri_phi0", dp)]
+                ("tri_phi0", dp), ("n_elems", C.c_int), ("n_mpairs", C.c_int), ("smod", C.c_double),
+                ("bmod", C.c_double), ("gel_dilation", C.c_double), ("elems", ip), ("inv_mats", dp),
+                ("areas", dp), ("mpairs", ip)]
 
 
 class OrParams(C.Structure):
@@ -42,20 +46,26 @@ class OrParams(C.Structure):
 
 class OrReport(C.Structure):
     _fields_ = [("rms_force", C.c_double), ("max_force", C.c_double), ("e_stretch", C.c_double),
-                ("e_bend", C.c_double), ("steps", C.c_int), ("converged", C.c_int)]
+                ("e_bend", C.c_double), ("steps", C.c_int), ("converged", C.c_int), ("e_gel", C.c_double)]
+
+
+class OrMesh(C.Structure):
+    _fields_ = [("net", OrNet), ("n_facets", C.c_int), ("n_areas", C.c_int), ("n_mpairs", C.c_int), ("facets", ip),
+                ("areas", dp),
+                ("mpairs", ip), ("minx", C.c_double), ("maxx", C.c_double)]
 
 
 def build(force=False):
     """Compiles libnr_oracle.so (gcc, seconds)."""
-    src = os.path.join(HERE, "nr_oracle.c")
     if force or not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "nr_oracle.h"))):
+            os.path.getmtime(os.path.join(HERE, f)) for f in SOURCES):
         subprocess.run(["bash", os.path.join(HERE, "build_oracle.sh")], check=True)
     return ORACLE_SO
 
 
 def build_ref():
-    """Builds oracle/_ref/liblsr_ref.so when the reference checkout exists."""
+    """Builds oracle/_ref/liblsr_ref.so (and libnmr_ref.so) when the reference
+    checkout exists."""
     subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
     return REF_SO if os.path.exists(REF_SO) else None
 
@@ -90,6 +100,20 @@ def lib():
                                C.c_int, dp]
         L.or_fire_batch.argtypes = [C.c_int, C.POINTER(OrModel), C.POINTER(dp), C.POINTER(OrParams),
                                     C.POINTER(OrReport), C.c_int]
+        L.or_read_network_mesh.argtypes = [C.c_char_p, C.POINTER(OrMesh)]
+        L.or_free_mesh.argtypes = [C.POINTER(OrMesh)]
+        L.or_mesh_pairs.restype = C.c_int
+        L.or_mesh_pairs.argtypes = [C.c_int, dp, C.c_double, C.c_double, ip]
+        L.or_inv_mats.argtypes = [C.c_int, dp, ip, dp]
+        L.or_dilate.argtypes = [C.c_int, dp, C.c_double, C.c_double, C.c_double]
+        L.or_gel_forces.argtypes = [C.POINTER(OrModel), dp, dp]
+        L.or_gel_energy.restype = C.c_double
+        L.or_gel_energy.argtypes = [C.POINTER(OrModel), dp]
+        L.or_preferred_dilation.restype = C.c_double
+        L.or_preferred_dilation.argtypes = [C.c_double] * 5
+        L.or_mesh_sweep.restype = C.c_int
+        L.or_mesh_sweep.argtypes = [C.POINTER(OrModel), dp, C.c_double, C.c_double, C.POINTER(OrParams), dp, dp,
+                                    dp, C.c_int, dp]
         _or = L
     return _or
 
@@ -152,7 +176,9 @@ def triples_of(points, edge_ij, edge_wrap, offset):
 class Model:
     """Holds numpy arrays alive behind an OrModel."""
 
-    def __init__(self, a, ks, kb, fcodes=None):
+    def __init__(self, a, ks, kb, fcodes=None, gel=None):
+        """gel: None or dict(elems (F,3), inv_mats (F,6), areas (F,), mpairs
+        (P,2), smod, bmod, dilation) -- the network_mesh_relax.cu model."""
         self.a = {k: v for k, v in a.items()}
         n = len(a["points"])
         self.edge_ij = np.ascontiguousarray(a["edge_ij"], np.int32)
@@ -183,6 +209,20 @@ class Model:
         m.bond_k = _d(self.bond_k)
         m.tri_kb = _d(self.tri_kb)
         m.tri_phi0 = _d(self.tri_phi0)
+        if gel is not None:
+            self.elems = np.ascontiguousarray(gel["elems"], np.int32).reshape(-1, 3)
+            self.inv_mats = np.ascontiguousarray(gel["inv_mats"], np.float64).reshape(-1, 6)
+            self.areas = np.ascontiguousarray(gel["areas"], np.float64)
+            self.mpairs = np.ascontiguousarray(gel["mpairs"], np.int32).reshape(-1, 2)
+            m.n_elems = len(self.elems)
+            m.n_mpairs = len(self.mpairs)
+            m.smod = gel["smod"]
+            m.bmod = gel["bmod"]
+            m.gel_dilation = gel["dilation"]
+            m.elems = _i(self.elems)
+            m.inv_mats = _d(self.inv_mats)
+            m.areas = _d(self.areas)
+            m.mpairs = _i(self.mpairs)
         self.m = m
         self.n = n
 
@@ -206,6 +246,22 @@ class Model:
         rep = OrReport()
         lib().or_fire(C.byref(self.m), _d(x), _d(v), _d(F), C.byref(params), C.byref(rep))
         return x, v, F, rep
+
+    def gel_energy(self, pos):
+        pos = np.ascontiguousarray(pos, np.float64)
+        return lib().or_gel_energy(C.byref(self.m), _d(pos))
+
+    def mesh_sweep(self, pos, miny, height, params, compr, shear, max_records=1000, keep_positions=True):
+        """network_mesh_relax.cu's compression then shear protocol on a
+        prepared (dilated) model; records of 9 values."""
+        x = np.ascontiguousarray(pos, np.float64).copy()
+        recs = np.zeros((max_records, 9))
+        shp = np.zeros((max_records, self.n, 2)) if keep_positions else None
+        c = np.ascontiguousarray(compr, np.float64)
+        s = np.ascontiguousarray(shear, np.float64)
+        nrec = lib().or_mesh_sweep(C.byref(self.m), _d(x), miny, height, C.byref(params), _d(c), _d(s), _d(recs),
+                                   max_records, _d(shp))
+        return recs[:nrec], (shp[:nrec] if shp is not None else None), x
 
     def sweep(self, pos, miny, yrange, params, compr, shear, max_records=1000, keep_positions=True):
         x = np.ascontiguousarray(pos, np.float64).copy()
@@ -282,6 +338,70 @@ def fire_batch(models, positions, prm, n_threads):
     return xs, [reps[i] for i in range(n)]
 
 
+# ------------------------------------------------------------ mesh composites
+
+def read_network_mesh(path, triple_offset=None):
+    """or_read_network_mesh -> (ok, dict); triples from or_get_triples with
+    period triple_offset (default: the file's offset)."""
+    L = lib()
+    mesh = OrMesh()
+    ok = L.or_read_network_mesh(str(path).encode(), C.byref(mesh))
+    net = mesh.net
+
+    def arr(ptr, shape, dtype):
+        n = int(np.prod(shape))
+        return np.ctypeslib.as_array(ptr, shape).astype(dtype) if n and ptr else np.zeros(shape, dtype)
+
+    a = {
+        "offset": net.offset, "miny": net.miny, "maxy": net.maxy, "minx": mesh.minx, "maxx": mesh.maxx,
+        "points": arr(net.points, (net.n_points, 2), np.float64),
+        "edge_ij": arr(net.edge_ij, (net.n_edges, 2), np.int32),
+        "edge_l0": arr(net.edge_l0, (net.n_edges,), np.float64),
+        "edge_wrap": arr(net.edge_wrap, (net.n_edges,), np.int8),
+        "facets": arr(mesh.facets, (mesh.n_facets, 3), np.int32),
+        "areas": arr(mesh.areas, (mesh.n_areas,), np.float64),
+        "mpairs": arr(mesh.mpairs, (mesh.n_mpairs, 2), np.int32),
+    }
+    L.or_free_mesh(C.byref(mesh))
+    if len(a["points"]):
+        a["tri_hjk"], a["tri_wrap"] = triples_of(a["points"], a["edge_ij"], a["edge_wrap"],
+                                                 a["offset"] if triple_offset is None else triple_offset)
+    else:
+        a["tri_hjk"], a["tri_wrap"] = np.zeros((0, 3), np.int32), np.zeros((0, 2), np.int8)
+    return bool(ok), a
+
+
+def mesh_pairs(points, offset, minx):
+    pts = np.ascontiguousarray(points, np.float64).reshape(-1, 2)
+    out = np.zeros((max(1, len(pts)), 2), np.int32)
+    n = lib().or_mesh_pairs(len(pts), _d(pts), float(offset), float(minx), _i(out))
+    return out[:n].copy()
+
+
+def inv_mats(pos, elems):
+    p = np.ascontiguousarray(pos, np.float64)
+    el = np.ascontiguousarray(elems, np.int32).reshape(-1, 3)
+    out = np.zeros((len(el), 6))
+    lib().or_inv_mats(len(el), _d(p), _i(el), _d(out))
+    return out
+
+
+def dilate(pos, minx, miny, factor):
+    x = np.ascontiguousarray(pos, np.float64).copy()
+    lib().or_dilate(len(x), _d(x), float(minx), float(miny), float(factor))
+    return x
+
+
+def preferred_dilation(ks, e_stretch_dilated, area, dilation, bmod):
+    return lib().or_preferred_dilation(float(ks), float(e_stretch_dilated), float(area), float(dilation), float(bmod))
+
+
+def mesh_gel(a, smod, bmod, dilation, inv=None):
+    """The gel dict Model takes, inverse matrices from a's points."""
+    return {"elems": a["facets"], "inv_mats": inv_mats(a["points"], a["facets"]) if inv is None else inv,
+            "areas": a["areas"], "mpairs": a["mpairs"], "smod": smod, "bmod": bmod, "dilation": dilation}
+
+
 # ---------------------------------------------------------------- reference
 
 _ref = None
@@ -353,3 +473,123 @@ def ref_affine_displace(pos, miny, yrange, xdisp, ydisp):
     x = np.ascontiguousarray(pos, np.float64).copy()
     ref_lib().ref_affine_displace(len(x), _d(x), miny, yrange, xdisp, ydisp)
     return x
+
+
+_ref_mesh = None
+
+
+def ref_mesh_lib():
+    """network_mesh_relax.cu compiled for the host, or None when unavailable."""
+    global _ref_mesh
+    if _ref_mesh is None:
+        if not os.path.exists(REF_MESH_SO):
+            return None
+        L = C.CDLL(REF_MESH_SO)
+        L.ref_load_mesh.restype = C.c_void_p
+        L.ref_load_mesh.argtypes = [C.c_char_p, C.c_int, C.c_double]
+        L.ref_free_mesh.argtypes = [C.c_void_p]
+        L.ref_mesh_info.argtypes = [C.c_void_p, ip, dp]
+        L.ref_mesh_arrays.argtypes = [C.c_void_p, dp, ip, dp, bp, ip, bp, ip, dp, ip]
+        L.ref_get_inv_mats.argtypes = [C.c_int, C.c_int, dp, ip, dp]
+        L.ref_dilate.argtypes = [C.c_int, dp, C.c_double, C.c_double, C.c_double]
+        L.ref_mesh_forces.argtypes = ([C.c_int] * 5 + [C.c_double] * 6 +
+                                      [dp, ip, dp, bp, ip, bp, ip, dp, dp, ip, ubp, dp])
+        L.ref_gel_energies.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, ip, dp, dp, dp]
+        L.ref_mesh_run_fire_md.argtypes = ([C.c_int] * 5 + [C.c_double] * 6 +
+                                           [dp, ip, dp, bp, ip, bp, ip, dp, dp, ip, ubp, dp, C.c_double, C.c_double,
+                                            C.c_int, C.c_int, dp, ip])
+        L.ref_mesh_do_relaxation_run.argtypes = ([C.c_char_p] * 4 + [C.c_double] * 5 +
+                                                 [dp, C.c_int, C.c_double, C.c_double, C.c_int, dp, dp])
+        L.ref_mesh_parse_batch_file.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int, dp, dp, ip,
+                                                dp, dp, ip, dp, dp]
+        L.ref_nmrelax_main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+        _ref_mesh = L
+    return _ref_mesh
+
+
+def ref_read_network_mesh(path, triple_offset=None):
+    """The reference's read_network_mesh (+ get_triples with period
+    triple_offset, default the file's offset) -> (ok, dict)."""
+    L = ref_mesh_lib()
+    h = L.ref_load_mesh(str(path).encode(), 1, -1.0 if triple_offset is None else float(triple_offset))
+    counts = (C.c_int * 6)()
+    box = (C.c_double * 5)()
+    ok = L.ref_mesh_info(h, counts, box)
+    n, e, t, f, p, na = list(counts)
+    a = {"points": np.zeros((n, 2)), "edge_ij": np.zeros((e, 2), np.int32), "edge_l0": np.zeros(e),
+         "edge_wrap": np.zeros(e, np.int8), "tri_hjk": np.zeros((t, 3), np.int32), "tri_wrap": np.zeros((t, 2), np.int8),
+         "facets": np.zeros((f, 3), np.int32), "areas": np.zeros(na), "mpairs": np.zeros((p, 2), np.int32)}
+    L.ref_mesh_arrays(h, _d(a["points"]), _i(a["edge_ij"]), _d(a["edge_l0"]), _b(a["edge_wrap"]), _i(a["tri_hjk"]),
+                      _b(a["tri_wrap"]), _i(a["facets"]), _d(a["areas"]), _i(a["mpairs"]))
+    L.ref_free_mesh(h)
+    a.update(offset=box[0], minx=box[1], miny=box[2], maxx=box[3], maxy=box[4])
+    return bool(ok), a
+
+
+def _ref_model_args(a, gel, fcodes):
+    ij = np.ascontiguousarray(a["edge_ij"], np.int32)
+    l0 = np.ascontiguousarray(a["edge_l0"], np.float64)
+    w = np.ascontiguousarray(a["edge_wrap"], np.int8)
+    hjk = np.ascontiguousarray(a["tri_hjk"], np.int32)
+    tw = np.ascontiguousarray(a["tri_wrap"], np.int8)
+    el = np.ascontiguousarray(gel["elems"], np.int32)
+    ar = np.ascontiguousarray(gel["areas"], np.float64)
+    inv = np.ascontiguousarray(gel["inv_mats"], np.float64)
+    mp = np.ascontiguousarray(gel["mpairs"], np.int32)
+    fc = np.ascontiguousarray(fcodes, np.uint8)
+    keep = (ij, l0, w, hjk, tw, el, ar, inv, mp, fc)
+    counts = [len(l0), len(hjk), len(el), len(mp)]
+    ptrs = [_i(ij), _d(l0), _b(w), _i(hjk), _b(tw), _i(el), _d(ar), _d(inv), _i(mp), fc.ctypes.data_as(ubp)]
+    return keep, counts, ptrs
+
+
+def ref_mesh_forces(a, pos, width, ks, kb, gel, fcodes):
+    """One force evaluation by the reference's kernels, run_fire_md's order."""
+    L = ref_mesh_lib()
+    x = np.ascontiguousarray(pos, np.float64)
+    F = np.zeros_like(x)
+    keep, counts, ptrs = _ref_model_args(a, gel, fcodes)
+    L.ref_mesh_forces(len(x), *counts, width, ks, kb, gel["smod"], gel["bmod"], gel["dilation"], _d(x), *ptrs, _d(F))
+    del keep
+    return F
+
+
+def ref_gel_energies(pos, gel):
+    L = ref_mesh_lib()
+    x = np.ascontiguousarray(pos, np.float64)
+    el = np.ascontiguousarray(gel["elems"], np.int32)
+    ar = np.ascontiguousarray(gel["areas"], np.float64)
+    inv = np.ascontiguousarray(gel["inv_mats"], np.float64)
+    out = np.zeros(len(el))
+    L.ref_gel_energies(len(x), len(el), gel["smod"], gel["bmod"], gel["dilation"], _d(x), _i(el), _d(ar), _d(inv),
+                       _d(out))
+    return out
+
+
+def ref_mesh_run_fire_md(a, pos, width, ks, kb, gel, fcodes, fire_params, mass, fcut, max_steps, nmin):
+    """network_mesh_relax.cu's run_fire_md (host-compiled) ->
+    (pos, report[4], steps)."""
+    L = ref_mesh_lib()
+    x = np.ascontiguousarray(pos, np.float64).copy()
+    keep, counts, ptrs = _ref_model_args(a, gel, fcodes)
+    rep = (C.c_double * 4)()
+    steps = C.c_int()
+    fp = np.ascontiguousarray(fire_params, np.float64)
+    L.ref_mesh_run_fire_md(len(x), *counts, width, ks, kb, gel["smod"], gel["bmod"], gel["dilation"], _d(x), *ptrs,
+                           _d(fp), mass, fcut, max_steps, nmin, rep, C.byref(steps))
+    del keep
+    return x, [rep[i] for i in range(4)], steps.value
+
+
+def ref_dilate(pos, minx, miny, factor):
+    x = np.ascontiguousarray(pos, np.float64).copy()
+    ref_mesh_lib().ref_dilate(len(x), _d(x), float(minx), float(miny), float(factor))
+    return x
+
+
+def ref_get_inv_mats(pos, elems):
+    p = np.ascontiguousarray(pos, np.float64)
+    el = np.ascontiguousarray(elems, np.int32).reshape(-1, 3)
+    out = np.zeros((len(el), 6))
+    ref_mesh_lib().ref_get_inv_mats(len(p), len(el), _d(p), _i(el), _d(out))
+    return out

@@ -5,6 +5,7 @@
  */
 #define _GNU_SOURCE
 #include "nr_oracle.h"
+#include "nr_oracle_internal.h"
 
 #include <float.h>
 #include <math.h>
@@ -17,16 +18,9 @@
 /* Line reader with std::getline / istream::eof semantics.                   */
 /* ------------------------------------------------------------------------ */
 
-typedef struct {
-    FILE *f;
-    int eof;
-    char *buf;
-    size_t cap;
-} or_lines;
-
 /* Reads the next line into r->buf (without '\n').  Sets r->eof when the end
  * of the file is reached before a '\n', as getline() on an ifstream does. */
-static const char *or_getline(or_lines *r) {
+const char *or_getline(or_lines *r) {
     ssize_t n = getline(&r->buf, &r->cap, r->f);
     if (n < 0) {
         r->eof = 1;
@@ -353,6 +347,7 @@ void or_forces(const or_model *m, const double *pos, double *F) {
             F[2 * k + 1] = F[2 * k + 1] + fky * (double)((ck & 2) >> 1);
         }
     }
+    if (m->bmod > 0) or_gel_forces(m, pos, F);
 }
 
 /* large_strain_relax.cu:472-490 and :493-523, each summed with the
@@ -488,6 +483,7 @@ int or_fire(const or_model *m, double *x, double *v, double *F, const or_fire_pa
     rep->steps = step;
     rep->converged = converged;
     or_energies(m, x, &rep->e_stretch, &rep->e_bend);
+    rep->e_gel = m->bmod > 0 ? or_gel_energy(m, x) : 0.0;
     free(scratch);
     return converged;
 }

@@ -59,6 +59,16 @@ typedef struct {
     const double *bond_k;
     const double *tri_kb;
     const double *tri_phi0;
+    /* Gel coupling of network_mesh_relax.cu (all zero / NULL = none): FEM
+     * triangles with their reference inverse matrices (get_inv_mats, :503-531,
+     * 6 per element) and areas, pairs of duplicate mesh vertices, shear and
+     * bulk moduli and the preferred dilation.  Active when bmod > 0 (:908, :952). */
+    int n_elems, n_mpairs;
+    double smod, bmod, gel_dilation;
+    const int *elems;       /* 3*n_elems */
+    const double *inv_mats; /* 6*n_elems */
+    const double *areas;    /* n_elems */
+    const int *mpairs;      /* 2*n_mpairs */
 } or_model;
 
 enum { OR_CRIT_RMS = 0, OR_CRIT_MAX = 1 };
@@ -75,6 +85,7 @@ typedef struct {
     double rms_force, max_force, e_stretch, e_bend;
     int steps;
     int converged;
+    double e_gel; /* report_data[3] of network_mesh_relax.cu's run_fire_md */
 } or_report;
 
 /* IO / topology (bit-exact restatements). */
@@ -122,6 +133,49 @@ double or_nonaffinity(int n_points, const double *pos0, const double *disp, doub
 
 void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_params *params, or_report *reps,
                    int n_threads);
+
+/* ---- network-mesh composites (network_mesh_relax.cu, nr_oracle_mesh.c) ---- */
+
+/* read_network_mesh (network_mesh_relax.cu:72-230): net as or_read_network
+ * fills it (offset, points, edges with l0, miny/maxy), plus facets (3F),
+ * areas (F), duplicate pairs (2P) and minx/maxx.  Returns 1 iff the
+ * reference's reader returns true. */
+typedef struct {
+    or_net net;
+    int n_facets, n_areas, n_mpairs; /* facets and areas read (they differ only on failure) */
+    int *facets;
+    double *areas;
+    int *mpairs;
+    double minx, maxx;
+} or_mesh;
+int or_read_network_mesh(const char *path, or_mesh *mesh);
+void or_free_mesh(or_mesh *mesh);
+/* The duplicate-vertex search of read_network_mesh (:219-227) over points;
+ * returns the number of pairs written to pairs (capacity 2*n_points ints). */
+int or_mesh_pairs(int n_points, const double *points, double offset, double minx, int *pairs);
+/* get_inv_mats (:503-531) from positions pos. */
+void or_inv_mats(int n_elems, const double *pos, const int *elems, double *inv_mats);
+/* dilate (:796-806) over the n_points nodes. */
+void or_dilate(int n_points, double *pos, double minx, double miny, double factor);
+/* gel_forces (:702-751) and duplicate_forces (:754-780) added to F, which
+ * holds the network forces (or_forces calls this when m->bmod > 0). */
+void or_gel_forces(const or_model *m, const double *pos, double *F);
+/* gel_energy (:674-699) summed as cublasDasum does (absolute values), with
+ * the canonical reduction. */
+double or_gel_energy(const or_model *m, const double *pos);
+/* The set-up of do_relaxation_run (:1256-1274): net_bmod = 2 E_s / area /
+ * dilation^2 from the stretch energy of the dilated network (0 when
+ * ks <= 0), and the preferred dilation dilation (bmod + net_bmod) / bmod. */
+double or_preferred_dilation(double ks, double e_stretch_dilated, double area, double dilation, double bmod);
+/* The compression then shear loops of network_mesh_relax.cu's
+ * do_relaxation_run (:1276-1376), strain mode, on a prepared model (pos
+ * dilated, m->gel_dilation the preferred dilation).  range = dilated height.
+ * Records (9 doubles) {curr_disp, max_comp, E_s, E_b, E_gel, rms, max|F|,
+ * steps, is_shear}; compression rows have curr_disp 0 and max_comp the
+ * compression, as the reference's edata file prints them. */
+int or_mesh_sweep(const or_model *m, double *pos, double miny, double range, const or_fire_params *p,
+                  const double compr[3], const double shear[3], double *records, int max_records,
+                  double *shear_pos);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,8 @@
 /*
  * Host stand-in for the four cuBLAS Level-1 routines the reference's FIRE
- * loop calls (large_strain_relax.cu:642, :655-690, :743, :751), in host
- * pointer mode, on host memory.  Test infrastructure only.
+ * loops call (large_strain_relax.cu:642, :655-690, :743, :751;
+ * network_mesh_relax.cu:917-970, :1030-1050, :1245), in host pointer mode,
+ * on host memory.  Test infrastructure only.
  *
  * axpy uses a fused multiply-add per element, as a GPU BLAS does; dot, nrm2
  * and asum are sequential sums in index order.  cuBLAS's own summation order

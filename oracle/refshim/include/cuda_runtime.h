@@ -1,15 +1,16 @@
 /*
  * Host stand-in for the CUDA runtime, used ONLY to compile the reference's
- * large_strain_relax.cu as plain C++ so that its own host logic
- * (read_network, get_triples, run_fire_md, do_relaxation_run) and its own
- * kernel bodies run sequentially on the CPU.  This is test infrastructure for
+ * large_strain_relax.cu and network_mesh_relax.cu as plain C++ so that their
+ * own host logic (readers, get_triples, run_fire_md, do_relaxation_run) and
+ * their own kernel bodies run sequentially on the CPU.  This is test infrastructure for
  * pinning the oracle; nothing in the product links it.
  *
  * "Device" memory is host memory.  Every allocation is padded to 3x its size
  * plus 4 KiB, zero-filled: the reference's affine_displace is launched over
  * 2N threads for N nodes (large_strain_relax.cu:928, :970, guard `>` at :533)
  * and bending_energies guards with `>` (:502), so both touch entries past the
- * end of their arrays.  On a GPU those writes land in whatever allocation
+ * end of their arrays; network_mesh_relax.cu's dilate and affine_displace
+ * are launched the same way (:1254, :1290).  On a GPU those writes land in whatever allocation
  * follows; here they land in the padding and are never read back.
  */
 #ifndef NR_REFSHIM_CUDA_RUNTIME_H
