@@ -255,9 +255,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
-    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5"],
+    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1"],
                     help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
-                         "first strain increment of its protocol, FIRE steps capped by --max-steps")
+                         "first strain increment of its protocol, FIRE steps capped by --max-steps; M1: the same "
+                         "for a network embedded in a gel (network_mesh_relax.cu, FP64 path)")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
@@ -432,7 +433,10 @@ SINGLE = {
     "C2": ("lattice 256x256, p=0.65, jitter 0.05, generator triples, seed 2", 1e-4, (0.01, 0.0)),
     "C5": ("lattice 1024x1024, p=0.65, jitter 0.05, generator triples, seed 5", 1e-4, (0.0025, 0.0)),
     "C3": ("Mikado, 15850 fibres of length 0.05, k = 1/l0, kb = kappa0/mean l0, seed 3", 1e-5, (0.0, -0.01)),
+    "M1": ("network in a gel (network_mesh_relax.cu): 1024x768 grid + copy column, p=0.65, no jitter, triples by "
+           "get_triples, 2 triangles per cell, seed 8; smod 0.3, bmod 1.0, dilation 0.02", 1e-4, (0.0025, 0.0)),
 }
+GEL_M1 = (0.3, 1.0, 0.02)
 
 
 def single_network(nr, name):
@@ -440,13 +444,31 @@ def single_network(nr, name):
         return nr.HostNetwork.lattice(256, 256, 0.65, 0.05, 2, line_triples=True), 1e-4, 0.1
     if name == "C5":
         return nr.HostNetwork.lattice(1024, 1024, 0.65, 0.05, 5, line_triples=True), 1e-4, 0.1
+    if name == "M1":
+        return nr.HostNetwork.lattice_mesh(1024, 768, 0.65, 0.0, 8).get_triples(), 1e-4, 0.1
     h = nr.HostNetwork.mikado(15850, 0.05, 1.0, 1e-5, 3)
     return h, 1.0, 0.05 * float(np.sqrt(h.arrays()["edge_l0"].min()))
 
 
+def mesh_cpu_baseline(h, gel, sx, sy, steps, threads=1):
+    """The oracle's FP64 FIRE (gel included) on the same composite, `steps`
+    iterations on one host thread: node-iterations/s."""
+    import oracle
+
+    a = h.arrays()
+    m = oracle.Model(a, 1.0, SINGLE["M1"][1], gel=oracle.mesh_gel(a, *gel))
+    H = a["maxy"] - a["miny"]
+    x0 = oracle.affine_displace(a["points"], a["miny"], H, sx * H, sy * H)
+    t0 = time.perf_counter()
+    _, _, _, rep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", max_steps=steps))
+    dt = time.perf_counter() - t0
+    return len(a["points"]) * rep.steps / dt, rep.steps, dt
+
+
 def single_network_arm(args):
-    """--workload C2|C3|C5: one large network relaxed by the cooperative
-    grid kernel (the whole GPU), FIRE steps capped: node-iterations/s."""
+    """--workload C2|C3|C5|M1: one large network relaxed by the cooperative
+    grid kernel (the whole GPU), FIRE steps capped: node-iterations/s.  M1
+    carries a gel (FP64 path)."""
     import torch
 
     import network_relaxation_gb300 as nr
@@ -455,7 +477,11 @@ def single_network_arm(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     h, kb, dt_max = single_network(nr, args.workload)
     info = h.info()
+    mesh = h.mesh_info()
     net = nr.Network(h, 1.0, kb)
+    if args.workload == "M1":
+        net.set_gel(*GEL_M1)
+        args.precision = "fp64"  # gel-coupled networks relax on the FP64 path
     H = net.maxy - net.miny
     sx, sy = SINGLE[args.workload][2]
     net.affine_displace(net.miny, H, sx * H, sy * H)
@@ -478,11 +504,18 @@ def single_network_arm(args):
             steps = rep.steps
     ms = float(np.mean(times))
     n, e, t = info.n_points, info.n_edges / info.n_points, info.n_triples / info.n_points
-    bpn = (145 + 17 * e + 14 * t) if args.precision == "fp64" else (73 + 24 * e + 12 * t)
+    g = mesh.n_facets / info.n_points if args.workload == "M1" else 0.0
+    bpn = (145 + 17 * e + 14 * t + 168 * g) if args.precision == "fp64" else (73 + 24 * e + 12 * t)
     hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
     rate = n * steps / (ms / 1e3)
     achieved = bpn * rate / 1e9
+    extra = {}
+    if args.workload == "M1" and rank == 0 and not args.no_cpu:
+        cpu_rate, cpu_steps, cpu_s = mesh_cpu_baseline(h, GEL_M1, sx, sy, 20)
+        extra["cpu_baseline"] = {"value": cpu_rate, "unit": "node-iterations/s", "cores": 1, "kind": "port",
+                                 "sample": "the oracle's FP64 FIRE with the gel, %d iterations of the same network "
+                                           "and strain step (%.1f s)" % (cpu_steps, cpu_s)}
     if rank == 0:
         print(json.dumps({
             "metric": "node-iterations/s, one network (%s), first strain step, FIRE capped at %d steps"
@@ -490,12 +523,13 @@ def single_network_arm(args):
             "value": rate, "unit": "node-iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "us_per_fire_step": 1e3 * ms / steps, "higher_is_better": True, "scaling": "replicas",
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
-            "config": {"workload": "%s: %s, N=%d E=%d T=%d" % (args.workload, SINGLE[args.workload][0], n,
-                                                                info.n_edges, info.n_triples),
+            "config": {"workload": "%s: %s, N=%d E=%d T=%d F=%d" % (args.workload, SINGLE[args.workload][0], n,
+                                                                     info.n_edges, info.n_triples, mesh.n_facets),
                        "precision": args.precision},
-            "gpu_launches": args.steps,
+            "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": None, "kernel": "k_fire_grid_mixed" if args.precision == "mixed" else "k_fire_grid"},
+            **extra,
         }))
     return 0
 
