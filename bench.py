@@ -255,10 +255,11 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
-    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1"],
+    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1"],
                     help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
                          "first strain increment of its protocol, FIRE steps capped by --max-steps; M1: the same "
-                         "for a network embedded in a gel (network_mesh_relax.cu, FP64 path)")
+                         "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
+                         "solve of sparse_relax.cpp on one large network")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
@@ -269,6 +270,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "L1":
+        return linear_response_arm(args)
     if args.workload != "C4":
         return single_network_arm(args)
 
@@ -531,6 +534,113 @@ def single_network_arm(args):
                          "traffic": None, "kernel": "k_fire_grid_mixed" if args.precision == "mixed" else "k_fire_grid"},
             **extra,
         }))
+    return 0
+
+
+L1 = dict(nx=1024, ny=1024, p=0.65, seed=10, ks=1.0, kb=1e-4, mu=0.01, shear=(0.0, 0.1, 0.01))
+
+
+def spr_cpu_baseline(n_side, budget_note):
+    """The same Jacobi-preconditioned CG on the host (scipy, one thread per
+    solve) for the same problem on an n_side^2 lattice: K assembled by the
+    oracle, the two unit loads to ||r|| <= 1e-12 ||b||.  (The reference's
+    SuiteSparseQR is not in this image; a sparse LU cannot factor these
+    matrices, which have the floppy modes of isolated clusters.)"""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    import network_relaxation_gb300 as nr
+    import oracle
+
+    h = nr.HostNetwork.lattice(n_side, n_side, L1["p"], 0.0, L1["seed"])
+    a = h.arrays()
+    rows, cols, vals = oracle.spr_stiffness(a, L1["ks"], L1["kb"], L1["mu"])
+    n = len(a["points"])
+    K = sp.coo_matrix((vals, (rows, cols)), shape=(2 * n, 2 * n)).tocsr()
+    K = K + sp.triu(K, 1).T
+    y = a["points"][:, 1]
+    free = np.repeat(~((y < a["miny"] + 1e-10) | (y > a["maxy"] - 1e-10)), 2)
+    bc = np.zeros((2 * n, 2))
+    bc[0::2, 1] = (y - a["miny"]) / (a["maxy"] - a["miny"])
+    bc[1::2, 0] = (a["miny"] - y) / (a["maxy"] - a["miny"])
+    Kff = K[free][:, free].tocsr()
+    rhs = -(K[free] @ bc)
+    d = Kff.diagonal()
+    M = sp.diags(np.where(d > 0, 1.0 / np.where(d > 0, d, 1.0), 0.0))
+    t0 = time.perf_counter()
+    for k in range(2):
+        u, info = sla.cg(Kff, rhs[:, k], rtol=1e-12, atol=0.0, M=M, maxiter=100000)
+        assert np.isfinite(u).all()
+    dt = time.perf_counter() - t0
+    return n, dt
+
+
+def linear_response_arm(args):
+    """--workload L1: sparse_relax.cpp's linear-response protocol on one
+    1024 x 1024 lattice (p = 0.65, collinear triples, background shear):
+    assembly excluded, the unit-load PCG solve plus every shear point of an
+    11-point protocol (residual, energies, displacement field to the host)
+    timed: node-solves/s = N x points / time."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    h = nr.HostNetwork.lattice(L1["nx"], L1["ny"], L1["p"], 0.0, L1["seed"])
+    n = h.n_points
+    spr = nr.Spr(h, L1["ks"], L1["kb"], L1["mu"])
+    info = spr.info()
+    W = info.maxx - info.minx
+    pts = [s * W for s in np.arange(L1["shear"][0], L1["shear"][1] + 1e-9, L1["shear"][2])]
+    host_u = torch.empty((n, 2), dtype=torch.float64).pin_memory()
+    times, solve_ms, iters = [], [], 0
+    stream = torch.cuda.current_stream()
+    for s in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        spr.solve(affine=True)
+        e1.record(stream)
+        for sh in pts:
+            rec = nr.SprRecord()
+            nr.check(spr._lib.nr_spr_point(spr._h, 0.0, float(sh), C.byref(rec),
+                                           C.cast(host_u.data_ptr(), C.POINTER(C.c_double)), None), "nr_spr_point")
+        e2.record(stream)
+        e2.synchronize()
+        if s >= args.warmup:
+            times.append(e0.elapsed_time(e2))
+            solve_ms.append(e0.elapsed_time(e1))
+            iters = max(spr.info().iterations)
+    info = spr.info()
+    ms = float(np.mean(times))
+    sms = float(np.mean(solve_ms))
+    nnz_full = 2 * info.nnz_upper  # upper entries, both triangles (the diagonal counted twice: negligible)
+    bytes_per_iter = 12.0 * nnz_full + 160.0 * info.n_free_dofs
+    achieved = bytes_per_iter * iters / (sms / 1e3) / 1e9
+    hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+           if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
+    extra = {}
+    if not args.no_cpu:
+        cn, cdt = spr_cpu_baseline(128, "")
+        extra["cpu_baseline"] = {"value": cn * len(pts) / cdt, "unit": "node-solves/s", "cores": 1, "kind": "port",
+                                 "sample": "the same Jacobi PCG in scipy (one thread), the two unit solves of the same "
+                                           "problem on a 128 x 128 lattice (%.2f s); the reference's SuiteSparseQR "
+                                           "is not in this image" % cdt}
+    print(json.dumps({
+        "metric": "node-solves/s, linear response of one network (L1: unit-load PCG + %d shear points)" % len(pts),
+        "value": n * len(pts) / (ms / 1e3), "unit": "node-solves/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "solve_ms": sms, "cg_iterations": iters,
+        "rel_residual": list(info.rel_residual), "higher_is_better": True, "scaling": "replicas",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "L1: lattice %dx%d, p=%g, no jitter, seed %d; ks %g, kb %g, mu %g; N=%d, free dofs %d, "
+                               "upper nnz %d, SELL entries %d" % (L1["nx"], L1["ny"], L1["p"], L1["seed"], L1["ks"],
+                                                                  L1["kb"], L1["mu"], n, info.n_free_dofs,
+                                                                  info.nnz_upper, info.sell_entries)},
+        "gpu_launches": args.steps * (1 + 5 * len(pts)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_spr_pcg"},
+        **extra,
+    }))
     return 0
 
 

@@ -322,6 +322,85 @@ int nr_mesh_run_fire_md(int num_dof, int npairs, int ntriples, int nelems, doubl
                         int max_steps, int nmin, double report_data[4], int *step_count, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Linear response (src/sparse_relax.cpp)                              */
+/* ------------------------------------------------------------------ */
+
+/* The reference's sp_relax does not run FIRE: it solves the harmonic
+ * (linearised) problem K_ff u = -(P^T K) bc for the free nodes, K the
+ * stiffness matrix of bond stretching (stiffness ks / l per bond,
+ * sparse_relax.cpp:280-323), linearised bending of the collinear triples
+ * (kb, :326-386) and background shear (mu, :390-429), P the projection that
+ * removes the clamped top and bottom rows (:560-605), bc the applied
+ * displacement field (affine, :528-538, or the top row only, :513-525). */
+typedef struct nr_spr nr_spr;
+
+typedef struct {
+    int n_points, n_free_dofs, n_triples;
+    long nnz_upper;    /* stored upper-triangle entries of K */
+    long sell_entries; /* device storage of the reduced matrix (SELL-32, padded) */
+    int iterations[2]; /* CG iterations of the last nr_spr_solve: unit compression, unit shear */
+    double rel_residual[2];
+    double minx, maxx, miny, maxy; /* read_network's ranges (max starts at FLT_MIN) */
+} nr_spr_info_t;
+
+/* One load point: what do_relaxation_run prints (SPR:820-870). */
+typedef struct {
+    double compression, shear; /* absolute displacements */
+    double e_total, e_ss, e_bend; /* linearised energies (:49-96) */
+    double residual;              /* ||rhs - K_ff u||_2, printed as "Residual RMS force" */
+    int iterations, status;
+} nr_spr_record;
+
+/* get_sparse_stiffness_mat (sparse_relax.cpp:434-480) on the host: the
+ * stored upper-triangle entries in (row, col) order, each the sum of its
+ * contributions in the reference's call order, |value| <= 1e-10 dropped
+ * (bit-identical to the reference).  Returns the count (arrays may be NULL
+ * to count) or a negative nr_status.  No GPU needed. */
+long nr_spr_assemble(const nr_host_network *net, double ks, double kb, double mu, long *rows, long *cols,
+                     double *vals);
+/* Assembles K (triples recomputed when kb > 0, as the reference does),
+ * the reduced system and uploads it. */
+int nr_spr_create(const nr_host_network *net, double ks, double kb, double mu, void *stream, nr_spr **out);
+int nr_spr_destroy(nr_spr *spr);
+void nr_spr_info(const nr_spr *spr, nr_spr_info_t *info);
+/* Solves the unit compression and unit shear loads of one loading mode
+ * (affine != 0: affine_displacement, else add_displacement) together by
+ * Jacobi-preconditioned CG to ||r|| <= tol ||b|| (the reference's SPQR
+ * solve, :793; on a singular system the minimum-norm solution, which is
+ * what its -n null-space removal intends).  NR_NOT_CONVERGED when
+ * max_iter is reached. */
+int nr_spr_solve(nr_spr *spr, int affine, double tol, int max_iter, void *stream);
+/* One load point from the unit solutions (linearity): u_final = bc + P u
+ * (:812-813), residual of this point's own system, energies.  u_final
+ * (2N doubles, host or device, may be NULL) receives the full
+ * displacement field (the .disp file's values). */
+int nr_spr_point(nr_spr *spr, double compression, double shear, nr_spr_record *rec, double *u_final, void *stream);
+
+/* sp_relax's batch file (sparse_relax.cpp:931-1037): base [tag] / ks kb mu
+ * / compression min max inc / shear min max inc. */
+typedef struct {
+    char base[1024];
+    char tag[256];
+    double ks, kb, mu;
+    double compr[3], shear[3];
+} nr_spr_spec;
+int nr_parse_spr_batch_file(const char *path, nr_spr_spec *spec);
+/* do_relaxation_run (sparse_relax.cpp:676-870) on one .dat file with the
+ * reference's outputs (log with "Residual RMS force", energy file, .disp
+ * files; empty names skip them).  strain_mode (-s): compression scaled by
+ * the height, shear by the width (:728-737); affine (default; -z clears
+ * it); itemize (-i): separate stretch+shear and bending columns. */
+int nr_spr_do_relaxation_run(const char *dat_name, const char *log_name, const char *disp_base, const char *e_name,
+                             const nr_spr_spec *spec, int strain_mode, int affine, int itemize);
+/* run_relaxation_batch (:1042-1093): increments of ranges narrower than
+ * 1e-10 become 1e12 (one value). */
+int nr_spr_relaxation_batch(const char *batch_file, int strain_mode, int affine, int itemize);
+/* The sp_relax command line (:1165-1232): -b batch [-s] [-z] [-i] [-n] [-g]
+ * (-n and -g accepted: CG already gives the null-space-free solution, and
+ * the solve always runs on the GPU). */
+int nr_sp_relax_main(int argc, char **argv);
+
+/* ------------------------------------------------------------------ */
 /* Post-relaxation analyses                                            */
 /* ------------------------------------------------------------------ */
 

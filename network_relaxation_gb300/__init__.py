@@ -17,7 +17,7 @@ from . import _capi
 from ._capi import (NR_CRIT_MAX, NR_CRIT_RMS, NR_ERR_CAPACITY, NR_ERR_CUDA, NR_ERR_INVALID, NR_ERR_IO,  # noqa: F401
                     NR_ERR_NONFINITE, NR_ERR_OOM, NR_ERR_PARSE, NR_ERR_TIMEOUT, NR_FP64, NR_MIXED,
                     NR_NOT_CONVERGED, NR_OK, BatchSpec, FireParams, MeshBatchSpec, MeshInfo, NetRelaxError, Report,
-                    StepRecord, check)
+                    SprInfo, SprRecord, SprSpec, StepRecord, check)
 
 __all__ = [
     "HostNetwork", "Network", "Batch", "fire_params", "read_network", "get_triples", "run_fire_md",
@@ -583,3 +583,81 @@ def nmrelax_main(argv):
     args = ["nmrelax"] + list(argv)
     arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
     return _capi.load().nr_nmrelax_main(len(args), arr)
+
+
+# ------------------------------------------------------------ linear response
+
+def spr_assemble(host, ks, kb, mu):
+    """get_sparse_stiffness_mat (sparse_relax.cpp:434): upper-triangle
+    (rows, cols, vals) in (row, col) order.  Host only."""
+    lib_ = _capi.load()
+    n = lib_.nr_spr_assemble(host.handle, float(ks), float(kb), float(mu), None, None, None)
+    if n < 0:
+        raise NetRelaxError(int(n), "nr_spr_assemble")
+    rows, cols, vals = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+    lib_.nr_spr_assemble(host.handle, float(ks), float(kb), float(mu), rows.ctypes.data_as(C.POINTER(C.c_long)),
+                         cols.ctypes.data_as(C.POINTER(C.c_long)), _dp(vals))
+    return rows, cols, vals
+
+
+class Spr:
+    """The linear-response problem of sparse_relax.cpp on the GPU (nr_spr)."""
+
+    def __init__(self, host, ks=1.0, kb=0.0, mu=0.0, stream=None):
+        self._lib = _capi.load()
+        out = C.c_void_p()
+        check(self._lib.nr_spr_create(host.handle, float(ks), float(kb), float(mu), _stream(stream), C.byref(out)),
+              "nr_spr_create")
+        self._h = out
+        self.n = host.n_points
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.nr_spr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def info(self):
+        i = SprInfo()
+        self._lib.nr_spr_info(self._h, C.byref(i))
+        return i
+
+    def solve(self, affine=True, tol=1e-12, max_iter=None, stream=None):
+        """The unit compression and shear loads (NR_OK or NR_NOT_CONVERGED)."""
+        if max_iter is None:
+            max_iter = max(1000, min(10 * self.info().n_free_dofs, 10_000_000))
+        return check(self._lib.nr_spr_solve(self._h, int(bool(affine)), float(tol), int(max_iter), _stream(stream)),
+                     "nr_spr_solve")
+
+    def point(self, compression, shear, want_u=True, stream=None):
+        """(SprRecord, full displacement field (N, 2) or None)."""
+        rec = SprRecord()
+        u = np.empty((self.n, 2), np.float64) if want_u else None
+        check(self._lib.nr_spr_point(self._h, float(compression), float(shear), C.byref(rec), _dp(u),
+                                     _stream(stream)), "nr_spr_point")
+        return rec, u
+
+
+def parse_spr_batch_file(path):
+    """parse_batch_file (sparse_relax.cpp:931): an SprSpec."""
+    spec = SprSpec()
+    check(_capi.load().nr_parse_spr_batch_file(str(path).encode(), C.byref(spec)), "parse_spr_batch_file",
+          ok=(NR_OK,))
+    return spec
+
+
+def spr_do_relaxation_run(dat_name, log_name, disp_base, e_name, spec, strain_mode=False, affine=True, itemize=False):
+    """do_relaxation_run (sparse_relax.cpp:676)."""
+    return check(_capi.load().nr_spr_do_relaxation_run(str(dat_name).encode(), str(log_name).encode(),
+                                                       str(disp_base).encode(), str(e_name).encode(), C.byref(spec),
+                                                       int(strain_mode), int(affine), int(itemize)),
+                 "spr_do_relaxation_run")
+
+
+def sp_relax_main(argv):
+    """The sp_relax command line (sparse_relax.cpp:1165)."""
+    args = ["sp_relax"] + list(argv)
+    arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
+    return _capi.load().nr_sp_relax_main(len(args), arr)

@@ -54,6 +54,22 @@ class StepRecord(C.Structure):
                 ("is_shear", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int), ("e_gel", C.c_double)]
 
 
+class SprInfo(C.Structure):
+    _fields_ = [("n_points", C.c_int), ("n_free_dofs", C.c_int), ("n_triples", C.c_int), ("nnz_upper", C.c_long),
+                ("sell_entries", C.c_long), ("iterations", C.c_int * 2), ("rel_residual", C.c_double * 2),
+                ("minx", C.c_double), ("maxx", C.c_double), ("miny", C.c_double), ("maxy", C.c_double)]
+
+
+class SprRecord(C.Structure):
+    _fields_ = [("compression", C.c_double), ("shear", C.c_double), ("e_total", C.c_double), ("e_ss", C.c_double),
+                ("e_bend", C.c_double), ("residual", C.c_double), ("iterations", C.c_int), ("status", C.c_int)]
+
+
+class SprSpec(C.Structure):
+    _fields_ = [("base", C.c_char * 1024), ("tag", C.c_char * 256), ("ks", C.c_double), ("kb", C.c_double),
+                ("mu", C.c_double), ("compr", C.c_double * 3), ("shear", C.c_double * 3)]
+
+
 class MeshInfo(C.Structure):
     _fields_ = [("n_facets", C.c_int), ("n_areas", C.c_int), ("n_mesh_pairs", C.c_int), ("minx", C.c_double),
                 ("maxx", C.c_double)]
@@ -122,6 +138,18 @@ SIGNATURES = {
                                       C.c_double, C.c_double, C.c_double, P, P, P, P, P, P, P, P, P, P, P, P,
                                       C.c_int, P, c_double_p, C.c_double, C.c_double, C.c_int, C.c_int, c_double_p,
                                       c_int_p, P]),
+    "nr_spr_assemble": (C.c_long, [P, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_long),
+                                    C.POINTER(C.c_long), c_double_p]),
+    "nr_spr_create": (C.c_int, [P, C.c_double, C.c_double, C.c_double, P, C.POINTER(P)]),
+    "nr_spr_destroy": (C.c_int, [P]),
+    "nr_spr_info": (None, [P, C.POINTER(SprInfo)]),
+    "nr_spr_solve": (C.c_int, [P, C.c_int, C.c_double, C.c_int, P]),
+    "nr_spr_point": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(SprRecord), c_double_p, P]),
+    "nr_parse_spr_batch_file": (C.c_int, [C.c_char_p, C.POINTER(SprSpec)]),
+    "nr_spr_do_relaxation_run": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(SprSpec),
+                                           C.c_int, C.c_int, C.c_int]),
+    "nr_spr_relaxation_batch": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int]),
+    "nr_sp_relax_main": (C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
     "nr_bond_strains": (C.c_int, [C.c_int, C.c_int, C.c_double, P, P, P, P, P, P]),
     "nr_linear_axial_energy": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, P, P, P, P, c_double_p, P]),
     "nr_nonaffinity": (C.c_int, [C.c_int, P, P, C.c_double, C.c_double, C.c_double, c_double_p, P]),

@@ -19,6 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnetrelax.so")
 CLI = os.path.join(HERE, "lsrelax")
 MESH_CLI = os.path.join(HERE, "nmrelax")
+SPR_CLI = os.path.join(HERE, "sp_relax")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -34,6 +35,7 @@ CUDA_UNITS = [
     ("api.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
     ("analysis.cu", ["--fmad=false"]),
+    ("spr.cu", ["--fmad=false"]),
 ]
 HOST_UNITS = ["host_network.cpp", "mesh_host.cpp", "generators.cpp", "driver.cpp"]
 
@@ -90,7 +92,7 @@ def build(verbose=False, force=False):
         tmp = LIB + ".tmp"
         _run([NVCC] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)
-    for cli, main in ((CLI, "lsrelax_main.cpp"), (MESH_CLI, "nmrelax_main.cpp")):
+    for cli, main in ((CLI, "lsrelax_main.cpp"), (MESH_CLI, "nmrelax_main.cpp"), (SPR_CLI, "sp_relax_main.cpp")):
         main_src = os.path.join(CSRC, main)
         if force or not _newer(cli, [main_src, LIB]):
             _run([CXX, "-std=c++17", "-O2", "-I", INCLUDE, main_src, "-o", cli, "-L", HERE, "-lnetrelax",
@@ -100,7 +102,7 @@ def build(verbose=False, force=False):
 
 def clean():
     shutil.rmtree(BUILD, ignore_errors=True)
-    for p in (LIB, CLI, MESH_CLI):
+    for p in (LIB, CLI, MESH_CLI, SPR_CLI):
         if os.path.exists(p):
             os.remove(p)
 

@@ -21,6 +21,7 @@
  * instead of falling through into -b with no argument.
  */
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -535,6 +536,204 @@ extern "C" {
 
 int nr_relaxation_batch(const char *batch_file, int precision, int criterion) {
     return relaxation_batch(batch_file, precision, criterion, 0, false);
+}
+
+/* parse_batch_file of sparse_relax.cpp:931-1037: blank and '#' lines are
+ * skipped before each of the four entries; the file must not end right
+ * after any of the first three. */
+int nr_parse_spr_batch_file(const char *path, nr_spr_spec *spec) {
+    if (!path || !spec) return fail(NR_ERR_INVALID, "nr_parse_spr_batch_file: null argument");
+    memset(spec, 0, sizeof(*spec));
+    std::ifstream input(path);
+    if (!input.is_open()) {
+        fprintf(stderr, "The file %s could not be read.\n", path);
+        return fail(NR_ERR_IO, std::string("cannot open ") + path);
+    }
+    std::string line;
+    auto next = [&](std::string &out) -> bool { /* next non-blank, non-comment line */
+        while (!input.eof()) {
+            std::getline(input, out);
+            if (out.empty() || out[0] == '#') continue;
+            return true;
+        }
+        return false;
+    };
+    bool got = false;
+    while (next(line)) {
+        std::vector<std::string> tok = split_ws(line);
+        if (!tok.empty()) {
+            snprintf(spec->base, sizeof(spec->base), "%s", tok[0].c_str());
+            if (tok.size() > 1) snprintf(spec->tag, sizeof(spec->tag), "%s", tok[1].c_str());
+            got = true;
+            break;
+        }
+    }
+    if (!got || input.eof()) {
+        fprintf(stderr, "Not enough information was found.\n");
+        return fail(NR_ERR_PARSE, "batch file: missing base name");
+    }
+    if (next(line) && (sscanf(line.c_str(), "%lf %lf %lf", &spec->ks, &spec->kb, &spec->mu) < 3 || spec->ks < 0 ||
+                       spec->kb < 0 || spec->mu < 0)) {
+        fprintf(stderr, "Error: invalid format for mechanical attributes.");
+        return fail(NR_ERR_PARSE, "batch file: invalid mechanical attributes");
+    }
+    for (int which = 0; which < 2; ++which) {
+        if (input.eof()) {
+            fprintf(stderr, "Not enough information was provided in the batch file.\n");
+            return fail(NR_ERR_PARSE, "batch file: truncated");
+        }
+        double *r = which == 0 ? spec->compr : spec->shear;
+        if (!next(line)) return fail(NR_ERR_PARSE, "batch file: missing strain range");
+        if (sscanf(line.c_str(), "%lf %lf %lf", &r[0], &r[1], &r[2]) < 3 || r[0] < 0 || r[1] < 0 || r[2] < 0 ||
+            r[1] < r[0]) {
+            fprintf(stderr, which == 0 ? "Error: invalid specification of compression."
+                                       : "Error: invalid format for mechanical attributes.");
+            return fail(NR_ERR_PARSE, "batch file: invalid strain range");
+        }
+    }
+    return NR_OK;
+}
+
+/* do_relaxation_run of sparse_relax.cpp:676-870. */
+int nr_spr_do_relaxation_run(const char *dat_name, const char *log_name, const char *disp_base, const char *e_name,
+                             const nr_spr_spec *spec, int strain_mode, int affine, int itemize) {
+    if (!dat_name || !spec) return fail(NR_ERR_INVALID, "nr_spr_do_relaxation_run: null argument");
+    FILE *log = (log_name && log_name[0]) ? fopen(log_name, "w") : nullptr;
+    const time_t start = time(nullptr);
+    nr_host_network *hn = nullptr;
+    int rc = nr_read_network(dat_name, &hn);
+    if (rc != NR_OK) {
+        fprintf(stderr, "A properly formatted network description could not be read.\n");
+        nr_host_network_free(hn);
+        if (log) fclose(log);
+        return rc;
+    }
+    nr_spr *spr = nullptr;
+    rc = nr_spr_create(hn, spec->ks, spec->kb, spec->mu, nullptr, &spr);
+    const int n = hn->n_points;
+    nr_host_network_free(hn);
+    if (rc != NR_OK) {
+        if (log) fclose(log);
+        return rc;
+    }
+    nr_spr_info_t info;
+    nr_spr_info(spr, &info);
+    double min_c = spec->compr[0], max_c = spec->compr[1], c_inc = spec->compr[2];
+    double min_s = spec->shear[0], max_s = spec->shear[1], s_inc = spec->shear[2];
+    if (strain_mode) { /* :728-737: the shear is scaled by the width */
+        min_c *= (info.maxy - info.miny);
+        max_c *= (info.maxy - info.miny);
+        c_inc *= (info.maxy - info.miny);
+        if (c_inc != c_inc) c_inc = FLT_MAX - max_c;
+        min_s *= (info.maxx - info.minx);
+        max_s *= (info.maxx - info.minx);
+        s_inc *= (info.maxx - info.minx);
+        if (s_inc != s_inc) s_inc = FLT_MAX - max_c;
+    }
+    const bool write_disps = disp_base && disp_base[0];
+    int disp_count = 1, num_digits = 1;
+    if (write_disps) num_digits = get_dec_digits(2 + (int)((max_c - min_c) / c_inc) + (int)((max_s - min_s) / s_inc));
+    FILE *efile = (e_name && e_name[0]) ? fopen(e_name, "w") : nullptr;
+    const int max_iter = std::max(1000, std::min(10 * info.n_free_dofs, 10000000));
+    rc = nr_spr_solve(spr, affine, 1e-12, max_iter, nullptr);
+    int worst = rc;
+    std::vector<double> u(2 * (size_t)n);
+    double compression = min_c;
+    while (rc >= 0 && compression < max_c + 1e-10) {
+        double shear = min_s;
+        while (shear < max_s + 1e-10) {
+            nr_spr_record rec;
+            rc = nr_spr_point(spr, compression, shear, &rec, write_disps ? u.data() : nullptr, nullptr);
+            if (rc < 0) break;
+            if (write_disps) {
+                const std::string name = report_name(disp_base, num_digits, disp_count++, "disp");
+                FILE *f = fopen(name.c_str(), "w");
+                if (f) {
+                    for (int i = 0; i < n; ++i) fprintf(f, "%2.10le\t%2.10le\n", u[2 * i], u[2 * i + 1]);
+                    fclose(f);
+                }
+            }
+            FILE *lf = log ? log : stdout;
+            fprintf(lf, "Residual RMS force: %2.10le\n", rec.residual);
+            FILE *ef = efile ? efile : stdout;
+            if (!itemize) fprintf(ef, "%12.8lf\t%12.8lf\t%12.10le\n", compression, shear, rec.e_total);
+            else fprintf(ef, "%12.8lf\t%12.8lf\t%12.10le\t%12.10le\n", compression, shear, rec.e_ss, rec.e_bend);
+            if (!(s_inc > 0)) break; /* the reference loops forever when an increment is 0 */
+            shear += s_inc;
+        }
+        if (!(c_inc > 0)) break;
+        compression += c_inc;
+    }
+    nr_spr_destroy(spr);
+    if (efile) fclose(efile);
+    if (log) {
+        fprintf(log, "Elapsed time: %d seconds.\n", (int)difftime(time(nullptr), start));
+        fclose(log);
+    }
+    if (rc < 0) {
+        fprintf(stderr, "Linear solve failed: %s\n", nr_last_error());
+        return rc;
+    }
+    return worst;
+}
+
+/* run_relaxation_batch of sparse_relax.cpp:1042-1093. */
+int nr_spr_relaxation_batch(const char *batch_file, int strain_mode, int affine, int itemize) {
+    nr_spr_spec spec;
+    int rc = nr_parse_spr_batch_file(batch_file, &spec);
+    if (rc != NR_OK) {
+        fprintf(stderr, "File parsing failed.\n");
+        return rc;
+    }
+    FileLists fl;
+    if (!file_lists(spec.base, "dat", spec.tag, fl)) {
+        fprintf(stderr, "File lists could not be read.\n");
+        return fail(NR_ERR_IO, "file lists could not be read");
+    }
+    if (spec.shear[1] - spec.shear[0] < 1e-10) spec.shear[2] = 1e12;
+    if (spec.compr[1] - spec.compr[0] < 1e-10) spec.compr[2] = 1e12;
+    int worst = NR_OK;
+    for (size_t i = 0; i < fl.dat.size(); ++i) {
+        /* argument order of the reference: dat, log, disp, edata */
+        rc = nr_spr_do_relaxation_run(fl.dat[i].c_str(), fl.log[i].c_str(), fl.disp[i].c_str(), fl.edat[i].c_str(),
+                                      &spec, strain_mode, affine, itemize);
+        if (rc < 0) worst = rc;
+        else if (rc == NR_NOT_CONVERGED && worst == NR_OK) worst = rc;
+    }
+    return worst;
+}
+
+/* main of sparse_relax.cpp:1165-1232 (getopt "b:ginsz"); the interactive
+ * mode (no -b) is not provided. */
+int nr_sp_relax_main(int argc, char **argv) {
+    const char *batch_file = nullptr;
+    int strain_mode = 0, affine = 1, itemize = 0;
+    for (int i = 1; i < argc; ++i) {
+        const std::string a = argv[i];
+        if (a == "-b") {
+            if (i + 1 >= argc) {
+                fprintf(stderr, "Option \"b\" requires a file name.\n");
+                return -1;
+            }
+            batch_file = argv[++i];
+        } else if (a == "-s") {
+            strain_mode = 1;
+        } else if (a == "-z") {
+            affine = 0;
+        } else if (a == "-i") {
+            itemize = 1;
+        } else if (a == "-g" || a == "-n") {
+            /* accepted: the solve runs on the GPU, and CG's solution has no null-space part */
+        } else {
+            fprintf(stderr, "Unrecognized option: %s\n", a.c_str());
+        }
+    }
+    if (!batch_file) {
+        fprintf(stderr, "Only batch mode (-b) is provided.\n");
+        return -1;
+    }
+    const int rc = nr_spr_relaxation_batch(batch_file, strain_mode, affine, itemize);
+    return rc < 0 ? 1 : 0;
 }
 
 int nr_mesh_relaxation_batch(const char *batch_file, int criterion) {

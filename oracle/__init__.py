@@ -15,7 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libnr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblsr_ref.so")
 REF_MESH_SO = os.path.join(HERE, "_ref", "libnmr_ref.so")
-SOURCES = ["nr_oracle.c", "nr_oracle_mesh.c", "nr_oracle.h", "nr_oracle_internal.h"]
+REF_SPR_SO = os.path.join(HERE, "_ref", "libspr_ref.so")
+SOURCES = ["nr_oracle.c", "nr_oracle_mesh.c", "nr_oracle_spr.c", "nr_oracle.h", "nr_oracle_internal.h"]
+lp = C.POINTER(C.c_long)
 
 dp = C.POINTER(C.c_double)
 ip = C.POINTER(C.c_int)
@@ -111,6 +113,12 @@ def lib():
         L.or_gel_energy.argtypes = [C.POINTER(OrModel), dp]
         L.or_preferred_dilation.restype = C.c_double
         L.or_preferred_dilation.argtypes = [C.c_double] * 5
+        L.or_spr_stiffness.restype = C.c_long
+        L.or_spr_stiffness.argtypes = [C.c_int, dp, C.c_int, ip, dp, bp, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_int, ip, bp, lp, lp, dp]
+        L.or_spr_energies.argtypes = [dp, C.c_int, ip, dp, bp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                      C.c_int, ip, bp, dp, dp, dp]
+        L.or_spr_bc.argtypes = [C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, ubp, dp]
         L.or_mesh_sweep.restype = C.c_int
         L.or_mesh_sweep.argtypes = [C.POINTER(OrModel), dp, C.c_double, C.c_double, C.POINTER(OrParams), dp, dp,
                                     dp, C.c_int, dp]
@@ -402,6 +410,94 @@ def mesh_gel(a, smod, bmod, dilation, inv=None):
             "areas": a["areas"], "mpairs": a["mpairs"], "smod": smod, "bmod": bmod, "dilation": dilation}
 
 
+# ------------------------------------------------------ linear response (SPR)
+
+def _spr_args(a):
+    """Arrays of network a with the triples get_sparse_stiffness_mat computes
+    itself (sparse_relax.cpp:444-446: get_triples on the points and bonds)."""
+    pts = np.ascontiguousarray(a["points"], np.float64)
+    ij = np.ascontiguousarray(a["edge_ij"], np.int32)
+    l0 = np.ascontiguousarray(a["edge_l0"], np.float64)
+    w = np.ascontiguousarray(a["edge_wrap"], np.int8)
+    hjk, tw = triples_of(pts, ij, w, a["offset"]) if len(pts) else (np.zeros((0, 3), np.int32),
+                                                                     np.zeros((0, 2), np.int8))
+    return pts, ij, l0, w, np.ascontiguousarray(hjk, np.int32), np.ascontiguousarray(tw, np.int8)
+
+
+def spr_stiffness(a, ks, kb, mu):
+    """get_sparse_stiffness_mat (sparse_relax.cpp:434): upper-triangle
+    triplets (rows, cols, vals) in (row, col) order."""
+    L = lib()
+    pts, ij, l0, w, hjk, tw = _spr_args(a)
+    args = (len(pts), _d(pts), len(l0), _i(ij), _d(l0), _b(w), float(a["offset"]), float(ks), float(kb), float(mu),
+            len(hjk), _i(hjk), _b(tw))
+    n = L.or_spr_stiffness(*args, None, None, None)
+    rows, cols, vals = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+    L.or_spr_stiffness(*args, rows.ctypes.data_as(lp), cols.ctypes.data_as(lp), _d(vals))
+    return rows, cols, vals
+
+
+def spr_energies(a, ks, kb, mu, u):
+    """get_stretch_shear_energy + get_bending_energy (sparse_relax.cpp:49-96)."""
+    pts, ij, l0, w, hjk, tw = _spr_args(a)
+    uu = np.ascontiguousarray(u, np.float64)
+    ess, eb = C.c_double(), C.c_double()
+    lib().or_spr_energies(_d(pts), len(l0), _i(ij), _d(l0), _b(w), float(a["offset"]), float(ks), float(kb),
+                          float(mu), len(hjk), _i(hjk), _b(tw), _d(uu), C.byref(ess), C.byref(eb))
+    return ess.value, eb.value
+
+
+def spr_protocol(a, ks, kb, mu, compr, shear, strain_mode=True, affine=True, minx=None, maxx=None):
+    # (run_relaxation_batch's rule that an increment of a range narrower than
+    # 1e-10 becomes 1e12 is the caller's.)
+    """do_relaxation_run of sparse_relax.cpp:676-870 restated with numpy on a
+    dense matrix (small networks): records of (compression, shear, e_total,
+    e_ss, e_bend, residual) and the full displacement fields.  The sparse
+    SPQR solve becomes a dense least-squares solve (the same solution for a
+    full-rank system)."""
+    pts = np.ascontiguousarray(a["points"], np.float64)
+    n = len(pts)
+    miny, maxy = a["miny"], a["maxy"]
+    if minx is None:
+        minx, maxx = pts[:, 0].min(), pts[:, 0].max()
+    y = pts[:, 1]
+    bottom = y < miny + 1e-10
+    top = y > maxy - 1e-10
+    free = ~(bottom | top)
+    (cmin, cmax, cinc), (smin, smax, sinc) = [list(v) for v in (compr, shear)]
+    if strain_mode:
+        cmin, cmax, cinc = (v * (maxy - miny) for v in (cmin, cmax, cinc))
+        smin, smax, sinc = (v * (maxx - minx) for v in (smin, smax, sinc))
+    rows, cols, vals = spr_stiffness(a, ks, kb, mu)
+    K = np.zeros((2 * n, 2 * n))
+    K[rows, cols] = vals
+    K[cols, rows] = vals
+    dof = np.repeat(free, 2)
+    Kff, Kfa = K[np.ix_(dof, dof)], K[dof, :]
+    bc = np.zeros(2 * n)
+    is_top = top.astype(np.uint8)
+    recs, fields = [], []
+    c = cmin
+    while c < cmax + 1e-10:
+        sh = smin
+        while sh < smax + 1e-10:
+            lib().or_spr_bc(n, _d(pts), miny, maxy, c, sh, int(affine), is_top.ctypes.data_as(ubp), _d(bc))
+            rhs = -(Kfa @ bc)
+            u = np.linalg.lstsq(Kff, rhs, rcond=None)[0]
+            uf = bc.copy()
+            uf[dof] += u
+            ess, eb = spr_energies(a, ks, kb, mu, uf)
+            recs.append((c, sh, ess + eb, ess, eb, float(np.linalg.norm(rhs - Kff @ u))))
+            fields.append(uf)
+            if not sinc > 0:  # the reference loops forever on a zero increment
+                break
+            sh += sinc
+        if not cinc > 0:
+            break
+        c += cinc
+    return recs, fields
+
+
 # ---------------------------------------------------------------- reference
 
 _ref = None
@@ -593,3 +689,65 @@ def ref_get_inv_mats(pos, elems):
     out = np.zeros((len(el), 6))
     ref_mesh_lib().ref_get_inv_mats(len(p), len(el), _d(p), _i(el), _d(out))
     return out
+
+
+_ref_spr = None
+
+
+def ref_spr_lib():
+    """sparse_relax.cpp compiled for the host (dense CHOLMOD / SPQR
+    stand-ins), or None when unavailable."""
+    global _ref_spr
+    if _ref_spr is None:
+        if not os.path.exists(REF_SPR_SO):
+            return None
+        L = C.CDLL(REF_SPR_SO)
+        L.ref_spr_load.restype = C.c_void_p
+        L.ref_spr_load.argtypes = [C.c_char_p]
+        L.ref_spr_free.argtypes = [C.c_void_p]
+        L.ref_spr_info.argtypes = [C.c_void_p, ip, dp]
+        L.ref_spr_arrays.argtypes = [C.c_void_p, dp, ip, dp, bp, ip, bp]
+        L.ref_spr_stiffness.restype = C.c_long
+        L.ref_spr_stiffness.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, lp, lp, dp]
+        L.ref_spr_energies.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, dp, dp, dp]
+        L.ref_spr_do_relaxation_run.argtypes = [C.c_char_p] * 4 + [C.c_double] * 3 + [dp, dp, C.c_int, C.c_int,
+                                                                                        C.c_int]
+        L.ref_spr_parse_batch_file.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int, dp, dp, dp]
+        L.ref_spr_main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+        _ref_spr = L
+    return _ref_spr
+
+
+class RefSpr:
+    """A network loaded by sparse_relax.cpp's own read_network / get_triples."""
+
+    def __init__(self, path):
+        self.L = ref_spr_lib()
+        self.h = self.L.ref_spr_load(str(path).encode())
+        counts = (C.c_int * 3)()
+        box = (C.c_double * 5)()
+        self.ok = bool(self.L.ref_spr_info(self.h, counts, box))
+        n, e, t = list(counts)
+        a = {"points": np.zeros((n, 2)), "edge_ij": np.zeros((e, 2), np.int32), "edge_l0": np.zeros(e),
+             "edge_wrap": np.zeros(e, np.int8), "tri_hjk": np.zeros((t, 3), np.int32), "tri_wrap": np.zeros((t, 1), np.int8)}
+        self.L.ref_spr_arrays(self.h, _d(a["points"]), _i(a["edge_ij"]), _d(a["edge_l0"]), _b(a["edge_wrap"]),
+                              _i(a["tri_hjk"]), _b(a["tri_wrap"]))
+        a.update(offset=box[0], minx=box[1], maxx=box[2], miny=box[3], maxy=box[4])
+        self.a = a
+
+    def stiffness(self, ks, kb, mu):
+        n = self.L.ref_spr_stiffness(self.h, ks, kb, mu, None, None, None)
+        rows, cols, vals = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n)
+        self.L.ref_spr_stiffness(self.h, ks, kb, mu, rows.ctypes.data_as(lp), cols.ctypes.data_as(lp), _d(vals))
+        return rows, cols, vals
+
+    def energies(self, ks, kb, mu, u):
+        uu = np.ascontiguousarray(u, np.float64)
+        ess, eb = C.c_double(), C.c_double()
+        self.L.ref_spr_energies(self.h, ks, kb, mu, _d(uu), C.byref(ess), C.byref(eb))
+        return ess.value, eb.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.ref_spr_free(self.h)
+            self.h = None

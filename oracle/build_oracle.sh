@@ -10,5 +10,5 @@ EXTRA=""
 if [ "$(uname -m)" = "x86_64" ] && grep -qw fma /proc/cpuinfo 2>/dev/null; then
     EXTRA="-mfma"
 fi
-"$CC" -std=c11 -O2 -fPIC -shared -ffp-contract=off $EXTRA -o "$HERE/libnr_oracle.so.tmp" "$HERE/nr_oracle.c" "$HERE/nr_oracle_mesh.c" -lm -lpthread
+"$CC" -std=c11 -O2 -fPIC -shared -ffp-contract=off $EXTRA -o "$HERE/libnr_oracle.so.tmp" "$HERE/nr_oracle.c" "$HERE/nr_oracle_mesh.c" "$HERE/nr_oracle_spr.c" -lm -lpthread
 mv "$HERE/libnr_oracle.so.tmp" "$HERE/libnr_oracle.so"

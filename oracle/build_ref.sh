@@ -2,7 +2,10 @@
 # Builds oracle/_ref/liblsr_ref.so and oracle/_ref/libnmr_ref.so: the
 # reference's own large_strain_relax.cu and network_mesh_relax.cu compiled as
 # host C++ (kernels run as sequential loops, cuBLAS Level-1 and the CUDA
-# runtime replaced by the stand-ins in oracle/refshim/include).
+# runtime replaced by the stand-ins in oracle/refshim/include); and
+# oracle/_ref/libspr_ref.so: sparse_relax.cpp, unchanged, against the dense
+# CHOLMOD / SPQR stand-ins of oracle/refshim/spr_include (SuiteSparse and
+# MKL are not in this image).
 #
 # The source is read where it lies and piped to the compiler with two textual
 # rewrites.  The first is the kernel-launch syntax, `k<<<grid, block>>>(args)`
@@ -41,6 +44,14 @@ host_compile "$SRC" lsr_reference_main "$OUT/lsr_ref.o"
 shim ref_api
 "$CXX" -shared -o "$OUT/liblsr_ref.so" "$OUT/lsr_ref.o" "$OUT/ref_api.o" "$OUT/shim_common.o"
 echo "build_ref: built $OUT/liblsr_ref.so"
+if [ -f "$REF/src/sparse_relax.cpp" ]; then
+    "$CXX" -x c++ -std=c++17 -O2 -fPIC -w -I "$HERE/refshim/spr_include" -I "$REF/src" \
+        -Dmain=spr_reference_main -c "$REF/src/sparse_relax.cpp" -o "$OUT/spr_ref.o"
+    "$CXX" -std=c++17 -O2 -fPIC -I "$HERE/refshim/spr_include" -c "$HERE/refshim/ref_spr_api.cpp" \
+        -o "$OUT/ref_spr_api.o"
+    "$CXX" -shared -o "$OUT/libspr_ref.so" "$OUT/spr_ref.o" "$OUT/ref_spr_api.o" "$OUT/shim_common.o"
+    echo "build_ref: built $OUT/libspr_ref.so"
+fi
 if [ -f "$MESH_SRC" ]; then
     host_compile "$MESH_SRC" nmr_reference_main "$OUT/nmr_ref.o"
     shim ref_mesh_api

@@ -177,6 +177,22 @@ int or_mesh_sweep(const or_model *m, double *pos, double miny, double range, con
                   const double compr[3], const double shear[3], double *records, int max_records,
                   double *shear_pos);
 
+/* ---- linear response (sparse_relax.cpp, nr_oracle_spr.c) ---- */
+
+/* get_sparse_stiffness_mat (sparse_relax.cpp:434-480): upper-triangle
+ * triplets in (row, col) order, values accumulated in the reference's call
+ * order, |value| <= 1e-10 dropped.  rows/cols/vals may be NULL to count. */
+long or_spr_stiffness(int n_points, const double *points, int n_edges, const int *edge_ij, const double *edge_l0,
+                      const signed char *edge_wrap, double offset, double ks, double kb, double mu, int n_triples,
+                      const int *tri_hjk, const signed char *tri_wrap, long *rows, long *cols, double *vals);
+/* get_stretch_shear_energy / get_bending_energy (:49-96), sequential sums. */
+void or_spr_energies(const double *points, int n_edges, const int *edge_ij, const double *edge_l0,
+                     const signed char *edge_wrap, double offset, double ks, double kb, double mu, int n_triples,
+                     const int *tri_hjk, const signed char *tri_wrap, const double *u, double *e_ss, double *e_bend);
+/* affine_displacement (:528-538) or add_displacement (:513-525). */
+void or_spr_bc(int n_points, const double *points, double miny, double maxy, double compression, double shear,
+               int affine, const unsigned char *is_top, double *bc);
+
 #ifdef __cplusplus
 }
 #endif
