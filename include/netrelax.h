@@ -67,7 +67,8 @@ typedef struct {
 /* read_network (large_strain_relax.cu:42-114): same parsing rules, same
  * rest lengths l0 = sqrt(dx*dx + dy*dy), same error cases.  On NR_ERR_PARSE
  * the partially read network is still returned in *out (the reference keeps
- * going with whatever it read); the caller frees it. */
+ * going with whatever it read); the caller frees it.  Lines are parsed on
+ * NR_IO_THREADS threads (default: all). */
 int nr_read_network(const char *path, nr_host_network **out);
 
 /* get_triples (large_strain_relax.cu:116-184): the collinear (antiparallel
@@ -96,6 +97,15 @@ void nr_host_network_arrays(const nr_host_network *net, double *points, int *edg
 void nr_host_network_fcodes(const nr_host_network *net, unsigned char *fcodes);
 /* Writes the .dat format read_network reads (%.17g, round-trips exactly). */
 int nr_write_network(const nr_host_network *net, const char *path);
+/* No reference counterpart: a binary copy of a host network (points, bonds,
+ * rest lengths, triples, per-item constants, mesh; little-endian, FNV-1a
+ * checksum) that loads without parsing and without get_triples.  A
+ * truncated or corrupt file gives NR_ERR_PARSE. */
+int nr_write_network_bin(const nr_host_network *net, const char *path);
+int nr_read_network_bin(const char *path, nr_host_network **out);
+/* report_displaced (large_strain_relax.cu:216-227): n_points xy pairs as
+ * "%2.10le\t%2.10le\n" lines (host array), formatted in parallel. */
+int nr_write_positions(const double *xy, int n_points, const char *path);
 void nr_host_network_free(nr_host_network *net);
 
 /* Synthetic inputs (no reference counterpart; the reference ships none).

@@ -102,6 +102,9 @@ SIGNATURES = {
                                       c_double_p, c_double_p]),
     "nr_host_network_fcodes": (None, [P, c_uchar_p]),
     "nr_write_network": (C.c_int, [P, C.c_char_p]),
+    "nr_write_network_bin": (C.c_int, [P, C.c_char_p]),
+    "nr_read_network_bin": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "nr_write_positions": (C.c_int, [c_double_p, C.c_int, C.c_char_p]),
     "nr_host_network_free": (None, [P]),
     "nr_gen_lattice": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_int, C.POINTER(P)]),
     "nr_gen_mikado": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(P)]),

@@ -37,7 +37,7 @@ CUDA_UNITS = [
     ("analysis.cu", ["--fmad=false"]),
     ("spr.cu", ["--fmad=false"]),
 ]
-HOST_UNITS = ["host_network.cpp", "mesh_host.cpp", "generators.cpp", "driver.cpp"]
+HOST_UNITS = ["host_network.cpp", "fast_io.cpp", "mesh_host.cpp", "generators.cpp", "driver.cpp"]
 
 
 def _run(cmd):

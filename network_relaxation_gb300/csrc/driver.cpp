@@ -308,12 +308,7 @@ int nr_do_relaxation_run(const char *net_file, const char *log_name, const char 
                         rep.e_stretch, rep.e_bend, rep.e_stretch + rep.e_bend);
             rc = nr_network_get_positions(net, pos.data(), nullptr);
             if (rc != NR_OK) break;
-            const std::string name = report_name(disp_base, num_digits, disp_count++, "pos");
-            FILE *f = fopen(name.c_str(), "w");
-            if (f) {
-                for (int i = 0; i < n_points; ++i) fprintf(f, "%2.10le\t%2.10le\n", pos[2 * i], pos[2 * i + 1]);
-                fclose(f);
-            }
+            nr::write_xy_file(report_name(disp_base, num_digits, disp_count++, "pos"), pos.data(), n_points);
             if (!(inc > 0)) break;
         }
     }
@@ -434,12 +429,7 @@ int nr_do_mesh_relaxation_run(const char *net_file, const char *log_name, const 
                         rep.e_stretch, rep.e_bend, rep.e_gel, rep.e_stretch + rep.e_bend + rep.e_gel);
             rc = nr_network_get_positions(net, pos.data(), nullptr);
             if (rc != NR_OK) break;
-            const std::string name = report_name(disp_base, num_digits, disp_count++, "pos");
-            FILE *f = fopen(name.c_str(), "w");
-            if (f) {
-                for (int i = 0; i < n_points; ++i) fprintf(f, "%2.10le\t%2.10le\n", pos[2 * i], pos[2 * i + 1]);
-                fclose(f);
-            }
+            nr::write_xy_file(report_name(disp_base, num_digits, disp_count++, "pos"), pos.data(), n_points);
             if (curr_disp < max_disp) rc = nr_affine_displace(net, miny, range, inc, 0, nullptr);
             if (!(inc > 0)) break;
         }
@@ -646,12 +636,7 @@ int nr_spr_do_relaxation_run(const char *dat_name, const char *log_name, const c
             rc = nr_spr_point(spr, compression, shear, &rec, write_disps ? u.data() : nullptr, nullptr);
             if (rc < 0) break;
             if (write_disps) {
-                const std::string name = report_name(disp_base, num_digits, disp_count++, "disp");
-                FILE *f = fopen(name.c_str(), "w");
-                if (f) {
-                    for (int i = 0; i < n; ++i) fprintf(f, "%2.10le\t%2.10le\n", u[2 * i], u[2 * i + 1]);
-                    fclose(f);
-                }
+                nr::write_xy_file(report_name(disp_base, num_digits, disp_count++, "disp"), u.data(), n);
             }
             FILE *lf = log ? log : stdout;
             fprintf(lf, "Residual RMS force: %2.10le\n", rec.residual);

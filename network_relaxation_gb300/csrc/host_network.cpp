@@ -1,18 +1,21 @@
 /*
- * Host-side network handling: the .dat reader (read_network), the triple
- * finder (get_triples), fcodes, writers, per-node incidence lists and the
- * error plumbing of the C ABI.
+ * Host-side network handling: the triple finder (get_triples), fcodes,
+ * per-node incidence lists and the error plumbing of the C ABI (the .dat
+ * reader and writer are in fast_io.cpp).
  *
  * Compiled with -ffp-contract=off: rest lengths and the triple test must
  * round exactly as the reference's host code (large_strain_relax.cu:97-99,
  * :157-168), which the host compiler builds without fused multiply-adds.
  */
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <string>
+#include <thread>
 
 #include "nr_internal.h"
 
@@ -91,59 +94,6 @@ const char *nr_status_string(int status) {
 const char *nr_last_error(void) { return nr::g_last_error.c_str(); }
 int nr_abi_version(void) { return NR_ABI_VERSION; }
 
-/* read_network, large_strain_relax.cu:42-114.  std::getline / eof() are
- * used exactly as the reference uses them so that short files fail at the
- * same point. */
-int nr_read_network(const char *path, nr_host_network **out) {
-    if (!path || !out) return fail(NR_ERR_INVALID, "nr_read_network: null argument");
-    *out = nullptr;
-    std::ifstream input(path);
-    if (!input.is_open()) return fail(NR_ERR_IO, std::string("cannot open ") + path);
-    auto *net = new nr_host_network();
-    *out = net;
-    std::string line;
-    int num_points = 0, num_edges = 0;
-    double offset = 0;
-    net->miny = FLT_MAX;
-    net->maxy = FLT_MIN;
-    std::getline(input, line);
-    int num_read = sscanf(line.c_str(), "%d %d %lf", &num_points, &num_edges, &offset);
-    if (num_read < 3 || offset < 0 || num_points <= 0 || num_edges < 0)
-        return fail(NR_ERR_PARSE, "Reading failed. The provided file has an invalid header.");
-    net->offset = offset;
-    while (!input.eof() && net->points.size() < 2 * (size_t)num_points) {
-        double x, y;
-        std::getline(input, line);
-        if (sscanf(line.c_str(), "%lf %lf", &x, &y) == 2) {
-            net->points.push_back(x);
-            net->points.push_back(y);
-            if (y < net->miny) net->miny = y;
-            if (y > net->maxy) net->maxy = y;
-        }
-    }
-    net->n_points = (int)(net->points.size() / 2);
-    if (input.eof()) return fail(NR_ERR_PARSE, "Reading failed. Too few points were read.");
-    while (!input.eof() && net->edge_l0.size() < (size_t)num_edges) {
-        int i1, i2;
-        signed char mult;
-        std::getline(input, line);
-        if (sscanf(line.c_str(), "%d %d %hhd\n", &i1, &i2, &mult) == 3) {
-            if (std::min(i1, i2) > -1 && std::max(i1, i2) < num_points) {
-                const double dx = net->points[2 * i2] + offset * mult - net->points[2 * i1];
-                const double dy = net->points[2 * i2 + 1] - net->points[2 * i1 + 1];
-                net->edge_ij.push_back(i1);
-                net->edge_ij.push_back(i2);
-                net->edge_l0.push_back(std::sqrt(dx * dx + dy * dy));
-                net->edge_wrap.push_back(mult);
-            } else {
-                return fail(NR_ERR_PARSE, "Reading failed due to an out-of-bounds point index.");
-            }
-        }
-    }
-    if (net->edge_l0.size() < (size_t)num_edges) return fail(NR_ERR_PARSE, "Too few edges were found.");
-    return NR_OK;
-}
-
 /* get_triples, large_strain_relax.cu:116-184.  Per-node adjacency in edge
  * order (forward wrap for the first endpoint, negated for the second),
  * hinges ascending, pairs i < j in list order, accepted when dot < 0 and
@@ -173,27 +123,46 @@ int nr_get_triples(nr_host_network *net) {
     net->tri_phi0.clear();
     const double *p = net->points.data();
     const double offset = net->offset;
-    for (int h = 0; h < n; ++h) {
-        const double x = p[2 * h], y = p[2 * h + 1];
-        for (int i = start[h]; i < start[h + 1]; ++i) {
-            const int j = nb[i];
-            const double dx2 = p[2 * j] + offset * nw[i] - x;
-            const double dy2 = p[2 * j + 1] - y;
-            for (int k2 = i + 1; k2 < start[h + 1]; ++k2) {
-                const int k = nb[k2];
-                const double dx3 = p[2 * k] + offset * nw[k2] - x;
-                const double dy3 = p[2 * k + 1] - y;
-                const double dot = dx2 * dx3 + dy2 * dy3;
-                const double mag_sq = (dx2 * dx2 + dy2 * dy2) * (dx3 * dx3 + dy3 * dy3);
-                if (dot < 0 && std::fabs(dot * dot - mag_sq) < 1e-10) {
-                    net->tri_hjk.push_back(h);
-                    net->tri_hjk.push_back(j);
-                    net->tri_hjk.push_back(k);
-                    net->tri_wrap.push_back(nw[i]);
-                    net->tri_wrap.push_back(nw[k2]);
+    /* hinges in contiguous ranges on several threads, results concatenated
+     * in hinge order: the same list as one pass */
+    const char *env = getenv("NR_IO_THREADS");
+    int threads = env ? atoi(env) : 0;
+    if (threads <= 0) threads = (int)std::thread::hardware_concurrency();
+    threads = std::max(1, std::min(threads, std::max(1, n / 16384)));
+    std::vector<std::vector<int>> hjk(threads);
+    std::vector<std::vector<signed char>> tw(threads);
+    auto work = [&](int t) {
+        const int h0 = (int)((long)n * t / threads), h1 = (int)((long)n * (t + 1) / threads);
+        for (int h = h0; h < h1; ++h) {
+            const double x = p[2 * h], y = p[2 * h + 1];
+            for (int i = start[h]; i < start[h + 1]; ++i) {
+                const int j = nb[i];
+                const double dx2 = p[2 * j] + offset * nw[i] - x;
+                const double dy2 = p[2 * j + 1] - y;
+                for (int k2 = i + 1; k2 < start[h + 1]; ++k2) {
+                    const int k = nb[k2];
+                    const double dx3 = p[2 * k] + offset * nw[k2] - x;
+                    const double dy3 = p[2 * k + 1] - y;
+                    const double dot = dx2 * dx3 + dy2 * dy3;
+                    const double mag_sq = (dx2 * dx2 + dy2 * dy2) * (dx3 * dx3 + dy3 * dy3);
+                    if (dot < 0 && std::fabs(dot * dot - mag_sq) < 1e-10) {
+                        hjk[t].push_back(h);
+                        hjk[t].push_back(j);
+                        hjk[t].push_back(k);
+                        tw[t].push_back(nw[i]);
+                        tw[t].push_back(nw[k2]);
+                    }
                 }
             }
         }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+    for (int t = 0; t < threads; ++t) {
+        net->tri_hjk.insert(net->tri_hjk.end(), hjk[t].begin(), hjk[t].end());
+        net->tri_wrap.insert(net->tri_wrap.end(), tw[t].begin(), tw[t].end());
     }
     return NR_OK;
 }
@@ -282,17 +251,6 @@ void nr_host_network_fcodes(const nr_host_network *net, unsigned char *fcodes) {
         const double y = net->points[2 * i + 1];
         fcodes[i] = (y < net->miny + 1e-10 || y > net->maxy - 1e-10) ? 0 : 3;
     }
-}
-
-int nr_write_network(const nr_host_network *net, const char *path) {
-    FILE *f = fopen(path, "w");
-    if (!f) return fail(NR_ERR_IO, std::string("cannot write ") + path);
-    fprintf(f, "%d %d %.17g\n", net->n_points, net->n_edges(), net->offset);
-    for (int i = 0; i < net->n_points; ++i) fprintf(f, "%.17g %.17g\n", net->points[2 * i], net->points[2 * i + 1]);
-    for (int e = 0; e < net->n_edges(); ++e)
-        fprintf(f, "%d %d %d\n", net->edge_ij[2 * e], net->edge_ij[2 * e + 1], (int)net->edge_wrap[e]);
-    fclose(f);
-    return NR_OK;
 }
 
 void nr_host_network_free(nr_host_network *net) { delete net; }

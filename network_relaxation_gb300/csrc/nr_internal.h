@@ -52,6 +52,10 @@ void build_incidence(int n_points, const int *edge_ij, int n_edges, const int *t
  * FLT_MIN). */
 void y_range(const std::vector<double> &points, double &miny, double &maxy);
 
+/* n xy pairs written as "%2.10le\t%2.10le\n" lines (report_displaced,
+ * large_strain_relax.cu:216-227), formatted in parallel. */
+bool write_xy_file(const std::string &name, const double *xy, long n);
+
 /* The duplicate-vertex search of read_network_mesh
  * (network_mesh_relax.cu:219-227): 2P indices. */
 void find_mesh_pairs(const std::vector<double> &points, double offset, double minx, std::vector<int> &pairs);
