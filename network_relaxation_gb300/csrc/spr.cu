@@ -15,12 +15,15 @@
  *    reference's and the oracle's.
  *  - The reduced system lives on the device in SELL-32 (rows in slices of
  *    32, each slice padded to its longest row, column-major inside the
- *    slice): a warp reads a slice's values and columns coalesced.
+ *    slice): a warp reads a slice's values and columns coalesced.  Rows are
+ *    sorted by length inside windows of 256 (SELL-C-sigma), so slices pad
+ *    little.
  *  - bc is linear in (compression, shear), so the protocol needs two
  *    solves: the unit compression and the unit shear loads, solved
- *    together (one matrix read per iteration for both) by a Jacobi-
- *    preconditioned conjugate gradient in one persistent cooperative
- *    kernel with budgeted grid barriers.  Every protocol point is then a
+ *    together (one matrix read per iteration for both) by a conjugate
+ *    gradient with a 2x2 block-Jacobi (per node) preconditioner, in its
+ *    single-reduction form (two grid barriers per iteration), in one
+ *    persistent cooperative kernel with budgeted grid barriers.  Every protocol point is then a
  *    linear combination, checked by its own residual ||rhs - K_ff u||
  *    (one SpMV) and followed by the energies (canonical tile sums).
  *  - On a rank-deficient system (floppy modes) CG from zero returns the
@@ -48,6 +51,7 @@ namespace {
 constexpr double kSprDrop = 1e-10; /* FLT_TOL, sparse_relax.cpp:45 */
 constexpr int kSprThreads = 512;
 constexpr int kSlice = 32;
+constexpr int kSigma = 256; /* rows sorted by length within windows of this size */
 
 /* ------------------------------------------------------------ assembly */
 
@@ -203,24 +207,29 @@ void assemble_upper(const nr_host_network &h, double ks, double kb, double mu, U
 /* ------------------------------------------------------------- device */
 
 struct SprScal {
-    double rz[2], alpha[2], beta[2], rr[2], bb[2];
+    double rho[2], mu[2], alpha[2], beta[2], rr[2], bb[2];
     int active[2], iters[2];
     int done, pad;
 };
 
+/* Reduced system in device order: free node k owns rows 2k (x) and 2k + 1
+ * (y); vectors hold the two right-hand sides (double2 per row). */
 struct SprDev {
     int nr, n_slices;
     const long *slice_ptr;
     const int *slice_w;
     const int *col;
     const double *val;
-    const double *dinv;
+    const double2 *mdiag; /* per node: inverse 2x2 diagonal block, (a00, a11) */
+    const double *moff;   /* per node: its off-diagonal a01 */
     const double2 *b;
-    double2 *x, *r, *p, *q;
-    double *part; /* 4 per block */
+    double2 *x, *r, *z, *p, *q, *s;
+    double *part; /* kParts per block */
     SprScal *sc;
     FireState *bar; /* barrier words */
 };
+
+constexpr int kParts = 8;
 
 __device__ __forceinline__ double2 spmv_row(const SprDev &d, int s, int lane, const double2 *v) {
     const long base = d.slice_ptr[s];
@@ -236,160 +245,183 @@ __device__ __forceinline__ double2 spmv_row(const SprDev &d, int s, int lane, co
     return make_double2(a0, a1);
 }
 
-/* Block sums of up to 4 values into part[blockIdx * 4 + k]. */
-__device__ void block_part4(double *s_red, double *part, double v0, double v1, double v2, double v3) {
+/* Block sums of kParts values into part[blockIdx * kParts + k]. */
+__device__ void block_parts(double *s_red, double *part, const double *v) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double v[4] = {v0, v1, v2, v3};
-    for (int k = 0; k < 4; ++k) {
-        const double s = warp_sum(v[k]);
-        if (lane == 0) s_red[warp * 4 + k] = s;
+    for (int k = 0; k < kParts; ++k) {
+        const double t = warp_sum(v[k]);
+        if (lane == 0) s_red[warp * kParts + k] = t;
     }
     __syncthreads();
-    if (threadIdx.x < 4) {
-        double s = 0.0;
-        for (int w = 0; w < nw; ++w) s = s + s_red[w * 4 + threadIdx.x];
-        part[blockIdx.x * 4 + threadIdx.x] = s;
+    if (threadIdx.x < kParts) {
+        double t = 0.0;
+        for (int w = 0; w < nw; ++w) t = t + s_red[w * kParts + threadIdx.x];
+        part[blockIdx.x * kParts + threadIdx.x] = t;
     }
     __syncthreads();
 }
 
-/* Totals of the 4 partial columns over G blocks (warp k sums column k:
- * lanes stride the blocks, then a butterfly); every thread gets them. */
-__device__ void total4(double *s_red, const double *part, int G, double *t) {
+/* Totals of the kParts partial columns over G blocks (warp k sums column
+ * k: lanes stride the blocks, then a butterfly); every thread gets them.
+ * Needs kParts warps. */
+__device__ void total_parts(double *s_red, const double *part, int G, double *t) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (warp < 4) {
-        double s = 0.0;
-        for (int b = lane; b < G; b += 32) s = s + __ldcg(part + b * 4 + warp);
-        s = warp_sum(s);
-        if (lane == 0) s_red[warp] = s;
+    if (warp < kParts) {
+        double v = 0.0;
+        for (int b = lane; b < G; b += 32) v = v + __ldcg(part + b * kParts + warp);
+        v = warp_sum(v);
+        if (lane == 0) s_red[warp] = v;
     }
     __syncthreads();
-    for (int k = 0; k < 4; ++k) t[k] = s_red[k];
+    for (int k = 0; k < kParts; ++k) t[k] = s_red[k];
     __syncthreads();
 }
 
-__device__ __forceinline__ double jac(const SprDev &d, int i, double v) { return d.dinv[i] * v; }
+/* z = M^-1 r for node k's two rows (2x2 block Jacobi), both right-hand sides. */
+__device__ __forceinline__ void precond(const SprDev &d, int k, double2 rx, double2 ry, double2 &zx, double2 &zy) {
+    const double2 m = d.mdiag[k];
+    const double o = d.moff[k];
+    zx = make_double2(fma(m.x, rx.x, o * ry.x), fma(m.x, rx.y, o * ry.y));
+    zy = make_double2(fma(o, rx.x, m.y * ry.x), fma(o, rx.y, m.y * ry.y));
+}
 
-/* Jacobi-PCG on K_ff x = b for the two right-hand sides of b (double2),
- * persistent over the grid; stops each rhs at ||r|| <= tol ||b||. */
+/* s = K z over the rows, with the row terms of rho = r.z and mu = z.s. */
+__device__ __forceinline__ void spmv_phase(const SprDev &d, int gwarp, int nwarps, int lane, double *acc) {
+    for (int sl = gwarp; sl < d.n_slices; sl += nwarps) {
+        const double2 sv = spmv_row(d, sl, lane, d.z);
+        const int row = sl * kSlice + lane;
+        if (row < d.nr) {
+            d.s[row] = sv;
+            const double2 rv = d.r[row], zv = d.z[row];
+            acc[0] = fma(rv.x, zv.x, acc[0]);
+            acc[1] = fma(rv.y, zv.y, acc[1]);
+            acc[2] = fma(zv.x, sv.x, acc[2]);
+            acc[3] = fma(zv.y, sv.y, acc[3]);
+        }
+    }
+}
+
+/* Block-Jacobi-preconditioned conjugate gradient in the single-reduction
+ * form of Chronopoulos and Gear (J. Comput. Appl. Math. 25, 1989): per
+ * iteration one fused vector pass (p = z + beta p, q = s + beta q,
+ * x += alpha p, r -= alpha q, z = M^-1 r) and one SpMV s = K z that also
+ * yields r.z and z.s, so two grid barriers.  Two right-hand sides at once;
+ * each stops at ||r|| <= tol ||b|| (then alpha = beta = 0 freeze it). */
 __global__ void __launch_bounds__(kSprThreads) k_spr_pcg(SprDev d, double tol, int max_iter,
                                                          unsigned long long budget_ns) {
-    __shared__ double s_red[(kSprThreads / 32) * 4];
+    __shared__ double s_red[(kSprThreads / 32) * kParts];
     const unsigned G = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = G * blockDim.x;
     const int lane = threadIdx.x & 31;
     const int gwarp = tid >> 5, nwarps = nth >> 5;
+    const int nn = d.nr / 2;
     bool last;
     volatile SprScal *vs = d.sc;
-    {
-        double rz0 = 0, rz1 = 0, bb0 = 0, bb1 = 0;
-        for (int i = tid; i < d.nr; i += nth) {
-            const double2 bi = d.b[i];
-            d.x[i] = make_double2(0.0, 0.0);
-            d.r[i] = bi;
-            const double2 z = make_double2(jac(d, i, bi.x), jac(d, i, bi.y));
-            d.p[i] = z;
-            rz0 = fma(bi.x, z.x, rz0);
-            rz1 = fma(bi.y, z.y, rz1);
-            bb0 = fma(bi.x, bi.x, bb0);
-            bb1 = fma(bi.y, bi.y, bb1);
-        }
-        block_part4(s_red, d.part, rz0, rz1, bb0, bb1);
-        if (!barrier_arrive(d.bar, G, budget_ns, last, 11)) return;
-        if (last) {
-            double t[4];
-            total4(s_red, d.part, G, t);
-            if (threadIdx.x == 0) {
-                SprScal *sc = d.sc;
-                sc->rz[0] = t[0];
-                sc->rz[1] = t[1];
-                sc->bb[0] = t[2];
-                sc->bb[1] = t[3];
-                for (int k = 0; k < 2; ++k) {
-                    sc->active[k] = t[2 + k] > 0 && t[k] != 0;
-                    sc->iters[k] = 0;
-                    sc->rr[k] = t[2 + k];
-                }
-                sc->done = !(sc->active[0] || sc->active[1]) || max_iter <= 0;
+    const double2 zero = make_double2(0.0, 0.0);
+    double acc[kParts];
+    /* r = b, z = M^-1 r, x = p = q = 0; b.b */
+    for (int k = 0; k < kParts; ++k) acc[k] = 0.0;
+    for (int k = tid; k < nn; k += nth) {
+        const double2 bx = d.b[2 * k], by = d.b[2 * k + 1];
+        double2 zx, zy;
+        precond(d, k, bx, by, zx, zy);
+        d.r[2 * k] = bx;
+        d.r[2 * k + 1] = by;
+        d.z[2 * k] = zx;
+        d.z[2 * k + 1] = zy;
+        d.x[2 * k] = d.x[2 * k + 1] = zero;
+        d.p[2 * k] = d.p[2 * k + 1] = zero;
+        d.q[2 * k] = d.q[2 * k + 1] = zero;
+        acc[4] = fma(bx.x, bx.x, fma(by.x, by.x, acc[4]));
+        acc[5] = fma(bx.y, bx.y, fma(by.y, by.y, acc[5]));
+    }
+    if (!barrier_arrive(d.bar, G, budget_ns, last, 21)) return;
+    if (last) barrier_release(d.bar);
+    spmv_phase(d, gwarp, nwarps, lane, acc);
+    block_parts(s_red, d.part, acc);
+    if (!barrier_arrive(d.bar, G, budget_ns, last, 22)) return;
+    if (last) {
+        double t[kParts];
+        total_parts(s_red, d.part, G, t);
+        if (threadIdx.x == 0) {
+            SprScal *sc = d.sc;
+            for (int k = 0; k < 2; ++k) {
+                sc->rho[k] = t[k];
+                sc->mu[k] = t[2 + k];
+                sc->bb[k] = t[4 + k];
+                sc->rr[k] = t[4 + k];
+                sc->iters[k] = 0;
+                sc->beta[k] = 0.0;
+                sc->active[k] = t[4 + k] > 0 && t[k] != 0 && t[2 + k] != 0;
+                sc->alpha[k] = sc->active[k] ? t[k] / t[2 + k] : 0.0;
             }
-            barrier_release(d.bar);
+            sc->done = !(sc->active[0] || sc->active[1]) || max_iter <= 0;
         }
+        barrier_release(d.bar);
     }
     for (;;) {
         if (vs->done) break;
-        /* q = K p, p.q */
-        double pq0 = 0, pq1 = 0;
-        for (int s = gwarp; s < d.n_slices; s += nwarps) {
-            const double2 qv = spmv_row(d, s, lane, d.p);
-            const int row = s * kSlice + lane;
-            if (row < d.nr) {
-                d.q[row] = qv;
-                const double2 pv = d.p[row];
-                pq0 = fma(pv.x, qv.x, pq0);
-                pq1 = fma(pv.y, qv.y, pq1);
+        const double al0 = vs->alpha[0], al1 = vs->alpha[1], be0 = vs->beta[0], be1 = vs->beta[1];
+        for (int k = 0; k < kParts; ++k) acc[k] = 0.0;
+        for (int k = tid; k < nn; k += nth) {
+            double2 rr2[2], zz2[2];
+            for (int c = 0; c < 2; ++c) {
+                const int i = 2 * k + c;
+                const double2 zv = d.z[i], sv = d.s[i];
+                double2 pv = d.p[i], qv = d.q[i], xv = d.x[i], rv = d.r[i];
+                pv.x = fma(be0, pv.x, zv.x);
+                pv.y = fma(be1, pv.y, zv.y);
+                qv.x = fma(be0, qv.x, sv.x);
+                qv.y = fma(be1, qv.y, sv.y);
+                xv.x = fma(al0, pv.x, xv.x);
+                xv.y = fma(al1, pv.y, xv.y);
+                rv.x = fma(-al0, qv.x, rv.x);
+                rv.y = fma(-al1, qv.y, rv.y);
+                d.p[i] = pv;
+                d.q[i] = qv;
+                d.x[i] = xv;
+                d.r[i] = rv;
+                rr2[c] = rv;
+                acc[4] = fma(rv.x, rv.x, acc[4]);
+                acc[5] = fma(rv.y, rv.y, acc[5]);
             }
+            precond(d, k, rr2[0], rr2[1], zz2[0], zz2[1]);
+            d.z[2 * k] = zz2[0];
+            d.z[2 * k + 1] = zz2[1];
         }
-        block_part4(s_red, d.part, pq0, pq1, 0.0, 0.0);
-        if (!barrier_arrive(d.bar, G, budget_ns, last, 12)) return;
+        if (!barrier_arrive(d.bar, G, budget_ns, last, 23)) return;
+        if (last) barrier_release(d.bar);
+        spmv_phase(d, gwarp, nwarps, lane, acc);
+        block_parts(s_red, d.part, acc);
+        if (!barrier_arrive(d.bar, G, budget_ns, last, 24)) return;
         if (last) {
-            double t[4];
-            total4(s_red, d.part, G, t);
-            if (threadIdx.x == 0)
-                for (int k = 0; k < 2; ++k)
-                    d.sc->alpha[k] = d.sc->active[k] && t[k] != 0 ? d.sc->rz[k] / t[k] : 0.0;
-            barrier_release(d.bar);
-        }
-        const double al0 = vs->alpha[0], al1 = vs->alpha[1];
-        /* x += alpha p, r -= alpha q, z = M^-1 r */
-        double rz0 = 0, rz1 = 0, rr0 = 0, rr1 = 0;
-        for (int i = tid; i < d.nr; i += nth) {
-            const double2 pv = d.p[i], qv = d.q[i];
-            double2 xv = d.x[i], rv = d.r[i];
-            xv.x = fma(al0, pv.x, xv.x);
-            xv.y = fma(al1, pv.y, xv.y);
-            rv.x = fma(-al0, qv.x, rv.x);
-            rv.y = fma(-al1, qv.y, rv.y);
-            d.x[i] = xv;
-            d.r[i] = rv;
-            rz0 = fma(rv.x, jac(d, i, rv.x), rz0);
-            rz1 = fma(rv.y, jac(d, i, rv.y), rz1);
-            rr0 = fma(rv.x, rv.x, rr0);
-            rr1 = fma(rv.y, rv.y, rr1);
-        }
-        block_part4(s_red, d.part, rz0, rz1, rr0, rr1);
-        if (!barrier_arrive(d.bar, G, budget_ns, last, 13)) return;
-        if (last) {
-            double t[4];
-            total4(s_red, d.part, G, t);
+            double t[kParts];
+            total_parts(s_red, d.part, G, t);
             if (threadIdx.x == 0) {
                 SprScal *sc = d.sc;
                 for (int k = 0; k < 2; ++k) {
                     if (!sc->active[k]) {
-                        sc->beta[k] = 0.0;
+                        sc->alpha[k] = sc->beta[k] = 0.0;
                         continue;
                     }
                     sc->iters[k]++;
-                    sc->rr[k] = t[2 + k];
-                    sc->beta[k] = sc->rz[k] != 0 ? t[k] / sc->rz[k] : 0.0;
-                    sc->rz[k] = t[k];
-                    if (!(t[2 + k] > tol * tol * sc->bb[k]) || t[k] == 0) sc->active[k] = 0;
+                    sc->rr[k] = t[4 + k];
+                    const double rho = t[k], mu = t[2 + k];
+                    const double beta = rho / sc->rho[k];
+                    const double den = mu - beta * rho / sc->alpha[k];
+                    if (!(t[4 + k] > tol * tol * sc->bb[k]) || rho == 0 || !(den != 0) || !isfinite(den)) {
+                        sc->active[k] = 0;
+                        sc->alpha[k] = sc->beta[k] = 0.0;
+                        continue;
+                    }
+                    sc->beta[k] = beta;
+                    sc->alpha[k] = rho / den;
+                    sc->rho[k] = rho;
                 }
                 sc->done = !(sc->active[0] || sc->active[1]) || sc->iters[0] >= max_iter || sc->iters[1] >= max_iter;
             }
             barrier_release(d.bar);
         }
-        if (vs->done) break;
-        const double be0 = vs->beta[0], be1 = vs->beta[1];
-        const int ac0 = vs->active[0], ac1 = vs->active[1];
-        for (int i = tid; i < d.nr; i += nth) {
-            const double2 rv = d.r[i];
-            double2 pv = d.p[i];
-            if (ac0) pv.x = fma(be0, pv.x, jac(d, i, rv.x));
-            if (ac1) pv.y = fma(be1, pv.y, jac(d, i, rv.y));
-            d.p[i] = pv;
-        }
-        if (!barrier_arrive(d.bar, G, budget_ns, last, 14)) return;
-        if (last) barrier_release(d.bar);
     }
 }
 
@@ -443,7 +475,7 @@ __global__ void k_spr_field(SprPointDev a) {
  * of its squares. */
 __global__ void __launch_bounds__(kSprThreads) k_spr_residual(SprDev d, const double *u, double c, double s,
                                                               double *part) {
-    __shared__ double s_red[(kSprThreads / 32) * 4];
+    __shared__ double s_red[(kSprThreads / 32) * kParts];
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int lane = threadIdx.x & 31, gwarp = tid >> 5, nwarps = nth >> 5;
     double acc = 0.0;
@@ -462,13 +494,14 @@ __global__ void __launch_bounds__(kSprThreads) k_spr_residual(SprDev d, const do
             acc = fma(rv, rv, acc);
         }
     }
-    block_part4(s_red, part, acc, 0.0, 0.0, 0.0);
+    double v[kParts] = {acc, 0, 0, 0, 0, 0, 0, 0};
+    block_parts(s_red, part, v);
 }
 
 __global__ void k_spr_sum_parts(const double *part, int G, double *out) {
-    __shared__ double s_red[64];
-    double t[4];
-    total4(s_red, part, G, t);
+    __shared__ double s_red[kParts];
+    double t[kParts];
+    total_parts(s_red, part, G, t);
     if (threadIdx.x == 0) *out = t[0];
 }
 
@@ -566,7 +599,8 @@ struct nr_spr {
     double ks = 0, kb = 0, mu = 0, offset = 0, miny = 0, maxy = 0, minx = 0, maxx = 0;
     int n_edges = 0, n_triples = 0;
     UpperK K;
-    std::vector<int> dof_map;           /* 2N */
+    std::vector<int> dof_map;           /* 2N: reduced row (host order) or -1 */
+    std::vector<int> perm;              /* device position -> reduced row */
     std::vector<unsigned char> top;     /* N */
     std::vector<double> points;         /* 2N, for the unit loads of either mode */
     int solved_affine = -1;             /* mode of the unit solutions on the device, -1: none */
@@ -753,15 +787,39 @@ int nr_spr_create(const nr_host_network *net, double ks, double kb, double mu, v
             }
         }
     }
-    /* SELL-32 */
+    /* SELL-32 with nodes sorted by row length inside windows of kSigma rows
+     * (SELL-C-sigma): slices of rows of similar length pad little, the
+     * window keeps neighbouring nodes together for the gathers, and a
+     * node's x and y rows stay adjacent (rows 2k, 2k + 1 of device node k)
+     * for the 2x2 block preconditioner.  perm: device row -> reduced row;
+     * columns are renumbered; each row keeps its column order, so its sum
+     * is unchanged. */
+    const int nn = S->nr / 2;
+    const auto row_len = [&](int r) { return rcnt[r + 1] - rcnt[r]; };
+    std::vector<int> pnode(nn);
+    for (int j = 0; j < nn; ++j) pnode[j] = j;
+    const int wnodes = kSigma / 2;
+    for (int w0 = 0; w0 < nn; w0 += wnodes) {
+        const int w1 = std::min(nn, w0 + wnodes);
+        std::stable_sort(pnode.begin() + w0, pnode.begin() + w1, [&](int a, int b) {
+            return std::max(row_len(2 * a), row_len(2 * a + 1)) > std::max(row_len(2 * b), row_len(2 * b + 1));
+        });
+    }
+    std::vector<int> perm(S->nr), inv(S->nr);
+    for (int k = 0; k < nn; ++k) {
+        perm[2 * k] = 2 * pnode[k];
+        perm[2 * k + 1] = 2 * pnode[k] + 1;
+    }
+    for (int k = 0; k < S->nr; ++k) inv[perm[k]] = k;
+    S->perm = perm;
     S->n_slices = (S->nr + kSlice - 1) / kSlice;
     std::vector<long> slice_ptr(S->n_slices + 1, 0);
     std::vector<int> slice_w(S->n_slices, 0);
     for (int sl = 0; sl < S->n_slices; ++sl) {
         int w = 0;
         for (int l = 0; l < kSlice; ++l) {
-            const int r = sl * kSlice + l;
-            if (r < S->nr) w = std::max(w, (int)(rcnt[r + 1] - rcnt[r]));
+            const int k = sl * kSlice + l;
+            if (k < S->nr) w = std::max(w, (int)row_len(perm[k]));
         }
         slice_w[sl] = w;
         slice_ptr[sl + 1] = slice_ptr[sl] + (long)w * kSlice;
@@ -771,19 +829,39 @@ int nr_spr_create(const nr_host_network *net, double ks, double kb, double mu, v
     std::vector<double> sval(S->sell_len, 0.0);
     for (int sl = 0; sl < S->n_slices; ++sl)
         for (int l = 0; l < kSlice; ++l) {
-            const int r = sl * kSlice + l;
-            for (int k = 0; k < slice_w[sl]; ++k) {
-                const long at = slice_ptr[sl] + (long)k * kSlice + l;
-                if (r < S->nr && k < rcnt[r + 1] - rcnt[r]) {
-                    scol[at] = rcol[rcnt[r] + k];
-                    sval[at] = rval[rcnt[r] + k];
+            const int k = sl * kSlice + l;
+            const int r = k < S->nr ? perm[k] : -1;
+            for (int q = 0; q < slice_w[sl]; ++q) {
+                const long at = slice_ptr[sl] + (long)q * kSlice + l;
+                if (r >= 0 && q < row_len(r)) {
+                    scol[at] = inv[rcol[rcnt[r] + q]];
+                    sval[at] = rval[rcnt[r] + q];
                 } else {
-                    scol[at] = r < S->nr ? r : 0; /* padding: a valid index, value 0 */
+                    scol[at] = k < S->nr ? k : 0; /* padding: a valid index, value 0 */
                 }
             }
         }
-    std::vector<double> dinv(S->nr);
-    for (int r = 0; r < S->nr; ++r) dinv[r] = diag[r] > 0 ? 1.0 / diag[r] : 0.0;
+    /* inverse of each node's 2x2 diagonal block (scalar Jacobi when the
+     * block is singular or nearly so) */
+    std::vector<double2> mdiag(std::max(1, nn));
+    std::vector<double> moff(std::max(1, nn));
+    for (int k = 0; k < nn; ++k) {
+        const int rx = perm[2 * k];
+        const double kxx = diag[rx], kyy = diag[rx + 1];
+        double kxy = 0.0;
+        for (long q = rcnt[rx]; q < rcnt[rx + 1]; ++q)
+            if (rcol[q] == rx + 1) kxy = rval[q];
+        const double det = kxx * kyy - kxy * kxy;
+        if (kxx > 0 && kyy > 0 && det > 1e-12 * kxx * kyy) {
+            mdiag[k] = make_double2(kyy / det, kxx / det);
+            moff[k] = -kxy / det;
+        } else {
+            mdiag[k] = make_double2(kxx > 0 ? 1.0 / kxx : 0.0, kyy > 0 ? 1.0 / kyy : 0.0);
+            moff[k] = 0.0;
+        }
+    }
+    std::vector<int> dof_dev(S->dof_map.size());
+    for (size_t f = 0; f < dof_dev.size(); ++f) dof_dev[f] = S->dof_map[f] >= 0 ? inv[S->dof_map[f]] : -1;
     /* energies: bonds, SPR's triples (recomputed like the reference) */
     std::vector<int4> bond(h.n_edges());
     for (int e = 0; e < h.n_edges(); ++e)
@@ -817,19 +895,22 @@ int nr_spr_create(const nr_host_network *net, double ks, double kb, double mu, v
     const size_t o_sw = img.put(slice_w.data(), slice_w.size());
     const size_t o_col = img.put(scol.data(), scol.size());
     const size_t o_val = img.put(sval.data(), sval.size());
-    const size_t o_dinv = img.put(dinv.data(), dinv.size());
+    const size_t o_md = img.put(mdiag.data(), mdiag.size());
+    const size_t o_mo = img.put(moff.data(), moff.size());
     const size_t o_b = img.add(sizeof(double2) * (S->nr + 1));
     const size_t o_x = img.add(sizeof(double2) * (S->nr + 1));
     const size_t o_r = img.add(sizeof(double2) * (S->nr + 1));
     const size_t o_p = img.add(sizeof(double2) * (S->nr + 1));
     const size_t o_q = img.add(sizeof(double2) * (S->nr + 1));
-    const size_t o_part = img.add(sizeof(double) * 4 * (size_t)blocks);
+    const size_t o_z = img.add(sizeof(double2) * (S->nr + 1));
+    const size_t o_s = img.add(sizeof(double2) * (S->nr + 1));
+    const size_t o_part = img.add(sizeof(double) * kParts * (size_t)blocks);
     S->pcg_blocks = blocks;
     S->rpart_blocks = 4 * sm_count_spr(); /* k_spr_residual's largest grid */
-    const size_t o_rpart = img.add(sizeof(double) * 4 * (size_t)S->rpart_blocks);
+    const size_t o_rpart = img.add(sizeof(double) * kParts * (size_t)S->rpart_blocks);
     const size_t o_sc = img.add(sizeof(SprScal));
     const size_t o_bar = img.add(sizeof(FireState));
-    const size_t o_map = img.put(S->dof_map.data(), S->dof_map.size());
+    const size_t o_map = img.put(dof_dev.data(), dof_dev.size());
     const size_t o_top = img.put(S->top.data(), S->top.size());
     const size_t o_ured = img.add(sizeof(double) * (S->nr + 1));
     const size_t o_uf = img.add(sizeof(double2) * (size_t)S->n);
@@ -854,12 +935,15 @@ int nr_spr_create(const nr_host_network *net, double ks, double kb, double mu, v
     d.slice_w = (const int *)(base + o_sw);
     d.col = (const int *)(base + o_col);
     d.val = (const double *)(base + o_val);
-    d.dinv = (const double *)(base + o_dinv);
+    d.mdiag = (const double2 *)(base + o_md);
+    d.moff = (const double *)(base + o_mo);
     d.b = (const double2 *)(base + o_b);
     d.x = (double2 *)(base + o_x);
     d.r = (double2 *)(base + o_r);
     d.p = (double2 *)(base + o_p);
     d.q = (double2 *)(base + o_q);
+    d.z = (double2 *)(base + o_z);
+    d.s = (double2 *)(base + o_s);
     d.part = (double *)(base + o_part);
     d.sc = (SprScal *)(base + o_sc);
     d.bar = (FireState *)(base + o_bar);
@@ -924,9 +1008,15 @@ int nr_spr_solve(nr_spr *S, int affine, double tol, int max_iter, void *stream) 
         S->rel_residual[0] = S->rel_residual[1] = 0;
         return NR_OK;
     }
-    std::vector<double> rhs2;
+    std::vector<double> rhs2, rhs_dev(2 * (size_t)S->nr);
     unit_rhs(*S, affine, rhs2);
-    SPR_TRY(cudaMemcpyAsync((void *)S->dev.b, rhs2.data(), sizeof(double) * rhs2.size(), cudaMemcpyHostToDevice, s));
+    for (int k = 0; k < S->nr; ++k) { /* device order */
+        rhs_dev[2 * (size_t)k] = rhs2[2 * (size_t)S->perm[k]];
+        rhs_dev[2 * (size_t)k + 1] = rhs2[2 * (size_t)S->perm[k] + 1];
+    }
+    SPR_TRY(cudaMemcpyAsync((void *)S->dev.b, rhs_dev.data(), sizeof(double) * rhs_dev.size(), cudaMemcpyHostToDevice,
+                            s));
+    SPR_TRY(cudaStreamSynchronize(s)); /* rhs_dev is a local */
     SPR_TRY(cudaMemsetAsync(S->dev.sc, 0, sizeof(SprScal), s));
     SPR_TRY(cudaMemsetAsync(S->dev.bar, 0, sizeof(FireState), s));
     const int blocks = S->pcg_blocks;
@@ -978,7 +1068,7 @@ int nr_spr_point(nr_spr *S, double compression, double shear, nr_spr_record *rec
     if (S->nr > 0) {
         const int blocks = std::max(1, std::min(S->rpart_blocks, (S->n_slices + 15) / 16));
         k_spr_residual<<<blocks, kSprThreads, 0, s>>>(S->dev, S->d_u_red, compression, shear, S->d_rpart);
-        k_spr_sum_parts<<<1, 128, 0, s>>>(S->d_rpart, blocks, S->d_scalar);
+        k_spr_sum_parts<<<1, 32 * kParts, 0, s>>>(S->d_rpart, blocks, S->d_scalar);
         SPR_TRY(cudaGetLastError());
     }
     const int use_ss = S->ks > 0 || S->mu > 0, use_bend = S->kb > 0;
