@@ -255,11 +255,12 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
-    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1"],
+    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1", "A1", "IO"],
                     help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
                          "first strain increment of its protocol, FIRE steps capped by --max-steps; M1: the same "
                          "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
-                         "solve of sparse_relax.cpp on one large network")
+                         "solve of sparse_relax.cpp on one large network; A1: the post-relaxation analyses; IO: "
+                         "reading and writing network files (host only)")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
@@ -272,6 +273,10 @@ def main():
         return reference_arm(args)
     if args.workload == "L1":
         return linear_response_arm(args)
+    if args.workload == "A1":
+        return analyses_arm(args)
+    if args.workload == "IO":
+        return io_arm(args)
     if args.workload != "C4":
         return single_network_arm(args)
 
@@ -655,6 +660,136 @@ def linear_response_arm(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None, "kernel": "k_spr_pcg"},
         **extra,
+    }))
+    return 0
+
+
+def analyses_arm(args):
+    """--workload A1: bond strains, linear axial energy and non-affinity
+    (strain_calc.cpp, axial_contribution.cpp, na_calc.cpp) of one
+    1024 x 1024 lattice (p = 0.65) and a seeded displacement field.  One
+    step = the three analyses; value on device-resident arrays, e2e with
+    host arrays (copies inside the timed region)."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+    import oracle
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    h = nr.HostNetwork.lattice(1024, 1024, 0.65, 0.05, 12)
+    a = h.arrays()
+    n, e = len(a["points"]), len(a["edge_l0"])
+    rng = np.random.default_rng(12)
+    disp = np.ascontiguousarray(rng.normal(0.0, 0.01, (n, 2)))
+    dev = torch.device("cuda:0")
+    t = lambda v, dt: torch.tensor(np.ascontiguousarray(v).reshape(-1), dtype=dt, device=dev)  # noqa: E731
+    d_p0, d_u = t(a["points"], torch.float64), t(disp, torch.float64)
+    d_ij, d_w = t(a["edge_ij"], torch.int32), t(a["edge_wrap"], torch.int8)
+    d_out = torch.empty(e, dtype=torch.float64, device=dev)
+    hp = [torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for v in (a["points"], disp, a["edge_ij"],
+                                                                           a["edge_wrap"])]
+    h_out = torch.empty(e, dtype=torch.float64).pin_memory()
+    lib = nr.lib()
+    vp = lambda x: C.c_void_p(x.data_ptr())  # noqa: E731
+    res = C.c_double()
+    W, miny = float(a["offset"]), float(a["miny"])
+
+    def step(p0, u, ij, w, out):
+        nr.check(lib.nr_bond_strains(n, e, W, vp(p0), vp(u), vp(ij), vp(w), vp(out), None), "nr_bond_strains")
+        nr.check(lib.nr_linear_axial_energy(n, e, W, 1.0, vp(p0), vp(u), vp(ij), vp(w), C.byref(res), None),
+                 "nr_linear_axial_energy")
+        nr.check(lib.nr_nonaffinity(n, vp(p0), vp(u), miny, 0.0, 0.01, C.byref(res), None), "nr_nonaffinity")
+
+    def timed(fn):
+        ts = []
+        for s in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            if s >= args.warmup:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    ms = timed(lambda: step(d_p0, d_u, d_ij, d_w, d_out))
+    ms_e2e = timed(lambda: step(hp[0], hp[1], hp[2], hp[3], h_out))
+    # algorithmic bytes: per node its two xy pairs (32 B) once per analysis; per bond i, j, wrap (9 B), and the
+    # strain written (8 B)
+    bytes_step = 3 * 32.0 * n + 2 * 9.0 * e + 8.0 * e
+    hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+           if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
+    achieved = bytes_step / (ms / 1e3) / 1e9
+    extra = {}
+    if not args.no_cpu:
+        t0 = time.perf_counter()
+        oracle.bond_strains(a, a["points"], disp)
+        oracle.linear_axial_energy(a, 1.0, a["points"], disp)
+        oracle.nonaffinity(a["points"], disp, miny, 0.0, 0.01)
+        cdt = time.perf_counter() - t0
+        extra["cpu_baseline"] = {"value": e / cdt, "unit": "bonds/s", "cores": 1, "kind": "port",
+                                 "sample": "the oracle's three analyses on the same network and field (%.2f s)" % cdt}
+    print(json.dumps({
+        "metric": "bonds/s through bond strains + linear axial energy + non-affinity (A1)",
+        "value": e / (ms / 1e3), "unit": "bonds/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": "A1: lattice 1024x1024, p=0.65, jitter 0.05, seed 12, "
+                                                    "displacements N(0, 0.01); N=%d E=%d" % (n, e)},
+        "e2e": {"value": e / (ms_e2e / 1e3), "unit": "bonds/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": int(3 * 32 * n + 2 * 9 * e), "d2h_bytes_per_step": int(8 * e + 16)},
+        "gpu_launches": args.steps * 7,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_bond_strains + k_tile_sums + k_final"},
+        **extra,
+    }))
+    return 0
+
+
+def io_arm(args):
+    """--workload IO (host only): a 1024 x 1024 lattice (p = 0.65) written
+    and read back as .dat with get_triples, and as the binary side-car;
+    the oracle's getline / sscanf restatement of read_network + get_triples
+    timed beside it.  value = nodes set up per second from .dat."""
+    import network_relaxation_gb300 as nr
+    import oracle
+
+    h = nr.HostNetwork.lattice(1024, 1024, 0.65, 0.05, 5)
+    n = h.n_points
+    d = os.environ.get("TMPDIR", "/tmp")
+    dat, binp = os.path.join(d, "nr_io_bench.dat"), os.path.join(d, "nr_io_bench.bin")
+    t = {}
+
+    def clock(name, fn):
+        ts = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        t[name] = float(np.median(ts))
+
+    clock("write_dat", lambda: h.write(dat))
+    clock("read_dat", lambda: nr.HostNetwork.read(dat))
+    h2 = nr.HostNetwork.read(dat)
+    clock("get_triples", lambda: h2.get_triples())
+    clock("write_bin", lambda: nr.lib().nr_write_network_bin(h2.handle, binp.encode()))
+    out = C.c_void_p()
+    clock("read_bin", lambda: nr.lib().nr_read_network_bin(binp.encode(), C.byref(out)))
+    t0 = time.perf_counter()
+    oracle.read_network(dat)
+    t_or = time.perf_counter() - t0
+    setup = t["read_dat"] + t["get_triples"]
+    print(json.dumps({
+        "metric": "nodes/s set up from a .dat file (read_network + get_triples), host (IO)",
+        "value": n / setup, "unit": "nodes/s", "n_gpus": 0, "steps": args.steps, "warmup": 0,
+        "ms_per_step": 1e3 * setup, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None,
+        "dtype": "text", "data": "synthetic",
+        "config": {"workload": "IO: lattice 1024x1024, p=0.65, jitter 0.05, seed 5; N=%d; %d host threads"
+                               % (n, os.cpu_count() or 1)},
+        "seconds": t, "gpu_launches": 0,
+        "cpu_baseline": {"value": n / t_or, "unit": "nodes/s", "cores": 1, "kind": "port",
+                         "sample": "the oracle's getline / sscanf restatement of read_network + get_triples on the "
+                                   "same file (%.2f s)" % t_or},
     }))
     return 0
 
