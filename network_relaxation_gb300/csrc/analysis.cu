@@ -102,14 +102,25 @@ __global__ void __launch_bounds__(kTile) k_final(const double *partials, int til
 }
 
 /* A device view of a caller array: the array itself when the device can
- * address it, else a device copy. */
+ * address it, else a device copy.  Scratch comes from the stream-ordered
+ * pool allocator (cudaMallocAsync / cudaFreeAsync on the call's stream):
+ * no device-wide synchronisation and no allocation cost after the pool
+ * has warmed up. */
 struct Staged {
     const void *dev = nullptr;
     void *own = nullptr;
+    cudaStream_t stream = nullptr;
     ~Staged() {
-        if (own) cudaFree(own);
+        if (own) cudaFreeAsync(own, stream);
     }
 };
+
+cudaError_t scratch_alloc(Staged &st, size_t bytes, cudaStream_t s) {
+    st.stream = s;
+    cudaError_t e = cudaMallocAsync(&st.own, bytes, s);
+    if (e != cudaSuccess) st.own = nullptr;
+    return e;
+}
 
 bool device_accessible(const void *p) {
     cudaPointerAttributes at;
@@ -129,12 +140,10 @@ int stage(const void *src, size_t bytes, cudaStream_t s, Staged &st) {
         st.dev = src;
         return NR_OK;
     }
-    cudaError_t e = cudaMalloc(&st.own, bytes);
-    if (e != cudaSuccess) {
-        st.own = nullptr;
+    cudaError_t e = scratch_alloc(st, bytes, s);
+    if (e != cudaSuccess)
         return fail(e == cudaErrorMemoryAllocation ? NR_ERR_OOM : NR_ERR_CUDA,
-                    std::string("analysis: cudaMalloc: ") + cudaGetErrorString(e));
-    }
+                    std::string("analysis: cudaMallocAsync: ") + cudaGetErrorString(e));
     e = cudaMemcpyAsync(st.own, src, bytes, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return fail(NR_ERR_CUDA, std::string("analysis: copy: ") + cudaGetErrorString(e));
     st.dev = st.own;
@@ -152,13 +161,11 @@ int sms() {
 template <class In, double (*Term)(const In &, int)>
 int canonical_total(const In &a, int n, double scale, double divisor, double *out, cudaStream_t s) {
     const int tiles = (n + kTile - 1) / kTile;
-    Staged part, res;
-    cudaError_t e = cudaMalloc(&part.own, sizeof(double) * (size_t)(tiles > 0 ? tiles : 1) + sizeof(double));
-    if (e != cudaSuccess) {
-        part.own = nullptr;
+    Staged part;
+    cudaError_t e = scratch_alloc(part, sizeof(double) * (size_t)(tiles > 0 ? tiles : 1) + sizeof(double), s);
+    if (e != cudaSuccess)
         return fail(e == cudaErrorMemoryAllocation ? NR_ERR_OOM : NR_ERR_CUDA,
-                    std::string("analysis: cudaMalloc: ") + cudaGetErrorString(e));
-    }
+                    std::string("analysis: cudaMallocAsync: ") + cudaGetErrorString(e));
     double *partials = (double *)part.own, *total = partials + (tiles > 0 ? tiles : 1);
     if (tiles > 0) k_tile_sums<In, Term><<<std::min(tiles, 8 * sms()), kTile, 0, s>>>(a, n, partials);
     k_final<<<1, kTile, 0, s>>>(partials, tiles, scale, divisor, total);
@@ -197,11 +204,9 @@ extern "C" int nr_bond_strains(int n_points, int npairs, double width, const dou
     if ((st = stage(e_offsets, (size_t)npairs, s, w)) != NR_OK) return st;
     double *dout = strains;
     if (!device_accessible(strains)) {
-        cudaError_t e = cudaMalloc(&out.own, sizeof(double) * (size_t)npairs);
-        if (e != cudaSuccess) {
-            out.own = nullptr;
-            return fail(NR_ERR_OOM, std::string("nr_bond_strains: cudaMalloc: ") + cudaGetErrorString(e));
-        }
+        cudaError_t e = scratch_alloc(out, sizeof(double) * (size_t)npairs, s);
+        if (e != cudaSuccess)
+            return fail(NR_ERR_OOM, std::string("nr_bond_strains: cudaMallocAsync: ") + cudaGetErrorString(e));
         dout = (double *)out.own;
     }
     const EdgeIn a{npairs, width, (const int *)ij.dev, (const signed char *)w.dev, (const double *)p0.dev,
