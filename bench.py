@@ -261,10 +261,12 @@ def main():
                          "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
                          "solve of sparse_relax.cpp on one large network; A1: the post-relaxation analyses; IO: "
                          "reading and writing network files (host only)")
+    ap.add_argument("--side", type=int, default=0,
+                    help="profiling case: lattice side of the L1 workload (default 1024; not a bench line)")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
-    profiling_case = args.largest > 0 or args.max_steps != 10_000_000
+    profiling_case = args.largest > 0 or args.max_steps != 10_000_000 or args.side > 0
     if profiling_case:
         args.no_cpu = args.no_fp64 = True
     if args.warmup < 3:
@@ -603,9 +605,11 @@ def linear_response_arm(args):
     import network_relaxation_gb300 as nr
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    h = nr.HostNetwork.lattice(L1["nx"], L1["ny"], L1["p"], 0.0, L1["seed"])
+    side = args.side or L1["nx"]
+    h = nr.HostNetwork.lattice(side, side, L1["p"], 0.0, L1["seed"])
     n = h.n_points
     spr = nr.Spr(h, L1["ks"], L1["kb"], L1["mu"])
+    cg_cap = args.max_steps if args.max_steps != 10_000_000 else None
     info = spr.info()
     W = info.maxx - info.minx
     pts = [s * W for s in np.arange(L1["shear"][0], L1["shear"][1] + 1e-9, L1["shear"][2])]
@@ -616,7 +620,7 @@ def linear_response_arm(args):
         torch.cuda.synchronize()
         e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         e0.record(stream)
-        spr.solve(affine=True)
+        spr.solve(affine=True, max_iter=cg_cap)
         e1.record(stream)
         for sh in pts:
             rec = nr.SprRecord()
@@ -653,7 +657,7 @@ def linear_response_arm(args):
         "rel_residual": list(info.rel_residual), "higher_is_better": True, "scaling": "replicas",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "L1: lattice %dx%d, p=%g, no jitter, seed %d; ks %g, kb %g, mu %g; N=%d, free dofs %d, "
-                               "upper nnz %d, SELL entries %d" % (L1["nx"], L1["ny"], L1["p"], L1["seed"], L1["ks"],
+                               "upper nnz %d, SELL entries %d" % (side, side, L1["p"], L1["seed"], L1["ks"],
                                                                   L1["kb"], L1["mu"], n, info.n_free_dofs,
                                                                   info.nnz_upper, info.sell_entries)},
         "gpu_launches": args.steps * (1 + 5 * len(pts)),

@@ -419,7 +419,10 @@ int nr_sp_relax_main(int argc, char **argv);
  * displacement field disp (2N doubles), bonds as in nr_run_fire_md
  * (pair_list 2E ints, e_offsets E wrap codes, width = x period).  Arrays
  * may be host or device memory; the calls return when the results are
- * written.  Totals use the library's fixed summation tree (reproducible;
+ * written.  Their scratch (device copies of host arrays, partial sums)
+ * comes from a stream-ordered memory pool the library keeps per device,
+ * which holds the largest scratch needed so far for the life of the
+ * process.  Totals use the library's fixed summation tree (reproducible;
  * the reference sums sequentially, so they agree to rounding).
  *
  * strain_calc.cpp:96-120 (get_strains): strains[b] = (l_final - l_initial)

@@ -17,8 +17,12 @@
  * are staged into device buffers, outputs are copied to wherever they
  * point (cudaMemcpyDefault); the calls return after the stream finishes.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 
 #include "nr_device.cuh"
@@ -115,9 +119,41 @@ struct Staged {
     }
 };
 
+/* The library's own stream-ordered pool on the current device, created on
+ * first use, whose release threshold keeps its memory mapped between calls
+ * (the default pool returns it at every synchronisation, and mapping it
+ * again costs more than the analyses themselves).  It holds at most the
+ * largest scratch the analyses have needed, for the life of the process.
+ * nullptr if pools are unsupported. */
+cudaMemPool_t scratch_pool() {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = pools.find(dev);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+        cudaGetLastError();
+        pool = nullptr;
+    } else {
+        cuuint64_t keep = ~(cuuint64_t)0;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pools[dev] = pool;
+    return pool;
+}
+
 cudaError_t scratch_alloc(Staged &st, size_t bytes, cudaStream_t s) {
     st.stream = s;
-    cudaError_t e = cudaMallocAsync(&st.own, bytes, s);
+    cudaMemPool_t pool = scratch_pool();
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(&st.own, bytes, pool, s) : cudaMallocAsync(&st.own, bytes, s);
     if (e != cudaSuccess) st.own = nullptr;
     return e;
 }
