@@ -261,6 +261,8 @@ def main():
                          "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
                          "solve of sparse_relax.cpp on one large network; A1: the post-relaxation analyses; IO: "
                          "reading and writing network files (host only)")
+    ap.add_argument("--reorder", default="none", choices=["none", "morton", "rcm"],
+                    help="renumber every network's nodes (nr_host_network_reorder) before the batch is built")
     ap.add_argument("--side", type=int, default=0,
                     help="profiling case: lattice side of the L1 workload (default 1024; not a bench line)")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
@@ -303,6 +305,9 @@ def main():
     if args.largest > 0:
         prm_list = sorted(prm_list, key=lambda q: -q["L"])[:args.largest]
     hosts = workloads.c4_networks(prm_list)
+    if args.reorder != "none":
+        for hn in hosts:
+            hn.reorder(args.reorder)
     kappa = np.array([q["kappa"] for q in prm_list])
     gamma = np.array([q["gamma"] for q in prm_list])
     batch = nr.Batch(hosts, 1.0, kappa, stream=sp)
@@ -396,7 +401,8 @@ def main():
             "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": "C4: 512 uneven diluted triangular lattices L~U{16..96}, p~U[0.55,0.75], "
                                    "kappa~logU[1e-5,1e-2], gamma~U[0,0.1], FIRE to max|F|<1e-10",
-                       "precision": args.precision, "networks_per_gpu": batch.n, "nodes_per_gpu": n_nodes,
+                       "precision": args.precision, "node_order": args.reorder if args.reorder != "none" else "generator (rows)",
+                       "networks_per_gpu": batch.n, "nodes_per_gpu": n_nodes,
                        "l2": "inputs larger than L2 (%.0f MB device data)" % (batch_bytes(batch) / 1e6),
                        "parallelism": "one batch per GPU" if world > 1 else "single GPU"},
             "e2e": {"value": total_nets / (e2e_step_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,

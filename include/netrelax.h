@@ -108,6 +108,18 @@ int nr_read_network_bin(const char *path, nr_host_network **out);
 int nr_write_positions(const double *xy, int n_points, const char *path);
 void nr_host_network_free(nr_host_network *net);
 
+/* Renumbers the nodes for locality (no reference counterpart; the
+ * reference keeps file order): NR_ORDER_MORTON sorts them along a Z-order
+ * curve of their positions, NR_ORDER_RCM by reverse Cuthill-McKee on the
+ * bond graph.  Points, bond / triple / facet / pair indices are remapped;
+ * bonds and triples keep their order (so per-node force sums, rest lengths
+ * and energies are unchanged, only permuted).  new_to_old (may be NULL)
+ * receives n_points entries: the old index of each new node.  Useful before
+ * nr_network_create / nr_batch_create for files numbered without locality:
+ * the cluster kernel cuts networks into contiguous index ranges. */
+enum { NR_ORDER_MORTON = 1, NR_ORDER_RCM = 2 };
+int nr_host_network_reorder(nr_host_network *net, int method, int *new_to_old);
+
 /* Synthetic inputs (no reference counterpart; the reference ships none).
  * Diluted triangular lattice, nx columns x ny rows, unit spacing, rows at
  * y = j*sqrt(3)/2, odd rows shifted by +0.5, x-periodic with period nx.

@@ -148,6 +148,14 @@ class HostNetwork:
         _capi.load().nr_host_network_mesh_info(self._h, C.byref(info))
         return info
 
+    def reorder(self, method="morton"):
+        """Renumbers the nodes for locality (nr_host_network_reorder);
+        returns new_to_old (the old index of each new node)."""
+        m = {"morton": _capi.NR_ORDER_MORTON, "rcm": _capi.NR_ORDER_RCM}[method]
+        perm = np.empty(self.n_points, np.int32)
+        check(_capi.load().nr_host_network_reorder(self._h, m, _ip(perm)), "nr_host_network_reorder")
+        return perm
+
     def write_mesh(self, path):
         check(_capi.load().nr_write_network_mesh(self._h, str(path).encode()), "nr_write_network_mesh")
 

@@ -28,6 +28,8 @@ NR_CRIT_RMS = 0
 NR_CRIT_MAX = 1
 NR_FP64 = 0
 NR_MIXED = 1
+NR_ORDER_MORTON = 1
+NR_ORDER_RCM = 2
 
 
 class HostInfo(C.Structure):
@@ -106,6 +108,7 @@ SIGNATURES = {
     "nr_read_network_bin": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "nr_write_positions": (C.c_int, [c_double_p, C.c_int, C.c_char_p]),
     "nr_host_network_free": (None, [P]),
+    "nr_host_network_reorder": (C.c_int, [P, C.c_int, c_int_p]),
     "nr_gen_lattice": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_int, C.POINTER(P)]),
     "nr_gen_mikado": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64, C.POINTER(P)]),
     "nr_network_create": (C.c_int, [P, C.c_double, C.c_double, P, C.POINTER(P)]),

@@ -1,17 +1,19 @@
 /*
  * Host side of network-mesh composites (network_mesh_relax.cu): the .nmc
  * reader (read_network_mesh), its duplicate-vertex search, a writer, and
- * accessors.  Compiled with -ffp-contract=off, like the .dat reader, so
+ * accessors; and node reordering for locality (Morton, RCM).  Compiled with -ffp-contract=off, like the .dat reader, so
  * rest lengths round exactly as the reference's host code.
  */
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <fstream>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "nr_internal.h"
 
@@ -204,3 +206,122 @@ void nr_host_network_mesh_arrays(const nr_host_network *net, int *facets, double
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------ node reordering */
+
+namespace {
+
+/* Z-order key of a point on a 2^16 x 2^16 grid over the bounding box. */
+uint32_t morton_key(double x, double y, double x0, double y0, double sx, double sy) {
+    auto q = [](double v) -> uint32_t {
+        if (!(v > 0)) return 0;
+        if (v >= 65535.0) return 65535;
+        return (uint32_t)v;
+    };
+    auto spread = [](uint32_t v) {
+        v = (v | (v << 8)) & 0x00FF00FFu;
+        v = (v | (v << 4)) & 0x0F0F0F0Fu;
+        v = (v | (v << 2)) & 0x33333333u;
+        v = (v | (v << 1)) & 0x55555555u;
+        return v;
+    };
+    return spread(q((x - x0) * sx)) | (spread(q((y - y0) * sy)) << 1);
+}
+
+/* Reverse Cuthill-McKee on the bond graph: breadth-first from a
+ * pseudo-peripheral node of every component (components in order of their
+ * lowest node), neighbours by increasing degree, then reversed. */
+std::vector<int> rcm_order(const nr_host_network &h) {
+    const int n = h.n_points;
+    std::vector<int> start(n + 1, 0);
+    for (int e = 0; e < h.n_edges(); ++e) {
+        start[h.edge_ij[2 * e] + 1]++;
+        start[h.edge_ij[2 * e + 1] + 1]++;
+    }
+    for (int i = 0; i < n; ++i) start[i + 1] += start[i];
+    std::vector<int> adj(start[n]), fill(start.begin(), start.end() - 1);
+    for (int e = 0; e < h.n_edges(); ++e) {
+        const int a = h.edge_ij[2 * e], b = h.edge_ij[2 * e + 1];
+        adj[fill[a]++] = b;
+        adj[fill[b]++] = a;
+    }
+    auto deg = [&](int v) { return start[v + 1] - start[v]; };
+    for (int v = 0; v < n; ++v)
+        std::stable_sort(adj.begin() + start[v], adj.begin() + start[v + 1],
+                         [&](int a, int b) { return deg(a) < deg(b); });
+    std::vector<int> order, level(n, -1);
+    order.reserve(n);
+    std::vector<char> seen(n, 0);
+    auto bfs = [&](int root, std::vector<int> &out) { /* returns the last level's first node */
+        out.clear();
+        std::vector<int> q{root};
+        level[root] = 0;
+        size_t head = 0;
+        while (head < q.size()) {
+            const int v = q[head++];
+            out.push_back(v);
+            for (int k = start[v]; k < start[v + 1]; ++k)
+                if (level[adj[k]] < 0) {
+                    level[adj[k]] = level[v] + 1;
+                    q.push_back(adj[k]);
+                }
+        }
+        int far = root;
+        for (int v : out)
+            if (level[v] > level[far] || (level[v] == level[far] && deg(v) < deg(far))) far = v;
+        for (int v : out) level[v] = -1;
+        return far;
+    };
+    std::vector<int> comp;
+    for (int s = 0; s < n; ++s) {
+        if (seen[s]) continue;
+        int root = s;
+        for (int it = 0; it < 2; ++it) root = bfs(root, comp); /* two sweeps: a pseudo-peripheral node */
+        bfs(root, comp);
+        for (int v : comp) seen[v] = 1;
+        order.insert(order.end(), comp.begin(), comp.end());
+    }
+    std::reverse(order.begin(), order.end());
+    return order;
+}
+
+}  // namespace
+
+extern "C" int nr_host_network_reorder(nr_host_network *net, int method, int *new_to_old) {
+    if (!net || net->n_points <= 0 || (method != NR_ORDER_MORTON && method != NR_ORDER_RCM))
+        return fail(NR_ERR_INVALID, "nr_host_network_reorder: bad arguments");
+    const int n = net->n_points;
+    std::vector<int> order(n); /* new position -> old node */
+    if (method == NR_ORDER_MORTON) {
+        double x0 = net->points[0], x1 = x0, y0 = net->points[1], y1 = y0;
+        for (int i = 0; i < n; ++i) {
+            x0 = std::min(x0, net->points[2 * i]);
+            x1 = std::max(x1, net->points[2 * i]);
+            y0 = std::min(y0, net->points[2 * i + 1]);
+            y1 = std::max(y1, net->points[2 * i + 1]);
+        }
+        const double sx = x1 > x0 ? 65535.0 / (x1 - x0) : 0.0, sy = y1 > y0 ? 65535.0 / (y1 - y0) : 0.0;
+        std::vector<uint32_t> key(n);
+        for (int i = 0; i < n; ++i) {
+            key[i] = morton_key(net->points[2 * i], net->points[2 * i + 1], x0, y0, sx, sy);
+            order[i] = i;
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    } else {
+        order = rcm_order(*net);
+    }
+    std::vector<int> old_to_new(n);
+    for (int k = 0; k < n; ++k) old_to_new[order[k]] = k;
+    std::vector<double> pts(2 * (size_t)n);
+    for (int k = 0; k < n; ++k) {
+        pts[2 * k] = net->points[2 * order[k]];
+        pts[2 * k + 1] = net->points[2 * order[k] + 1];
+    }
+    net->points.swap(pts);
+    for (int &v : net->edge_ij) v = old_to_new[v];
+    for (int &v : net->tri_hjk) v = old_to_new[v];
+    for (int &v : net->facets) v = old_to_new[v];
+    for (int &v : net->mesh_pairs) v = old_to_new[v];
+    if (new_to_old) std::copy(order.begin(), order.end(), new_to_old);
+    return NR_OK;
+}
