@@ -234,6 +234,16 @@ typedef struct {
 int nr_sweep(nr_network *dnet, double miny, double yrange, const nr_fire_params *params, const double compr[3],
              const double shear[3], nr_step_record *records, int max_records, int *n_records,
              double *shear_positions, void *stream);
+/* nr_sweep with the whole protocol captured in one CUDA graph and launched
+ * once: no host round trip between strain steps; the records and shear
+ * positions are read after the last step (device buffers of 2*N doubles
+ * per recorded shear step).  Same arguments and the same results, bit for
+ * bit.  A mixed-precision network of up to 4096 nodes (relaxed in one CTA
+ * under host control) is swept as nr_sweep does.  After a failed step the
+ * network's positions are those after the last step. */
+int nr_sweep_graph(nr_network *dnet, double miny, double yrange, const nr_fire_params *params,
+                   const double compr[3], const double shear[3], nr_step_record *records, int max_records,
+                   int *n_records, double *shear_positions, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Drop-in for run_fire_md with the reference's own device arrays      */

@@ -364,11 +364,12 @@ class Network:
         return recs, (pos[:nrec.value] if pos is not None else None)
 
     def sweep(self, compr, shear, params=None, miny=None, yrange=None, keep_positions=False, max_records=100000,
-              stream=None):
+              stream=None, graph=False):
         """The compression-then-shear protocol of do_relaxation_run.  Returns
-        (records, shear_positions or None)."""
-        return self._sweep(self._lib.nr_sweep, "nr_sweep", compr, shear, params, miny, yrange, keep_positions,
-                           max_records, stream)
+        (records, shear_positions or None).  graph=True runs the whole
+        protocol as one CUDA graph (nr_sweep_graph)."""
+        fn, name = (self._lib.nr_sweep_graph, "nr_sweep_graph") if graph else (self._lib.nr_sweep, "nr_sweep")
+        return self._sweep(fn, name, compr, shear, params, miny, yrange, keep_positions, max_records, stream)
 
 
 class Batch:

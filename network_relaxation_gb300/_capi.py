@@ -123,6 +123,8 @@ SIGNATURES = {
     "nr_energies": (C.c_int, [P, c_double_p, c_double_p, P]),
     "nr_sweep": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,
                            C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
+    "nr_sweep_graph": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,
+                                 C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
     "nr_run_fire_md": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, P, P, P, P, P, P, P,
                                  P, P, c_double_p, C.c_double, C.c_double, C.c_int, C.c_int, c_double_p, c_int_p, P]),
     "nr_read_network_mesh": (C.c_int, [C.c_char_p, C.POINTER(P)]),

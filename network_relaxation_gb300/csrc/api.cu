@@ -439,51 +439,84 @@ static int sm_count() {
     return sms > 0 ? sms : 1;
 }
 
-/* One network over the whole GPU (FP64 cooperative kernel + energies). */
-static int relax_single_fp64(DeviceSet &S, int i, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
-    NetDev d = S.dev[i];
+/* Launch plan of one network relaxed by a persistent cooperative kernel
+ * over the whole GPU: FP64 (d.sub and d.n_units set here) or mixed. */
+struct GridPlan {
+    NetDev d;
+    int blocks, energy_blocks;
+    bool mixed;
+};
+
+/* Mixed precision, one network: up to kMixedCtaNodes nodes the whole
+ * relaxation runs in one CTA with u in shared memory (no grid barriers);
+ * larger networks use the cooperative kernel over the whole GPU. */
+constexpr int kMixedCtaNodes = 4096;
+
+static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
+    g.d = S.dev[i];
+    g.mixed = mixed;
     const int sms = sm_count();
-    int sub = 8;
-    while (sub > 1 && d.n_tiles * (8 / sub) < sms) sub /= 2;
-    d.sub = sub;
-    d.n_units = d.n_tiles * (8 / sub);
-    int max_blocks = 0;
-    NR_CUDA_TRY(fp64_grid_max_blocks(sub, d.use_gel != 0, &max_blocks));
-    const int blocks = std::max(1, std::min(d.n_units, max_blocks));
-    NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
-    NR_CUDA_TRY(launch_fp64_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
-    NR_CUDA_TRY(launch_energies(d, energy_blocks(d, sms), stream));
-    FireState st;
-    NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
-    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (mixed) {
+        g.blocks = mixed_grid_blocks(g.d.n);
+        if (g.blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
+        if ((size_t)5 * g.blocks > (size_t)4 * g.d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
+    } else {
+        int sub = 8;
+        while (sub > 1 && g.d.n_tiles * (8 / sub) < sms) sub /= 2;
+        g.d.sub = sub;
+        g.d.n_units = g.d.n_tiles * (8 / sub);
+        int max_blocks = 0;
+        NR_CUDA_TRY(fp64_grid_max_blocks(sub, g.d.use_gel != 0, &max_blocks));
+        g.blocks = std::max(1, std::min(g.d.n_units, max_blocks));
+    }
+    g.energy_blocks = energy_blocks(g.d, sms);
+    return NR_OK;
+}
+
+/* Enqueues one relaxation without waiting for it: the FIRE state zeroed,
+ * the persistent kernel, the energies.  Only stream work, so a stream
+ * capture records it into a graph. */
+static int enqueue_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream_t stream) {
+    NR_CUDA_TRY(cudaMemsetAsync(g.d.st, 0, sizeof(FireState), stream));
+    if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    else NR_CUDA_TRY(launch_fp64_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    NR_CUDA_TRY(launch_energies(g.d, g.energy_blocks, stream));
+    return NR_OK;
+}
+
+/* The report of a finished relaxation and its status (errors recorded). */
+static int report_status(const FireState &st, const NetDev &d, nr_report *rep) {
     fill_report(st, d, rep);
     if (rep->status == NR_ERR_TIMEOUT) return fail(NR_ERR_TIMEOUT, "grid barrier wait budget exceeded");
     if (rep->status < 0) return fail(rep->status, "relaxation produced non-finite forces");
     return rep->status;
 }
 
+static int relax_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
+    int rc = enqueue_grid(g, prm, stream);
+    if (rc != NR_OK) return rc;
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, g.d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    return report_status(st, g.d, rep);
+}
+
+/* One network over the whole GPU (FP64 cooperative kernel + energies). */
+static int relax_single_fp64(DeviceSet &S, int i, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
+    GridPlan g;
+    int rc = grid_plan(S, i, false, g);
+    if (rc != NR_OK) return rc;
+    return relax_grid(g, prm, stream, rep);
+}
+
 static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps);
 
-/* Mixed precision, one network: up to kMixedCtaNodes nodes the whole
- * relaxation runs in one CTA with u in shared memory (no grid barriers);
- * larger networks use the cooperative kernel over the whole GPU. */
 static int relax_single_mixed(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *rep) {
-    constexpr int kMixedCtaNodes = 4096;
-    NetDev d = S.dev[0];
-    if (d.n <= kMixedCtaNodes) return relax_set_batch(S, prm, stream, rep);
-    const int blocks = mixed_grid_blocks(d.n);
-    if (blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
-    if ((size_t)5 * blocks > (size_t)4 * d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
-    NR_CUDA_TRY(cudaMemsetAsync(d.st, 0, sizeof(FireState), stream));
-    NR_CUDA_TRY(launch_mixed_grid(d, to_dev(prm), blocks, barrier_budget_ns(), stream));
-    NR_CUDA_TRY(launch_energies(d, energy_blocks(d, sm_count()), stream));
-    FireState st;
-    NR_CUDA_TRY(cudaMemcpyAsync(&st, d.st, sizeof(FireState), cudaMemcpyDeviceToHost, stream));
-    NR_CUDA_TRY(cudaStreamSynchronize(stream));
-    fill_report(st, d, rep);
-    if (rep->status == NR_ERR_TIMEOUT) return fail(NR_ERR_TIMEOUT, "grid barrier wait budget exceeded");
-    if (rep->status < 0) return fail(rep->status, "relaxation produced non-finite forces");
-    return rep->status;
+    if (S.dev[0].n <= kMixedCtaNodes) return relax_set_batch(S, prm, stream, rep);
+    GridPlan g;
+    int rc = grid_plan(S, 0, true, g);
+    if (rc != NR_OK) return rc;
+    return relax_grid(g, prm, stream, rep);
 }
 
 /* Launch plan of the distributed-shared-memory kernel: cluster size and
@@ -808,6 +841,145 @@ static int run_fire_md_impl(const char *who, int num_dof, int npairs, int ntripl
     return rc;
 }
 
+/* One strain step of do_relaxation_run's protocol: the affine increment
+ * and the values its record reports. */
+struct SweepStep {
+    double xdisp, ydisp, curr, maxc;
+    int is_shear;
+};
+
+/* The steps of do_relaxation_run (large_strain_relax.cu:924-999):
+ * compression from compr[0] to compr[1] by compr[2], then shear likewise,
+ * in units of yrange, with the reference's loop arithmetic (a 1e-10 slack
+ * on the bound).  A zero increment makes one step, where the reference
+ * loops forever. */
+static int sweep_steps(double smult, const double compr[3], const double shear[3], std::vector<SweepStep> &out) {
+    constexpr size_t kMaxSteps = (size_t)1 << 24;
+    out.clear();
+    double min_disp = compr[0] * smult, max_disp = compr[1] * smult, inc = compr[2] * smult;
+    double curr_disp = 0.0;
+    if (max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            if (out.size() >= kMaxSteps) return fail(NR_ERR_INVALID, "sweep: more than 2^24 strain steps");
+            out.push_back({0.0, -inc, 0.0, curr_disp, 0});
+            if (!(inc > 0)) break;
+        }
+    }
+    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
+    min_disp = shear[0] * smult;
+    max_disp = shear[1] * smult;
+    inc = shear[2] * smult;
+    if (max_disp > 0) {
+        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
+            if (out.size() >= kMaxSteps) return fail(NR_ERR_INVALID, "sweep: more than 2^24 strain steps");
+            out.push_back({inc, 0.0, curr_disp, max_comp, 1});
+            if (!(inc > 0)) break;
+        }
+    }
+    return NR_OK;
+}
+
+static void record_step(const SweepStep &t, const nr_report &rep, nr_step_record &R) {
+    R.curr_disp = t.curr;
+    R.max_comp = t.maxc;
+    R.e_stretch = rep.e_stretch;
+    R.e_bend = rep.e_bend;
+    R.e_gel = rep.e_gel;
+    R.rms_force = rep.rms_force;
+    R.max_force = rep.max_force;
+    R.steps = rep.steps;
+    R.is_shear = t.is_shear;
+    R.status = rep.status;
+    R.fp64_steps = rep.fp64_steps;
+}
+
+/* Stream, graph and buffers of one captured sweep, released on every path
+ * (cudaFree waits for the device). */
+struct SweepGraphRes {
+    cudaStream_t cs = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FireState *states = nullptr;
+    double2 *snaps = nullptr;
+    ~SweepGraphRes() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (states) cudaFree(states);
+        if (snaps) cudaFree(snaps);
+        if (cs) cudaStreamDestroy(cs);
+    }
+};
+
+/* The whole strain sweep as one CUDA graph.  Per step: the affine
+ * increment, the relaxation (enqueue_grid), and device-to-device copies of
+ * the FIRE state and, for a recorded shear step, of the positions.  One
+ * graph launch, then the host reads all records.  The kernels and their
+ * arguments are the step-by-step sweep's, so are the results, bit for bit.
+ * After a failed step the graph still runs the later ones; the records
+ * stop before the failure, as in the step-by-step sweep. */
+static int sweep_graph(DeviceSet &S, const GridPlan &g, double miny, double yrange, const nr_fire_params &prm,
+                       const std::vector<SweepStep> &steps, nr_step_record *records, int max_records, int *n_records,
+                       double *shear_positions, cudaStream_t user) {
+    const size_t n_steps = steps.size();
+    const size_t n_rec = std::min(n_steps, (size_t)std::max(max_records, 0));
+    const size_t n_nodes = (size_t)S.total_nodes;
+    std::vector<long> snap_of(n_rec, -1);
+    size_t n_snap = 0;
+    if (shear_positions)
+        for (size_t k = 0; k < n_rec; k++)
+            if (steps[k].is_shear) snap_of[k] = (long)n_snap++;
+    SweepGraphRes r;
+    NR_CUDA_TRY(cudaStreamSynchronize(user));
+    NR_CUDA_TRY(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    NR_CUDA_TRY(cudaMalloc(&r.states, sizeof(FireState) * n_steps));
+    if (n_snap) NR_CUDA_TRY(cudaMalloc(&r.snaps, sizeof(double2) * n_nodes * n_snap));
+    NR_CUDA_TRY(cudaStreamBeginCapture(r.cs, cudaStreamCaptureModeThreadLocal));
+    int rc = NR_OK;
+    for (size_t k = 0; k < n_steps && rc == NR_OK; k++) {
+        const SweepStep &t = steps[k];
+        cudaError_t e = launch_affine(S.x_all, (int)S.total_nodes, miny, yrange, t.xdisp, t.ydisp, r.cs);
+        if (e == cudaSuccess) {
+            rc = enqueue_grid(g, prm, r.cs);
+            if (rc != NR_OK) break;
+            e = cudaMemcpyAsync(r.states + k, g.d.st, sizeof(FireState), cudaMemcpyDeviceToDevice, r.cs);
+        }
+        if (e == cudaSuccess && k < n_rec && snap_of[k] >= 0)
+            e = cudaMemcpyAsync(r.snaps + n_nodes * snap_of[k], S.x_all, sizeof(double2) * n_nodes,
+                                cudaMemcpyDeviceToDevice, r.cs);
+        if (e != cudaSuccess) rc = fail(NR_ERR_CUDA, std::string("sweep capture: ") + cudaGetErrorString(e));
+    }
+    const cudaError_t ec = cudaStreamEndCapture(r.cs, &r.graph);
+    if (rc != NR_OK) return rc;
+    if (ec != cudaSuccess) return fail(NR_ERR_CUDA, std::string("sweep capture: ") + cudaGetErrorString(ec));
+    NR_CUDA_TRY(cudaGraphInstantiate(&r.exec, r.graph, 0));
+    NR_CUDA_TRY(cudaGraphLaunch(r.exec, r.cs));
+    std::vector<FireState> st(n_steps);
+    NR_CUDA_TRY(cudaMemcpyAsync(st.data(), r.states, sizeof(FireState) * n_steps, cudaMemcpyDeviceToHost, r.cs));
+    NR_CUDA_TRY(cudaStreamSynchronize(r.cs));
+    std::vector<nr_report> reps(n_steps);
+    size_t n_ok = n_steps;
+    int err = NR_OK, worst = NR_OK;
+    for (size_t k = 0; k < n_steps; k++) {
+        const int s = report_status(st[k], g.d, &reps[k]);
+        if (s < 0) {
+            n_ok = k;
+            err = s;
+            break;
+        }
+        if (s == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+    }
+    const size_t n_out = std::min(n_ok, n_rec);
+    for (size_t k = 0; k < n_out; k++) {
+        record_step(steps[k], reps[k], records[k]);
+        if (snap_of[k] >= 0)
+            NR_CUDA_TRY(cudaMemcpyAsync(shear_positions + 2 * n_nodes * k, r.snaps + n_nodes * snap_of[k],
+                                        sizeof(double2) * n_nodes, cudaMemcpyDefault, r.cs));
+    }
+    NR_CUDA_TRY(cudaStreamSynchronize(r.cs));
+    *n_records = (int)n_out;
+    return err != NR_OK ? err : worst;
+}
+
 }  // namespace nr
 
 using namespace nr;
@@ -910,58 +1082,56 @@ int nr_sweep(nr_network *d, double miny, double yrange, const nr_fire_params *pa
     if (rc != NR_OK) return rc;
     if (!(yrange > 0)) return fail(NR_ERR_INVALID, "nr_sweep: yrange must be positive");
     *n_records = 0;
-    const double smult = yrange;
+    std::vector<SweepStep> steps;
+    rc = sweep_steps(yrange, compr, shear, steps);
+    if (rc != NR_OK) return rc;
     const size_t n2 = 2 * (size_t)d->set.total_nodes;
     int worst = NR_OK;
-    auto one = [&](double xdisp, double ydisp, double curr, double maxc, int is_shear) -> int {
-        int r = nr_affine_displace(d, miny, yrange, xdisp, ydisp, stream);
-        if (r != NR_OK) return r;
+    for (const SweepStep &t : steps) {
+        rc = nr_affine_displace(d, miny, yrange, t.xdisp, t.ydisp, stream);
+        if (rc != NR_OK) return rc;
         nr_report rep;
-        r = nr_relax(d, params, &rep, stream);
-        if (r < 0) return r;
-        if (r == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
+        rc = nr_relax(d, params, &rep, stream);
+        if (rc < 0) return rc;
+        if (rc == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
         if (*n_records < max_records) {
-            nr_step_record &R = records[*n_records];
-            R.curr_disp = curr;
-            R.max_comp = maxc;
-            R.e_stretch = rep.e_stretch;
-            R.e_bend = rep.e_bend;
-            R.e_gel = rep.e_gel;
-            R.rms_force = rep.rms_force;
-            R.max_force = rep.max_force;
-            R.steps = rep.steps;
-            R.is_shear = is_shear;
-            R.status = rep.status;
-            R.fp64_steps = rep.fp64_steps;
-            if (is_shear && shear_positions) {
-                r = nr_network_get_positions(d, shear_positions + n2 * (size_t)(*n_records), stream);
-                if (r != NR_OK) return r;
+            record_step(t, rep, records[*n_records]);
+            if (t.is_shear && shear_positions) {
+                rc = nr_network_get_positions(d, shear_positions + n2 * (size_t)(*n_records), stream);
+                if (rc != NR_OK) return rc;
             }
             (*n_records)++;
         }
-        return NR_OK;
-    };
-    double min_disp = compr[0] * smult, max_disp = compr[1] * smult, inc = compr[2] * smult;
-    double curr_disp = 0.0;
-    if (max_disp > 0) {
-        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
-            rc = one(0, -inc, 0.0, curr_disp, 0);
-            if (rc < 0) return rc;
-            if (!(inc > 0)) break; /* the reference loops forever when inc == 0 */
-        }
-    }
-    const double max_comp = max_disp > min_disp ? curr_disp - inc : max_disp;
-    min_disp = shear[0] * smult;
-    max_disp = shear[1] * smult;
-    inc = shear[2] * smult;
-    if (max_disp > 0) {
-        for (curr_disp = min_disp; curr_disp <= max_disp + 1e-10; curr_disp += inc) {
-            rc = one(inc, 0, curr_disp, max_comp, 1);
-            if (rc < 0) return rc;
-            if (!(inc > 0)) break;
-        }
     }
     return worst;
+}
+
+int nr_sweep_graph(nr_network *d, double miny, double yrange, const nr_fire_params *params, const double compr[3],
+                   const double shear[3], nr_step_record *records, int max_records, int *n_records,
+                   double *shear_positions, void *stream) {
+    if (!d || !compr || !shear || !n_records || (max_records > 0 && !records))
+        return fail(NR_ERR_INVALID, "nr_sweep_graph: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    if (!(yrange > 0)) return fail(NR_ERR_INVALID, "nr_sweep_graph: yrange must be positive");
+    const bool mixed = params->precision == NR_MIXED;
+    const NetDev &d0 = d->set.dev[0];
+    if (mixed && d0.use_gel) return fail(NR_ERR_INVALID, "nr_sweep_graph: a gel-coupled network relaxes in FP64 only");
+    /* A small network's mixed relaxation is steered between launches by the
+     * host (one CTA, escalation): it is swept step by step. */
+    if (mixed && d0.n <= kMixedCtaNodes)
+        return nr_sweep(d, miny, yrange, params, compr, shear, records, max_records, n_records, shear_positions,
+                        stream);
+    *n_records = 0;
+    std::vector<SweepStep> steps;
+    rc = sweep_steps(yrange, compr, shear, steps);
+    if (rc != NR_OK || steps.empty()) return rc;
+    clear_error();
+    GridPlan g;
+    rc = grid_plan(d->set, 0, mixed, g);
+    if (rc != NR_OK) return rc;
+    return sweep_graph(d->set, g, miny, yrange, *params, steps, records, max_records, n_records, shear_positions,
+                       as_stream(stream));
 }
 
 int nr_run_fire_md(int num_dof, int npairs, int ntriples, double width, double ks, double kb, double *d_pos,

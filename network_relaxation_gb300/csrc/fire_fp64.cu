@@ -323,7 +323,7 @@ cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &pp, &bb};
     const void *k = d.use_gel ? (const void *)k_fire_grid<true> : (const void *)k_fire_grid<false>;
-    return cudaLaunchCooperativeKernel(k, dim3(blocks), dim3(32 * d.sub), args, grid_smem_bytes(d.sub), stream);
+    return launch_cooperative(k, blocks, 32 * d.sub, args, grid_smem_bytes(d.sub), stream);
 }
 
 cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream) {

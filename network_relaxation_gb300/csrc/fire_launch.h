@@ -9,6 +9,24 @@
 
 namespace nr {
 
+/* A cooperative launch (all CTAs co-resident, as the grid barriers need),
+ * expressed as a launch attribute so that stream capture records it as a
+ * cooperative kernel node of a CUDA graph. */
+inline cudaError_t launch_cooperative(const void *kernel, int blocks, int threads, void **args, size_t smem,
+                                      cudaStream_t stream) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, kernel, args);
+}
+
 cudaError_t fp64_grid_max_blocks(int sub, bool gel, int *max_blocks);
 cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                              cudaStream_t stream);

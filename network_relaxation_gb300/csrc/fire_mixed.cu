@@ -469,10 +469,8 @@ cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int block
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &pp, &bb};
     if (grid_threads(d.n) == 1024)
-        return cudaLaunchCooperativeKernel((const void *)k_fire_grid_mixed<1024>, dim3(blocks), dim3(1024), args, 0,
-                                           stream);
-    return cudaLaunchCooperativeKernel((const void *)k_fire_grid_mixed<512>, dim3(blocks), dim3(512), args, 0,
-                                       stream);
+        return launch_cooperative((const void *)k_fire_grid_mixed<1024>, blocks, 1024, args, 0, stream);
+    return launch_cooperative((const void *)k_fire_grid_mixed<512>, blocks, 512, args, 0, stream);
 }
 
 }  // namespace nr

@@ -3,7 +3,7 @@
  * (jmichelstl/network_relaxation, src/large_strain_relax.cu), in plain C.
  *
  * TEST INFRASTRUCTURE ONLY.  The test suite, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg use it as the checker; the product never links,
+ * bench.py's CPU-baseline leg use it to check results against; the product never links,
  * loads or calls it.
  *
  * Parity pin: tests/test_oracle_vs_reference.py checks this restatement

@@ -137,6 +137,32 @@ def test_sweep_matches_oracle(cuda):
     assert np.array_equal(pos[shear_rows], opos[[i for i, o in enumerate(orecs) if o[7] == 1]])
 
 
+def _rec(r):
+    return (r.curr_disp, r.max_comp, r.e_stretch, r.e_bend, r.rms_force, r.max_force, r.steps, r.is_shear,
+            r.status)
+
+
+def test_sweep_graph_equals_step_by_step_sweep(cuda):
+    """The protocol captured in one CUDA graph gives the step-by-step
+    sweep's records and shear positions bit for bit (and so the oracle's:
+    test_sweep_matches_oracle)."""
+    h, _ = lattice(16, 0.7, 9)
+    prm = nr.fire_params(fcut=1e-10, criterion="max", **FIRE)
+    compr, shear = [0.01, 0.02, 0.01], [0.01, 0.03, 0.01]
+    recs, pos = nr.Network(h, ks=1.0, kb=1e-3).sweep(compr, shear, prm, keep_positions=True, graph=True)
+    precs, ppos = nr.Network(h, ks=1.0, kb=1e-3).sweep(compr, shear, prm, keep_positions=True)
+    assert len(recs) == len(precs) == 5
+    assert [_rec(r) for r in recs] == [_rec(r) for r in precs]
+    rows = [i for i, r in enumerate(precs) if r.is_shear]
+    assert np.array_equal(pos[rows], ppos[rows])
+    # Steps past max_records still run: the final positions agree.
+    g, p = nr.Network(h, ks=1.0, kb=1e-3), nr.Network(h, ks=1.0, kb=1e-3)
+    r2, _ = g.sweep(compr, shear, prm, max_records=2, graph=True)
+    p2, _ = p.sweep(compr, shear, prm, max_records=2)
+    assert [_rec(r) for r in r2] == [_rec(r) for r in p2] and len(r2) == 2
+    assert np.array_equal(g.positions(), p.positions())
+
+
 def test_run_fire_md_dropin(cuda):
     """The reference's own argument list, device arrays from torch."""
     import torch

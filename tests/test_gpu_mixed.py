@@ -179,3 +179,19 @@ def test_mixed_mikado_certified(cuda):
         m = oracle.Model(a, 1.0, 1.0)
         assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
         assert m.energies(x) == (reps[i].e_stretch, reps[i].e_bend)
+
+
+def test_sweep_graph_mixed_grid_equals_step_by_step(cuda):
+    """5184 nodes: the cooperative mixed kernel, captured in one CUDA graph
+    per sweep; its integer-only atomics keep it deterministic, so the graph
+    and the step-by-step sweep agree bit for bit."""
+    h = nr.HostNetwork.lattice(72, 72, 0.65, 0.0, 3).get_triples()
+    prm = nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **FIRE)
+    recs, pos = nr.Network(h, ks=1.0, kb=1e-3).sweep([0, 0, 0], [0.01, 0.02, 0.01], prm, keep_positions=True,
+                                                     graph=True)
+    precs, ppos = nr.Network(h, ks=1.0, kb=1e-3).sweep([0, 0, 0], [0.01, 0.02, 0.01], prm, keep_positions=True)
+    key = lambda r: (r.curr_disp, r.e_stretch, r.e_bend, r.max_force, r.steps, r.fp64_steps, r.status)
+    assert len(recs) == len(precs) == 2
+    assert [key(r) for r in recs] == [key(r) for r in precs]
+    assert all(r.status == nr.NR_OK and r.max_force < 1e-10 for r in recs)
+    assert np.array_equal(pos, ppos)
