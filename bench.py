@@ -255,12 +255,12 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
-    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1", "A1", "IO"],
+    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1", "A1", "IO", "S1"],
                     help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
                          "first strain increment of its protocol, FIRE steps capped by --max-steps; M1: the same "
                          "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
                          "solve of sparse_relax.cpp on one large network; A1: the post-relaxation analyses; IO: "
-                         "reading and writing network files (host only)")
+                         "reading and writing network files (host only); S1: the C1 strain sweep as one CUDA graph")
     ap.add_argument("--reorder", default="none", choices=["none", "morton", "rcm"],
                     help="renumber every network's nodes (nr_host_network_reorder) before the batch is built")
     ap.add_argument("--side", type=int, default=0,
@@ -281,6 +281,8 @@ def main():
         return analyses_arm(args)
     if args.workload == "IO":
         return io_arm(args)
+    if args.workload == "S1":
+        return sweep_arm(args)
     if args.workload != "C4":
         return single_network_arm(args)
 
@@ -547,6 +549,92 @@ def single_network_arm(args):
                          "traffic": None, "kernel": "k_fire_grid_mixed" if args.precision == "mixed" else "k_fire_grid"},
             **extra,
         }))
+    return 0
+
+
+S1 = dict(L=32, p=0.65, seed=1, ks=1.0, kb=1e-3, compr=(0.0, 0.0, 0.0), shear=(0.01, 0.1, 0.01))
+
+
+def sweep_arm(args):
+    """--workload S1: the strain protocol of do_relaxation_run on C1 (32 x 32
+    lattice, p = 0.65, k = 1, kappa = 1e-3; shear 0.01 .. 0.1 by 0.01, ten
+    warm-started relaxations to max|F| < 1e-10, FP64), as one CUDA graph
+    (nr_sweep_graph) and step by step (nr_sweep).  One step = the whole
+    sweep from the unstrained positions; strain steps/s.  The sweep call is
+    synchronous: it is timed with CUDA events on the caller's stream around
+    the call.  e2e adds the H2D of the start positions from pinned memory
+    and the D2H of every shear step's relaxed positions and records."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    h = nr.HostNetwork.lattice(S1["L"], S1["L"], S1["p"], 0.0, S1["seed"]).get_triples()
+    info = h.info()
+    net = nr.Network(h, S1["ks"], S1["kb"])
+    x0 = torch.from_numpy(net.positions()).pin_memory()
+    prm = fire_params(nr, "fp64")
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+
+    def run(graph, keep):
+        return net.sweep(S1["compr"], S1["shear"], prm, keep_positions=keep, graph=graph,
+                         stream=stream.cuda_stream)
+
+    def timed(graph, keep):
+        times, recs = [], None
+        for s in range(args.warmup + args.steps):
+            net.set_positions(x0.numpy())
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if keep:
+                net.set_positions(x0.numpy())
+            recs, pos = run(graph, keep)
+            e1.record(stream)
+            e1.synchronize()
+            if s >= args.warmup:
+                times.append(e0.elapsed_time(e1))
+        return float(np.mean(times)), recs
+
+    clocks.start()
+    ms_graph, recs = timed(True, False)
+    clk = clocks.stop()
+    ms_plain, precs = timed(False, False)
+    ms_e2e, _ = timed(True, True)
+    n_steps = len(recs)
+    fire_steps = sum(r.steps for r in recs)
+    same = [(r.e_stretch, r.e_bend, r.steps) for r in recs] == [(r.e_stretch, r.e_bend, r.steps) for r in precs]
+    line = {
+        "metric": "strain steps/s, C1 shear protocol (10 relaxations to max|F|<1e-10, FP64) as one CUDA graph",
+        "value": n_steps / (ms_graph / 1e3), "unit": "strain steps/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "replicas",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "S1: lattice 32x32, p=0.65, no jitter, seed 1, triples by get_triples; ks 1, kb 1e-3; "
+                               "shear 0.01 0.1 0.01; N=%d E=%d T=%d" % (info.n_points, info.n_edges, info.n_triples),
+                   "l2": "inputs are 0.1 MB (L2-resident by design: a latency-bound workload)"},
+        "step_by_step": {"value": n_steps / (ms_plain / 1e3), "ms_per_step": ms_plain,
+                         "records_equal_to_graph": same},
+        "fire_steps_per_sweep": fire_steps, "us_per_fire_step": 1e3 * ms_graph / fire_steps,
+        "e2e": {"value": n_steps / (ms_e2e / 1e3), "unit": "strain steps/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": 16 * info.n_points,
+                "d2h_bytes_per_step": 16 * info.n_points * n_steps + 64 * n_steps},
+        "gpu_launches": 5 * n_steps * args.steps,
+        "clocks": clk,
+    }
+    if not args.no_cpu:
+        import oracle
+
+        a = h.arrays()
+        H = a["maxy"] - a["miny"]
+        t0 = time.perf_counter()
+        orecs, _, _ = oracle.Model(a, S1["ks"], S1["kb"]).sweep(
+            a["points"], a["miny"], H, oracle.params(fcut=1e-10, criterion="max", max_steps=10_000_000),
+            list(S1["compr"]), list(S1["shear"]))
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(orecs) / dt, "unit": "strain steps/s", "cores": 1, "kind": "port",
+                                "sample": "the oracle's whole sweep, %d shear steps (%.1f s)" % (len(orecs), dt)}
+    print(json.dumps(line))
     return 0
 
 
