@@ -154,6 +154,8 @@ def test_invalid_arguments_are_errors_not_crashes(built):
     with pytest.raises(nr.NetRelaxError):
         nr.HostNetwork.from_arrays(pts, ij, w, 1.0)
     assert lib.nr_relax(None, None, None, None) == nr.NR_ERR_INVALID
+    for fn in (lib.nr_sweep, lib.nr_sweep_graph):
+        assert fn(None, 0.0, 1.0, None, None, None, None, 0, None, None, None) == nr.NR_ERR_INVALID
     assert "invalid" in lib.nr_status_string(nr.NR_ERR_INVALID).decode()
 
 
