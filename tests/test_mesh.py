@@ -248,3 +248,95 @@ def test_live_reference_random_meshes(seed, tmp_path):
         x[j] = x[i] + [a["offset"], 0.0]
     F = oracle.Model(a, 0.0, 0.0, fcodes=fc, gel=gel).forces(x)
     assert np.array_equal(F, oracle.ref_mesh_forces(a, x, a["offset"], 0.0, 0.0, gel, fc))
+
+
+# ------------------------------------------------------ fuzzed .nmc files
+
+def _fuzz_mesh(path, rng):
+    """A generated composite written as .nmc, then mutated line by line:
+    dropped, duplicated or junk lines (so lines shift between sections and
+    are parsed as the next section's), tabs, trailing fields, CRLF, negative
+    areas, out-of-range indices, wraps outside a char's range, truncation."""
+    src = path + ".src"
+    nr.HostNetwork.lattice_mesh(int(rng.integers(3, 8)), int(rng.integers(3, 6)), float(rng.uniform(0.5, 1.0)),
+                                float(rng.uniform(0, 0.2)), seed=int(rng.integers(1, 1000))).write_mesh(src)
+    lines = open(src).read().split("\n")
+    os.remove(src)
+    n = int(lines[0].split()[0])
+    out = [lines[0]]
+    for ln in lines[1:]:
+        r = rng.random()
+        if r < 0.002:
+            continue
+        if r < 0.004:
+            out.append(ln)
+        elif r < 0.02:
+            out.append("# junk")
+        elif r < 0.04:
+            out.append("")
+        f = ln.split()
+        if f and rng.random() < 0.004:
+            if len(f) == 1:
+                f[0] = rng.choice(["-1.5", "0", "1e-300", "0x1p-2"])
+            elif len(f) == 3 and "." not in ln:
+                k = int(rng.integers(3))
+                f[k] = str(rng.choice([-1, n, n + 5, 200, -300]))
+            ln = rng.choice([" ", "\t", "  "]).join(f)
+        if rng.random() < 0.01:
+            ln += " 7"
+        out.append(ln)
+    text = "\n".join(out)
+    if rng.random() < 0.3:
+        text = text.replace("\n", "\r\n")
+    if rng.random() < 0.15:
+        text = text[: int(len(text) * rng.uniform(0.3, 1.0))]
+    with open(path, "w") as fh:
+        fh.write(text)
+
+
+def _same_mesh(a, b, ok_a, ok_b, label, triples=False):
+    assert ok_a == ok_b, label
+    for k in ("points", "edge_ij", "edge_wrap", "facets", "areas", "mpairs") + (("tri_hjk", "tri_wrap") if triples
+                                                                                 else ()):
+        assert np.array_equal(np.asarray(a[k]).reshape(-1), np.asarray(b[k]).reshape(-1)), (label, k)
+    assert [float(v).hex() for v in a["edge_l0"]] == [float(v).hex() for v in b["edge_l0"]], label
+    if ok_a:
+        for k in ("offset", "minx", "miny", "maxx", "maxy"):
+            assert float(a[k]).hex() == float(b[k]).hex(), (label, k)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_mesh_reader_on_fuzzed_files(seed, tmp_path):
+    """nr_read_network_mesh returns what the oracle's restatement of
+    read_network_mesh does, accept / reject verdict and partial arrays
+    included."""
+    rng = np.random.default_rng(1000 + seed)
+    path = str(tmp_path / "f.nmc")
+    _fuzz_mesh(path, rng)
+    ok_o, a = oracle.read_network_mesh(path)
+    try:
+        h = nr.HostNetwork.read_mesh(path, strict=False)
+    except nr.NetRelaxError:
+        assert not ok_o and len(a["points"]) == 0, path
+        return
+    b = dict(h.arrays())
+    b.update(minx=h.mesh_info().minx, maxx=h.mesh_info().maxx)
+    ok_n = True
+    try:
+        nr.HostNetwork.read_mesh(path)
+    except nr.NetRelaxError:
+        ok_n = False
+    _same_mesh(a, b, ok_o, ok_n, "seed %d" % seed)
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_live_reference_mesh_reader_on_fuzzed_files(seed, tmp_path):
+    """The oracle's reader against the reference's own read_network_mesh
+    (and get_triples) on the same fuzzed files."""
+    _need_ref()
+    rng = np.random.default_rng(1000 + seed)
+    path = str(tmp_path / "f.nmc")
+    _fuzz_mesh(path, rng)
+    ok_o, a = oracle.read_network_mesh(path)
+    ok_r, r = oracle.ref_read_network_mesh(path)
+    _same_mesh(a, r, ok_o, ok_r, "seed %d" % seed, triples=ok_o and ok_r)
