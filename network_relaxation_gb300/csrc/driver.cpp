@@ -55,10 +55,14 @@ bool read_line(std::ifstream &input, std::string &line) {
     return !(line.empty() || line[0] == '#');
 }
 
+/* split_line (large_strain_relax.cu:229): tokens separated by spaces and
+ * tabs, of the line up to its first NUL (the reference strtok's a strcpy'd
+ * copy). */
 std::vector<std::string> split_ws(const std::string &line) {
     std::vector<std::string> out;
     std::string cur;
     for (char c : line) {
+        if (c == '\0') break;
         if (c == ' ' || c == '\t') {
             if (!cur.empty()) out.push_back(cur);
             cur.clear();
@@ -168,11 +172,14 @@ static int parse_batch(const char *path, nr_batch_spec *spec, nr_mesh_batch_spec
         return fail(NR_ERR_PARSE, "batch file: invalid mechanical attributes");
     }
     if (!read_line(input, line)) return fail(NR_ERR_PARSE, "batch file: missing FIRE parameters");
+    /* parse_doubles (large_strain_relax.cu:247): a token counts when sscanf
+     * returns nonzero, so a token of only '\r' (sscanf gives EOF) repeats
+     * the previous value; before any value it is 0 here (the reference's
+     * variable is uninitialised). */
     std::vector<double> fp;
-    for (const std::string &s : split_ws(line)) {
-        double v;
-        if (sscanf(s.c_str(), "%lf", &v) == 1) fp.push_back(v);
-    }
+    double v = 0.0;
+    for (const std::string &s : split_ws(line))
+        if (sscanf(s.c_str(), "%lf", &v) != 0) fp.push_back(v);
     if (fp.size() < 5) {
         fprintf(stderr, "Too few FIRE parameters were supplied. 8 are needed.\n");
         return fail(NR_ERR_PARSE, "batch file: too few FIRE parameters");

@@ -65,10 +65,16 @@ def build(force=False):
     return ORACLE_SO
 
 
+_ref_built = False
+
+
 def build_ref():
     """Builds oracle/_ref/liblsr_ref.so (and libnmr_ref.so) when the reference
-    checkout exists."""
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
+    checkout exists; once per process."""
+    global _ref_built
+    if not _ref_built:
+        subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, stdout=subprocess.DEVNULL)
+        _ref_built = True
     return REF_SO if os.path.exists(REF_SO) else None
 
 

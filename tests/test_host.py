@@ -165,3 +165,120 @@ def test_lsrelax_cli_usage_errors(built):
     assert r.returncode != 0 and "No batch file was specified" in r.stderr
     r = subprocess.run([exe, "-b", "/nonexistent/batch.txt"], capture_output=True, text=True)
     assert r.returncode != 0 and "could not be read" in r.stderr
+
+
+def _fuzz_batch(path, rng, kind):
+    """A batch file of one of the three grammars (lsrelax, nmrelax,
+    sp_relax) with random values and the mistakes users make: comments,
+    blank lines, tabs, CRLF (often with a space before the CR), too few or
+    non-numeric values, negative values, reversed ranges, NUL bytes inside
+    a line, truncation.  sp_relax files are never truncated: the
+    reference's parser returns an uninitialised flag when the file ends
+    before the shear line, so their entry lines are never empty either."""
+
+    def num(lo, hi):
+        v = float(rng.uniform(lo, hi))
+        return rng.choice(["%r" % v, "%.3g" % v, "%d" % int(v), "%.2e" % v])
+
+    def vals(k, lo, hi, ordered=False):
+        if rng.random() < 0.85:
+            lo = 0.0  # mostly valid values, so that accepted files are common too
+        x = [float(rng.uniform(lo, hi)) for _ in range(k)]
+        if ordered and rng.random() < 0.9:
+            x[:2] = sorted(x[:2])
+        out = [rng.choice(["%r" % v, "%.3g" % v, "%d" % int(v), "%.2e" % v]) for v in x]
+        if rng.random() < 0.1:
+            out.insert(int(rng.integers(len(out) + 1)), rng.choice(["abc", "1e", "0x10", "nan", "-"]))
+        if rng.random() < 0.08:
+            out = out[: int(rng.integers(len(out) + 1))]
+        return rng.choice([" ", "\t", "  "]).join(out)
+
+    base = rng.choice(["nets/lat", "a", "./x_y", "dir/sub/net"]) + (" tag%d" % rng.integers(9) if rng.random() < 0.5
+                                                                     else "")
+    if kind == "spr":
+        # An empty entry line would shift the later entries up and leave the
+        # shear line missing: a junk line stands in for it.
+        lines = [base] + [vals(3, lo, hi, o) or "x" for lo, hi, o in ((-0.2, 3, False), (-0.01, 0.2, True),
+                                                                       (-0.01, 0.2, True))]
+    else:
+        lines = [base, vals(2 if kind == "lsr" else int(rng.integers(2, 6)), -0.2, 3),
+                 vals(int(rng.integers(4, 9)), -0.1, 2),
+                 "%d %s %s %d" % (rng.integers(-2, 8), num(-0.02, 2), num(-1e-10, 1e-8), rng.integers(-5, 10 ** 6)),
+                 vals(3, -0.01, 0.2, True), vals(3, -0.01, 0.2, True)]
+        if rng.random() < 0.1:
+            lines[3] = " ".join(lines[3].split()[: int(rng.integers(4))])
+    crlf = rng.random() < 0.3
+    out = []
+    for ln in lines:
+        while rng.random() < 0.2:
+            out.append(rng.choice(["# comment", "", "#"]))
+        if rng.random() < (0.4 if crlf else 0.1):
+            ln += " "
+        if rng.random() < 0.05 and len(ln) > 2:
+            k = int(rng.integers(1, len(ln)))
+            ln = ln[:k] + "\0" + ln[k:]
+        out.append(ln)
+    text = "\n".join(out) + ("\n" if rng.random() < 0.7 else "")
+    if crlf:
+        text = text.replace("\n", "\r\n")
+    if kind != "spr" and rng.random() < 0.1:
+        text = text[: int(len(text) * rng.uniform(0.5, 1.0))]
+    with open(path, "wb") as f:
+        f.write(text.encode())
+
+
+def _ref_parse(kind, path):
+    """The reference's own parse_batch_file of that grammar: (ok, values)."""
+    base, tag = C.create_string_buffer(1024), C.create_string_buffer(256)
+    fp, cr, sh = (C.c_double * 5)(), (C.c_double * 3)(), (C.c_double * 3)()
+    mass, fcut, nmin, nmax = C.c_double(), C.c_double(), C.c_int(), C.c_int()
+    if kind == "spr":
+        mech = (C.c_double * 3)()
+        ok = oracle.ref_spr_lib().ref_spr_parse_batch_file(path.encode(), base, 1024, tag, 256, mech, cr, sh)
+        return bool(ok), (base.value, tag.value, list(mech), list(cr), list(sh))
+    if kind == "nmr":
+        mech = (C.c_double * 5)()
+        ok = oracle.ref_mesh_lib().ref_mesh_parse_batch_file(path.encode(), base, 1024, tag, 256, mech, fp,
+                                                             C.byref(nmin), C.byref(mass), C.byref(fcut),
+                                                             C.byref(nmax), cr, sh)
+    else:
+        ks, kb = C.c_double(), C.c_double()
+        ok = oracle.ref_lib().ref_parse_batch_file(path.encode(), base, 1024, tag, 256, C.byref(ks), C.byref(kb),
+                                                   fp, C.byref(nmin), C.byref(mass), C.byref(fcut), C.byref(nmax),
+                                                   cr, sh)
+        mech = [ks.value, kb.value]
+    return bool(ok), (base.value, tag.value, list(mech), list(fp), nmin.value, mass.value, fcut.value, nmax.value,
+                      list(cr), list(sh))
+
+
+def _lib_parse(kind, path):
+    if kind == "spr":
+        s = nr.parse_spr_batch_file(path)
+        return (s.base, s.tag, [s.ks, s.kb, s.mu], list(s.compr), list(s.shear))
+    if kind == "nmr":
+        m = nr.parse_mesh_batch_file(path)
+        s, mech = m.net, [m.net.ks, m.net.kb, m.bmod, m.smod, m.dilation]
+    else:
+        s = nr.parse_batch_file(path)
+        mech = [s.ks, s.kb]
+    return (s.base, s.tag, mech, list(s.fire_params), s.nmin, s.mass, s.fcut, s.nmax, list(s.compr), list(s.shear))
+
+
+@pytest.mark.parametrize("kind", ["lsr", "nmr", "spr"])
+@pytest.mark.parametrize("seed", range(120))
+def test_parse_batch_file_on_fuzzed_files_matches_live_reference(built, tmp_path, kind, seed):
+    """The three batch-file parsers against the reference's own, verdict and
+    values, on fuzzed files."""
+    if oracle.build_ref() is None or oracle.ref_lib() is None:
+        pytest.skip("reference checkout not available (golden fixtures cover this case)")
+    rng = np.random.default_rng(seed)
+    path = str(tmp_path / "batch.txt")
+    _fuzz_batch(path, rng, kind)
+    ok_r, r = _ref_parse(kind, path)
+    try:
+        got = _lib_parse(kind, path)
+    except nr.NetRelaxError:
+        assert not ok_r, open(path, "rb").read()
+        return
+    assert ok_r, open(path, "rb").read()
+    assert repr(got) == repr(r), open(path, "rb").read()
