@@ -152,3 +152,23 @@ def test_positions_writer_matches_report_displaced(tmp_path):
     nr.check(nr.lib().nr_write_positions(xy.ctypes.data_as(nr.C.POINTER(nr.C.c_double)), len(xy), path.encode()),
              "write_positions")
     assert open(path).read() == "".join("%2.10le\t%2.10le\n" % (x, y) for x, y in xy)
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_oracle_reader_matches_live_reference_on_fuzzed_files(seed, tmp_path):
+    """The oracle's restatement against the reference's own read_network
+    (and get_triples) built for the host, on the same fuzzed files."""
+    if oracle.build_ref() is None or oracle.ref_lib() is None:
+        pytest.skip("reference checkout not available (golden fixtures cover this case)")
+    rng = np.random.default_rng(seed)
+    path = str(tmp_path / "f.dat")
+    _fuzz_file(path, rng, int(rng.integers(1, 60)), int(rng.integers(0, 90)))
+    ok_o, a = oracle.read_network(path)
+    ok_r, r = oracle.ref_read_network(path)
+    assert ok_o == ok_r
+    keys = ("points", "edge_ij", "edge_wrap") + (("tri_hjk", "tri_wrap") if ok_o else ())
+    for k in keys:
+        assert np.array_equal(a[k], r[k]), k
+    assert [float(v).hex() for v in a["edge_l0"]] == [float(v).hex() for v in r["edge_l0"]]
+    if ok_o:
+        assert (a["offset"], a["miny"], a["maxy"]) == (r["offset"], r["miny"], r["maxy"])
