@@ -37,6 +37,17 @@ static unsigned long long barrier_budget_ns() {
     return (unsigned long long)(ms * 1e6);
 }
 
+/* Failure injection on the host for the wait-budget test:
+ * NR_TEST_STALL_BARRIER=k makes the FP64 grid kernel's barriers wait for k
+ * CTAs that were never launched, so the first wait runs out of its budget
+ * and the relaxation ends with NR_ERR_TIMEOUT (no fault; the context stays
+ * usable).  Unset or 0 in normal use. */
+static unsigned barrier_stall() {
+    const char *env = getenv("NR_TEST_STALL_BARRIER");
+    const int k = env ? atoi(env) : 0;
+    return k > 0 && k < 1024 ? (unsigned)k : 0u;
+}
+
 struct Image {
     std::vector<char> bytes;
     size_t add(size_t nbytes, size_t align = 256) {
@@ -479,7 +490,7 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
 static int enqueue_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream_t stream) {
     NR_CUDA_TRY(cudaMemsetAsync(g.d.st, 0, sizeof(FireState), stream));
     if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
-    else NR_CUDA_TRY(launch_fp64_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    else NR_CUDA_TRY(launch_fp64_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), barrier_stall(), stream));
     NR_CUDA_TRY(launch_energies(g.d, g.energy_blocks, stream));
     return NR_OK;
 }

@@ -122,19 +122,22 @@ __device__ void reduce_parts(const NetDev &d, double *s_red, double &P, double &
 
 /* kGel: the network carries a gel (network_mesh_relax.cu); the instance
  * without it has no gel code. */
+/* stall > 0 makes every grid barrier wait for that many CTAs that do not
+ * exist, so the first wait runs out of its budget: the failure-detection
+ * test of the wait budget (NR_TEST_STALL_BARRIER). */
 template <bool kGel>
-__global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget_ns) {
+__global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget_ns, unsigned stall) {
     extern __shared__ double s_units[];
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
-    const unsigned G = gridDim.x;
+    const unsigned G = gridDim.x, GB = G + stall;
     Scal s;
     bool last;
     const int item0 = blockIdx.x * blockDim.x + threadIdx.x, istride = G * blockDim.x;
     items_pass<kGel>(d, item0, istride);
-    if (!barrier_arrive(d.st, G, budget_ns, last, 4)) return;
+    if (!barrier_arrive(d.st, GB, budget_ns, last, 4)) return;
     if (last) barrier_release(d.st);
     pass_b<kGel>(d, 0.0, true, blockIdx.x, G, s_units);
-    if (!barrier_arrive(d.st, G, budget_ns, last, 1)) return;
+    if (!barrier_arrive(d.st, GB, budget_ns, last, 1)) return;
     if (last) {
         double P, V2, F2, M2;
         reduce_parts(d, s_red, P, V2, F2, M2);
@@ -148,13 +151,13 @@ __global__ void k_fire_grid(NetDev d, FireParamsDev p, unsigned long long budget
         scal_load(s, d.st);
         pass_a(d, s, blockIdx.x, G);
         if (s.done) break;
-        if (!barrier_arrive(d.st, G, budget_ns, last, 2)) return;
+        if (!barrier_arrive(d.st, GB, budget_ns, last, 2)) return;
         if (last) barrier_release(d.st);
         items_pass<kGel>(d, item0, istride);
-        if (!barrier_arrive(d.st, G, budget_ns, last, 5)) return;
+        if (!barrier_arrive(d.st, GB, budget_ns, last, 5)) return;
         if (last) barrier_release(d.st);
         pass_b<kGel>(d, s.dtm, false, blockIdx.x, G, s_units);
-        if (!barrier_arrive(d.st, G, budget_ns, last, 3)) return;
+        if (!barrier_arrive(d.st, GB, budget_ns, last, 3)) return;
         if (last) {
             double P, V2, F2, M2;
             reduce_parts(d, s_red, P, V2, F2, M2);
@@ -317,11 +320,12 @@ cudaError_t fp64_grid_max_blocks(int sub, bool gel, int *max_blocks) {
 }
 
 cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
-                             cudaStream_t stream) {
+                             unsigned stall, cudaStream_t stream) {
     NetDev dd = d;
     FireParamsDev pp = p;
     unsigned long long bb = budget_ns;
-    void *args[] = {&dd, &pp, &bb};
+    unsigned ss = stall;
+    void *args[] = {&dd, &pp, &bb, &ss};
     const void *k = d.use_gel ? (const void *)k_fire_grid<true> : (const void *)k_fire_grid<false>;
     return launch_cooperative(k, blocks, 32 * d.sub, args, grid_smem_bytes(d.sub), stream);
 }

@@ -28,8 +28,10 @@ inline cudaError_t launch_cooperative(const void *kernel, int blocks, int thread
 }
 
 cudaError_t fp64_grid_max_blocks(int sub, bool gel, int *max_blocks);
+/* stall: CTAs that never arrive, added to every grid barrier's count (0 in
+ * normal use; the wait-budget test sets 1). */
 cudaError_t launch_fp64_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
-                             cudaStream_t stream);
+                             unsigned stall, cudaStream_t stream);
 cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream);
 cudaError_t fp64_batch_max_blocks(int *max_blocks);
 cudaError_t launch_fp64_batch(const NetDev *nets_dev, int n_nets, const FireParamsDev &p, int *queue_dev,

@@ -211,3 +211,28 @@ def test_relax_bitwise_mikado(cuda):
     assert rep.status == nr.NR_OK and rep.steps == orep.steps
     assert np.array_equal(net.positions(), xo)
     assert rep.e_stretch == orep.e_stretch and rep.e_bend == orep.e_bend
+
+
+def test_grid_barrier_wait_budget_runs_out_without_a_fault(cuda, monkeypatch):
+    """Failure detection without a GPU fault.  NR_TEST_STALL_BARRIER=1 makes
+    the FP64 grid kernel's barriers wait for a CTA that was never launched.
+    Each wait gives up after its budget (NR_BARRIER_BUDGET_MS), every CTA
+    returns, and the relaxation reports NR_ERR_TIMEOUT.  The context stays
+    usable: the next relaxation of the same network equals the oracle's."""
+    h, a = lattice(12, 0.65, 7)
+    H = a["maxy"] - a["miny"]
+    net = nr.Network(h, ks=1.0, kb=1e-3)
+    net.affine_displace(a["miny"], H, 0.02 * H, 0.0)
+    prm = nr.fire_params(fcut=1e-10, criterion="max", **FIRE)
+    monkeypatch.setenv("NR_TEST_STALL_BARRIER", "1")
+    monkeypatch.setenv("NR_BARRIER_BUDGET_MS", "20")
+    with pytest.raises(nr.NetRelaxError) as e:
+        net.relax(prm)
+    assert e.value.status == nr.NR_ERR_TIMEOUT
+    monkeypatch.delenv("NR_TEST_STALL_BARRIER")
+    monkeypatch.delenv("NR_BARRIER_BUDGET_MS")
+    rep = net.relax(prm)  # the stalled launch stopped before its first drift: x is the strained start
+    x0 = oracle.affine_displace(a["points"], a["miny"], H, 0.02 * H, 0.0)
+    x_or, _, _, orep = oracle.Model(a, 1.0, 1e-3).fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
+    assert rep.status == nr.NR_OK and rep.steps == orep.steps
+    assert np.array_equal(net.positions(), x_or)
