@@ -90,6 +90,18 @@ class HostNetwork:
         return cls(out)
 
     @classmethod
+    def read_bin(cls, path):
+        """A network saved by write_bin (nr_read_network_bin): no parsing, no
+        get_triples; a truncated or corrupt file raises NR_ERR_PARSE."""
+        out = C.c_void_p()
+        st = _capi.load().nr_read_network_bin(str(path).encode(), C.byref(out))
+        if st != NR_OK:
+            if out.value:
+                _capi.load().nr_host_network_free(out)
+            raise NetRelaxError(st, "read_network_bin(%s)" % path)
+        return cls(out)
+
+    @classmethod
     def from_arrays(cls, points, edge_ij, edge_wrap, offset, edge_l0=None):
         points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 2)
         edge_ij = np.ascontiguousarray(edge_ij, dtype=np.int32).reshape(-1, 2)
@@ -229,6 +241,11 @@ class HostNetwork:
 
     def write(self, path):
         check(_capi.load().nr_write_network(self._h, str(path).encode()), "nr_write_network")
+
+    def write_bin(self, path):
+        """Binary side-car of this network (nr_write_network_bin): arrays as
+        stored, triples and mesh included, FNV-1a checksum."""
+        check(_capi.load().nr_write_network_bin(self._h, str(path).encode()), "nr_write_network_bin")
 
 
 def read_network(path):

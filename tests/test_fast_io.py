@@ -126,10 +126,8 @@ def test_binary_side_car(tmp_path):
     h.set_bond_k(np.linspace(1, 2, h.info().n_edges))
     a = h.arrays()
     path = str(tmp_path / "n.bin")
-    nr.check(nr.lib().nr_write_network_bin(h.handle, path.encode()), "write_bin")
-    out = nr.C.c_void_p()
-    nr.check(nr.lib().nr_read_network_bin(path.encode(), nr.C.byref(out)), "read_bin")
-    b = nr.HostNetwork(out).arrays()
+    h.write_bin(path)
+    b = nr.HostNetwork.read_bin(path).arrays()
     for k in ("points", "edge_ij", "edge_l0", "edge_wrap", "tri_hjk", "tri_wrap", "bond_k", "facets", "areas",
               "mpairs"):
         assert np.array_equal(a[k], b[k]), k
@@ -138,9 +136,11 @@ def test_binary_side_car(tmp_path):
     data = bytearray(open(path, "rb").read())
     data[len(data) // 2] ^= 0x40
     open(path, "wb").write(bytes(data))
-    assert nr.lib().nr_read_network_bin(path.encode(), nr.C.byref(out)) == nr.NR_ERR_PARSE
-    open(path, "wb").write(bytes(data[: len(data) // 3]))
-    assert nr.lib().nr_read_network_bin(path.encode(), nr.C.byref(out)) == nr.NR_ERR_PARSE
+    for bad in (bytes(data), bytes(data[: len(data) // 3])):
+        open(path, "wb").write(bad)
+        with pytest.raises(nr.NetRelaxError) as e:
+            nr.HostNetwork.read_bin(path)
+        assert e.value.status == nr.NR_ERR_PARSE
 
 
 def test_positions_writer_matches_report_displaced(tmp_path):
