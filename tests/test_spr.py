@@ -78,14 +78,19 @@ def test_spr_batch_parser_matches_golden():
         assert [s.ks, s.kb, s.mu] == r["mech"] and list(s.compr) == r["compr"] and list(s.shear) == r["shear"]
 
 
-@pytest.mark.parametrize("seed", [1, 2])
+@pytest.mark.parametrize("seed", range(12))
 def test_live_reference_random_networks(seed, tmp_path):
+    """Diluted lattices (with and without jitter) and Mikado networks (odd
+    seeds: bonds of every direction, near-collinear segment pairs)."""
     if oracle.ref_spr_lib() is None and (oracle.build_ref() is None or oracle.ref_spr_lib() is None):
         pytest.skip("reference checkout not present")
-    rng = np.random.default_rng(seed)
+    rng = np.random.default_rng(100 + seed)
     path = str(tmp_path / "r.dat")
-    h = nr.HostNetwork.lattice(int(rng.integers(5, 16)), int(rng.integers(4, 12)), float(rng.uniform(0.5, 1.0)),
-                               float(rng.choice([0.0, 0.05])), seed)
+    if seed % 2:
+        h = nr.HostNetwork.mikado(int(rng.integers(60, 200)), 0.25, 1.0, 1e-3, seed + 1)
+    else:
+        h = nr.HostNetwork.lattice(int(rng.integers(5, 20)), int(rng.integers(4, 14)), float(rng.uniform(0.45, 1.0)),
+                                   float(rng.choice([0.0, 0.05, 0.2])), seed + 1)
     h.write(path)
     r = oracle.RefSpr(path)
     a = _net_from(path)
