@@ -870,9 +870,8 @@ def io_arm(args):
     clock("read_dat", lambda: nr.HostNetwork.read(dat))
     h2 = nr.HostNetwork.read(dat)
     clock("get_triples", lambda: h2.get_triples())
-    clock("write_bin", lambda: nr.lib().nr_write_network_bin(h2.handle, binp.encode()))
-    out = C.c_void_p()
-    clock("read_bin", lambda: nr.lib().nr_read_network_bin(binp.encode(), C.byref(out)))
+    clock("write_bin", lambda: h2.write_bin(binp))
+    clock("read_bin", lambda: nr.HostNetwork.read_bin(binp))
     t0 = time.perf_counter()
     oracle.read_network(dat)
     t_or = time.perf_counter() - t0

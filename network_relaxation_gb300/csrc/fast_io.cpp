@@ -395,7 +395,7 @@ namespace nr {
 namespace {
 
 constexpr char kBinMagic[8] = {'N', 'R', 'N', 'E', 'T', 'B', 'I', 'N'};
-constexpr uint32_t kBinVersion = 1;
+constexpr uint32_t kBinVersion = 2; /* 2: the checksum covers the header */
 
 struct BinHeader {
     char magic[8];
@@ -412,6 +412,27 @@ uint64_t fnv1a(uint64_t h, const void *data, size_t n) {
         h *= 1099511628211ULL;
     }
     return h;
+}
+
+constexpr uint64_t kFnvBasis = 14695981039346656037ULL;
+
+/* FNV-1a of the header with its checksum field zeroed: the checksum starts
+ * here, so a damaged count, box or offset is caught like damaged data. */
+uint64_t header_sum(const BinHeader &h) {
+    BinHeader z = h;
+    z.checksum = 0;
+    return fnv1a(kFnvBasis, &z, sizeof(z));
+}
+
+/* Payload bytes the header announces (counts already range-checked). */
+uint64_t payload_bytes(const BinHeader &h) {
+    const uint64_t n = (uint64_t)h.n_points, e = (uint64_t)h.n_edges, t = (uint64_t)h.n_triples;
+    uint64_t b = 16 * n + 17 * e + 14 * t + 12 * (uint64_t)h.n_facets + 8 * (uint64_t)h.n_areas +
+                 8 * (uint64_t)h.n_pairs;
+    if (h.flags & 1u) b += 8 * e;
+    if (h.flags & 2u) b += 8 * t;
+    if (h.flags & 4u) b += 8 * t;
+    return b;
 }
 
 struct Payload {
@@ -462,7 +483,7 @@ int nr_write_network_bin(const nr_host_network *net, const char *path) {
     pl.add(net->facets);
     pl.add(net->areas);
     pl.add(net->mesh_pairs);
-    uint64_t c = 14695981039346656037ULL;
+    uint64_t c = nr::header_sum(h);
     for (auto &part : pl.parts) c = nr::fnv1a(c, part.first, part.second);
     h.checksum = c;
     FILE *f = fopen(path, "wb");
@@ -483,9 +504,19 @@ int nr_read_network_bin(const char *path, nr_host_network **out) {
     if (fread(&h, sizeof(h), 1, f) != 1 || memcmp(h.magic, nr::kBinMagic, 8) != 0 || h.version != nr::kBinVersion ||
         h.n_points <= 0 || h.n_points > (1LL << 30) || h.n_edges < 0 || h.n_edges > (1LL << 31) || h.n_triples < 0 ||
         h.n_triples > (1LL << 31) || h.n_facets < 0 || h.n_facets > (1LL << 31) || h.n_pairs < 0 ||
-        h.n_pairs > (1LL << 30) || h.n_areas < 0 || h.n_areas > h.n_facets) {
+        h.n_pairs > (1LL << 30) || h.n_areas < 0 || h.n_areas > h.n_facets || h.flags > 7u) {
         fclose(f);
         return fail(NR_ERR_PARSE, std::string("not a network binary: ") + path);
+    }
+    /* The file must hold exactly the announced payload: checked before
+     * anything is allocated, so a damaged count cannot ask for gigabytes. */
+    long here = ftell(f);
+    bool size_ok = here >= 0 && fseek(f, 0, SEEK_END) == 0;
+    const long end = size_ok ? ftell(f) : -1;
+    size_ok = size_ok && end >= here && (uint64_t)(end - here) == nr::payload_bytes(h) && fseek(f, here, SEEK_SET) == 0;
+    if (!size_ok) {
+        fclose(f);
+        return fail(NR_ERR_PARSE, std::string("truncated or corrupt network binary: ") + path);
     }
     auto *net = new nr_host_network();
     net->n_points = (int)h.n_points;
@@ -520,7 +551,7 @@ int nr_read_network_bin(const char *path, nr_host_network **out) {
     pl.add(net->areas);
     pl.add(net->mesh_pairs);
     bool ok = true;
-    uint64_t c = 14695981039346656037ULL;
+    uint64_t c = nr::header_sum(h);
     for (auto &part : pl.parts) {
         if (part.second) ok = ok && fread((void *)part.first, 1, part.second, f) == part.second;
         c = nr::fnv1a(c, part.first, part.second);

@@ -143,6 +143,36 @@ def test_binary_side_car(tmp_path):
         assert e.value.status == nr.NR_ERR_PARSE
 
 
+def test_binary_side_car_rejects_every_damaged_file(tmp_path):
+    """Flipped bits anywhere (header fields included), truncation and
+    trailing bytes all give NR_ERR_PARSE; a count damaged to billions is
+    caught by the file size before anything is allocated."""
+    h = nr.HostNetwork.lattice_mesh(12, 9, 0.7, 0.1, 2).get_triples()
+    path = str(tmp_path / "n.bin")
+    h.write_bin(path)
+    good = open(path, "rb").read()
+    rng = np.random.default_rng(3)
+    for t in range(400):
+        data = bytearray(good)
+        if t % 3 == 0:
+            k = int(rng.integers(len(data))) if t % 2 else int(rng.integers(112))  # 112-byte header
+            data[k] ^= int(rng.integers(1, 256))
+        elif t % 3 == 1:
+            data = data[: int(rng.integers(len(data)))]
+        else:
+            data += bytes(int(v) for v in rng.integers(0, 256, int(rng.integers(1, 40))))
+        open(path, "wb").write(bytes(data))
+        with pytest.raises(nr.NetRelaxError) as e:
+            nr.HostNetwork.read_bin(path)
+        assert e.value.status == nr.NR_ERR_PARSE, t
+    data = bytearray(good)
+    data[24:32] = (2 ** 31).to_bytes(8, "little")  # n_edges
+    open(path, "wb").write(bytes(data))
+    with pytest.raises(nr.NetRelaxError) as e:
+        nr.HostNetwork.read_bin(path)
+    assert e.value.status == nr.NR_ERR_PARSE
+
+
 def test_positions_writer_matches_report_displaced(tmp_path):
     """"%2.10le\t%2.10le" per node, as report_displaced writes .pos files."""
     rng = np.random.default_rng(4)
