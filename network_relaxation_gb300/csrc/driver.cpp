@@ -21,6 +21,7 @@
  * instead of falling through into -b with no argument.
  */
 #include <algorithm>
+#include <cctype>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -483,44 +484,116 @@ static int relaxation_batch(const char *batch_file, int precision, int criterion
     return worst;
 }
 
-/* Both command lines: -b batch [-x bx] [-y by] [-a] [-i], --precision,
- * --criterion. */
+/* The reference's getopt(3) loops (large_strain_relax.cu:1055,
+ * network_mesh_relax.cu:1432, sparse_relax.cpp:1177) with their option
+ * strings, scanned without getopt's global state: options may be grouped
+ * ("-ib f"), an argument attached ("-bfile") or in the next word (taken
+ * even if it starts with '-'), "--" ends the options, and other words are
+ * skipped (getopt moves them to the end, where the reference ignores
+ * them).  opt(c, arg) gets each option (arg null when a required argument
+ * is missing; c = '?' and arg = the character for an unknown one);
+ * long_opt(name, value) gets "--name=value", or "--name value" for the
+ * names in long_valued: this library's additions.  A negative return from
+ * either ends the scan. */
+template <class Opt, class LongOpt>
+static int scan_options(int argc, char **argv, const char *spec, const std::vector<std::string> &long_valued,
+                        Opt opt, LongOpt long_opt) {
+    for (int i = 1; i < argc; ++i) {
+        const char *a = argv[i];
+        if (strcmp(a, "--") == 0) break;
+        if (a[0] != '-' || a[1] == '\0') continue;
+        int rc = 0;
+        if (a[1] == '-') {
+            std::string name = a + 2, value;
+            const size_t eq = name.find('=');
+            const char *v = nullptr;
+            if (eq != std::string::npos) {
+                value = name.substr(eq + 1);
+                name.resize(eq);
+                v = value.c_str();
+            } else if (i + 1 < argc && std::find(long_valued.begin(), long_valued.end(), name) != long_valued.end()) {
+                v = argv[++i];
+            }
+            rc = long_opt(name, v);
+        } else {
+            for (int j = 1; a[j] && rc >= 0; ++j) {
+                const char c = a[j];
+                const char *p = c == ':' ? nullptr : strchr(spec, c);
+                if (!p) {
+                    fprintf(stderr, "%s: invalid option -- '%c'\n", argv[0], c); /* getopt's own message */
+                    const char unknown[2] = {c, 0};
+                    rc = opt('?', unknown);
+                } else if (p[1] == ':') {
+                    const char *arg = a[j + 1] ? a + j + 1 : (i + 1 < argc ? argv[++i] : nullptr);
+                    if (!arg) fprintf(stderr, "%s: option requires an argument -- '%c'\n", argv[0], c);
+                    rc = opt(c, arg);
+                    break;
+                } else {
+                    rc = opt(c, nullptr);
+                }
+            }
+        }
+        if (rc < 0) return rc;
+    }
+    return 0;
+}
+
+static int unknown_option(const char *c) {
+    if (isprint((unsigned char)c[0])) fprintf(stderr, "Unrecognized option: %c\n", c[0]);
+    else fprintf(stderr, "Unknown option character.\n");
+    return 0;
+}
+
+/* Both command lines: -b batch [-x bx] [-y by] [-a] [-i] (as the
+ * reference's, except that -a works: there it falls through into -b and
+ * copies a null optarg), plus --precision fp64|mixed, --criterion rms|max. */
 static int cli_main(int argc, char **argv, bool mesh) {
     const char *batch_file = nullptr;
     int precision = NR_FP64, criterion = NR_CRIT_RMS, absolute = 0;
-    for (int i = 1; i < argc; ++i) {
-        const std::string a = argv[i];
-        auto need = [&](const char *what) -> const char * {
-            if (i + 1 >= argc) {
-                fprintf(stderr, "Option \"%s\" requires %s.\n", a.c_str() + 1, what);
-                return nullptr;
+    const int rc0 = scan_options(
+        argc, argv, "ab:ix:y:", {"precision", "criterion"},
+        [&](char c, const char *arg) -> int {
+            switch (c) {
+            case 'a': absolute = 1; return 0;
+            case 'i': return 0; /* itemize: accepted and unused, as in the reference */
+            case 'b':
+                if (!arg) {
+                    fprintf(stderr, "Option \"b\" requires a file name.\n");
+                    return -1;
+                }
+                batch_file = arg;
+                return 0;
+            case 'x':
+            case 'y': {
+                int v = 0;
+                if (!arg) {
+                    fprintf(stderr, "Option \"%c\" requires a block dimension.\n", c);
+                    /* the reference's else-if chain reports a missing x twice */
+                    if (c == 'x') fprintf(stderr, "Unrecognized option: x\n");
+                }
+                else if (sscanf(arg, "%d", &v) < 1) fprintf(stderr, "Option \"%c\" requires an integer.\n", c);
+                else if (v < 1) fprintf(stderr, "Block dimensions must be positive.\n");
+                else printf("Block %c dimension: %d\n", c, v);
+                return 0;
             }
-            return argv[++i];
-        };
-        if (a == "-b") {
-            batch_file = need("a file name");
-            if (!batch_file) return -1;
-        } else if (a == "-x" || a == "-y") {
-            const char *v = need("a block dimension");
-            int bx = 0;
-            if (v && sscanf(v, "%d", &bx) == 1 && bx >= 1)
-                printf("Block %s dimension: %d\n", a == "-x" ? "x" : "y", bx);
-        } else if (a == "-a") {
-            absolute = 1;
-        } else if (a == "-i") {
-            /* itemize: accepted and unused, as in the reference */
-        } else if (a == "--precision") {
-            const char *v = need("fp64 or mixed");
-            if (!v) return -1;
-            precision = strcmp(v, "mixed") == 0 ? NR_MIXED : NR_FP64;
-        } else if (a == "--criterion") {
-            const char *v = need("rms or max");
-            if (!v) return -1;
-            criterion = strcmp(v, "max") == 0 ? NR_CRIT_MAX : NR_CRIT_RMS;
-        } else {
-            fprintf(stderr, "Unrecognized option: %s\n", a.c_str());
-        }
-    }
+            default: return unknown_option(arg);
+            }
+        },
+        [&](const std::string &name, const char *v) -> int {
+            if (name != "precision" && name != "criterion") {
+                fprintf(stderr, "Unrecognized option: --%s\n", name.c_str());
+                return 0;
+            }
+            if (!v) {
+                fprintf(stderr, "Option \"%s\" requires %s.\n", name.c_str(),
+                        name == "precision" ? "fp64 or mixed" : "rms or max");
+                return -1;
+            }
+            if (name == "precision") precision = strcmp(v, "mixed") == 0 ? NR_MIXED : NR_FP64;
+            else criterion = strcmp(v, "max") == 0 ? NR_CRIT_MAX : NR_CRIT_RMS;
+            return 0;
+        });
+    if (rc0 < 0) return -1;
     if (!batch_file) {
         fprintf(stderr, "No batch file was specified.\n");
         return -1;
@@ -700,26 +773,30 @@ int nr_spr_relaxation_batch(const char *batch_file, int strain_mode, int affine,
 int nr_sp_relax_main(int argc, char **argv) {
     const char *batch_file = nullptr;
     int strain_mode = 0, affine = 1, itemize = 0;
-    for (int i = 1; i < argc; ++i) {
-        const std::string a = argv[i];
-        if (a == "-b") {
-            if (i + 1 >= argc) {
-                fprintf(stderr, "Option \"b\" requires a file name.\n");
-                return -1;
+    const int rc0 = scan_options(
+        argc, argv, "b:ginsz", {},
+        [&](char c, const char *arg) -> int {
+            switch (c) {
+            case 'b':
+                if (!arg) {
+                    fprintf(stderr, "Option \"b\" requires a file name.\n");
+                    return -1;
+                }
+                batch_file = arg;
+                return 0;
+            case 's': strain_mode = 1; return 0;
+            case 'z': affine = 0; return 0;
+            case 'i': itemize = 1; return 0;
+            case 'g':
+            case 'n': return 0; /* accepted: the solve runs on the GPU, and CG's solution has no null-space part */
+            default: return unknown_option(arg);
             }
-            batch_file = argv[++i];
-        } else if (a == "-s") {
-            strain_mode = 1;
-        } else if (a == "-z") {
-            affine = 0;
-        } else if (a == "-i") {
-            itemize = 1;
-        } else if (a == "-g" || a == "-n") {
-            /* accepted: the solve runs on the GPU, and CG's solution has no null-space part */
-        } else {
-            fprintf(stderr, "Unrecognized option: %s\n", a.c_str());
-        }
-    }
+        },
+        [&](const std::string &name, const char *) -> int {
+            fprintf(stderr, "Unrecognized option: --%s\n", name.c_str());
+            return 0;
+        });
+    if (rc0 < 0) return -1;
     if (!batch_file) {
         fprintf(stderr, "Only batch mode (-b) is provided.\n");
         return -1;

@@ -5,6 +5,7 @@ import json
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -282,3 +283,49 @@ def test_parse_batch_file_on_fuzzed_files_matches_live_reference(built, tmp_path
         return
     assert ok_r, open(path, "rb").read()
     assert repr(got) == repr(r), open(path, "rb").read()
+
+
+_REF_MAIN = """
+import ctypes as C, sys
+sys.path.insert(0, %r)
+import oracle
+args = [a.encode() for a in sys.argv[1:]]
+rc = getattr(oracle, sys.argv[1])().%s(len(args) - 1, (C.c_char_p * (len(args) - 1))(*args[1:]))
+sys.exit(rc & 255)
+"""
+
+
+@pytest.mark.parametrize("args", ["", "-b", "-b/nonexistent", "-ib /nonexistent", "-x abc -b /nonexistent",
+                                  "-x0 -b /nonexistent", "-x 64 -b /nonexistent", "-z -b /nonexistent",
+                                  "-- -b /nonexistent", "extra -b /nonexistent", "-y -b /nonexistent",
+                                  "-b /nonexistent -x", "-i -x 3 -y 2 -b /nonexistent"])
+@pytest.mark.parametrize("prog", ["lsrelax", "nmrelax"])
+def test_lsrelax_options_match_the_reference_main(built, args, prog):
+    """Option scanning as the reference's getopt loops (large_strain_relax.cu:
+    1055, network_mesh_relax.cu:1432): grouped flags, attached arguments,
+    '--', operands, and the same messages.  The one difference is the exit
+    status after a failed batch: 1 here, 0 in the reference."""
+    if oracle.build_ref() is None or oracle.ref_lib() is None or oracle.ref_mesh_lib() is None:
+        pytest.skip("reference checkout not available")
+    exe = os.path.join(ROOT, "network_relaxation_gb300", prog)
+    entry, lib = ("ref_lsrelax_main", "ref_lib") if prog == "lsrelax" else ("ref_nmrelax_main", "ref_mesh_lib")
+    mine = subprocess.run([prog] + args.split(), executable=exe, capture_output=True, text=True, timeout=60)
+    ref = subprocess.run([sys.executable, "-c", _REF_MAIN % (ROOT, entry), lib, prog] + args.split(),
+                         capture_output=True, text=True, timeout=60)
+    assert (mine.stdout, mine.stderr) == (ref.stdout, ref.stderr)
+    assert mine.returncode == ref.returncode or (ref.returncode == 0 and mine.returncode == 1)
+
+
+@pytest.mark.parametrize("args", ["-b", "-b/nonexistent", "-sz -b /nonexistent", "-q -b /nonexistent",
+                                  "-gn -ib /nonexistent", "op -s -b /nonexistent"])
+def test_sp_relax_options_match_the_reference_main(built, args):
+    """sparse_relax.cpp's getopt loop (:1177), batch mode only (without -b
+    the reference asks questions on standard input)."""
+    if oracle.build_ref() is None or oracle.ref_spr_lib() is None:
+        pytest.skip("reference checkout not available")
+    exe = os.path.join(ROOT, "network_relaxation_gb300", "sp_relax")
+    mine = subprocess.run(["sp_relax"] + args.split(), executable=exe, capture_output=True, text=True, timeout=60)
+    ref = subprocess.run([sys.executable, "-c", _REF_MAIN % (ROOT, "ref_spr_main"), "ref_spr_lib", "sp_relax"]
+                         + args.split(), capture_output=True, text=True, timeout=60, stdin=subprocess.DEVNULL)
+    assert (mine.stdout, mine.stderr) == (ref.stdout, ref.stderr)
+    assert mine.returncode == ref.returncode or (ref.returncode == 0 and mine.returncode == 1)
