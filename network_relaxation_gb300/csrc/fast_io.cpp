@@ -1,7 +1,8 @@
 /*
- * Network files at scale: a parallel .dat reader with the reference's exact
- * line semantics (read_network, large_strain_relax.cu:42-114), a parallel
- * writer, and a binary side-car that also keeps the triples.
+ * Network files at scale: parallel .dat and .nmc readers with the
+ * reference's exact line semantics (read_network, large_strain_relax.cu:
+ * 42-114; read_network_mesh, network_mesh_relax.cu:72-230), parallel
+ * writers, and a binary side-car that also keeps the triples.
  *
  * Reader.  The reference reads line by line with std::getline / eof() and
  * sscanf.  Here the file is read at once and cut into the same lines (a
@@ -185,6 +186,39 @@ EdgeLine parse_edge(const char *b, const char *e) {
     return r;
 }
 
+struct FacetLine {
+    int i1, i2, i3;
+    int n;
+};
+
+/* sscanf(line, "%d %d %d\n", ...) */
+FacetLine parse_facet(const char *b, const char *e) {
+    FacetLine r{0, 0, 0, 0};
+    const char *p = b;
+    skip_space(p, e);
+    if (p == e) {
+        r.n = -1;
+        return r;
+    }
+    long v[3];
+    int k = 0;
+    while (k < 3 && strict_int(p, e, v[k])) {
+        ++k;
+        skip_space(p, e);
+        if (p == e) break;
+    }
+    if (k == 3 || p == e) {
+        r.n = k;
+        r.i1 = k > 0 ? (int)v[0] : 0;
+        r.i2 = k > 1 ? (int)v[1] : 0;
+        r.i3 = k > 2 ? (int)v[2] : 0;
+        return r;
+    }
+    const std::string line(b, e);
+    r.n = sscanf(line.c_str(), "%d %d %d\n", &r.i1, &r.i2, &r.i3);
+    return r;
+}
+
 /* The file cut into std::getline's lines; the last line is the one whose
  * reading sets eof.  end points at the first NUL of a line (sscanf's view). */
 struct Lines {
@@ -353,6 +387,185 @@ int nr_write_network(const nr_host_network *net, const char *path) {
 }
 
 
+
+/* read_network_mesh, network_mesh_relax.cu:72-230: header "N E F offset",
+ * then points, edges "i j wrap", facets "i j k" and areas, with the
+ * reference's getline / eof() / sscanf semantics (see the file comment).
+ * Each line is parsed in parallel as the type its position gives it in a
+ * well-formed file; the sequential state machine parses any other line it
+ * meets (a junk line shifts the rest) on the spot.  On NR_ERR_PARSE the
+ * partially read network is still returned. */
+int nr_read_network_mesh(const char *path, nr_host_network **out) {
+    if (!path || !out) return fail(NR_ERR_INVALID, "nr_read_network_mesh: null argument");
+    *out = nullptr;
+    nr::Lines L;
+    if (!L.load(path)) return fail(NR_ERR_IO, std::string("cannot open ") + path);
+    auto *net = new nr_host_network();
+    *out = net;
+    const size_t nl = L.count();
+    auto eof_after = [&](size_t line) { return line + 1 >= nl; };
+    int num_points = 0, num_edges = 0, num_facets = 0;
+    double offset = 0;
+    net->minx = FLT_MAX;
+    net->miny = FLT_MAX;
+    net->maxx = FLT_MIN;
+    net->maxy = FLT_MIN;
+    {
+        const std::string header(L.begin[0], L.end[0]);
+        const int num_read = sscanf(header.c_str(), "%d %d %d %lf", &num_points, &num_edges, &num_facets, &offset);
+        if (num_read < 4 || offset < 0 || num_points <= 0 || num_edges < 0 || num_facets < 0)
+            return fail(NR_ERR_PARSE, "Reading failed. The provided file has an invalid header.");
+    }
+    net->offset = offset;
+    /* the line ranges of a well-formed file, parsed in parallel */
+    const size_t lo_p = 1, lo_e = lo_p + (size_t)num_points, lo_f = lo_e + (size_t)num_edges,
+                 lo_a = lo_f + (size_t)num_facets, hi = lo_a + (size_t)num_facets;
+    auto clip = [&](size_t v) { return std::min(v, nl); };
+    std::vector<nr::PointLine> pl(clip(lo_e) - clip(lo_p)), al(clip(hi) - clip(lo_a));
+    std::vector<nr::EdgeLine> el(clip(lo_f) - clip(lo_e));
+    std::vector<nr::FacetLine> fl(clip(lo_a) - clip(lo_f));
+    const int threads = nr::io_threads();
+    nr::parallel_ranges((long)(clip(hi) - clip(lo_p)), threads, [&](long b, long e) {
+        for (long k = b; k < e; ++k) {
+            const size_t li = lo_p + (size_t)k;
+            if (li < lo_e) pl[li - lo_p] = nr::parse_point(L.begin[li], L.end[li]);
+            else if (li < lo_f) el[li - lo_e] = nr::parse_edge(L.begin[li], L.end[li]);
+            else if (li < lo_a) fl[li - lo_f] = nr::parse_facet(L.begin[li], L.end[li]);
+            else al[li - lo_a] = nr::parse_point(L.begin[li], L.end[li]);
+        }
+    });
+    auto point_at = [&](size_t li) {
+        return li >= lo_p && li < lo_p + pl.size() ? pl[li - lo_p] : nr::parse_point(L.begin[li], L.end[li]);
+    };
+    auto area_at = [&](size_t li) {
+        return li >= lo_a && li < lo_a + al.size() ? al[li - lo_a] : nr::parse_point(L.begin[li], L.end[li]);
+    };
+    auto edge_at = [&](size_t li) {
+        return li >= lo_e && li < lo_e + el.size() ? el[li - lo_e] : nr::parse_edge(L.begin[li], L.end[li]);
+    };
+    auto facet_at = [&](size_t li) {
+        return li >= lo_f && li < lo_f + fl.size() ? fl[li - lo_f] : nr::parse_facet(L.begin[li], L.end[li]);
+    };
+    size_t cur = 1;
+    bool eof = eof_after(0);
+    net->points.reserve(2 * (size_t)std::min<long>(num_points, (long)nl));
+    while (!eof && net->points.size() < 2 * (size_t)num_points) {
+        const nr::PointLine r = point_at(cur);
+        eof = eof_after(cur++);
+        if (r.n == 2) {
+            net->points.push_back(r.x);
+            net->points.push_back(r.y);
+            if (r.x < net->minx) net->minx = r.x;
+            if (r.y < net->miny) net->miny = r.y;
+            if (r.x > net->maxx) net->maxx = r.x;
+            if (r.y > net->maxy) net->maxy = r.y;
+        }
+    }
+    net->n_points = (int)(net->points.size() / 2);
+    if (eof) return fail(NR_ERR_PARSE, "Reading failed. Too few points were read.");
+    bool bad_index = false;
+    while (!eof && net->edge_wrap.size() < (size_t)num_edges) {
+        const nr::EdgeLine r = edge_at(cur);
+        eof = eof_after(cur++);
+        if (r.n == 3) {
+            if (std::min(r.i1, r.i2) > -1 && std::max(r.i1, r.i2) < num_points) {
+                net->edge_ij.push_back(r.i1);
+                net->edge_ij.push_back(r.i2);
+                net->edge_wrap.push_back(r.mult);
+            } else {
+                bad_index = true;
+                break;
+            }
+        }
+    }
+    const size_t ne = net->edge_wrap.size();
+    net->edge_l0.resize(ne);
+    const double *p = net->points.data();
+    nr::parallel_ranges((long)ne, threads, [&](long b, long e) {
+        for (long k = b; k < e; ++k) {
+            const int i1 = net->edge_ij[2 * k], i2 = net->edge_ij[2 * k + 1];
+            const double dx = p[2 * i2] + offset * net->edge_wrap[k] - p[2 * i1];
+            const double dy = p[2 * i2 + 1] - p[2 * i1 + 1];
+            net->edge_l0[k] = std::sqrt(dx * dx + dy * dy);
+        }
+    });
+    if (bad_index) return fail(NR_ERR_PARSE, "Reading failed due to an out-of-bounds point index.");
+    if (ne < (size_t)num_edges) return fail(NR_ERR_PARSE, "Too few edges were read.");
+    if (eof && num_facets > 0) return fail(NR_ERR_PARSE, "The file ended before facets could be read.");
+    auto in_bounds = [&](int v) { return v >= 0 && v <= num_points - 1; };
+    while (!eof && net->facets.size() < 3 * (size_t)num_facets) {
+        const nr::FacetLine r = facet_at(cur);
+        eof = eof_after(cur++);
+        if (r.n == 3) {
+            if (!(in_bounds(r.i1) && in_bounds(r.i2) && in_bounds(r.i3)))
+                return fail(NR_ERR_PARSE, "Reading failed due to an out-of-bounds point index.");
+            net->facets.push_back(r.i1);
+            net->facets.push_back(r.i2);
+            net->facets.push_back(r.i3);
+        }
+    }
+    if (net->facets.size() < 3 * (size_t)num_facets) return fail(NR_ERR_PARSE, "Too few facets were read.");
+    if (eof && num_facets > 0) return fail(NR_ERR_PARSE, "The file ended before facets could be read.");
+    while (!eof && net->areas.size() < (size_t)num_facets) {
+        const nr::PointLine r = area_at(cur); /* sscanf("%lf") == 1: the first value parsed */
+        eof = eof_after(cur++);
+        if (r.n >= 1) {
+            if (r.x > 0) net->areas.push_back(r.x);
+            else return fail(NR_ERR_PARSE, "An illegal area was specified.");
+        }
+    }
+    if (net->areas.size() < (size_t)num_facets) return fail(NR_ERR_PARSE, "Too few areas were specified.");
+    nr::find_mesh_pairs(net->points, offset, net->minx, net->mesh_pairs);
+    return NR_OK;
+}
+
+/* Writes the format nr_read_network_mesh reads (%.17g, round-trips
+ * exactly), formatted in parallel like nr_write_network. */
+int nr_write_network_mesh(const nr_host_network *net, const char *path) {
+    if (!net || !path) return fail(NR_ERR_INVALID, "nr_write_network_mesh: null argument");
+    FILE *f = fopen(path, "w");
+    if (!f) return fail(NR_ERR_IO, std::string("cannot write ") + path);
+    fprintf(f, "%d %d %d %.17g\n", net->n_points, net->n_edges(), net->n_facets(), net->offset);
+    const int threads = nr::io_threads();
+    const int chunks = std::max(1, threads * 4);
+    const long counts[4] = {net->n_points, net->n_edges(), net->n_facets(), net->n_facets()};
+    for (int section = 0; section < 4; ++section) {
+        const long n = counts[section];
+        std::vector<std::string> outs(chunks);
+        const long per = (n + chunks - 1) / chunks;
+        nr::parallel_ranges(chunks, threads, [&](long cb, long ce) {
+            char line[128];
+            for (long c = cb; c < ce; ++c) {
+                for (long i = c * per; i < std::min(n, (c + 1) * per); ++i) {
+                    char *q = line, *end = line + sizeof(line);
+                    if (section == 0) {
+                        q = std::to_chars(q, end, net->points[2 * i], std::chars_format::general, 17).ptr;
+                        *q++ = ' ';
+                        q = std::to_chars(q, end, net->points[2 * i + 1], std::chars_format::general, 17).ptr;
+                    } else if (section == 1) {
+                        q = std::to_chars(q, end, net->edge_ij[2 * i]).ptr;
+                        *q++ = ' ';
+                        q = std::to_chars(q, end, net->edge_ij[2 * i + 1]).ptr;
+                        *q++ = ' ';
+                        q = std::to_chars(q, end, (int)net->edge_wrap[i]).ptr;
+                    } else if (section == 2) {
+                        for (int v = 0; v < 3; ++v) {
+                            if (v) *q++ = ' ';
+                            q = std::to_chars(q, end, net->facets[3 * i + v]).ptr;
+                        }
+                    } else {
+                        q = std::to_chars(q, end, net->areas[i], std::chars_format::general, 17).ptr;
+                    }
+                    *q++ = '\n';
+                    outs[c].append(line, (size_t)(q - line));
+                }
+            }
+        });
+        for (const std::string &s : outs) fwrite(s.data(), 1, s.size(), f);
+    }
+    const bool ok = fclose(f) == 0;
+    return ok ? NR_OK : fail(NR_ERR_IO, std::string("cannot write ") + path);
+}
 
 }  // extern "C"
 
