@@ -16,6 +16,7 @@ ORACLE_SO = os.path.join(HERE, "libnr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "liblsr_ref.so")
 REF_MESH_SO = os.path.join(HERE, "_ref", "libnmr_ref.so")
 REF_SPR_SO = os.path.join(HERE, "_ref", "libspr_ref.so")
+REF_NA_SO = os.path.join(HERE, "_ref", "libna_ref.so")
 SOURCES = ["nr_oracle.c", "nr_oracle_mesh.c", "nr_oracle_spr.c", "nr_oracle.h", "nr_oracle_internal.h"]
 lp = C.POINTER(C.c_long)
 
@@ -333,6 +334,25 @@ def nonaffinity(pos0, disp, miny, axial_strain, shear_strain):
     p0 = np.ascontiguousarray(pos0, np.float64)
     u = np.ascontiguousarray(disp, np.float64)
     return lib().or_nonaffinity(len(p0), _d(p0), _d(u), float(miny), float(axial_strain), float(shear_strain))
+
+
+_ref_na = None
+
+
+def ref_nonaffinity(pos0, disp, minx, miny, axial_strain, shear_strain):
+    """The reference's own calc_na_val (na_calc.cpp:308-327, a sequential
+    sum), built for the host by build_ref.sh; None where it is not built."""
+    global _ref_na
+    if _ref_na is None:
+        if not os.path.exists(REF_NA_SO):
+            return None
+        _ref_na = C.CDLL(REF_NA_SO)
+        _ref_na.ref_calc_na_val.restype = C.c_double
+        _ref_na.ref_calc_na_val.argtypes = [C.c_int, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double]
+    p0 = np.ascontiguousarray(pos0, np.float64)
+    u = np.ascontiguousarray(disp, np.float64)
+    return _ref_na.ref_calc_na_val(len(p0), _d(p0), _d(u), float(minx), float(miny), float(axial_strain),
+                                   float(shear_strain))
 
 
 def canon_sum(terms):

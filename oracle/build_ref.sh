@@ -5,7 +5,9 @@
 # runtime replaced by the stand-ins in oracle/refshim/include); and
 # oracle/_ref/libspr_ref.so: sparse_relax.cpp, unchanged, against the dense
 # CHOLMOD / SPQR stand-ins of oracle/refshim/spr_include (SuiteSparse and
-# MKL are not in this image).
+# MKL are not in this image); the analysis programs strain_calc and
+# axial_contribution as executables; and oracle/_ref/libna_ref.so:
+# na_calc.cpp against the std stand-ins of oracle/refshim/boost_include.
 #
 # The source is read where it lies and piped to the compiler with two textual
 # rewrites.  The first is the kernel-launch syntax, `k<<<grid, block>>>(args)`
@@ -59,8 +61,7 @@ if [ -f "$MESH_SRC" ]; then
     echo "build_ref: built $OUT/libnmr_ref.so"
 fi
 # The analysis programs strain_calc.cpp and axial_contribution.cpp need only
-# the standard library: built unchanged as executables.  (na_calc.cpp needs
-# Boost, which is absent: not built.)
+# the standard library: built unchanged as executables.
 for prog in strain_calc axial_contribution; do
     if "$CXX" -std=c++17 -O2 -w "$REF/src/$prog.cpp" -o "$OUT/$prog"; then
         echo "build_ref: built $OUT/$prog"
@@ -68,3 +69,17 @@ for prog in strain_calc axial_contribution; do
         echo "build_ref: $prog not built"
     fi
 done
+# na_calc.cpp includes Boost.Filesystem and Boost.Regex, which are absent:
+# it is compiled unchanged against the std::filesystem / std::regex
+# stand-ins of oracle/refshim/boost_include, with main renamed, into
+# oracle/_ref/libna_ref.so beside a C entry point to its calc_na_val.
+if [ -f "$REF/src/na_calc.cpp" ]; then
+    if "$CXX" -x c++ -std=c++17 -O2 -fPIC -w -I "$HERE/refshim/boost_include" -Dmain=na_reference_main \
+           -c "$REF/src/na_calc.cpp" -o "$OUT/na_ref.o" &&
+       "$CXX" -std=c++17 -O2 -fPIC -c "$HERE/refshim/ref_na_api.cpp" -o "$OUT/ref_na_api.o" &&
+       "$CXX" -shared -o "$OUT/libna_ref.so" "$OUT/na_ref.o" "$OUT/ref_na_api.o"; then
+        echo "build_ref: built $OUT/libna_ref.so"
+    else
+        echo "build_ref: na_calc not built"
+    fi
+fi

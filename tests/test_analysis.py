@@ -1,7 +1,9 @@
 """Post-relaxation analyses: the oracle restatement pinned against the
 reference's own strain_calc and axial_contribution (outputs committed in
-tests/golden/analysis/, made by make_analysis_golden.py) and against
-known answers for calc_na_val (na_calc.cpp needs Boost, absent here)."""
+tests/golden/analysis/, made by make_analysis_golden.py), against known
+answers for calc_na_val, and against the reference's own calc_na_val
+(na_calc.cpp built for the host against std stand-ins for its Boost
+headers) where the checkout exists."""
 import json
 import os
 
@@ -55,3 +57,24 @@ def test_nonaffinity_known_answers(built):
     assert oracle.nonaffinity(P, shifted, y0, -0.02, 0.03) == 0.5 * 0.5 + 0.25 * 0.25
     seq = np.mean(((disp[:, 0] - (P[:, 1] - y0) * 0.01) ** 2 + (disp[:, 1] - (P[:, 1] - y0) * 0.0) ** 2))
     assert abs(oracle.nonaffinity(P, disp, y0, 0.0, 0.01) - seq) <= 1e-14 * seq
+
+
+def test_nonaffinity_matches_reference_calc_na_val(built):
+    """The reference's sequential sum, restated in Python, equals its
+    calc_na_val bit for bit; the oracle's canonical sum is within 1e-14."""
+    import pytest
+
+    if oracle.build_ref() is None or oracle.ref_nonaffinity(np.zeros((1, 2)), np.zeros((1, 2)), 0, 0, 0, 0) is None:
+        pytest.skip("reference checkout not available")
+    a, disp = small()
+    P = a["points"]
+    rng = np.random.default_rng(5)
+    for axial, shear in ((0.0, 0.01), (-0.02, 0.03), (0.05, 0.0)):
+        u = disp + rng.normal(0, 1e-3, disp.shape)
+        ref = oracle.ref_nonaffinity(P, u, P[:, 0].min(), a["miny"], axial, shear)
+        s = 0.0
+        for (x, y), (ux, uy) in zip(P.tolist(), u.tolist()):
+            ex, ey = (y - a["miny"]) * shear, (y - a["miny"]) * axial
+            s += (ux - ex) * (ux - ex) + (uy - ey) * (uy - ey)
+        assert s / len(P) == ref
+        assert abs(oracle.nonaffinity(P, u, a["miny"], axial, shear) - ref) <= 1e-14 * ref
