@@ -846,9 +846,10 @@ def analyses_arm(args):
 
 def io_arm(args):
     """--workload IO (host only): a 1024 x 1024 lattice (p = 0.65) written
-    and read back as .dat with get_triples, and as the binary side-car;
-    the oracle's getline / sscanf restatement of read_network + get_triples
-    timed beside it.  value = nodes set up per second from .dat."""
+    and read back as .dat with get_triples, and as the binary side-car; the
+    M1 composite written and read back as .nmc; the oracle's getline /
+    sscanf restatement of read_network + get_triples timed beside it.
+    value = nodes set up per second from .dat."""
     import network_relaxation_gb300 as nr
     import oracle
 
@@ -872,6 +873,10 @@ def io_arm(args):
     clock("get_triples", lambda: h2.get_triples())
     clock("write_bin", lambda: h2.write_bin(binp))
     clock("read_bin", lambda: nr.HostNetwork.read_bin(binp))
+    m = nr.HostNetwork.lattice_mesh(1024, 768, 0.65, 0.0, 8)  # the M1 composite (network_mesh_relax.cu's .nmc)
+    nmc = os.path.join(d, "nr_io_bench.nmc")
+    clock("write_nmc", lambda: m.write_mesh(nmc))
+    clock("read_nmc", lambda: nr.HostNetwork.read_mesh(nmc))
     t0 = time.perf_counter()
     oracle.read_network(dat)
     t_or = time.perf_counter() - t0
