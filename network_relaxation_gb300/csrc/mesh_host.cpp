@@ -11,6 +11,7 @@
 #include <cstdint>
 #include <cstring>
 #include <map>
+#include <memory_resource>
 #include <string>
 #include <vector>
 
@@ -40,7 +41,11 @@ struct MeshPointLess {
  * with x < minx + 1e-10, in map order, with the entry found at
  * (x + offset, y). */
 void find_mesh_pairs(const std::vector<double> &points, double offset, double minx, std::vector<int> &pairs) {
-    std::map<MeshPoint, int, MeshPointLess> pmap;
+    /* The same red-black tree as std::map (hence the same answers on
+     * near-duplicates, where PointComp is not a strict order), with its
+     * nodes carved from one buffer instead of one allocation each. */
+    std::pmr::monotonic_buffer_resource arena(64 * (points.size() / 2 + 16));
+    std::pmr::map<MeshPoint, int, MeshPointLess> pmap(&arena);
     for (size_t i = 0; i + 1 < points.size(); i += 2) pmap.insert({MeshPoint{points[i], points[i + 1]}, (int)(i / 2)});
     pairs.clear();
     for (auto it = pmap.begin(); it != pmap.end() && it->first.x < minx + kPointTol; ++it) {
