@@ -269,7 +269,9 @@ static double or_block256(const double *lanes) {
     return or_tree8(w);
 }
 
-/* Canonical reduction: terms are grouped in tiles of 256 consecutive items
+/* The fixed summation order that replaces cublasDasum (large_strain_relax.cu:743, :751) and the
+ * cuBLAS dot / nrm2 reductions of run_fire_md, whose order is unspecified.
+ * Canonical reduction: terms are grouped in tiles of 256 consecutive items
  * (missing items are 0); each tile is reduced by or_block256; tile sums are
  * accumulated per lane (lane k sums tiles k, k+256, ... in order, starting
  * from tile k) and the 256 lane sums are reduced by or_block256. */
@@ -413,6 +415,9 @@ static or_sums or_fire_sums(int n, const double *v, const double *F, double *scr
     return s;
 }
 
+/* run_fire_md, large_strain_relax.cu:596-762: FIRE from v = 0 and dt = dt_max, velocity-Verlet drift and
+ * kicks (:655-677), P = F.v and mixing (:686-691), dt / alpha adaption (:694-713), the stop test (:716,
+ * RMS or max criterion), energies after the loop (:723-751); reductions by or_canon_sum. */
 int or_fire(const or_model *m, double *x, double *v, double *F, const or_fire_params *p, or_report *rep) {
     const int n = m->n_points;
     const long ndof = 2L * n;
@@ -570,6 +575,8 @@ static void *or_batch_worker(void *arg) {
     return NULL;
 }
 
+/* or_fire over n independent networks on n_threads host threads (the CPU baseline of batches; the
+ * reference relaxes its file list one network at a time, large_strain_relax.cu:1040-1042). */
 void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_params *params, or_report *reps,
                    int n_threads) {
     or_batch_job job = {n, models, pos, params, reps, 0, PTHREAD_MUTEX_INITIALIZER};
@@ -582,6 +589,7 @@ void or_fire_batch(int n, const or_model *models, double **pos, const or_fire_pa
 
 /* ----- post-relaxation analyses (strain_calc, axial_contribution, na_calc) ----- */
 
+/* strain_calc.cpp:96-120: the engineering strain of every bond under a displacement field. */
 void or_bond_strains(int n_edges, const int *edge_ij, const signed char *wrap, double width, const double *pos0,
                      const double *disp, double *strains) {
     for (int b = 0; b < n_edges; ++b) {
@@ -597,6 +605,8 @@ void or_bond_strains(int n_edges, const int *edge_ij, const signed char *wrap, d
     }
 }
 
+/* axial_contribution.cpp:64-70, 176-190: the linearised stretch energy of a displacement field
+ * (summed by or_canon_sum). */
 double or_linear_axial_energy(int n_edges, const int *edge_ij, const signed char *wrap, double width, double k,
                               const double *pos0, const double *disp) {
     double *terms = (double *)malloc(sizeof(double) * (size_t)(n_edges > 0 ? n_edges : 1));
@@ -617,6 +627,8 @@ double or_linear_axial_energy(int n_edges, const int *edge_ij, const signed char
     return e * k;
 }
 
+/* calc_na_val, na_calc.cpp:308-327: the mean squared deviation from the affine field (summed by
+ * or_canon_sum; the reference sums in node order). */
 double or_nonaffinity(int n_points, const double *pos0, const double *disp, double miny, double axial_strain,
                       double shear_strain) {
     double *terms = (double *)malloc(sizeof(double) * (size_t)(n_points > 0 ? n_points : 1));
