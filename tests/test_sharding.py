@@ -1,5 +1,7 @@
-"""Multi-process (world_size 2, gloo, CPU) test of the batch sharding and
-the timing reduction used by bench.py under torchrun."""
+"""Multi-process (world_size 2 and 4, gloo, CPU) tests of the batch
+sharding and the timing reduction used by bench.py under torchrun, and of a
+rank leaving between steps (the others learn of it at their next
+reduction, as an error)."""
 import os
 import socket
 
@@ -35,21 +37,55 @@ def _worker(rank, world, port, out):
     dist.destroy_process_group()
 
 
-def test_two_rank_sharding_and_reduction():
+@pytest.mark.parametrize("world", [2, 4])
+def test_rank_sharding_and_reduction(world):
     port = _free_port()
     mgr = mp.Manager()
     out = mgr.dict()
-    mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
-    r0, r1 = out[0], out[1]
-    assert r0[:3] == (0, 2, 0) and r1[:3] == (1, 2, 1)
+    mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
+    res = [out[r] for r in range(world)]
+    assert [r[:3] for r in res] == [(r, world, r) for r in range(world)]
     # disjoint seeds, rank 0 is the single-GPU workload
-    assert not set(r0[3]) & set(r1[3])
+    seeds = [set(r[3]) for r in res]
+    assert sum(len(x) for x in seeds) == len(set().union(*seeds)) == 8 * world
     from network_relaxation_gb300 import workloads
 
-    assert r0[3] == [q["seed"] for q in workloads.c4_params(n=8)]
+    assert res[0][3] == [q["seed"] for q in workloads.c4_params(n=8)]
     # max over ranks of the step time, sum of the networks
-    assert r0[4] == r1[4] == 20.0
-    assert r0[5] == r1[5] == 16
+    assert all(r[4] == 10.0 * world and r[5] == 8 * world for r in res)
+
+
+def _worker_leaves(rank, world, port, out):
+    """Rank 1 leaves between steps (nothing in flight); rank 0's next
+    reduction must end with an error, not wait forever."""
+    import datetime
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from network_relaxation_gb300 import sharding
+
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=5))
+    sharding.reduce_timing(dist, 1.0, 1)  # one step together
+    if rank == 1:
+        out[1] = "left"
+        os._exit(0)
+    try:
+        sharding.reduce_timing(dist, 2.0, 1)
+        out[0] = "no error"
+    except Exception as e:  # gloo reports the lost peer or the timeout
+        out[0] = "error " + type(e).__name__
+
+
+def test_rank_that_leaves_is_detected_by_the_next_reduction():
+    port = _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_worker_leaves, args=(2, port, out), nprocs=2, join=True)
+    assert out[1] == "left"
+    assert out[0].startswith("error"), out[0]
 
 
 def test_single_process_reduction_is_identity():
