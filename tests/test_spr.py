@@ -106,3 +106,28 @@ def _net_from(path):
     ok, a = oracle.read_network(path)
     assert ok
     return a
+
+
+@pytest.mark.parametrize("seed", [3, 4, 5])
+def test_fire_energy_tends_to_the_linear_response(seed):
+    """The two programs agree in the small-strain limit: the energy of the
+    oracle's FIRE relaxation (large_strain_relax.cu) over the linear-response
+    energy (sparse_relax.cpp) tends to 1, the difference shrinking in
+    proportion to the strain (shear, then compression; diluted lattices with
+    straight rest triples, so the two bending models coincide)."""
+    h = nr.HostNetwork.lattice(12, 12, 0.8, 0.0, seed).get_triples()
+    a = h.arrays()
+    H = a["maxy"] - a["miny"]
+    for shear in (True, False):
+        dev = []
+        for s, fcut in ((1e-4, 1e-13), (1e-5, 1e-14)):
+            c_rng, s_rng = ([0.0, 0.0, 1.0], [s, s, 1.0]) if shear else ([s, s, 1.0], [0.0, 0.0, 1.0])
+            recs, _ = oracle.spr_protocol(a, 1.0, 1e-2, 0.0, c_rng, s_rng, strain_mode=False)
+            e_lin = recs[0][2]
+            x0 = oracle.affine_displace(a["points"], a["miny"], H, s if shear else 0.0, 0.0 if shear else -s)
+            _, _, _, rep = oracle.Model(a, 1.0, 1e-2).fire(x0, oracle.params(fcut=fcut, criterion="max",
+                                                                            max_steps=400_000))
+            assert rep.max_force < fcut
+            dev.append((rep.e_stretch + rep.e_bend) / e_lin - 1)
+        assert abs(dev[1]) < 2e-6, dev
+        assert abs(dev[1]) < 0.2 * abs(dev[0]) + 1e-9, dev  # O(strain)
