@@ -113,8 +113,10 @@ def test_fire_energy_tends_to_the_linear_response(seed):
     """The two programs agree in the small-strain limit: the energy of the
     oracle's FIRE relaxation (large_strain_relax.cu) over the linear-response
     energy (sparse_relax.cpp) tends to 1, the difference shrinking in
-    proportion to the strain (shear, then compression; diluted lattices with
-    straight rest triples, so the two bending models coincide)."""
+    proportion to the strain (shear, then compression).  The lattices have
+    unit rest lengths and straight rest triples: sparse_relax.cpp's spring
+    constant is ks/l0 (SPR:292-303) where large_strain_relax.cu's is ks, so
+    the two describe the same network only when l0 = 1."""
     h = nr.HostNetwork.lattice(12, 12, 0.8, 0.0, seed).get_triples()
     a = h.arrays()
     H = a["maxy"] - a["miny"]
