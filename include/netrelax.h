@@ -486,10 +486,16 @@ int nr_nonaffinity(int n_points, const double *pos0, const double *disp, double 
  * in nr_last_error.  A node index outside [0, n_points) makes the energy
  * NaN.  The first call on each device looks up the scratch array's device
  * address (this can load the library's device code): make that first call
- * before any stream capture.  Every call uses the same scratch array, so
- * calls that overlap on the GPU (other streams or host threads) race: the
- * caller must order them.  Nothing in the array needs clearing between
- * calls.  Asynchronous on `stream`. */
+ * before any stream capture.  The address is looked up again on every call,
+ * so the entry point stays valid after cudaDeviceReset.  Every call uses the
+ * same scratch array, so calls that overlap on the GPU (other streams or
+ * host threads) race: issue all calls on one stream, or order calls on
+ * different streams with events.  `stream` NULL (0) is the legacy default
+ * stream, which orders the call after, and before, the work of every
+ * blocking stream of the device; pass a framework's own stream (or
+ * cudaStreamPerThread) to keep the call in that stream's order instead.
+ * Nothing in the array needs clearing between calls.  Asynchronous on
+ * `stream`. */
 #define NR_NOALLOC_MAX_ITEMS 4194304
 int nr_energies_noalloc(int n_points, int npairs, int ntriples, double width, double ks, double kb,
                         const double *d_pos, const int *d_pair_list, const double *d_lengths,

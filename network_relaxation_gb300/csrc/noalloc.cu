@@ -15,9 +15,10 @@
  *
  * The array lives in the library's device image: every GPU that loads the
  * library holds its 256 KiB until the process exits.  Every call shares
- * it, so calls that overlap on the GPU race.  Each call writes every
- * partial its final pass reads before reading it, so nothing has to start
- * at zero and nothing is cleared.
+ * it, so calls that overlap on the GPU race: issue every call on one
+ * stream, or order calls on different streams with events.  Each call writes
+ * every partial its final pass reads before reading it, so nothing has to
+ * start at zero and nothing is cleared.
  */
 #include <cuda_runtime.h>
 
@@ -104,11 +105,16 @@ __global__ void __launch_bounds__(kTile) k_noalloc_energy_final(RefNet v, const 
     }
 }
 
-/* Device address of g_energy_scratch for the current device, looked up
- * once per device (the symbol's host-side name is not a device address). */
+/* Device address of g_energy_scratch on the current device.  The symbol's
+ * host-side name is not a device address, so it is looked up with
+ * cudaGetSymbolAddress on every call: the lookup is cheap once the module is
+ * loaded, and a fresh lookup stays right after cudaDeviceReset or after the
+ * primary context was released and retained again, when the module may load
+ * at another address.  The first lookup on a device can load the library's
+ * device code, which is why the first call must come before any stream
+ * capture.  Only the SM count is cached. */
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
-double *g_scratch_ptr[kMaxDevices];
 int g_sm_count[kMaxDevices];
 
 int scratch_for_current_device(double **ptr, int *sms) {
@@ -116,21 +122,19 @@ int scratch_for_current_device(double **ptr, int *sms) {
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(NR_ERR_CUDA, std::string("nr_energies_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(NR_ERR_CAPACITY, "nr_energies_noalloc: device ordinal beyond 63");
+    double *p = nullptr;
+    e = cudaGetSymbolAddress((void **)&p, g_energy_scratch);
+    if (e != cudaSuccess)
+        return fail(NR_ERR_CUDA, std::string("nr_energies_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        double *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_energy_scratch);
-        if (e != cudaSuccess)
-            return fail(NR_ERR_CUDA,
-                        std::string("nr_energies_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    if (g_sm_count[dev] <= 0) {
         int n = 0;
         e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (e != cudaSuccess)
             return fail(NR_ERR_CUDA, std::string("nr_energies_noalloc: cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
         g_sm_count[dev] = n > 0 ? n : 1;
-        g_scratch_ptr[dev] = p;
     }
-    *ptr = g_scratch_ptr[dev];
+    *ptr = p;
     *sms = g_sm_count[dev];
     return NR_OK;
 }

@@ -188,6 +188,74 @@ def triples_of(points, edge_ij, edge_wrap, offset):
     return hjk, tw
 
 
+def _splitmix64(seed, count):
+    """The first `count` outputs of SplitMix64 (Steele, Lea & Flood, OOPSLA
+    2014) from `seed`, as uint64: output k mixes seed + (k + 1) * golden."""
+    with np.errstate(over="ignore"):
+        z = np.uint64(seed) + (np.arange(1, count + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def gen_lattice(nx, ny, p, seed, jitter=0.0):
+    """Restatement of the library's diluted triangular lattice (the
+    synthetic inputs of the benchmarks; the reference ships none): nx x ny
+    nodes, unit spacing, rows at y = j sqrt(3)/2, odd rows shifted by +0.5,
+    x-periodic with period nx.  SplitMix64 draws, in order: with jitter > 0
+    two per node (dx, dy in U(-jitter, jitter); rows 0 and ny-1 move in x
+    only), then per node in row-major order three, one for each of its right,
+    up-left and up-right bonds, kept when the draw is below p.  Rest lengths
+    as read_network computes them (large_strain_relax.cu:97-99).  No
+    triples (use triples_of).  Returns the dict read_network returns."""
+    n = nx * ny
+    row = np.sqrt(3.0) / 2.0
+    jj, ii = np.divmod(np.arange(n), nx)
+    pts = np.empty((n, 2))
+    pts[:, 0] = ii + 0.5 * (jj & 1)
+    pts[:, 1] = jj * row
+    k0 = 0
+    if jitter > 0:
+        u = (_splitmix64(seed, 2 * n) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        dx = jitter * (2.0 * u[0::2] - 1.0)
+        dy = jitter * (2.0 * u[1::2] - 1.0)
+        pts[:, 0] += dx
+        inner = (jj != 0) & (jj != ny - 1)
+        pts[inner, 1] += dy[inner]
+        k0 = 2 * n
+    u = (_splitmix64(seed, k0 + 3 * n)[k0:] >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    u = u.reshape(n, 3)
+    odd = (jj & 1) == 1
+    cand = []  # (node order, slot, i, j, wrap)
+    right = (jj * nx + (ii + 1) % nx, np.where(ii == nx - 1, 1, 0))
+    up_l_i = np.where(odd, ii, ii - 1)
+    up_l = ((jj + 1) * nx + np.where(up_l_i < 0, up_l_i + nx, up_l_i), np.where(up_l_i < 0, -1, 0))
+    up_r_i = np.where(odd, ii + 1, ii)
+    up_r = ((jj + 1) * nx + np.where(up_r_i >= nx, up_r_i - nx, up_r_i), np.where(up_r_i >= nx, 1, 0))
+    has_up = jj + 1 < ny
+    keep = np.stack([u[:, 0] < p, has_up & (u[:, 1] < p), has_up & (u[:, 2] < p)], axis=1)
+    other = np.stack([right[0], up_l[0], up_r[0]], axis=1)
+    wrap = np.stack([right[1], up_l[1], up_r[1]], axis=1)
+    src = np.repeat(np.arange(n)[:, None], 3, axis=1)
+    ij = np.stack([src[keep], other[keep]], axis=1).astype(np.int32)
+    w = wrap[keep].astype(np.int8)
+    dxb = pts[ij[:, 1], 0] + nx * w.astype(np.float64) - pts[ij[:, 0], 0]
+    dyb = pts[ij[:, 1], 1] - pts[ij[:, 0], 1]
+    l0 = np.sqrt(dxb * dxb + dyb * dyb)
+    y = pts[:, 1]
+    miny = min(float(np.finfo(np.float32).max), float(y.min()))
+    maxy = max(float(np.finfo(np.float32).tiny), float(y.max()))
+    return {"offset": float(nx), "miny": miny, "maxy": maxy, "points": pts, "edge_ij": ij, "edge_l0": l0,
+            "edge_wrap": w, "tri_hjk": np.zeros((0, 3), np.int32), "tri_wrap": np.zeros((0, 2), np.int8)}
+
+
+def lattice_with_triples(nx, ny, p, seed):
+    """gen_lattice plus get_triples (large_strain_relax.cu:116-184)."""
+    a = gen_lattice(nx, ny, p, seed)
+    a["tri_hjk"], a["tri_wrap"] = triples_of(a["points"], a["edge_ij"], a["edge_wrap"], a["offset"])
+    return a
+
+
 class Model:
     """Holds numpy arrays alive behind an OrModel."""
 

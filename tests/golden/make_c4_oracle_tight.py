@@ -1,0 +1,70 @@
+"""Converged FP64 reference energies for the 512-network uneven batch
+(config C4), written to c4_oracle_tight.json.
+
+A FIRE run stopped at max|F| < 1e-10 is not at the energy minimum: on the
+softest networks of the batch the FP64 oracle's own energy at that point is
+up to ~5e-9 (relative) above the minimum it is approaching, because the
+remaining force sits in modes whose stiffness is tiny and E - E_min ~
+|F|^2 / (2 lambda).  Two correct relaxations that stop at max|F| < 1e-10 by
+different trajectories (FP64 and mixed precision) therefore cannot agree to
+1e-10 relative through their stopping points alone.  This script continues
+the oracle's own relaxation of every network from its max|F| < 1e-10 state
+(FIRE restarted there, v = 0) to max|F| < 1e-12, where the energy has
+settled to ~1e-13 relative, and records those energies (the converged FP64
+energies that the mixed-precision path is measured against) and how far,
+as the largest node displacement, the oracle's max|F| < 1e-10 state lies
+from the converged one.  The first
+stage reproduces c4_oracle.json exactly (checked).  CPU only (about an hour
+on 8 cores):
+    python tests/golden/make_c4_oracle_tight.py [threads]
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+import oracle  # noqa: E402
+from network_relaxation_gb300 import workloads  # noqa: E402
+
+FCUT_TIGHT = 1e-12
+
+
+def main():
+    threads = int(sys.argv[1]) if len(sys.argv) > 1 else os.cpu_count()
+    golden = json.load(open(os.path.join(HERE, "c4_oracle.json")))
+    prm = workloads.c4_params()
+    hosts = workloads.c4_networks(prm)
+    models, starts = [], []
+    for q, h in zip(prm, hosts):
+        a = h.arrays()
+        H = a["maxy"] - a["miny"]
+        models.append(oracle.Model(a, 1.0, q["kappa"]))
+        starts.append(oracle.affine_displace(a["points"], a["miny"], H, q["gamma"] * H, 0.0))
+    t = time.time()
+    xs, reps = oracle.fire_batch(models, starts, oracle.params(fcut=1e-10, criterion="max", max_steps=10**7), threads)
+    for r, g in zip(reps, golden["networks"]):
+        assert r.steps == g["steps"] and r.e_stretch.hex() == g["e_stretch"] and r.e_bend.hex() == g["e_bend"]
+    xs2, reps2 = oracle.fire_batch(models, xs, oracle.params(fcut=FCUT_TIGHT, criterion="max", max_steps=10**7),
+                                   threads)
+    wall = time.time() - t
+    rows = []
+    for x1, x2, r1, r2 in zip(xs, xs2, reps, reps2):
+        # the oracle's own distance, at max|F| < 1e-10, from the converged
+        # state: largest node displacement, in lattice spacings
+        dx = float(np.sqrt(((x1 - x2) ** 2).sum(1)).max())
+        rows.append(dict(steps_polish=r2.steps, converged=r2.converged, e_stretch=r2.e_stretch.hex(),
+                         e_bend=r2.e_bend.hex(), max_force=r2.max_force, dx_max_at_1e-10=dx))
+    out = {"fcut": FCUT_TIGHT, "criterion": "max", "start": "c4_oracle.json states (max|F| < 1e-10)",
+           "threads": threads, "wall_s": wall, "networks": rows}
+    with open(os.path.join(HERE, "c4_oracle_tight.json"), "w") as f:
+        json.dump(out, f, indent=0)
+    print("C4 converged oracle: %d networks, %.0f s on %d threads" % (len(rows), wall, threads))
+
+
+if __name__ == "__main__":
+    main()

@@ -92,3 +92,66 @@ def test_single_process_reduction_is_identity():
     from network_relaxation_gb300 import sharding
 
     assert sharding.reduce_timing(None, 3.5, 7) == (3.5, 7)
+
+
+def _worker_split(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from network_relaxation_gb300 import sharding
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    idx, params = sharding.split_c4_params(rank, world)
+    # each rank "relaxes" its share: reports carry the index and the seed
+    vals = [(float(i), float(q["seed"])) for i, q in zip(idx, params)]
+    rows = sharding.gather_reports(dist, idx, vals, 512, 2)
+    cost = sum(sharding.expected_cost(q) for q in params)
+    out[rank] = (idx, rows, cost, max(sharding.expected_cost(q) for q in params))
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("world", [2, 4])
+def test_one_batch_split_across_ranks_covers_every_network_once_and_balances(world):
+    """Split mode: ONE 512-network batch partitioned by LPT on expected cost;
+    every network on exactly one rank, the reports gathered in batch order on
+    every rank, and the predicted loads within one network's cost of each
+    other (the LPT bound)."""
+    port = _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_worker_split, args=(world, port, out), nprocs=world, join=True)
+    res = [out[r] for r in range(world)]
+    all_idx = sorted(i for r in res for i in r[0])
+    assert all_idx == list(range(512))
+    from network_relaxation_gb300 import workloads
+
+    seeds = [q["seed"] for q in workloads.c4_params()]
+    for r in res:
+        assert [row[0] for row in r[1]] == [float(i) for i in range(512)]
+        assert [row[1] for row in r[1]] == [float(s) for s in seeds]
+    loads = [r[2] for r in res]
+    assert max(loads) - min(loads) <= max(r[3] for r in res)
+
+
+def test_lpt_split_balances_the_oracle_step_counts():
+    """The expected-cost model ranks the uneven batch well enough that the
+    split's TRUE FP64 work (the oracle's step counts x N) is balanced: the
+    largest rank within 5 % (2 ranks) / 15 % (4 ranks) / 30 % (8 ranks) of the
+    mean."""
+    import json
+
+    from network_relaxation_gb300 import sharding, workloads
+
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "c4_oracle.json")))["networks"]
+    true = [r["steps"] * r["n_points"] for r in golden]
+    params = workloads.c4_params()
+    assert [q["seed"] for q in params] == [r["seed"] for r in golden]
+    for world, bound in ((2, 1.05), (4, 1.15), (8, 1.30)):
+        parts = sharding.lpt_partition([sharding.expected_cost(q) for q in params], world)
+        assert sorted(i for p in parts for i in p) == list(range(512))
+        loads = [sum(true[i] for i in p) for p in parts]
+        assert max(loads) <= bound * sum(loads) / world, (world, loads)
+    assert sharding.lpt_partition([5.0, 1.0, 1.0, 3.0], 2) == [[0], [1, 2, 3]]
+    assert sharding.gather_reports(None, [2, 0], [(1.0,), (2.0,)], 3, 1) == [(2.0,), None, (1.0,)]

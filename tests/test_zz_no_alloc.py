@@ -92,3 +92,45 @@ def test_energies_noalloc_rejects_oversize(cuda):
     st = call_noalloc(lib, torch, a, t, 1.0, 1e-3, out, npairs=MAX_ITEMS + 1)
     assert st == NR_ERR_CAPACITY
     assert "capacity" in lib.nr_last_error().decode()
+
+
+def test_energies_noalloc_bad_index_gives_nan(cuda):
+    """A bond index outside [0, n_points) makes the stretch energy NaN (the
+    kernel skips the read instead of reading out of bounds); the bend
+    energy, from valid triples, is unchanged."""
+    import torch
+
+    lib = _capi.load()
+    a, x, (es, eb) = sheared_network(16, 0.65, 14, 1.0, 1e-3, 0.02)
+    a = dict(a)
+    a["edge_ij"] = a["edge_ij"].copy()
+    a["edge_ij"][3, 1] = len(a["points"])
+    t = device_layout(torch, a, x)
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    assert call_noalloc(lib, torch, a, t, 1.0, 1e-3, out) == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.isnan(got[0]) and got[1] == eb
+
+
+def test_energies_noalloc_zero_stiffness_and_no_triples(cuda):
+    """ks <= 0 leaves the stretch term at 0 with the bend term unchanged; a
+    network with bonds and no triples (null triple arrays) returns 0."""
+    import torch
+
+    lib = _capi.load()
+    a, x, (es, eb) = sheared_network(20, 0.65, 15, 1.0, 1e-3, 0.02)
+    t = device_layout(torch, a, x)
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+    assert call_noalloc(lib, torch, a, t, 0.0, 1e-3, out) == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert got[0] == 0.0 and got[1] == eb
+    vp = lambda tensor: C.c_void_p(tensor.data_ptr())  # noqa: E731
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = lib.nr_energies_noalloc(len(a["points"]), len(a["edge_l0"]), 0, a["offset"], 1.0, 1e-3, vp(t["pos"]),
+                                 vp(t["pairs"]), vp(t["lengths"]), vp(t["e_off"]), None, None, vp(out), stream)
+    assert st == 0, lib.nr_last_error().decode()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert got[0] == es and got[1] == 0.0
