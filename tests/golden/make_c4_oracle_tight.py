@@ -58,7 +58,7 @@ def main():
         # state: largest node displacement, in lattice spacings
         dx = float(np.sqrt(((x1 - x2) ** 2).sum(1)).max())
         rows.append(dict(steps_polish=r2.steps, converged=r2.converged, e_stretch=r2.e_stretch.hex(),
-                         e_bend=r2.e_bend.hex(), max_force=r2.max_force, dx_max_at_1e-10=dx))
+                         e_bend=r2.e_bend.hex(), max_force=r2.max_force, dx_max_at_1e_10=dx))
     out = {"fcut": FCUT_TIGHT, "criterion": "max", "start": "c4_oracle.json states (max|F| < 1e-10)",
            "threads": threads, "wall_s": wall, "networks": rows}
     with open(os.path.join(HERE, "c4_oracle_tight.json"), "w") as f:
