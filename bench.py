@@ -291,9 +291,16 @@ def main():
                     help="renumber every network's nodes (nr_host_network_reorder) before the batch is built")
     ap.add_argument("--side", type=int, default=0,
                     help="profiling case: lattice side of the L1 workload (default 1024; not a bench line)")
+    ap.add_argument("--fcut", type=float, default=1e-10,
+                    help="C4 stop criterion max|F| < fcut of the measured precision (at most 1e-10: the metric's "
+                         "criterion is met at any tighter value)")
+    ap.add_argument("--dump", default="",
+                    help="write the per-network reports of the last C4 relaxation to this JSON file")
     ap.add_argument("--max-steps", type=int, default=10_000_000,
                     help="profiling case: FIRE step cap (networks may stop unconverged; not a bench line)")
     args = ap.parse_args()
+    if not args.fcut <= 1e-10:
+        ap.error("--fcut must be at most 1e-10")
     profiling_case = args.largest > 0 or args.max_steps != 10_000_000 or args.side > 0
     if profiling_case:
         args.no_cpu = args.no_fp64 = True
@@ -355,6 +362,7 @@ def main():
     out_host = torch.empty_like(start_host).pin_memory()
     prm = fire_params(nr, args.precision)
     prm.max_steps = args.max_steps
+    prm.fcut = args.fcut
     reps_arr = (nr.Report * batch.n)()
 
     def step_device():
@@ -407,6 +415,13 @@ def main():
         if not profiling_case and not all(reps_arr[i].status == 0 for i in range(batch.n)):
             raise RuntimeError("end-to-end step: a network did not converge")
     e2e_step_ms, _ = sharding.reduce_timing(dist, float(np.mean(e2e_ms)), batch.n, device="cuda")
+    if args.dump and rank == 0:
+        with open(args.dump, "w") as f:
+            json.dump({"fcut": args.fcut, "precision": args.precision, "batch_index": batch_idx,
+                       "networks": [dict(steps=r.steps, fp64_steps=r.fp64_steps, status=r.status,
+                                         e_stretch=r.e_stretch.hex(), e_bend=r.e_bend.hex(), max_force=r.max_force,
+                                         stress=[r.stress_xx, r.stress_yy, r.stress_xy])
+                                    for r in (reps_arr[i] for i in range(batch.n))]}, f)
     h2d = n_nodes * 16
     d2h = n_nodes * 16 + batch.n * C.sizeof(nr.Report)
 

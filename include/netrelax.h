@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define NR_ABI_VERSION 1
+#define NR_ABI_VERSION 2
 
 /* Replaces the reference's bool returns (true = ran, false = cudaMalloc
  * failed; large_strain_relax.cu:541-548, :596).  NR_OK and
@@ -175,6 +175,18 @@ typedef struct {
     int reserved;
     double e_gel;     /* report_data[3] of network_mesh_relax.cu's run_fire_md
                          (0 without a gel) */
+    /* No reference counterpart (the reference reports no stress): the
+     * stress of the stretch and bending forces at the returned positions,
+     * sigma = W / A with the virial W = -sum_n r_n (x) F_n (per bond
+     * W_ab = r_a f_b, r = r_j - r_i the minimum image, f the force on i; per
+     * triple W_ab = -(a_a F_j,b + b_a F_k,b), a, b its arms) and A = the x
+     * period times (maxy - miny) of the network as created.  stress_xy is
+     * (1/A) dE/dgamma under the affine shear of affine_displace, stress_yy
+     * the same for a y stretch: the secant shear modulus at strain gamma is
+     * 2 (E - E_0) / (A gamma^2), the tangent one d stress_xy / d gamma.  The
+     * FP64 path computes it with the canonical sums (bit-reproducible); the
+     * gel of network_mesh_relax.cu adds no term. */
+    double stress_xx, stress_yy, stress_xy;
 } nr_report;
 
 /* ------------------------------------------------------------------ */
@@ -212,6 +224,11 @@ int nr_forces(nr_network *dnet, double *host_f, void *stream);
  * :743, :751). */
 int nr_energies(nr_network *dnet, double *e_stretch, double *e_bend, void *stream);
 
+/* No reference counterpart: stress {xx, yy, xy} (as nr_report's) and the
+ * energies {E_stretch, E_bend} at the current positions, with the canonical
+ * sums of nr_energies. */
+int nr_stress(nr_network *dnet, double stress[3], double energies[2], void *stream);
+
 /* One record per relaxation of the strain protocol (the values
  * do_relaxation_run prints, large_strain_relax.cu:942-954, :983-994). */
 typedef struct {
@@ -223,6 +240,7 @@ typedef struct {
     int status;
     int fp64_steps;
     double e_gel; /* gel energy (nr_mesh_sweep; 0 without a gel) */
+    double stress_xx, stress_yy, stress_xy; /* as in nr_report */
 } nr_step_record;
 
 /* The compression-then-shear loops of do_relaxation_run
@@ -550,6 +568,10 @@ typedef struct {
     /* 0: displacements are strain * (maxy - miny) (the reference's only
      * reachable mode); 1: absolute displacements (lsrelax -a). */
     int absolute;
+    /* No reference counterpart: nonzero appends the shear and normal stress
+     * (nr_report stress_xy, stress_yy) as two more columns to every _edata
+     * line (lsrelax --stress); 0 keeps the reference's five columns. */
+    int stress_columns;
 } nr_batch_spec;
 
 /* parse_batch_file (large_strain_relax.cu:297-383): six non-comment lines. */
@@ -573,8 +595,8 @@ int nr_do_relaxation_run(const char *net_file, const char *log_name, const char 
 int nr_relaxation_batch(const char *batch_file, int precision, int criterion);
 
 /* The lsrelax command line (large_strain_relax.cu:1047-1126):
- * -b batch [-x bx] [-y by] [-a] [-i], plus --precision fp64|mixed and
- * --criterion rms|max. */
+ * -b batch [-x bx] [-y by] [-a] [-i], plus --precision fp64|mixed,
+ * --criterion rms|max and --stress (two stress columns in _edata). */
 int nr_lsrelax_main(int argc, char **argv);
 
 /* nmrelax (network_mesh_relax.cu): the same driver for networks embedded in

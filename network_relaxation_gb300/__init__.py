@@ -329,6 +329,15 @@ class Network:
         check(self._lib.nr_energies(self._h, C.byref(es), C.byref(eb), _stream(stream)), "nr_energies")
         return es.value, eb.value
 
+    def stress(self, stream=None):
+        """(stress {xx, yy, xy}, energies {E_stretch, E_bend}) at the current
+        positions: the virial of the stretch and bending forces over the
+        network's area (nr_stress)."""
+        st = (C.c_double * 3)()
+        en = (C.c_double * 2)()
+        check(self._lib.nr_stress(self._h, st, en, _stream(stream)), "nr_stress")
+        return np.array(st[:]), (en[0], en[1])
+
     # ---- gel coupling (network_mesh_relax.cu) ----
 
     def set_gel(self, smod, bmod, dilation):

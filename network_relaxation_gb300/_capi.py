@@ -47,13 +47,15 @@ class FireParams(C.Structure):
 class Report(C.Structure):
     _fields_ = [("rms_force", C.c_double), ("e_stretch", C.c_double), ("e_bend", C.c_double),
                 ("max_force", C.c_double), ("steps", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int),
-                ("reserved", C.c_int), ("e_gel", C.c_double)]
+                ("reserved", C.c_int), ("e_gel", C.c_double), ("stress_xx", C.c_double), ("stress_yy", C.c_double),
+                ("stress_xy", C.c_double)]
 
 
 class StepRecord(C.Structure):
     _fields_ = [("curr_disp", C.c_double), ("max_comp", C.c_double), ("e_stretch", C.c_double),
                 ("e_bend", C.c_double), ("rms_force", C.c_double), ("max_force", C.c_double), ("steps", C.c_int),
-                ("is_shear", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int), ("e_gel", C.c_double)]
+                ("is_shear", C.c_int), ("status", C.c_int), ("fp64_steps", C.c_int), ("e_gel", C.c_double),
+                ("stress_xx", C.c_double), ("stress_yy", C.c_double), ("stress_xy", C.c_double)]
 
 
 class SprInfo(C.Structure):
@@ -80,7 +82,8 @@ class MeshInfo(C.Structure):
 class BatchSpec(C.Structure):
     _fields_ = [("base", C.c_char * 1024), ("tag", C.c_char * 256), ("ks", C.c_double), ("kb", C.c_double),
                 ("fire_params", C.c_double * 5), ("nmin", C.c_int), ("mass", C.c_double), ("fcut", C.c_double),
-                ("nmax", C.c_int), ("compr", C.c_double * 3), ("shear", C.c_double * 3), ("absolute", C.c_int)]
+                ("nmax", C.c_int), ("compr", C.c_double * 3), ("shear", C.c_double * 3), ("absolute", C.c_int),
+                ("stress_columns", C.c_int)]
 
 
 class MeshBatchSpec(C.Structure):
@@ -121,6 +124,7 @@ SIGNATURES = {
     "nr_relax": (C.c_int, [P, C.POINTER(FireParams), C.POINTER(Report), P]),
     "nr_forces": (C.c_int, [P, c_double_p, P]),
     "nr_energies": (C.c_int, [P, c_double_p, c_double_p, P]),
+    "nr_stress": (C.c_int, [P, c_double_p, c_double_p, P]),
     "nr_sweep": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,
                            C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),
     "nr_sweep_graph": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,

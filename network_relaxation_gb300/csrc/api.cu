@@ -289,7 +289,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         const int tiles = (h.n_points + kTile - 1) / kTile;
         o.part = img.add(sizeof(double) * 4 * (size_t)tiles * 8);
         const int tb = (ne + kTile - 1) / kTile, tt = (nt + kTile - 1) / kTile, tg = (nf + kTile - 1) / kTile;
-        o.epart = img.add(sizeof(double) * 3 * (size_t)std::max(1, std::max(tb, std::max(tt, tg))));
+        o.epart = img.add(sizeof(double) * kEpartLists * (size_t)std::max(1, std::max(tb, std::max(tt, tg))));
         S.miny.push_back(h.miny);
         S.maxy.push_back(h.maxy);
     }
@@ -333,6 +333,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         d.ks = ks[i];
         d.kb = kb[i];
         d.sqrt_dof = std::sqrt((double)(2L * d.n));
+        d.area = h.offset * (h.maxy - h.miny);
         d.x = S.x_all + S.node_off[i];
         d.v = S.v_all + S.node_off[i];
         d.f = S.f_all + S.node_off[i];
@@ -438,6 +439,10 @@ static void fill_report(const FireState &st, const NetDev &d, nr_report *rep) {
     rep->steps = st.step;
     rep->fp64_steps = st.fp64_steps;
     rep->reserved = 0;
+    const double inv_a = d.area > 0 ? 1.0 / d.area : 0.0;
+    rep->stress_xx = st.vir[0] * inv_a;
+    rep->stress_yy = st.vir[1] * inv_a;
+    rep->stress_xy = st.vir[2] * inv_a;
     if (st.abort_flag) rep->status = NR_ERR_TIMEOUT;
     else if (st.status != 0) rep->status = st.status;
     else rep->status = st.converged ? NR_OK : NR_NOT_CONVERGED;
@@ -902,6 +907,9 @@ static void record_step(const SweepStep &t, const nr_report &rep, nr_step_record
     R.is_shear = t.is_shear;
     R.status = rep.status;
     R.fp64_steps = rep.fp64_steps;
+    R.stress_xx = rep.stress_xx;
+    R.stress_yy = rep.stress_yy;
+    R.stress_xy = rep.stress_xy;
 }
 
 /* Stream, graph and buffers of one captured sweep, released on every path
@@ -1084,6 +1092,20 @@ int nr_energies(nr_network *d, double *e_stretch, double *e_bend, void *stream) 
     return NR_OK;
 }
 
+int nr_stress(nr_network *d, double stress[3], double energies[2], void *stream) {
+    if (!d || !stress || !energies) return fail(NR_ERR_INVALID, "nr_stress: null argument");
+    const NetDev &dv = d->set.dev[0];
+    NR_CUDA_TRY(launch_energies(dv, energy_blocks(dv, sm_count()), as_stream(stream)));
+    FireState st;
+    NR_CUDA_TRY(cudaMemcpyAsync(&st, dv.st, sizeof(FireState), cudaMemcpyDeviceToHost, as_stream(stream)));
+    NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    const double inv_a = dv.area > 0 ? 1.0 / dv.area : 0.0;
+    for (int c = 0; c < 3; ++c) stress[c] = st.vir[c] * inv_a;
+    energies[0] = st.e_stretch;
+    energies[1] = st.e_bend;
+    return NR_OK;
+}
+
 int nr_sweep(nr_network *d, double miny, double yrange, const nr_fire_params *params, const double compr[3],
              const double shear[3], nr_step_record *records, int max_records, int *n_records,
              double *shear_positions, void *stream) {
@@ -1261,6 +1283,9 @@ int nr_mesh_sweep(nr_network *d, double miny, double height, const nr_fire_param
             R.is_shear = is_shear;
             R.status = rep.status;
             R.fp64_steps = rep.fp64_steps;
+            R.stress_xx = rep.stress_xx;
+            R.stress_yy = rep.stress_yy;
+            R.stress_xy = rep.stress_xy;
             if (is_shear && shear_positions) {
                 r = nr_network_get_positions(d, shear_positions + n2 * (size_t)(*n_records), stream);
                 if (r != NR_OK) return r;

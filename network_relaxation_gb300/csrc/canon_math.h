@@ -123,6 +123,35 @@ NR_HD double bend_energy(double ax, double ay, double bx, double by, double kb, 
     return ((0.5 * kb) * dth) * dth;
 }
 
+/* Virial of one bond, W = -sum over its two nodes of r_n (x) F_n with the
+ * minimum-image vector r = r_j - r_i and the force f on i (j gets -f):
+ * W_ab = r_a f_b.  Summed over bonds and triples and divided by the area,
+ * W_xy is the shear stress sigma_xy = (1/A) dE/dgamma under the affine map
+ * x += gamma (y - miny) that affine_displace applies
+ * (large_strain_relax.cu:527-537), W_yy the normal stress under y +=
+ * eps (y - miny), W_xx under x += eps x (the x period scaled with it). */
+NR_HD void bond_virial(double x1, double y1, double x2, double y2, double wW, double l0, double k, double &wxx,
+                       double &wyy, double &wxy) {
+    double fx, fy;
+    bond_force(x1, y1, x2, y2, wW, l0, k, fx, fy);
+    const double rx = (x2 + wW) - x1, ry = y2 - y1;
+    wxx = rx * fx;
+    wyy = ry * fy;
+    wxy = ry * fx;
+}
+
+/* Virial of one bending triple with arms a = r_hj, b = r_hk:
+ * W_ab = -(a_a F_j,b + b_a F_k,b) (the hinge's -(F_j + F_k) sits at the
+ * origin of the arms). */
+NR_HD void bend_virial(double ax, double ay, double bx, double by, double kb, double phi0, double &wxx, double &wyy,
+                       double &wxy) {
+    double fjx, fjy, fkx, fky;
+    bend_force(ax, ay, bx, by, kb, phi0, fjx, fjy, fkx, fky);
+    wxx = -fma(ax, fjx, bx * fkx);
+    wyy = -fma(ay, fjy, by * fky);
+    wxy = -fma(ay, fjx, by * fkx);
+}
+
 /* Per-node reduction terms of the FIRE loop. */
 NR_HD double dot2(double ax, double ay, double bx, double by) { return fma(ax, bx, ay * by); }
 

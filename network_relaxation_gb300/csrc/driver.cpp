@@ -296,9 +296,12 @@ int nr_do_relaxation_run(const char *net_file, const char *log_name, const char 
             nr_report rep;
             rc = relax(0, -inc, rep);
             if (rc < 0) break;
-            if (edata_file)
-                fprintf(edata_file, "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le\n", 0., curr_disp, rep.e_stretch,
+            if (edata_file) {
+                fprintf(edata_file, "%12.0lf\t%12.10lf\t%12.8le\t%12.8le\t%12.8le", 0., curr_disp, rep.e_stretch,
                         rep.e_bend, rep.e_stretch + rep.e_bend);
+                if (spec->stress_columns) fprintf(edata_file, "\t%12.8le\t%12.8le", rep.stress_xy, rep.stress_yy);
+                fputc('\n', edata_file);
+            }
             if (!(inc > 0)) break;
         }
     }
@@ -311,9 +314,12 @@ int nr_do_relaxation_run(const char *net_file, const char *log_name, const char 
             nr_report rep;
             rc = relax(inc, 0, rep);
             if (rc < 0) break;
-            if (edata_file)
-                fprintf(edata_file, "%12.10lf\t%12.10lf\t%12.10le\t%12.10le\t%12.10le\n", curr_disp, max_comp,
+            if (edata_file) {
+                fprintf(edata_file, "%12.10lf\t%12.10lf\t%12.10le\t%12.10le\t%12.10le", curr_disp, max_comp,
                         rep.e_stretch, rep.e_bend, rep.e_stretch + rep.e_bend);
+                if (spec->stress_columns) fprintf(edata_file, "\t%12.10le\t%12.10le", rep.stress_xy, rep.stress_yy);
+                fputc('\n', edata_file);
+            }
             rc = nr_network_get_positions(net, pos.data(), nullptr);
             if (rc != NR_OK) break;
             nr::write_xy_file(report_name(disp_base, num_digits, disp_count++, "pos"), pos.data(), n_points);
@@ -458,11 +464,13 @@ int nr_do_mesh_relaxation_run(const char *net_file, const char *log_name, const 
 
 }  // extern "C"
 
-static int relaxation_batch(const char *batch_file, int precision, int criterion, int absolute, bool mesh) {
+static int relaxation_batch(const char *batch_file, int precision, int criterion, int absolute, bool mesh,
+                            int stress_columns = 0) {
     nr_mesh_batch_spec mspec;
     int rc = mesh ? nr_parse_mesh_batch_file(batch_file, &mspec) : nr_parse_batch_file(batch_file, &mspec.net);
     nr_batch_spec &spec = mspec.net;
     spec.absolute = absolute;
+    spec.stress_columns = stress_columns;
     if (rc != NR_OK) {
         fprintf(stderr, "Parsing of the batch file failed.\n");
         return rc;
@@ -546,10 +554,11 @@ static int unknown_option(const char *c) {
 
 /* Both command lines: -b batch [-x bx] [-y by] [-a] [-i] (as the
  * reference's, except that -a works: there it falls through into -b and
- * copies a null optarg), plus --precision fp64|mixed, --criterion rms|max. */
+ * copies a null optarg), plus --precision fp64|mixed, --criterion rms|max
+ * and (lsrelax) --stress. */
 static int cli_main(int argc, char **argv, bool mesh) {
     const char *batch_file = nullptr;
-    int precision = NR_FP64, criterion = NR_CRIT_RMS, absolute = 0;
+    int precision = NR_FP64, criterion = NR_CRIT_RMS, absolute = 0, stress_columns = 0;
     const int rc0 = scan_options(
         argc, argv, "ab:ix:y:", {"precision", "criterion"},
         [&](char c, const char *arg) -> int {
@@ -580,6 +589,10 @@ static int cli_main(int argc, char **argv, bool mesh) {
             }
         },
         [&](const std::string &name, const char *v) -> int {
+            if (name == "stress" && !mesh) {
+                stress_columns = 1;
+                return 0;
+            }
             if (name != "precision" && name != "criterion") {
                 fprintf(stderr, "Unrecognized option: --%s\n", name.c_str());
                 return 0;
@@ -598,7 +611,7 @@ static int cli_main(int argc, char **argv, bool mesh) {
         fprintf(stderr, "No batch file was specified.\n");
         return -1;
     }
-    const int rc = relaxation_batch(batch_file, precision, criterion, absolute, mesh);
+    const int rc = relaxation_batch(batch_file, precision, criterion, absolute, mesh, stress_columns);
     return rc < 0 ? 1 : 0;
 }
 

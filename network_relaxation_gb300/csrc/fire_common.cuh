@@ -348,12 +348,13 @@ __device__ __forceinline__ void scal_load(Scal &s, const FireState *st_) {
     s.done = st->done; s.converged = st->converged; s.status = st->status;
 }
 
-/* Energy partials of bond, triple and gel-element tiles (t0, t0 + tstride,
- * ... over the three lists in that order), tiles of 256 items reduced by the
- * CTA's first 256 threads (8 warps; s_red holds 8 doubles).  The CTA must
- * have at least 256 threads; threads beyond the first 256 only take part in
- * the barriers.  Partials of list c go to epart[c * M + tile], M the largest
- * tile count of the three. */
+/* Energy and virial partials of bond, triple and gel-element tiles (t0,
+ * t0 + tstride, ... over the three lists in that order), tiles of 256 items
+ * reduced by the CTA's first 256 threads (8 warps; s_red holds 32 doubles).
+ * The CTA must have at least 256 threads; threads beyond the first 256 only
+ * take part in the barriers.  Partial q of a tile goes to epart[q * M +
+ * tile], M the largest tile count of the three lists: bonds E, W_xx, W_yy,
+ * W_xy at q = 0..3, triples at 4..7, gel elements (energy only) at 8. */
 __device__ __forceinline__ int energy_stride(const NetDev &d) {
     const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
     const int tg = (d.n_elems + kTile - 1) / kTile;
@@ -375,13 +376,15 @@ __device__ inline void energy_tiles(const NetDev &d, int t0, int tstride, double
         const int tile = cat == 0 ? t : (cat == 1 ? t - nb : t - nb - nt);
         const int n_items = cat == 0 ? d.n_edges : (cat == 1 ? d.n_triples : d.n_elems);
         const int item = in_tile ? tile * kTile + threadIdx.x : n_items;
-        double e = 0.0;
+        double e = 0.0, wxx = 0.0, wyy = 0.0, wxy = 0.0;
         if (item < n_items) {
             if (cat == 0) {
                 const int4 r = d.bond[item];
                 const double2 p1 = d.x[r.x], p2 = d.x[r.y];
                 const double k = d.bond_k ? d.bond_k[item] : d.ks;
-                e = bond_energy(p1.x, p1.y, p2.x, p2.y, wrap_shift(r.z, W), d.bond_l0[item], k);
+                const double wW = wrap_shift(r.z, W), l0 = d.bond_l0[item];
+                e = bond_energy(p1.x, p1.y, p2.x, p2.y, wW, l0, k);
+                bond_virial(p1.x, p1.y, p2.x, p2.y, wW, l0, k, wxx, wyy, wxy);
             } else if (cat == 1) {
                 const int4 r = d.tri[item];
                 const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
@@ -391,30 +394,54 @@ __device__ inline void energy_tiles(const NetDev &d, int t0, int tstride, double
                 const double kb = d.tri_kb ? d.tri_kb[item] : d.kb;
                 const double phi0 = d.tri_phi0 ? d.tri_phi0[item] : 0.0;
                 e = bend_energy(ax, ay, bx, by, kb, phi0);
+                bend_virial(ax, ay, bx, by, kb, phi0, wxx, wyy, wxy);
             } else if (kGel) {
                 e = gel_energy_abs(d, item);
             }
         }
         if (in_tile) { /* warp-uniform: kTile is a multiple of 32 */
             e = warp_sum(e);
-            if (lane == 0) s_red[warp] = e;
+            wxx = warp_sum(wxx);
+            wyy = warp_sum(wyy);
+            wxy = warp_sum(wxy);
+            if (lane == 0) {
+                s_red[warp] = e;
+                s_red[8 + warp] = wxx;
+                s_red[16 + warp] = wyy;
+                s_red[24 + warp] = wxy;
+            }
         }
         __syncthreads();
-        if (threadIdx.x == 0) d.epart[(size_t)cat * M + tile] = tree8(s_red);
+        if (threadIdx.x < 4 && (cat < 2 || threadIdx.x == 0)) {
+            const int q = cat == 2 ? 8 : 4 * cat + threadIdx.x;
+            d.epart[(size_t)q * M + tile] = tree8(s_red + 8 * threadIdx.x);
+        }
         __syncthreads();
     }
 }
 
-__device__ inline void energy_final(const NetDev &d, double *s_red, double &es, double &eb, double &eg) {
+/* Totals of the energy pass: energies and the virial {W_xx, W_yy, W_xy}
+ * (bond sum + triple sum; the gel contributes no virial). */
+__device__ inline void energy_final(const NetDev &d, double *s_red, double &es, double &eb, double &eg,
+                                    double *vir = nullptr) {
     const int tb = (d.n_edges + kTile - 1) / kTile, tt = (d.n_triples + kTile - 1) / kTile;
     const int tg = (d.n_elems + kTile - 1) / kTile;
     const size_t M = (size_t)energy_stride(d);
     es = 0.0;
     eb = 0.0;
     eg = 0.0;
-    if (d.use_bonds && d.n_edges > 0) es = final_sum(d.epart, tb, 8, s_red);
-    if (d.use_triples && d.n_triples > 0) eb = final_sum(d.epart + M, tt, 8, s_red);
-    if (d.use_gel && d.n_elems > 0) eg = final_sum(d.epart + 2 * M, tg, 8, s_red);
+    double wb[3] = {0.0, 0.0, 0.0}, wt[3] = {0.0, 0.0, 0.0};
+    const bool bonds = d.use_bonds && d.n_edges > 0, tris = d.use_triples && d.n_triples > 0;
+    if (bonds) es = final_sum(d.epart, tb, 8, s_red);
+    if (tris) eb = final_sum(d.epart + 4 * M, tt, 8, s_red);
+    if (d.use_gel && d.n_elems > 0) eg = final_sum(d.epart + 8 * M, tg, 8, s_red);
+    if (vir) {
+        for (int c = 0; c < 3; ++c) {
+            if (bonds) wb[c] = final_sum(d.epart + (1 + c) * M, tb, 8, s_red);
+            if (tris) wt[c] = final_sum(d.epart + (5 + c) * M, tt, 8, s_red);
+            vir[c] = wb[c] + wt[c];
+        }
+    }
 }
 
 }  // namespace nr

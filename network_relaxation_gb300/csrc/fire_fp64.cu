@@ -177,12 +177,13 @@ __global__ void k_energy_tiles(NetDev d) {
 
 __global__ void k_energy_final(NetDev d) {
     __shared__ double s_red[32]; /* one slot per warp, up to 1024 threads */
-    double es, eb, eg;
-    energy_final(d, s_red, es, eb, eg);
+    double es, eb, eg, vir[3];
+    energy_final(d, s_red, es, eb, eg, vir);
     if (threadIdx.x == 0) {
         d.st->e_stretch = es;
         d.st->e_bend = eb;
         d.st->e_gel = eg;
+        for (int c = 0; c < 3; ++c) d.st->vir[c] = vir[c];
     }
 }
 
@@ -223,13 +224,14 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
         }
         __syncthreads();
         energy_tiles<false>(d, 0, 1, s_red);
-        double es, eb, eg;
-        energy_final(d, s_red, es, eb, eg);
+        double es, eb, eg, vir[3];
+        energy_final(d, s_red, es, eb, eg, vir);
         if (threadIdx.x == 0) {
             scal_store(d.st, s_sc);
             d.st->e_stretch = es;
             d.st->e_bend = eb;
             d.st->e_gel = eg;
+            for (int c = 0; c < 3; ++c) d.st->vir[c] = vir[c];
         }
         __syncthreads();
     }

@@ -620,16 +620,17 @@ struct MixShared {
     Coef coef;
 };
 
-/* Canonical FP64 energies of the network into st (one CTA).  Kept out of
+/* Canonical FP64 energies and virial of the network into st (one CTA).  Kept out of
  * line, like anchor_eval: the FP64 code's register demand stays out of the
  * FP32 loop. */
 static __device__ __noinline__ void mixed_energies(const NetDev &d, double *s_red) {
     energy_tiles<false>(d, 0, 1, s_red);
-    double es, eb, eg;
-    energy_final(d, s_red, es, eb, eg);
+    double es, eb, eg, vir[3];
+    energy_final(d, s_red, es, eb, eg, vir);
     if (threadIdx.x == 0) {
         d.st->e_stretch = es;
         d.st->e_bend = eb;
+        for (int c = 0; c < 3; ++c) d.st->vir[c] = vir[c];
     }
 }
 

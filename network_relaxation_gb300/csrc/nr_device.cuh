@@ -14,6 +14,10 @@
  *   bptr/bent      int[N+1]/int[2E]  incidence: (bond << 1) | role
  *   tptr/tent      int[N+1]/int[3T]  incidence: (triple << 2) | role
  *   part           double[4 * n_units]  reduction partials
+ *   epart          double[9 * M]  energy pass tile partials, M = the largest
+ *                                 tile count of bonds, triples, elements:
+ *                                 bonds E, Wxx, Wyy, Wxy at q = 0..3,
+ *                                 triples at 4..7, gel elements E at 8
  * Networks embedded in a gel (network_mesh_relax.cu) add
  *   elem           int4[F]      FEM triangle {v1, v2, v3, 0}
  *   elem_inv       double[6F]   reference inverse matrix (get_inv_mats layout)
@@ -36,6 +40,7 @@
 namespace nr {
 
 constexpr int kTile = 256;
+constexpr int kEpartLists = 9; /* lists of the energy pass partials (epart) */
 constexpr int kChunk = 32;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -68,7 +73,8 @@ struct __align__(128) FireState {
     int anchor_now; /* mixed precision: the team re-anchors before the next pass */
     int yielded;    /* mixed precision: left at an anchor for a larger cluster (fire_dsm.cu) */
     double e_gel;   /* gel energy (networks embedded in a gel) */
-    int pad[8];
+    double vir[3];  /* virial {W_xx, W_yy, W_xy} of the stretch and bending forces */
+    int pad[2];
     unsigned int bar_count, bar_gen, abort_flag, timeout_site;
     unsigned int pad2[28];
 };
@@ -77,6 +83,7 @@ struct NetDev {
     int n, n_edges, n_triples, n_tiles;
     int use_bonds, use_triples, sub, n_units; /* sub = chunks per reduction unit (1,2,4,8) */
     double width, ks, kb, sqrt_dof;
+    double area; /* width x (maxy - miny) at creation: stress = virial / area */
     double2 *x, *v, *f;
     const unsigned char *fcode;
     const int4 *bond;

@@ -103,6 +103,8 @@ def lib():
         L.or_nonaffinity.argtypes = [C.c_int, dp, dp, C.c_double, C.c_double, C.c_double]
         L.or_forces.argtypes = [C.POINTER(OrModel), dp, dp]
         L.or_energies.argtypes = [C.POINTER(OrModel), dp, dp, dp]
+        L.or_virial.argtypes = [C.POINTER(OrModel), dp, dp]
+        L.or_virial.restype = None
         L.or_fire.argtypes = [C.POINTER(OrModel), dp, dp, dp, C.POINTER(OrParams), C.POINTER(OrReport)]
         L.or_sweep.restype = C.c_int
         L.or_sweep.argtypes = [C.POINTER(OrModel), dp, C.c_double, C.c_double, C.POINTER(OrParams), dp, dp, dp,
@@ -320,6 +322,14 @@ class Model:
         es, eb = C.c_double(), C.c_double()
         lib().or_energies(C.byref(self.m), _d(pos), C.byref(es), C.byref(eb))
         return es.value, eb.value
+
+    def virial(self, pos):
+        """{W_xx, W_yy, W_xy} of the stretch and bending forces at pos
+        (or_virial); the stress is W / area."""
+        pos = np.ascontiguousarray(pos, np.float64)
+        w = np.zeros(3)
+        lib().or_virial(C.byref(self.m), _d(pos), _d(w))
+        return w
 
     def fire(self, pos, params):
         """Relaxes pos (copied); returns (pos, vel, forces, OrReport)."""

@@ -391,6 +391,66 @@ void or_energies(const or_model *m, const double *pos, double *e_stretch, double
     }
 }
 
+/* Virial W = -sum_n r_n (x) F_n of the stretch and bending forces (no
+ * counterpart in the reference, which reports no stress; the benchmark spec's
+ * "stresses" output).  Per bond, with r = r_j - r_i (minimum image) and f the
+ * stretch force on i of large_strain_relax.cu:386-414: W_ab = r_a f_b.  Per
+ * triple, with arms a = r_hj, b = r_hk and the bending forces F_j, F_k of
+ * :417-469: W_ab = -(a_a F_j,b + b_a F_k,b).  Each component is summed over
+ * bonds and over triples separately with or_canon_sum, the two sums added:
+ * w = {W_xx, W_yy, W_xy}.  sigma = W / area; W_xy = dE/dgamma under the
+ * affine shear of :527-537. */
+void or_virial(const or_model *m, const double *pos, double w[3]) {
+    const double W = m->width;
+    double wb[3] = {0.0, 0.0, 0.0}, wt[3] = {0.0, 0.0, 0.0};
+    if (m->ks > 0 && m->n_edges > 0) {
+        double *terms = (double *)malloc(sizeof(double) * 3 * (size_t)m->n_edges);
+        for (int b = 0; b < m->n_edges; ++b) {
+            const int i1 = m->edge_ij[2 * b], i2 = m->edge_ij[2 * b + 1];
+            const double k = m->bond_k ? m->bond_k[b] : m->ks;
+            const double l0 = m->edge_l0[b];
+            const double wW = (double)m->edge_wrap[b] * W;
+            const double x1 = pos[2 * i1], y1 = pos[2 * i1 + 1];
+            const double x2 = pos[2 * i2], y2 = pos[2 * i2 + 1];
+            const double rx0 = (x1 - x2) - wW, ry0 = y1 - y2;
+            const double inv = 1.0 / sqrt(fma(rx0, rx0, ry0 * ry0));
+            const double sc = k * fma(-l0, inv, 1.0);
+            const double fx = sc * ((x2 + wW) - x1);
+            const double fy = sc * (y2 - y1);
+            const double rx = (x2 + wW) - x1, ry = y2 - y1;
+            terms[b] = rx * fx;
+            terms[m->n_edges + b] = ry * fy;
+            terms[2 * (size_t)m->n_edges + b] = ry * fx;
+        }
+        for (int c = 0; c < 3; ++c) wb[c] = or_canon_sum(terms + (size_t)c * m->n_edges, m->n_edges);
+        free(terms);
+    }
+    if (m->kb > 0 && m->n_triples > 0) {
+        double *terms = (double *)malloc(sizeof(double) * 3 * (size_t)m->n_triples);
+        for (int t = 0; t < m->n_triples; ++t) {
+            const int h = m->tri_hjk[3 * t], j = m->tri_hjk[3 * t + 1], k = m->tri_hjk[3 * t + 2];
+            const double kb = m->tri_kb ? m->tri_kb[t] : m->kb;
+            const double phi0 = m->tri_phi0 ? m->tri_phi0[t] : 0.0;
+            const double wj = (double)m->tri_wrap[2 * t] * W, wk = (double)m->tri_wrap[2 * t + 1] * W;
+            const double xh = pos[2 * h], yh = pos[2 * h + 1];
+            const double ax = (pos[2 * j] + wj) - xh, ay = pos[2 * j + 1] - yh;
+            const double bx = (pos[2 * k] + wk) - xh, by = pos[2 * k + 1] - yh;
+            const double c = fma(ax, by, -(ay * bx));
+            const double d = fma(ax, bx, ay * by);
+            const double g = kb * (or_atan2(-c, -d) - phi0);
+            const double g2 = g / fma(ax, ax, ay * ay);
+            const double g3 = g / fma(bx, bx, by * by);
+            const double fjx = -ay * g2, fjy = ax * g2, fkx = by * g3, fky = -bx * g3;
+            terms[t] = -fma(ax, fjx, bx * fkx);
+            terms[m->n_triples + t] = -fma(ay, fjy, by * fky);
+            terms[2 * (size_t)m->n_triples + t] = -fma(ay, fjx, by * fkx);
+        }
+        for (int c = 0; c < 3; ++c) wt[c] = or_canon_sum(terms + (size_t)c * m->n_triples, m->n_triples);
+        free(terms);
+    }
+    for (int c = 0; c < 3; ++c) w[c] = wb[c] + wt[c];
+}
+
 /* ------------------------------------------------------------------------ */
 /* FIRE (large_strain_relax.cu:596-762)                                      */
 /* ------------------------------------------------------------------------ */

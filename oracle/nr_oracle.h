@@ -102,6 +102,9 @@ double or_canon_sum(const double *terms, long n);
 /* Physics. */
 void or_forces(const or_model *m, const double *pos, double *forces);
 void or_energies(const or_model *m, const double *pos, double *e_stretch, double *e_bend);
+/* Virial {W_xx, W_yy, W_xy} of the stretch and bending forces (stress times
+ * area); see nr_oracle.c. */
+void or_virial(const or_model *m, const double *pos, double w[3]);
 int or_fire(const or_model *m, double *pos, double *vel, double *forces, const or_fire_params *p, or_report *rep);
 
 /* Strain protocol of do_relaxation_run (large_strain_relax.cu:917-999),

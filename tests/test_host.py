@@ -23,7 +23,7 @@ def test_library_exports_every_header_symbol(built):
     lib = nr.lib()
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.nr_abi_version() == 1
+    assert lib.nr_abi_version() == 2
     out = subprocess.run(["nm", "-D", "--defined-only", nr._capi.LIB_PATH], capture_output=True, text=True).stdout
     exported = set(re.findall(r" T (nr_[a-z0-9_]+)", out))
     assert names <= exported
