@@ -21,12 +21,39 @@
  *   k_fire_batch  many networks, one CTA per network, persistent over a
  *                 device work queue; __syncthreads only.
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "fire_common.cuh"
 #include "fire_launch.h"
 
 namespace nr {
+
+/* Pass A of node i: mixing / zeroing from the previous step's scalars,
+ * drift, half kick. */
+__device__ __forceinline__ void pass_a_node(const NetDev &d, const Scal &s, int i) {
+    double2 xi = d.x[i], vi = d.v[i];
+    const double2 fi = d.f[i];
+    if (s.mix_pending) {
+        vi.x = fma(s.mix_na, vi.x, vi.x);
+        vi.y = fma(s.mix_na, vi.y, vi.y);
+        vi.x = fma(s.mix_a, fi.x, vi.x);
+        vi.y = fma(s.mix_a, fi.y, vi.y);
+        if (s.zero_v) vi = make_double2(0.0, 0.0);
+    }
+    if (!s.done) {
+        xi.x = fma(s.dt, vi.x, xi.x);
+        xi.y = fma(s.dt, vi.y, xi.y);
+        xi.x = fma(s.dtsq, fi.x, xi.x);
+        xi.y = fma(s.dtsq, fi.y, xi.y);
+        vi.x = fma(s.dtm, fi.x, vi.x);
+        vi.y = fma(s.dtm, fi.y, vi.y);
+        d.x[i] = xi;
+    }
+    d.v[i] = vi;
+}
 
 /* Pass A over the nodes of units u = u0, u0+ustride, ... */
 __device__ void pass_a(const NetDev &d, const Scal &s, int u0, int ustride) {
@@ -34,25 +61,7 @@ __device__ void pass_a(const NetDev &d, const Scal &s, int u0, int ustride) {
     for (int u = u0; u < d.n_units; u += ustride) {
         const int i = (u * d.sub + warp) * kChunk + lane;
         if (i >= d.n) continue;
-        double2 xi = d.x[i], vi = d.v[i];
-        const double2 fi = d.f[i];
-        if (s.mix_pending) {
-            vi.x = fma(s.mix_na, vi.x, vi.x);
-            vi.y = fma(s.mix_na, vi.y, vi.y);
-            vi.x = fma(s.mix_a, fi.x, vi.x);
-            vi.y = fma(s.mix_a, fi.y, vi.y);
-            if (s.zero_v) vi = make_double2(0.0, 0.0);
-        }
-        if (!s.done) {
-            xi.x = fma(s.dt, vi.x, xi.x);
-            xi.y = fma(s.dt, vi.y, xi.y);
-            xi.x = fma(s.dtsq, fi.x, xi.x);
-            xi.y = fma(s.dtsq, fi.y, xi.y);
-            vi.x = fma(s.dtm, fi.x, vi.x);
-            vi.y = fma(s.dtm, fi.y, vi.y);
-            d.x[i] = xi;
-        }
-        d.v[i] = vi;
+        pass_a_node(d, s, i);
     }
 }
 
@@ -237,6 +246,121 @@ __global__ void __launch_bounds__(256) k_fire_batch(const NetDev *nets, int n_ne
     }
 }
 
+/* ------------------------------------------------------------------ */
+/* One thread-block cluster per network (FP64)                          */
+/* ------------------------------------------------------------------ */
+
+/* The FP64 step of k_fire_grid with the software grid barrier replaced by
+ * the hardware cluster barrier: a network is relaxed by the C CTAs (C SMs,
+ * up to 16) of one cluster.  Every warp of the cluster takes 32-node chunks
+ * (unit = one chunk: the canonical reduction with sub = 1), items are spread
+ * over all the cluster's threads, and after the barrier that ends pass B
+ * EVERY CTA reduces the unit partials itself, in the canonical order, so
+ * every CTA's thread 0 advances an identical copy of the FIRE scalars and no
+ * fourth barrier is needed.  Same operations on the same values as
+ * k_fire_grid and the oracle: the same bits.  On small networks the grid
+ * kernel's step is set by the latency of its three software barriers (about
+ * 40 us); these barriers are hardware ones.  Persistent over a work queue:
+ * one network (nr_relax) or a batch (nr_batch_relax). */
+template <bool kGel>
+__global__ void __launch_bounds__(kTile, 1)
+    k_fire_cluster(const NetDev *nets, int n_nets, FireParamsDev p, int *queue, const int *order) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ double s_red[32];
+    __shared__ NetDev s_d;
+    __shared__ Scal s_sc;
+    __shared__ int s_slot;
+    const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wpc = blockDim.x >> 5;
+    const int gw = rank * wpc + warp, nw = C * wpc; /* warps of the cluster */
+    for (;;) {
+        if (rank == 0 && threadIdx.x == 0) s_slot = atomicAdd(queue, 1);
+        cl.sync();
+        const int slot = *cl.map_shared_rank(&s_slot, 0);
+        /* every CTA has read rank 0's slot before any CTA may exit or rank 0
+         * overwrites it for the next network */
+        cl.sync();
+        if (slot >= n_nets) return;
+        if (threadIdx.x == 0) s_d = nets[order ? order[slot] : slot];
+        __syncthreads();
+        const NetDev &d = s_d;
+        const int n_units = d.n_tiles * 8; /* 32-node chunks, padded to whole tiles */
+        const int item0 = rank * blockDim.x + threadIdx.x, istride = C * blockDim.x;
+        bool init = true;
+        for (;;) {
+            if (!init) {
+                for (int u = gw; u * kChunk < d.n; u += nw) {
+                    const int i = u * kChunk + lane;
+                    if (i < d.n) pass_a_node(d, s_sc, i);
+                }
+                if (s_sc.done) break;
+                cl.sync();
+            }
+            items_pass<kGel>(d, item0, istride);
+            cl.sync();
+            /* pass B: gather, half kick (v = 0 at the start), unit partials */
+            const double dtm = init ? 0.0 : s_sc.dtm;
+            for (int u = gw; u < n_units; u += nw) {
+                const int i = u * kChunk + lane;
+                double tP = 0.0, tV = 0.0, tF = 0.0;
+                if (i < d.n) {
+                    double fx, fy;
+                    node_force_items<kGel>(d, i, fx, fy);
+                    double2 vi;
+                    if (init) {
+                        vi = make_double2(0.0, 0.0);
+                    } else {
+                        vi = d.v[i];
+                        vi.x = fma(dtm, fx, vi.x);
+                        vi.y = fma(dtm, fy, vi.y);
+                    }
+                    d.v[i] = vi;
+                    d.f[i] = make_double2(fx, fy);
+                    tP = dot2(vi.x, vi.y, fx, fy);
+                    tV = dot2(vi.x, vi.y, vi.x, vi.y);
+                    tF = dot2(fx, fy, fx, fy);
+                }
+                const double sP = warp_sum(tP), sV = warp_sum(tV), sF = warp_sum(tF), sM = warp_max(tF);
+                if (lane == 0) {
+                    d.part[u] = sP;
+                    d.part[(size_t)n_units + u] = sV;
+                    d.part[2 * (size_t)n_units + u] = sF;
+                    d.part[3 * (size_t)n_units + u] = sM;
+                }
+            }
+            cl.sync();
+            /* every CTA: the canonical totals and the FIRE scalars */
+            const double P = final_sum(d.part, d.n_tiles, 1, s_red);
+            const double V2 = final_sum(d.part + n_units, d.n_tiles, 1, s_red);
+            const double F2 = final_sum(d.part + 2 * (size_t)n_units, d.n_tiles, 1, s_red);
+            const double M2 = final_max(d.part + 3 * (size_t)n_units, n_units, s_red);
+            if (threadIdx.x == 0) {
+                if (init) scal_init(s_sc, p, F2, M2, d.sqrt_dof);
+                else scal_step(s_sc, p, P, V2, F2, M2, d.sqrt_dof);
+            }
+            __syncthreads();
+            init = false;
+        }
+        cl.sync();
+        energy_tiles<kGel>(d, rank, C, s_red);
+        cl.sync();
+        if (rank == 0) {
+            double es, eb, eg, vir[3];
+            energy_final(d, s_red, es, eb, eg, vir);
+            if (threadIdx.x == 0) {
+                scal_store(d.st, s_sc);
+                d.st->e_stretch = es;
+                d.st->e_bend = eb;
+                d.st->e_gel = eg;
+                for (int c = 0; c < 3; ++c) d.st->vir[c] = vir[c];
+            }
+        }
+        cl.sync();
+    }
+}
+
 __global__ void k_forces(NetDev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
@@ -356,6 +480,52 @@ cudaError_t fp64_batch_max_blocks(int *max_blocks) {
     if (e != cudaSuccess) return e;
     *max_blocks = per_sm * sms;
     return cudaSuccess;
+}
+
+/* Clusters of C CTAs that fit the GPU at once (0: the size cannot run). */
+cudaError_t fp64_cluster_max_active(int cluster, bool gel, int *out) {
+    const void *k = gel ? (const void *)k_fire_cluster<true> : (const void *)k_fire_cluster<false>;
+    cudaError_t e;
+    if (cluster > 8 && (e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) != cudaSuccess)
+        return e;
+    int dev, sms;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((sms / cluster) * cluster);
+    cfg.blockDim = dim3(kTile);
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    *out = 0;
+    return cudaOccupancyMaxActiveClusters(out, k, &cfg);
+}
+
+cudaError_t launch_fp64_cluster(const NetDev *nets_dev, int n_nets, int cluster, bool gel, const FireParamsDev &p,
+                                int *queue_dev, const int *order_dev, cudaStream_t stream) {
+    if (cluster < 1 || cluster > 16) return cudaErrorInvalidValue;
+    int max_clusters = 0;
+    cudaError_t e = fp64_cluster_max_active(cluster, gel, &max_clusters);
+    if (e != cudaSuccess) return e;
+    if (max_clusters < 1) return cudaErrorLaunchOutOfResources;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(std::max(1, std::min(n_nets, max_clusters)) * cluster);
+    cfg.blockDim = dim3(kTile);
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if ((e = cudaMemsetAsync(queue_dev, 0, sizeof(int), stream)) != cudaSuccess) return e;
+    if (gel) return cudaLaunchKernelEx(&cfg, k_fire_cluster<true>, nets_dev, n_nets, p, queue_dev, order_dev);
+    return cudaLaunchKernelEx(&cfg, k_fire_cluster<false>, nets_dev, n_nets, p, queue_dev, order_dev);
 }
 
 cudaError_t launch_forces(const NetDev &d, cudaStream_t stream) {

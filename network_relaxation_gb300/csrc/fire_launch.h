@@ -36,6 +36,12 @@ cudaError_t launch_energies(const NetDev &d, int blocks, cudaStream_t stream);
 cudaError_t fp64_batch_max_blocks(int *max_blocks);
 cudaError_t launch_fp64_batch(const NetDev *nets_dev, int n_nets, const FireParamsDev &p, int *queue_dev,
                               int blocks, cudaStream_t stream);
+/* FP64 relaxation with one thread-block cluster of `cluster` CTAs (1..16)
+ * per network, persistent over the queue (order_dev may be null): the
+ * same bits as launch_fp64_grid. */
+cudaError_t fp64_cluster_max_active(int cluster, bool gel, int *out);
+cudaError_t launch_fp64_cluster(const NetDev *nets_dev, int n_nets, int cluster, bool gel, const FireParamsDev &p,
+                                int *queue_dev, const int *order_dev, cudaStream_t stream);
 cudaError_t launch_forces(const NetDev &d, cudaStream_t stream);
 cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
                           cudaStream_t stream);

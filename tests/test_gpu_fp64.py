@@ -62,8 +62,21 @@ def test_affine_bitexact(cuda):
     assert np.array_equal(net.positions(), x)
 
 
+@pytest.fixture(params=["cluster16", "cluster4", "grid"])
+def fp64_kernel(request, monkeypatch):
+    """The single-network FP64 kernel: one thread-block cluster of 16 or 4
+    CTAs (hardware cluster barriers; the default for small networks) or the
+    cooperative grid kernel (software grid barriers).  The same bits."""
+    if request.param == "grid":
+        monkeypatch.setenv("NR_FP64_CLUSTER_NODES", "0")
+    else:
+        monkeypatch.setenv("NR_FP64_CLUSTER_NODES", "100000000")
+        monkeypatch.setenv("NR_FP64_CLUSTER", request.param[len("cluster"):])
+    return request.param
+
+
 @pytest.mark.parametrize("crit", ["rms", "max"])
-def test_relax_bitwise_c1(cuda, crit):
+def test_relax_bitwise_c1(cuda, crit, fp64_kernel):
     """32x32, p=0.65, kappa=1e-3: one shear increment of 0.01, relaxed."""
     h, a = lattice(32, 0.65, 1)
     N = len(a["points"])
@@ -81,7 +94,7 @@ def test_relax_bitwise_c1(cuda, crit):
     assert rep.rms_force == orep.rms_force and rep.max_force == orep.max_force
 
 
-def test_step_cap_reports_not_converged(cuda):
+def test_step_cap_reports_not_converged(cuda, fp64_kernel):
     h, a = lattice(16, 0.65, 2)
     net = nr.Network(h, ks=1.0, kb=1e-3)
     H = a["maxy"] - a["miny"]
@@ -93,8 +106,12 @@ def test_step_cap_reports_not_converged(cuda):
     assert np.array_equal(net.positions(), xo)
 
 
-def test_batch_equals_oracle(cuda):
-    """Uneven batch: every network bit-identical to its oracle run."""
+@pytest.mark.parametrize("team", ["1", "4", "16"])
+def test_batch_equals_oracle(cuda, team, monkeypatch):
+    """Uneven batch: every network bit-identical to its oracle run, with one
+    CTA per network (k_fire_batch) and with thread-block clusters of 4 and
+    16 CTAs per network (k_fire_cluster)."""
+    monkeypatch.setenv("NR_FP64_BATCH_CLUSTER", team)
     hosts, arrs, gam = [], [], []
     rng = np.random.default_rng(11)
     for i in range(12):
@@ -120,7 +137,7 @@ def test_batch_equals_oracle(cuda):
         assert reps[i].e_stretch == orep.e_stretch and reps[i].e_bend == orep.e_bend
 
 
-def test_sweep_matches_oracle(cuda):
+def test_sweep_matches_oracle(cuda, fp64_kernel):
     h, a = lattice(16, 0.7, 9)
     net = nr.Network(h, ks=1.0, kb=1e-3)
     prm = nr.fire_params(fcut=1e-10, criterion="max", **FIRE)
@@ -142,7 +159,7 @@ def _rec(r):
             r.status)
 
 
-def test_sweep_graph_equals_step_by_step_sweep(cuda):
+def test_sweep_graph_equals_step_by_step_sweep(cuda, fp64_kernel):
     """The protocol captured in one CUDA graph gives the step-by-step
     sweep's records and shear positions bit for bit (and so the oracle's:
     test_sweep_matches_oracle)."""
@@ -163,7 +180,7 @@ def test_sweep_graph_equals_step_by_step_sweep(cuda):
     assert np.array_equal(g.positions(), p.positions())
 
 
-def test_run_fire_md_dropin(cuda):
+def test_run_fire_md_dropin(cuda, fp64_kernel):
     """The reference's own argument list, device arrays from torch."""
     import torch
 
@@ -195,7 +212,7 @@ def test_run_fire_md_dropin(cuda):
     assert report == [orep.rms_force, orep.e_stretch, orep.e_bend]
 
 
-def test_relax_bitwise_mikado(cuda):
+def test_relax_bitwise_mikado(cuda, fp64_kernel):
     """C3-type network (Mikado fibres: per-bond k = 1/l0, per-triple kb and
     rest angles, x-periodic wraps): one shear increment, FP64 relaxation
     identical to the oracle.  dt_max follows the stiffest bond."""
@@ -224,6 +241,7 @@ def test_grid_barrier_wait_budget_runs_out_without_a_fault(cuda, monkeypatch):
     net = nr.Network(h, ks=1.0, kb=1e-3)
     net.affine_displace(a["miny"], H, 0.02 * H, 0.0)
     prm = nr.fire_params(fcut=1e-10, criterion="max", **FIRE)
+    monkeypatch.setenv("NR_FP64_CLUSTER_NODES", "0")  # the grid kernel, whose barriers are software ones
     monkeypatch.setenv("NR_TEST_STALL_BARRIER", "1")
     monkeypatch.setenv("NR_BARRIER_BUDGET_MS", "20")
     with pytest.raises(nr.NetRelaxError) as e:
@@ -236,3 +254,58 @@ def test_grid_barrier_wait_budget_runs_out_without_a_fault(cuda, monkeypatch):
     x_or, _, _, orep = oracle.Model(a, 1.0, 1e-3).fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
     assert rep.status == nr.NR_OK and rep.steps == orep.steps
     assert np.array_equal(net.positions(), x_or)
+
+
+@pytest.mark.parametrize("cache", ["1", "0"])
+def test_run_fire_md_dropin_sweep_reuses_image(cuda, cache, monkeypatch):
+    """The reference calls run_fire_md once per strain step on the same
+    device arrays (large_strain_relax.cu:931, :973).  The drop-in keeps the
+    device image it built while the arrays, sizes, constants and contents
+    stay the same (a device checksum), and rebuilds it when a value changes
+    in place: three warm-started shear steps bit-identical to the oracle's,
+    then a rest length changed in place and the next step equal to the
+    oracle's on the changed network.  NR_DROPIN_CACHE=0 rebuilds every call:
+    the same bits."""
+    import torch
+
+    monkeypatch.setenv("NR_DROPIN_CACHE", cache)
+    h, a = lattice(20, 0.7, 23)
+    N = len(a["points"])
+    H = a["maxy"] - a["miny"]
+    fc = h.fcodes()
+    dev = cuda
+    x = a["points"].copy()
+    d_pos = torch.tensor(x.reshape(-1), dtype=torch.float64, device=dev)
+    d_vel = torch.zeros_like(d_pos)
+    d_f = torch.zeros_like(d_pos)
+    d_pairs = torch.tensor(a["edge_ij"].reshape(-1), dtype=torch.int32, device=dev)
+    d_len = torch.tensor(a["edge_l0"], dtype=torch.float64, device=dev)
+    d_eoff = torch.tensor(a["edge_wrap"], dtype=torch.int8, device=dev)
+    d_tri = torch.tensor(a["tri_hjk"].reshape(-1), dtype=torch.int32, device=dev)
+    d_toff = torch.tensor(a["tri_wrap"].reshape(-1), dtype=torch.int8, device=dev)
+    d_fc = torch.tensor(fc, dtype=torch.uint8, device=dev)
+    fcut = 1e-10 / np.sqrt(2 * N)
+    m = oracle.Model(a, 1.0, 1e-3, fc)
+
+    def step(model):
+        nonlocal x
+        x = oracle.affine_displace(x, a["miny"], H, 0.01 * H, 0.0)
+        d_pos.copy_(torch.tensor(x.reshape(-1), dtype=torch.float64, device=dev))
+        torch.cuda.synchronize()
+        st, rep, steps = nr.run_fire_md(2 * N, len(a["edge_l0"]), len(a["tri_hjk"]), a["offset"], 1.0, 1e-3,
+                                        d_pos.data_ptr(), d_vel.data_ptr(), d_f.data_ptr(), d_pairs.data_ptr(),
+                                        d_len.data_ptr(), d_eoff.data_ptr(), d_tri.data_ptr(), d_toff.data_ptr(),
+                                        d_fc.data_ptr(), [0.1, 0.99, 0.1, 1.1, 0.5], 1.0, fcut, 10**6, 5)
+        xo, _, _, orep = model.fire(x, oracle.params(fcut=fcut, criterion="rms", **FIRE))
+        assert st == nr.NR_OK and steps == orep.steps
+        assert np.array_equal(d_pos.cpu().numpy().reshape(-1, 2), xo)
+        assert rep == [orep.rms_force, orep.e_stretch, orep.e_bend]
+        x = xo
+
+    for _ in range(3):
+        step(m)
+    a2 = dict(a)
+    a2["edge_l0"] = a["edge_l0"].copy()
+    a2["edge_l0"][5] *= 1.01
+    d_len[5] = float(a2["edge_l0"][5])
+    step(oracle.Model(a2, 1.0, 1e-3, fc))
