@@ -32,6 +32,7 @@ CUDA_UNITS = [
     ("fire_fp64.cu", ["--fmad=false"]),
     ("fire_mixed.cu", ["--fmad=false"]),
     ("fire_dsm.cu", ["--fmad=false"]),
+    ("fire_tile.cu", ["--fmad=false"]),
     ("api.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
     ("analysis.cu", ["--fmad=false"]),

@@ -106,7 +106,13 @@ struct DeviceSet {
     /* second stream and events for the concurrent single-CTA launch */
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    /* tiled layout of a single large network (fire_tile.cu); tile_ctas = 0:
+     * none */
+    NetTile tile{};
+    char *tile_mem = nullptr;
+    int tile_ctas = 0;
     ~DeviceSet() {
+        if (tile_mem) cudaFree(tile_mem);
         if (arena) cudaFree(arena);
         if (side) cudaStreamDestroy(side);
         if (ev_fork) cudaEventDestroy(ev_fork);
@@ -176,6 +182,105 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
     o.dsm_tent = img.put(dtent.data(), dtent.size());
 }
 
+/* Networks of at least NR_TILE_MIN_NODES nodes (default 131072) relaxed
+ * alone in mixed precision use the tiled kernel, tiles of about
+ * NR_TILE_NODES nodes (default 1024). */
+static int tile_min_nodes() {
+    const char *env = getenv("NR_TILE_MIN_NODES");
+    return env ? std::max(1, atoi(env)) : 131072;
+}
+static int tile_target_nodes() {
+    const char *env = getenv("NR_TILE_NODES");
+    const int v = env ? atoi(env) : 1024;
+    return v >= 64 && v <= 8192 ? v : 1024;
+}
+
+/* Builds and uploads the tiled layout of network 0 of S (one allocation);
+ * leaves S.tile_ctas = 0 when the network does not fit its encoding or the
+ * kernel cannot launch. */
+static int build_tile_set(const nr_host_network &h, const Incidence &inc, DeviceSet &S, cudaStream_t stream) {
+    int dev = 0, sms = 0;
+    NR_CUDA_TRY(cudaGetDevice(&dev));
+    NR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const NetDev &d = S.dev[0];
+    TileHost th;
+    /* two CTAs per SM is the design point (tiles of ~1000 nodes fit twice) */
+    if (build_tile_layout(h, inc, d.use_bonds != 0, d.use_triples != 0, 2 * sms, tile_target_nodes(), th) != NR_OK)
+        return NR_OK;
+    NetTile &tl = S.tile;
+    tl = NetTile{};
+    tl.n_tiles = th.n_tiles;
+    tl.max_nodes = th.max_nodes;
+    tl.max_bonds = th.max_bonds;
+    tl.max_tris = th.max_tris;
+    const int ctas = tile_grid_ctas(tile_smem(tl));
+    if (ctas < 1) {
+        cudaGetLastError();
+        return NR_OK;
+    }
+    Image img;
+    const size_t o_node_off = img.put(th.node_off.data(), th.node_off.size());
+    const size_t o_n_own = img.put(th.n_own.data(), th.n_own.size());
+    const size_t o_n_halo = img.put(th.n_halo.data(), th.n_halo.size());
+    const size_t o_own_off = img.put(th.own_off.data(), th.own_off.size());
+    const size_t o_bond_off = img.put(th.bond_off.data(), th.bond_off.size());
+    const size_t o_tri_off = img.put(th.tri_off.data(), th.tri_off.size());
+    const size_t o_inc_off = img.put(th.inc_off.data(), th.inc_off.size());
+    const size_t o_node = img.put(th.node.data(), th.node.size());
+    const size_t o_bref = img.put(th.bref.data(), th.bref.size());
+    const size_t o_tref = img.put(th.tref.data(), th.tref.size());
+    const size_t o_bid = img.put(th.bid.data(), th.bid.size());
+    const size_t o_tid = img.put(th.tid.data(), th.tid.size());
+    const size_t o_iptr = img.put(th.iptr.data(), th.iptr.size());
+    const size_t o_inc = img.put(th.inc.data(), th.inc.size());
+    const size_t nb = th.bid.size(), nt = th.tid.size(), nn = (size_t)d.n;
+    const size_t o_mb = img.add(sizeof(float4) * nb), o_sk = img.add(sizeof(float2) * nb);
+    const size_t o_arms = img.add(sizeof(float4) * nt), o_pk = img.add(sizeof(float2) * nt);
+    const size_t o_u1 = img.add(sizeof(float4) * nn), o_v1 = img.add(sizeof(float2) * nn),
+                 o_f1 = img.add(sizeof(float2) * nn);
+    const size_t o_cpart = img.add(sizeof(float) * 5 * 2 * (size_t)ctas);
+    const size_t o_dpart = img.add(sizeof(double) * 2 * (size_t)ctas);
+    const size_t o_bar = img.add(sizeof(unsigned long long));
+    cudaError_t e = cudaMalloc((void **)&S.tile_mem, img.bytes.size());
+    if (e != cudaSuccess) {
+        S.tile_mem = nullptr;
+        return fail(e == cudaErrorMemoryAllocation ? NR_ERR_OOM : NR_ERR_CUDA,
+                    std::string("cudaMalloc (tile layout): ") + cudaGetErrorString(e));
+    }
+    NR_CUDA_TRY(cudaMemcpyAsync(S.tile_mem, img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    char *b = S.tile_mem;
+    tl.node_off = (const int *)(b + o_node_off);
+    tl.n_own = (const int *)(b + o_n_own);
+    tl.n_halo = (const int *)(b + o_n_halo);
+    tl.own_off = (const int *)(b + o_own_off);
+    tl.bond_off = (const int *)(b + o_bond_off);
+    tl.tri_off = (const int *)(b + o_tri_off);
+    tl.inc_off = (const int *)(b + o_inc_off);
+    tl.node = (const int *)(b + o_node);
+    tl.bref = (const unsigned *)(b + o_bref);
+    tl.tref = (const uint2 *)(b + o_tref);
+    tl.bid = (const int *)(b + o_bid);
+    tl.tid = (const int *)(b + o_tid);
+    tl.iptr = (const unsigned short *)(b + o_iptr);
+    tl.inc = (const unsigned short *)(b + o_inc);
+    tl.mb = (float4 *)(b + o_mb);
+    tl.sk = (float2 *)(b + o_sk);
+    tl.arms = (float4 *)(b + o_arms);
+    tl.pk = (float2 *)(b + o_pk);
+    tl.u[0] = d.u;
+    tl.v[0] = d.vf;
+    tl.f[0] = d.ff;
+    tl.u[1] = (float4 *)(b + o_u1);
+    tl.v[1] = (float2 *)(b + o_v1);
+    tl.f[1] = (float2 *)(b + o_f1);
+    tl.cpart = (float *)(b + o_cpart);
+    tl.dpart = (double *)(b + o_dpart);
+    tl.bar = (unsigned long long *)(b + o_bar);
+    S.tile_ctas = ctas;
+    return NR_OK;
+}
+
 static int build_set(int n, const nr_host_network *const *nets, const double *ks, const double *kb,
                      const unsigned char *const *fcodes_in, cudaStream_t stream, DeviceSet &S) {
     if (n <= 0) return fail(NR_ERR_INVALID, "network count must be positive");
@@ -211,6 +316,8 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     S.dsm.assign(n, NetDsm{});
     S.gel.assign(n, NetGel{});
     std::vector<NetOff> off(n);
+    const bool want_tile = n == 1 && nets[0]->n_points >= tile_min_nodes();
+    Incidence inc0;
     for (int i = 0; i < n; ++i) {
         const nr_host_network &h = *nets[i];
         memcpy(img.bytes.data() + x_off + sizeof(double2) * S.node_off[i], h.points.data(),
@@ -285,6 +392,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.eent = img.put(eent.data(), eent.size());
         o.partner = img.put(partner.data(), partner.size());
         build_dsm_layout(h, inc, img, o, S.dsm[i]);
+        if (want_tile && i == 0) inc0 = std::move(inc);
         if (S.dsm[i].bsub <= 0) S.dsm_ok = false;
         S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
@@ -398,6 +506,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         NR_CUDA_TRY(launch_inv_mats((const double *)S.dev[i].x, (const int *)S.gel[i].elem, 4, S.dev[i].n_elems,
                                     S.gel[i].elem_inv, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (want_tile) return build_tile_set(*nets[0], inc0, S, stream);
     return NR_OK;
 }
 
@@ -465,6 +574,8 @@ struct GridPlan {
     int *queue;
     int blocks, energy_blocks, cluster;
     bool mixed;
+    bool tile;   /* mixed: the tiled kernel (fire_tile.cu) */
+    NetTile tl;
 };
 
 /* Mixed precision, one network: up to kMixedCtaNodes nodes the whole
@@ -495,8 +606,14 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
     g.queue = S.queue;
     g.mixed = mixed;
     g.cluster = 0;
+    g.tile = false;
     const int sms = sm_count();
-    if (mixed) {
+    const char *mk = getenv("NR_MIX_KERNEL");
+    if (mixed && S.tile_ctas > 0 && !(mk && strcmp(mk, "grid") == 0)) {
+        g.tile = true;
+        g.tl = S.tile;
+        g.blocks = S.tile_ctas;
+    } else if (mixed) {
         g.blocks = mixed_grid_blocks(g.d.n);
         if (g.blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
         if ((size_t)5 * g.blocks > (size_t)4 * g.d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
@@ -528,7 +645,8 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
  * capture records it into a graph. */
 static int enqueue_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream_t stream) {
     NR_CUDA_TRY(cudaMemsetAsync(g.d.st, 0, sizeof(FireState), stream));
-    if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    if (g.tile) NR_CUDA_TRY(launch_mixed_tile(g.d, g.tl, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    else if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
     else if (g.cluster > 0) {
         /* the cluster kernel takes its energies itself */
         NR_CUDA_TRY(launch_fp64_cluster(g.d_dev, 1, g.cluster, g.d.use_gel != 0, to_dev(prm), g.queue, nullptr,

@@ -5,7 +5,11 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "nr_device.cuh"
+
+struct nr_host_network;
 
 namespace nr {
 
@@ -73,6 +77,23 @@ cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int 
 /* (launch_mixed_dsm: cap > 0 limits the number of clusters launched.)
  * Clusters of the given plan that fit the GPU at once. */
 cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out);
+/* Host arrays of a NetTile layout (fire_tile.cu). */
+struct TileHost {
+    int n_tiles = 0, max_nodes = 0, max_bonds = 0, max_tris = 0;
+    std::vector<int> node_off, n_own, n_halo, own_off, bond_off, tri_off, inc_off, node, bid, tid;
+    std::vector<unsigned> bref;
+    std::vector<uint2> tref;
+    std::vector<unsigned short> iptr, inc;
+};
+struct Incidence;
+/* The tiled mixed-precision kernel for one large network: layout, launch
+ * width (co-resident CTAs for its shared memory) and launch. */
+int build_tile_layout(const ::nr_host_network &h, const Incidence &inc, bool use_bonds, bool use_triples,
+                      int ctas, int target_nodes, TileHost &out);
+size_t tile_smem(const NetTile &tl);
+int tile_grid_ctas(size_t smem);
+cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas,
+                              unsigned long long budget_ns, cudaStream_t stream);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,
                               cudaStream_t stream);

@@ -108,7 +108,7 @@ struct NetDev {
     double2 *bfrc;  /* FP64 path: force of every bond on its first endpoint */
     double4 *tfrc;  /* FP64 path: (F_j, F_k) of every triple */
     double *part;   /* 4 * n_units partial sums (P, V2, F2, maxF2) */
-    double *epart;  /* 3 * max(bond, triple, element tiles) energy partials */
+    double *epart;  /* kEpartLists * max(bond, triple, element tiles) energy partials */
     FireState *st;
     /* gel coupling (network_mesh_relax.cu), read only when use_gel; kept
      * behind one pointer so the descriptor the mixed-precision kernels
@@ -150,6 +150,49 @@ struct NetDsm {
     const int *bidx;                          /* per bond slot: bond index */
     const int4 *tref;                         /* per triple slot: references of h, j, k; triple index */
     const int *bent, *tent;
+};
+
+/* Layout of one large network for the tiled mixed-precision kernel
+ * (fire_tile.cu).  Nodes are binned into spatial tiles; a tile lists its own
+ * nodes (ascending index) and then its halo: the other nodes that the
+ * tile's items reach.  The tile's items are every bond with an endpoint and
+ * every triple with a node among its own nodes (ascending global index; an
+ * item on a tile boundary belongs to every tile it touches and is evaluated
+ * by each of them).  Everything a tile reads in a FIRE step is stored
+ * tile-major, so a step streams through it:
+ *   node_off[t] .. node_off[t] + n_own[t] + n_halo[t]   node ids (own, then halo)
+ *   bond_off[t] .. bond_off[t+1]   bond items: local node refs {i, j}, anchor
+ *                                  record {ra hi, lo}, {|ra| - l0, k}, bond id
+ *   tri_off[t]  .. tri_off[t+1]    triple items: local refs {h, j, k},
+ *                                  anchor arms, {theta_a - pi, kb}, triple id
+ *   inc_off[t]  .. per own node its entries in the canonical incidence
+ *                                  order (bonds, then triples): bond entry
+ *                                  slot << 1 | role, triple entry 0x8000 |
+ *                                  slot << 2 | role (slots local to the tile);
+ *                                  node k of the tile's own nodes has entries
+ *                                  iptr[own_off[t] + t + k] .. [.. + k + 1]
+ *                                  (offsets relative to inc_off[t])
+ * State of a step is double buffered ({u, v, F} read from one copy and the
+ * next step's written to the other), so a tile may recompute the drift of
+ * its halo nodes from the step's inputs while their owners write theirs. */
+struct NetTile {
+    int n_tiles, max_nodes, max_bonds, max_tris; /* max_nodes: own + halo */
+    const int *node_off, *n_own, *n_halo, *own_off, *bond_off, *tri_off, *inc_off;
+    const int *node;          /* node ids */
+    const unsigned *bref;     /* per bond item: local i | local j << 16 */
+    const uint2 *tref;        /* per triple item: local h | local j << 16, local k */
+    const int *bid, *tid;     /* global bond / triple id of each item */
+    float4 *mb;               /* per bond item: anchor vector i -> j, {hi.x, hi.y, lo.x, lo.y} */
+    float2 *sk;               /* per bond item: {|ra| - l0, k} */
+    float4 *arms;             /* per triple item: anchor arms {a.x, a.y, b.x, b.y} */
+    float2 *pk;               /* per triple item: {theta_a - pi, kb} */
+    const unsigned short *iptr; /* per own node (tile-major): first entry, relative to inc_off; n_own + 1 per tile */
+    const unsigned short *inc;  /* incidence entries */
+    float4 *u[2];             /* double-buffered state, by node */
+    float2 *v[2], *f[2];
+    float *cpart;             /* per CTA step totals (5 floats each) */
+    double *dpart;            /* per CTA FP64 anchor totals (2 doubles each) */
+    unsigned long long *bar;  /* grid barrier counter (monotonic) */
 };
 
 /* ----- reductions ----- */

@@ -1,5 +1,5 @@
 """Converged FP64 reference energies for the 512-network uneven batch
-(config C4), written to c4_oracle_tight.json.
+(config C4), written to c4_oracle_polish.json.
 
 A FIRE run stopped at max|F| < 1e-10 is not at the energy minimum: on the
 softest networks of the batch the FP64 oracle's own energy at that point is
@@ -16,7 +16,7 @@ as the largest node displacement, the oracle's max|F| < 1e-10 state lies
 from the converged one.  The first
 stage reproduces c4_oracle.json exactly (checked).  CPU only (about an hour
 on 8 cores):
-    python tests/golden/make_c4_oracle_tight.py [threads]
+    python tests/golden/make_c4_oracle_polish.py [threads]
 """
 import json
 import os
@@ -53,15 +53,18 @@ def main():
                                    threads)
     wall = time.time() - t
     rows = []
-    for x1, x2, r1, r2 in zip(xs, xs2, reps, reps2):
+    for i, (x1, x2, r1, r2) in enumerate(zip(xs, xs2, reps, reps2)):
         # the oracle's own distance, at max|F| < 1e-10, from the converged
-        # state: largest node displacement, in lattice spacings
+        # state: relative energy and largest node displacement (lattice
+        # spacings)
         dx = float(np.sqrt(((x1 - x2) ** 2).sum(1)).max())
-        rows.append(dict(steps_polish=r2.steps, converged=r2.converged, e_stretch=r2.e_stretch.hex(),
-                         e_bend=r2.e_bend.hex(), max_force=r2.max_force, dx_max_at_1e_10=dx))
+        e1, e2 = r1.e_stretch + r1.e_bend, r2.e_stretch + r2.e_bend
+        rows.append(dict(index=i, steps_polish=r2.steps, converged=r2.converged, e_stretch=r2.e_stretch.hex(),
+                         e_bend=r2.e_bend.hex(), max_force=r2.max_force, rel_change=(e1 - e2) / e2,
+                         dx_max_at_1e_10=dx))
     out = {"fcut": FCUT_TIGHT, "criterion": "max", "start": "c4_oracle.json states (max|F| < 1e-10)",
            "threads": threads, "wall_s": wall, "networks": rows}
-    with open(os.path.join(HERE, "c4_oracle_tight.json"), "w") as f:
+    with open(os.path.join(HERE, "c4_oracle_polish.json"), "w") as f:
         json.dump(out, f, indent=0)
     print("C4 converged oracle: %d networks, %.0f s on %d threads" % (len(rows), wall, threads))
 

@@ -12,9 +12,22 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 FIRE = dict(alpha0=0.1, falpha=0.99, dt_max=0.1, finc=1.1, fdec=0.5, nmin=5, mass=1.0)
-# Both runs stop at max|F| < 1e-10 from different trajectories; their
-# energies differ by O(|F|^2 / lambda_min).
-ENERGY_RTOL = 1e-8
+# Both runs stop at max|F| < 1e-10 from different trajectories.  The bar is
+# 1e-10 relative to the FP64 oracle's energy, plus ten times the oracle's own
+# distance from the converged minimum (its relaxation continued from that
+# state to max|F| < 1e-13): on soft networks the energy at max|F| < 1e-10 is
+# not settled to 1e-10 in either precision (E - E_min ~ |F|^2 / (2 lambda)
+# with lambda the softest stiffness), and the mixed path must stop as close to
+# the minimum as the FP64 path does, within that factor.
+ENERGY_RTOL = 1e-10
+UNSETTLED_FACTOR = 10.0
+
+
+def energy_bar(m, x_or, e_or, fire=None):
+    """Allowed |E_mixed - E_or| for the oracle state x_or of energy e_or."""
+    _, _, _, r = m.fire(x_or, oracle.params(fcut=1e-13, criterion="max", **(fire or FIRE)))
+    e_star = r.e_stretch + r.e_bend
+    return ENERGY_RTOL * abs(e_or) + UNSETTLED_FACTOR * abs(e_or - e_star)
 
 
 def batch_case(n_nets, seed, L_range=(8, 40), jitter=0.0):
@@ -52,16 +65,24 @@ def test_mixed_batch_certified_and_matches_fp64_oracle(cuda, jitter):
         assert es == r.e_stretch and eb == r.e_bend
         H = a["maxy"] - a["miny"]
         x0 = oracle.affine_displace(a["points"], a["miny"], H, gam[i] * H, 0.0)
-        _, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
+        x_or, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
         e_or = orep.e_stretch + orep.e_bend
-        assert abs(es + eb - e_or) <= ENERGY_RTOL * e_or
+        assert abs(es + eb - e_or) <= energy_bar(m, x_or, e_or)
         # the anchor is re-taken rarely: FP64 evaluations are a small
         # fraction of the iterations
         assert r.fp64_steps <= max(20, r.steps // 50)
 
 
-def test_mixed_single_network_grid_kernel(cuda):
-    """A network above the one-CTA size runs on the cooperative kernel."""
+@pytest.mark.parametrize("kernel", ["grid", "tile"])
+def test_mixed_single_network_grid_kernel(cuda, kernel, monkeypatch):
+    """A network above the one-CTA size runs on a cooperative kernel over the
+    whole GPU: the grid kernel (four passes per step) or the tiled one (one
+    grid barrier per step; forced here on a small network, so its tiles are
+    small and most items lie on tile boundaries)."""
+    if kernel == "grid":
+        monkeypatch.setenv("NR_MIX_KERNEL", "grid")
+    else:
+        monkeypatch.setenv("NR_TILE_MIN_NODES", "5000")
     h = nr.HostNetwork.lattice(80, 80, 0.8, 0.0, 5).get_triples()
     a = h.arrays()
     H = a["maxy"] - a["miny"]
@@ -73,9 +94,9 @@ def test_mixed_single_network_grid_kernel(cuda):
     m = oracle.Model(a, 1.0, 1e-2)
     assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
     x0 = oracle.affine_displace(a["points"], a["miny"], H, 0.02 * H, 0.0)
-    _, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
+    x_or, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **FIRE))
     e_or = orep.e_stretch + orep.e_bend
-    assert abs(rep.e_stretch + rep.e_bend - e_or) <= ENERGY_RTOL * e_or
+    assert abs(rep.e_stretch + rep.e_bend - e_or) <= energy_bar(m, x_or, e_or)
 
 
 def test_mixed_step_cap_reports_fp64_state(cuda):
@@ -195,3 +216,44 @@ def test_sweep_graph_mixed_grid_equals_step_by_step(cuda):
     assert [key(r) for r in recs] == [key(r) for r in precs]
     assert all(r.status == nr.NR_OK and r.max_force < 1e-10 for r in recs)
     assert np.array_equal(pos, ppos)
+
+
+@pytest.mark.parametrize("case", ["jitter", "mikado"])
+def test_mixed_tile_kernel_certified(cuda, case, monkeypatch):
+    """The tiled kernel on a jittered lattice with generator triples (rest
+    angles) and on a Mikado network (per-bond k, per-triple kb, wraps):
+    every state certified by the oracle's FP64 force, energies within the
+    bar, and the tiled sweep as one CUDA graph equal to the step-by-step
+    sweep."""
+    monkeypatch.setenv("NR_TILE_MIN_NODES", "1000")
+    monkeypatch.setenv("NR_TILE_NODES", "128")
+    if case == "jitter":
+        h = nr.HostNetwork.lattice(70, 70, 0.8, 0.05, 17, line_triples=True)
+        ks, kb, fire = 1.0, 1e-2, dict(FIRE)
+    else:
+        h = nr.HostNetwork.mikado(1400, 0.1, 1.0, 1e-3, 8)
+        ks, kb = 1.0, 1.0
+        fire = dict(FIRE, dt_max=0.05 * float(np.sqrt(h.arrays()["edge_l0"].min())))
+    a = h.arrays()
+    assert len(a["points"]) > 4096  # above the one-CTA size: a grid-wide kernel
+    H = a["maxy"] - a["miny"]
+    net = nr.Network(h, ks, kb)
+    net.affine_displace(a["miny"], H, 0.02 * H, 0.0)
+    prm = nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **fire)
+    rep = net.relax(prm)
+    assert rep.status == nr.NR_OK and rep.max_force < 1e-10
+    x = net.positions()
+    m = oracle.Model(a, ks, kb)
+    assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
+    assert m.energies(x) == (rep.e_stretch, rep.e_bend)
+    x0 = oracle.affine_displace(a["points"], a["miny"], H, 0.02 * H, 0.0)
+    x_or, _, _, orep = m.fire(x0, oracle.params(fcut=1e-10, criterion="max", **fire))
+    e_or = orep.e_stretch + orep.e_bend
+    assert abs(rep.e_stretch + rep.e_bend - e_or) <= energy_bar(m, x_or, e_or, fire)
+    # the sweep, captured as one graph, equals the step-by-step sweep
+    net2 = nr.Network(h, ks, kb)
+    r1, p1 = net2.sweep((0.0, 0.0, 0.0), (0.01, 0.02, 0.01), prm, keep_positions=True)
+    net3 = nr.Network(h, ks, kb)
+    r2, p2 = net3.sweep((0.0, 0.0, 0.0), (0.01, 0.02, 0.01), prm, keep_positions=True, graph=True)
+    assert [(r.e_stretch, r.e_bend, r.steps) for r in r1] == [(r.e_stretch, r.e_bend, r.steps) for r in r2]
+    assert all(np.array_equal(u, w) for u, w in zip(p1, p2))
