@@ -278,7 +278,10 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
-    ap.add_argument("--workload", default="C4", choices=["C4", "C2", "C3", "C5", "M1", "L1", "A1", "IO", "S1"],
+    ap.add_argument("--strain-steps", type=int, default=0,
+                    help="P3/P5: run the first K strain steps of the protocol (default: all)")
+    ap.add_argument("--workload", default="C4",
+                    choices=["C4", "C2", "C3", "C5", "M1", "L1", "A1", "IO", "S1", "P3", "P5"],
                     help="C4: the 512-network batch (the headline); C2/C3/C5: one large network on the whole GPU, "
                          "first strain increment of its protocol, FIRE steps capped by --max-steps; M1: the same "
                          "for a network embedded in a gel (network_mesh_relax.cu, FP64 path); L1: the linear-response "
@@ -318,6 +321,8 @@ def main():
         return io_arm(args)
     if args.workload == "S1":
         return sweep_arm(args)
+    if args.workload in PROTOCOLS:
+        return protocol_arm(args)
     if args.workload != "C4":
         return single_network_arm(args)
 
@@ -771,6 +776,105 @@ def sweep_arm(args):
         line["cpu_baseline"] = {"value": len(orecs) / dt, "unit": "strain steps/s", "cores": 1, "kind": "port",
                                 "sample": "the oracle's whole sweep, %d shear steps (%.1f s)" % (len(orecs), dt)}
     print(json.dumps(line))
+    return 0
+
+
+# The strain protocols of configs C5 and C3 (do_relaxation_run's loops,
+# large_strain_relax.cu:924-999): network, compression and shear ranges.
+PROTOCOLS = {
+    "P5": dict(net="C5", compr=(0.0, 0.0, 0.0), shear=(0.0025, 0.5, 0.0025),
+               what="C5 network, quasi-static simple shear to gamma = 0.5 in 200 warm-started steps"),
+    "P3": dict(net="C3", compr=(0.01, 0.2, 0.01), shear=(0.0, 0.0, 0.0),
+               what="C3 Mikado network, uniaxial compression to 0.2 in 20 warm-started steps"),
+}
+
+
+def protocol_arm(args):
+    """--workload P5|P3: the strain protocol of C5 / C3 run end to end as
+    one CUDA graph per precision (nr_sweep_graph: affine increment, FIRE
+    relaxation to max|F| < 1e-10 (capped at --fire-cap steps), energies and
+    stress per step, no host round trip), mixed precision (the tiled kernel)
+    and FP64 (the grid kernel) side by side from the same start.  Reports
+    both curves (energy and stress per strain step), the mixed-vs-FP64 error
+    of each converged step, wall times and the mixed kernel's algorithmic
+    HBM throughput.  --strain-steps K runs the protocol's first K steps."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    pr = PROTOCOLS[args.workload]
+    h, kb, dt_max = single_network(nr, pr["net"])
+    info = h.info()
+    compr, shear = list(pr["compr"]), list(pr["shear"])
+    k = args.strain_steps
+    if k > 0:  # truncate the protocol to its first k steps
+        for rng in (compr, shear):
+            if rng[1] > 0 and rng[2] > 0:
+                n_here = int(round((rng[1] - rng[0]) / rng[2])) + 1
+                take = min(n_here, k)
+                rng[1] = rng[0] + (take - 1) * rng[2]
+                k -= take
+            elif rng[1] > 0:
+                k -= 1
+            if k <= 0 and rng is compr:
+                shear[1] = 0.0
+                break
+    cap = min(args.max_steps, args.fire_cap) if args.fire_cap != 2000 else args.max_steps
+    stream = torch.cuda.current_stream()
+    out = {}
+    for prec in ("mixed", "fp64"):
+        net = nr.Network(h, 1.0, kb)
+        x0 = net.positions()
+        prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
+                             max_steps=cap, criterion="max", precision=prec)
+        net.set_positions(x0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        recs, _ = net.sweep(compr, shear, prm, graph=True, stream=stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        out[prec] = (e0.elapsed_time(e1), recs)
+        net.close()
+    ms_m, rm = out["mixed"]
+    ms_d, rd = out["fp64"]
+    n = info.n_points
+    bpn = 73 + 24 * info.n_edges / n + 12 * info.n_triples / n
+    fire_m = sum(r.steps for r in rm)
+    achieved = bpn * n * fire_m / (ms_m / 1e3) / 1e9
+    hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
+           if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
+    both = [(a, b) for a, b in zip(rm, rd) if a.status == 0 and b.status == 0]
+    e_err = [abs((a.e_stretch + a.e_bend) - (b.e_stretch + b.e_bend)) / abs(b.e_stretch + b.e_bend) for a, b in both]
+    sxy_err = [abs(a.stress_xy - b.stress_xy) / max(abs(b.stress_xy), 1e-300) for a, b in both]
+    syy_err = [abs(a.stress_yy - b.stress_yy) / max(abs(b.stress_yy), 1e-300) for a, b in both]
+
+    def curve(rs):
+        return [{"strain": (r.curr_disp if r.is_shear else r.max_comp) / (info.maxy - info.miny),
+                 "fire_steps": r.steps, "status": r.status, "energy": r.e_stretch + r.e_bend,
+                 "stress_xy": r.stress_xy, "stress_yy": r.stress_yy} for r in rs]
+
+    print(json.dumps({
+        "metric": "strain steps/s of the %s protocol, mixed precision, one CUDA graph" % args.workload,
+        "value": len(rm) / (ms_m / 1e3), "unit": "strain steps/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": ms_m, "higher_is_better": True, "scaling": "replicas", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "%s: %s; N=%d E=%d T=%d; FIRE to max|F|<1e-10, at most %d steps per strain step"
+                               % (args.workload, pr["what"], n, info.n_edges, info.n_triples, cap),
+                   "strain_steps_run": len(rm), "compression": compr, "shear": shear},
+        "fp64": {"value": len(rd) / (ms_d / 1e3), "ms_per_protocol": ms_d, "fire_steps": sum(r.steps for r in rd)},
+        "mixed_fire_steps": fire_m, "us_per_fire_step_mixed": 1e3 * ms_m / max(1, fire_m),
+        "us_per_fire_step_fp64": 1e3 * ms_d / max(1, sum(r.steps for r in rd)),
+        "converged_both": len(both),
+        "mixed_vs_fp64": {"energy_rel_max": max(e_err) if e_err else None,
+                          "stress_xy_rel_max": max(sxy_err) if sxy_err else None,
+                          "stress_yy_rel_max": max(syy_err) if syy_err else None},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_fire_tile_mixed (mixed sweep)"},
+        "curve_mixed": curve(rm), "curve_fp64": curve(rd),
+        "gpu_launches": 4 * (len(rm) + len(rd)),
+    }))
     return 0
 
 
