@@ -33,6 +33,7 @@ CUDA_UNITS = [
     ("fire_mixed.cu", ["--fmad=false"]),
     ("fire_dsm.cu", ["--fmad=false"]),
     ("fire_tile.cu", ["--fmad=false"]),
+    ("fire_dsm64.cu", ["--fmad=false"]),
     ("api.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
     ("analysis.cu", ["--fmad=false"]),

@@ -120,7 +120,7 @@ struct DeviceSet {
     }
 };
 
-/* Sub-block layout of one network for the distributed-shared-memory kernel
+/* Sub-block layout of one network for the distributed-shared-memory kernels
  * (NetDsm, nr_device.cuh): item slots grouped by the sub-block of the
  * bond's node i / the triple's hinge, in index order within a group; node
  * references and resolved incidence entries.  m.bsub = 0 when the network
@@ -128,7 +128,10 @@ struct DeviceSet {
 static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Image &img, NetOff &o, NetDsm &m) {
     const int n = h.n_points, ne = h.n_edges(), nt = h.n_triples();
     memset(&m, 0, sizeof(m));
-    const int bsub = (n + kDsmParts - 1) / kDsmParts;
+    /* sub-blocks of a whole number of 32-node chunks: a CTA's nodes then
+     * start on a chunk boundary, which the FP64 cluster kernel's canonical
+     * reduction (32-node units) needs */
+    const int bsub = kChunk * ((n + kDsmParts * kChunk - 1) / (kDsmParts * kChunk));
     const bool fits = n <= (1 << 20) && bsub <= 0xffff;
     auto part = [&](int v) { return v / bsub; };
     auto ref = [&](int v) { return (part(v) << 16) | (v % bsub); };
@@ -576,7 +579,49 @@ struct GridPlan {
     bool mixed;
     bool tile;   /* mixed: the tiled kernel (fire_tile.cu) */
     NetTile tl;
+    /* FP64 on a cluster: the distributed-shared-memory kernel (dsm64) with
+     * its per-CTA maxima, else the L2 one */
+    bool dsm64;
+    const NetDsm *m_dev;
+    int bmax, emax, tmax;
 };
+
+/* Per-CTA maxima of the FP64 distributed-shared-memory kernel for clusters
+ * of C CTAs over the networks `subset` of S (all when null); false when the
+ * set has no sub-block layout or its state does not fit shared memory. */
+static bool fp64_dsm_plan(const DeviceSet &S, int C, int &bmax, int &emax, int &tmax,
+                          const std::vector<int> *subset = nullptr) {
+    if (!S.dsm_ok || C < 1 || C > kDsmParts) return false;
+    const int spr = kDsmParts / C;
+    bmax = emax = tmax = 0;
+    const int count = subset ? (int)subset->size() : S.n_nets;
+    for (int j = 0; j < count; ++j) {
+        const int i = subset ? (*subset)[j] : j;
+        const NetDsm &m = S.dsm[i];
+        const NetDev &d = S.dev[i];
+        if (d.use_gel) return false;
+        bmax = std::max(bmax, spr * m.bsub);
+        for (int r = 0; r < C; ++r) {
+            if (d.use_bonds) emax = std::max(emax, m.bo[(r + 1) * spr] - m.bo[r * spr]);
+            if (d.use_triples) tmax = std::max(tmax, m.to[(r + 1) * spr] - m.to[r * spr]);
+        }
+    }
+    int active = 0;
+    if (dsm64_max_active(C, std::max(bmax, 1), std::max(emax, 1), std::max(tmax, 1), &active) != cudaSuccess ||
+        active < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+/* NR_FP64_KERNEL: dsm (default), l2 (k_fire_cluster) or grid. */
+static int fp64_kernel_choice() {
+    const char *env = getenv("NR_FP64_KERNEL");
+    if (env && strcmp(env, "l2") == 0) return 1;
+    if (env && strcmp(env, "grid") == 0) return 2;
+    return 0;
+}
 
 /* Mixed precision, one network: up to kMixedCtaNodes nodes the whole
  * relaxation runs in one CTA with u in shared memory (no grid barriers);
@@ -607,6 +652,9 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
     g.mixed = mixed;
     g.cluster = 0;
     g.tile = false;
+    g.dsm64 = false;
+    g.m_dev = S.dsm_array + i;
+    g.bmax = g.emax = g.tmax = 0;
     const int sms = sm_count();
     const char *mk = getenv("NR_MIX_KERNEL");
     if (mixed && S.tile_ctas > 0 && !(mk && strcmp(mk, "grid") == 0)) {
@@ -618,11 +666,17 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
         if (g.blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
         if ((size_t)5 * g.blocks > (size_t)4 * g.d.n_tiles * 8) return fail(NR_ERR_CAPACITY, "reduction scratch too small");
     } else {
-        if (g.d.n <= fp64_cluster_nodes()) {
+        const int choice = fp64_kernel_choice();
+        if (g.d.n <= fp64_cluster_nodes() && choice != 2) {
             int c = fp64_cluster_ctas(), active = 0;
-            while (c > 1 && (fp64_cluster_max_active(c, g.d.use_gel != 0, &active) != cudaSuccess || active < 1)) {
-                cudaGetLastError();
-                c /= 2;
+            const std::vector<int> one{i};
+            if (choice == 0 && fp64_dsm_plan(S, c, g.bmax, g.emax, g.tmax, &one)) {
+                g.dsm64 = true;
+            } else {
+                while (c > 1 && (fp64_cluster_max_active(c, g.d.use_gel != 0, &active) != cudaSuccess || active < 1)) {
+                    cudaGetLastError();
+                    c /= 2;
+                }
             }
             g.cluster = c;
             g.blocks = c;
@@ -648,9 +702,13 @@ static int enqueue_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream
     if (g.tile) NR_CUDA_TRY(launch_mixed_tile(g.d, g.tl, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
     else if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
     else if (g.cluster > 0) {
-        /* the cluster kernel takes its energies itself */
-        NR_CUDA_TRY(launch_fp64_cluster(g.d_dev, 1, g.cluster, g.d.use_gel != 0, to_dev(prm), g.queue, nullptr,
-                                        stream));
+        /* the cluster kernels take their energies themselves */
+        if (g.dsm64)
+            NR_CUDA_TRY(launch_fp64_dsm(g.d_dev, g.m_dev, 1, g.cluster, g.bmax, g.emax, g.tmax, to_dev(prm), g.queue,
+                                        nullptr, stream));
+        else
+            NR_CUDA_TRY(launch_fp64_cluster(g.d_dev, 1, g.cluster, g.d.use_gel != 0, to_dev(prm), g.queue, nullptr,
+                                            stream));
         return NR_OK;
     } else NR_CUDA_TRY(launch_fp64_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), barrier_stall(), stream));
     NR_CUDA_TRY(launch_energies(g.d, g.energy_blocks, stream));
@@ -879,7 +937,11 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
         }
     } else {
         const int c = fp64_batch_cluster(S.max_nodes);
-        if (c > 1) {
+        int bmax = 0, emax = 0, tmax = 0;
+        if (c > 1 && fp64_kernel_choice() == 0 && fp64_dsm_plan(S, c, bmax, emax, tmax)) {
+            NR_CUDA_TRY(launch_fp64_dsm(S.dev_array, S.dsm_array, S.n_nets, c, bmax, emax, tmax, to_dev(prm), S.queue,
+                                        S.order, stream));
+        } else if (c > 1) {
             NR_CUDA_TRY(launch_fp64_cluster(S.dev_array, S.n_nets, c, false, to_dev(prm), S.queue, S.order, stream));
         } else {
             int max_blocks = 0;

@@ -46,6 +46,15 @@ cudaError_t launch_fp64_batch(const NetDev *nets_dev, int n_nets, const FirePara
 cudaError_t fp64_cluster_max_active(int cluster, bool gel, int *out);
 cudaError_t launch_fp64_cluster(const NetDev *nets_dev, int n_nets, int cluster, bool gel, const FireParamsDev &p,
                                 int *queue_dev, const int *order_dev, cudaStream_t stream);
+/* FP64 relaxation with the step's state in distributed shared memory
+ * (fire_dsm64.cu): one cluster of `cluster` CTAs per network over the
+ * NetDsm layout, per-CTA maxima of nodes, bond slots and triple slots.  The
+ * same bits as launch_fp64_grid. */
+size_t dsm64_smem_bytes(int bmax, int emax, int tmax);
+cudaError_t dsm64_max_active(int cluster, int bmax, int emax, int tmax, int *out);
+cudaError_t launch_fp64_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
+                            int emax, int tmax, const FireParamsDev &p, int *queue_dev, const int *order_dev,
+                            cudaStream_t stream);
 cudaError_t launch_forces(const NetDev &d, cudaStream_t stream);
 cudaError_t launch_affine(double2 *x, int n, double miny, double yrange, double xdisp, double ydisp,
                           cudaStream_t stream);

@@ -130,9 +130,10 @@ struct NetGel {
     const int *partner;
 };
 
-/* Layout of a network for the distributed-shared-memory cluster kernel
- * (fire_dsm.cu).  Nodes are cut into 16 sub-blocks of bsub consecutive
- * nodes; a cluster of C CTAs gives CTA r the 16/C sub-blocks
+/* Layout of a network for the distributed-shared-memory cluster kernels
+ * (fire_dsm.cu, fire_dsm64.cu).  Nodes are cut into 16 sub-blocks of bsub
+ * consecutive nodes, bsub a multiple of 32; a cluster of C CTAs gives CTA r
+ * the 16/C sub-blocks
  * [r 16/C, (r+1) 16/C), so one layout serves C = 1, 2, 4, 8, 16.  A bond
  * belongs to the sub-block of its node i, a triple to that of its hinge;
  * item slots list each sub-block's items in index order, so every CTA's

@@ -62,16 +62,19 @@ def test_affine_bitexact(cuda):
     assert np.array_equal(net.positions(), x)
 
 
-@pytest.fixture(params=["cluster16", "cluster4", "grid"])
+@pytest.fixture(params=["dsm16", "dsm4", "l2_16", "grid"])
 def fp64_kernel(request, monkeypatch):
     """The single-network FP64 kernel: one thread-block cluster of 16 or 4
-    CTAs (hardware cluster barriers; the default for small networks) or the
+    CTAs with the step's state in distributed shared memory (the default for
+    small networks), a cluster of 16 with the state in global memory, or the
     cooperative grid kernel (software grid barriers).  The same bits."""
+    kind, _, c = request.param.partition("_") if "_" in request.param else (request.param[:3], "", request.param[3:])
     if request.param == "grid":
         monkeypatch.setenv("NR_FP64_CLUSTER_NODES", "0")
     else:
         monkeypatch.setenv("NR_FP64_CLUSTER_NODES", "100000000")
-        monkeypatch.setenv("NR_FP64_CLUSTER", request.param[len("cluster"):])
+        monkeypatch.setenv("NR_FP64_CLUSTER", c)
+        monkeypatch.setenv("NR_FP64_KERNEL", "l2" if kind == "l2" else "dsm")
     return request.param
 
 
@@ -106,12 +109,16 @@ def test_step_cap_reports_not_converged(cuda, fp64_kernel):
     assert np.array_equal(net.positions(), xo)
 
 
-@pytest.mark.parametrize("team", ["1", "4", "16"])
+@pytest.mark.parametrize("team", ["1", "4", "16", "8-l2"])
 def test_batch_equals_oracle(cuda, team, monkeypatch):
     """Uneven batch: every network bit-identical to its oracle run, with one
-    CTA per network (k_fire_batch) and with thread-block clusters of 4 and
-    16 CTAs per network (k_fire_cluster)."""
-    monkeypatch.setenv("NR_FP64_BATCH_CLUSTER", team)
+    CTA per network (k_fire_batch), with thread-block clusters of 4 and 16
+    CTAs per network holding the state in distributed shared memory
+    (k_fire_dsm64), and with clusters of 8 holding it in global memory
+    (k_fire_cluster)."""
+    c, _, kind = team.partition("-")
+    monkeypatch.setenv("NR_FP64_BATCH_CLUSTER", c)
+    monkeypatch.setenv("NR_FP64_KERNEL", kind or "dsm")
     hosts, arrs, gam = [], [], []
     rng = np.random.default_rng(11)
     for i in range(12):
