@@ -521,6 +521,32 @@ int nr_energies_noalloc(int n_points, int npairs, int ntriples, double width, do
                         double *d_energies, void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Launch policy and the per-GPU tuning table                          */
+/* ------------------------------------------------------------------ */
+
+/* No reference counterpart (the reference's only launch knob is the block
+ * shape, -x/-y, large_strain_relax.cu:1053-1090).  Each launch choice made
+ * per size class -- kernel variant, CTAs per network, tile size, thresholds
+ * between kernels, threads per CTA, escalation -- reads a named knob: the
+ * environment variable of that name if set, else the loaded tuning table,
+ * else the built-in default.  The table is loaded on first use from
+ * NR_TUNING_FILE, else from tuning/<device name>.txt beside the library
+ * (written by the autotuner, network_relaxation_gb300/autotune.py, from
+ * measurements on that GPU).  Lines are "NAME value"; '#' starts a comment.
+ * nr_tuning_load replaces the table (returns the entry count, NR_ERR_IO or
+ * NR_ERR_PARSE); nr_tuning_value returns a knob's numeric value as the
+ * library sees it (NaN when unset); nr_tuning_source names the table in use
+ * ("" for none; valid until the next nr_tuning_load). */
+int nr_tuning_load(const char *path);
+double nr_tuning_value(const char *name);
+const char *nr_tuning_source(void);
+
+/* No reference counterpart: the launch plan the library picks for this
+ * network and precision (NR_FP64 / NR_MIXED) as text, e.g. "k_fire_dsm64
+ * cluster=16" (NUL-terminated, truncated to cap). */
+int nr_network_plan(nr_network *dnet, int precision, char *buf, size_t cap);
+
+/* ------------------------------------------------------------------ */
 /* Batched relaxation of many independent networks in one launch       */
 /* ------------------------------------------------------------------ */
 

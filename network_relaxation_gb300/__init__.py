@@ -329,6 +329,13 @@ class Network:
         check(self._lib.nr_energies(self._h, C.byref(es), C.byref(eb), _stream(stream)), "nr_energies")
         return es.value, eb.value
 
+    def plan(self, precision="fp64"):
+        """The launch plan the library picks for this network (nr_network_plan)."""
+        buf = C.create_string_buffer(256)
+        check(self._lib.nr_network_plan(self._h, {"fp64": NR_FP64, "mixed": NR_MIXED}[precision], buf, 256),
+              "nr_network_plan")
+        return buf.value.decode()
+
     def stress(self, stream=None):
         """(stress {xx, yy, xy}, energies {E_stretch, E_bend}) at the current
         positions: the virial of the stretch and bending forces over the

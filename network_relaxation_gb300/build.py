@@ -35,6 +35,7 @@ CUDA_UNITS = [
     ("fire_tile.cu", ["--fmad=false"]),
     ("fire_dsm64.cu", ["--fmad=false"]),
     ("api.cu", []),
+    ("tuning.cu", []),
     ("noalloc.cu", ["--fmad=false"]),
     ("analysis.cu", ["--fmad=false"]),
     ("spr.cu", ["--fmad=false"]),

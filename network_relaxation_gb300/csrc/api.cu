@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -189,11 +190,11 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
  * alone in mixed precision use the tiled kernel, tiles of about
  * NR_TILE_NODES nodes (default 1024). */
 static int tile_min_nodes() {
-    const char *env = getenv("NR_TILE_MIN_NODES");
+    const char *env = knob("NR_TILE_MIN_NODES");
     return env ? std::max(1, atoi(env)) : 131072;
 }
 static int tile_target_nodes() {
-    const char *env = getenv("NR_TILE_NODES");
+    const char *env = knob("NR_TILE_NODES");
     const int v = env ? atoi(env) : 1024;
     return v >= 64 && v <= 8192 ? v : 1024;
 }
@@ -617,7 +618,7 @@ static bool fp64_dsm_plan(const DeviceSet &S, int C, int &bmax, int &emax, int &
 
 /* NR_FP64_KERNEL: dsm (default), l2 (k_fire_cluster) or grid. */
 static int fp64_kernel_choice() {
-    const char *env = getenv("NR_FP64_KERNEL");
+    const char *env = knob("NR_FP64_KERNEL");
     if (env && strcmp(env, "l2") == 0) return 1;
     if (env && strcmp(env, "grid") == 0) return 2;
     return 0;
@@ -636,11 +637,11 @@ constexpr int kMixedCtaNodes = 4096;
  * grid barriers; beyond about ten thousand nodes the FP64 work of the step
  * needs more than 16 SMs. */
 static int fp64_cluster_nodes() {
-    const char *env = getenv("NR_FP64_CLUSTER_NODES");
+    const char *env = knob("NR_FP64_CLUSTER_NODES");
     return env ? std::max(0, atoi(env)) : 16384;
 }
 static int fp64_cluster_ctas() {
-    const char *env = getenv("NR_FP64_CLUSTER");
+    const char *env = knob("NR_FP64_CLUSTER");
     const int c = env ? atoi(env) : 16;
     return c == 1 || c == 2 || c == 4 || c == 8 || c == 16 ? c : 16;
 }
@@ -656,7 +657,7 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
     g.m_dev = S.dsm_array + i;
     g.bmax = g.emax = g.tmax = 0;
     const int sms = sm_count();
-    const char *mk = getenv("NR_MIX_KERNEL");
+    const char *mk = knob("NR_MIX_KERNEL");
     if (mixed && S.tile_ctas > 0 && !(mk && strcmp(mk, "grid") == 0)) {
         g.tile = true;
         g.tl = S.tile;
@@ -762,9 +763,9 @@ struct DsmPlan {
  * keeps them in global memory).  False when the batch has no layout,
  * NR_MIX_KERNEL=l2 asks for the global-memory kernels, or nothing fits. */
 static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl, const std::vector<int> *subset = nullptr) {
-    const char *k = getenv("NR_MIX_KERNEL");
+    const char *k = knob("NR_MIX_KERNEL");
     if (!S.dsm_ok || (k && strcmp(k, "l2") == 0)) return false;
-    const char *rk = getenv("NR_DSM_RESIDENT");
+    const char *rk = knob("NR_DSM_RESIDENT");
     const bool allow_res = !(rk && atoi(rk) == 0);
     const size_t limit = dsm_smem_limit();
     for (int C = 1; C <= kDsmParts; C *= 2) {
@@ -802,7 +803,7 @@ static bool dsm_plan(const DeviceSet &S, int forced, int least, DsmPlan &pl, con
 /* Fraction of idle clusters at which running networks escalate to clusters
  * twice as large: NR_ESCALATE (default 0.25; 0 disables). */
 static double escalate_fraction() {
-    const char *env = getenv("NR_ESCALATE");
+    const char *env = knob("NR_ESCALATE");
     const double f = env ? atof(env) : 0.25;
     return f > 0 && f <= 1 ? f : 0.0;
 }
@@ -816,7 +817,7 @@ static double escalate_fraction() {
 /* Networks of at most this many nodes run one per CTA beside the clusters
  * in the first phase (NR_SOLO_NODES; 0 disables). */
 static int solo_nodes() {
-    const char *env = getenv("NR_SOLO_NODES");
+    const char *env = knob("NR_SOLO_NODES");
     return env ? std::max(0, atoi(env)) : 2304;
 }
 
@@ -909,7 +910,7 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
  * team size, but its makespan is one soft network's 10^5-10^6 steps on its
  * team: a wider team finishes it sooner. */
 static int fp64_batch_cluster(int max_nodes) {
-    const char *env = getenv("NR_FP64_BATCH_CLUSTER");
+    const char *env = knob("NR_FP64_BATCH_CLUSTER");
     if (env) {
         const int c = atoi(env);
         return c == 2 || c == 4 || c == 8 || c == 16 ? c : 1;
@@ -921,7 +922,7 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     S.launches = 0;
     if (prm.precision == NR_MIXED) {
-        const char *env = getenv("NR_CLUSTER");
+        const char *env = knob("NR_CLUSTER");
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
         DsmPlan pl;
         if (dsm_plan(S, env ? cluster : 0, cluster, pl)) {
@@ -1475,6 +1476,28 @@ int nr_energies(nr_network *d, double *e_stretch, double *e_bend, void *stream) 
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     *e_stretch = st.e_stretch;
     *e_bend = st.e_bend;
+    return NR_OK;
+}
+
+int nr_network_plan(nr_network *d, int precision, char *buf, size_t cap) {
+    if (!d || !buf || cap == 0 || (precision != NR_FP64 && precision != NR_MIXED))
+        return fail(NR_ERR_INVALID, "nr_network_plan: bad arguments");
+    const NetDev &d0 = d->set.dev[0];
+    char out[256];
+    if (precision == NR_MIXED && d0.n <= kMixedCtaNodes) {
+        snprintf(out, sizeof out, "batch kernels, one network (%d nodes <= %d)", d0.n, kMixedCtaNodes);
+    } else {
+        GridPlan g;
+        const int rc = grid_plan(d->set, 0, precision == NR_MIXED, g);
+        if (rc != NR_OK) return rc;
+        if (g.tile)
+            snprintf(out, sizeof out, "k_fire_tile_mixed ctas=%d tiles=%d max_tile_nodes=%d", g.blocks, g.tl.n_tiles,
+                     g.tl.max_nodes);
+        else if (g.mixed) snprintf(out, sizeof out, "k_fire_grid_mixed ctas=%d", g.blocks);
+        else if (g.cluster > 0) snprintf(out, sizeof out, "%s cluster=%d", g.dsm64 ? "k_fire_dsm64" : "k_fire_cluster", g.cluster);
+        else snprintf(out, sizeof out, "k_fire_grid ctas=%d sub=%d", g.blocks, g.d.sub);
+    }
+    snprintf(buf, cap, "%s", out);
     return NR_OK;
 }
 

@@ -24,6 +24,7 @@
  * Compiled with --fmad=false; FP32 expressions use explicit fmaf().
  */
 #include "mixed_common.cuh"
+#include "nr_internal.h"
 
 namespace nr {
 
@@ -632,7 +633,7 @@ static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, 
  * latency) and 512 when the CTA is resident (few items per thread: the
  * 128-register budget keeps the step free of spills). */
 static int dsm_threads(bool resident) {
-    const char *env = getenv("NR_MIX_THREADS");
+    const char *env = knob("NR_MIX_THREADS");
     if (env && (atoi(env) == 512 || atoi(env) == 1024)) return atoi(env);
     return resident ? 512 : 1024;
 }

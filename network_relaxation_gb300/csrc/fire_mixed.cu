@@ -8,6 +8,7 @@
  * expressions use explicit fmaf().
  */
 #include "mixed_common.cuh"
+#include "nr_internal.h"
 
 namespace nr {
 
@@ -221,7 +222,7 @@ int mixed_cluster_size(int max_nodes) {
  * FP64 anchor code out of line) ran C4-sized networks 1.3-1.6x faster per
  * step than 512. */
 static int mixed_threads() {
-    const char *env = getenv("NR_MIX_THREADS");
+    const char *env = knob("NR_MIX_THREADS");
     return env && atoi(env) == 512 ? 512 : 1024;
 }
 
@@ -445,7 +446,7 @@ __global__ void __launch_bounds__(NT, 1) k_fire_grid_mixed(NetDev d, FireParamsD
  * 1M nodes 102 vs 153 us per step), 512 below (grid barriers dominate:
  * 65K nodes 19.6 vs 22.6 us). */
 static int grid_threads(int n) {
-    const char *env = getenv("NR_MIX_THREADS");
+    const char *env = knob("NR_MIX_THREADS");
     if (env && (atoi(env) == 512 || atoi(env) == 1024)) return atoi(env);
     return n > 152 * 1024 ? 1024 : 512;
 }

@@ -42,6 +42,10 @@ void clear_error();
  * first endpoint before second) and every triple (in index order, hinge, j,
  * k) touching the node.  Entry encodings: bond (b << 1) | role,
  * triple (t << 2) | role. */
+/* A launch-policy knob: the environment variable `name`, else the tuning
+ * table's entry of that name (tuning.cu), else null. */
+const char *knob(const char *name);
+
 struct Incidence {
     std::vector<int> bptr, bent, tptr, tent;
 };
