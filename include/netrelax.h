@@ -577,6 +577,20 @@ int nr_batch_affine_displace(nr_batch *b, const double *miny, const double *yran
  * lives on the device; a network retires when it meets its criterion).
  * params: one nr_fire_params for all.  reports: n entries (host). */
 int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports, void *stream);
+/* No reference counterpart (the reference sweeps one network at a time):
+ * the compression-then-shear protocol of do_relaxation_run
+ * (large_strain_relax.cu:924-999) in strain mode on every network of the
+ * batch at once, each network's displacements scaled by its own
+ * maxy - miny; per step one affine increment of every network and one
+ * batched relaxation, warm-started from the previous step.  The steps are
+ * counted in strain units (the same for every network).  graph != 0 records
+ * the whole protocol as one CUDA graph and launches it once (escalation to
+ * larger clusters is decided on the device); graph = 0 enqueues the same
+ * work directly.  records: step-major, n_networks per step, up to max_steps
+ * steps; *n_steps receives the protocol's step count.  The positions after
+ * the sweep are the last step's. */
+int nr_batch_sweep(nr_batch *b, const nr_fire_params *params, const double compr[3], const double shear[3],
+                   nr_step_record *records, int max_steps, int *n_steps, int graph, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* Driver, batch files and CLI                                         */

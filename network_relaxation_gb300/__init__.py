@@ -461,6 +461,21 @@ class Batch:
         check(st, "nr_batch_relax")
         return [reps[i] for i in range(self.n)]
 
+    def sweep(self, compr, shear, params=None, graph=True, max_steps=100000, stream=None):
+        """The strain protocol on every network at once (nr_batch_sweep);
+        returns records[step][network].  graph=True records the whole
+        protocol as one CUDA graph."""
+        params = params or fire_params()
+        c = (C.c_double * 3)(*[float(v) for v in compr])
+        s = (C.c_double * 3)(*[float(v) for v in shear])
+        recs = (StepRecord * (max_steps * self.n))()
+        ns = C.c_int()
+        st = self._lib.nr_batch_sweep(self._h, C.byref(params), c, s, recs, int(max_steps), C.byref(ns), int(bool(graph)),
+                                      _stream(stream))
+        check(st, "nr_batch_sweep")
+        k = min(ns.value, max_steps)
+        return [[recs[j * self.n + i] for i in range(self.n)] for j in range(k)]
+
 
 def _analysis_arrays(pos0, disp, edges):
     p0 = np.ascontiguousarray(pos0, np.float64).reshape(-1, 2)

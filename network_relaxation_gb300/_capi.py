@@ -125,6 +125,8 @@ SIGNATURES = {
     "nr_forces": (C.c_int, [P, c_double_p, P]),
     "nr_energies": (C.c_int, [P, c_double_p, c_double_p, P]),
     "nr_stress": (C.c_int, [P, c_double_p, c_double_p, P]),
+    "nr_batch_sweep": (C.c_int, [P, C.POINTER(FireParams), c_double_p, c_double_p, C.POINTER(StepRecord), C.c_int,
+                                 c_int_p, C.c_int, P]),
     "nr_tuning_load": (C.c_int, [C.c_char_p]),
     "nr_tuning_value": (C.c_double, [C.c_char_p]),
     "nr_tuning_source": (C.c_char_p, []),

@@ -849,7 +849,8 @@ static int solo_split(const DeviceSet &S, const DsmPlan &pl, DsmPlan &ps, int &c
     return (int)small.size();
 }
 
-static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl, cudaStream_t stream) {
+static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl, cudaStream_t stream,
+                            bool capture = false) {
     const double frac = escalate_fraction();
     int n_run = S.n_nets;
     const int *order_dev = S.order;
@@ -866,6 +867,49 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
         }
         n_run = S.n_nets - n_small;
     }
+    /* Device-side escalation (the default; NR_ESCALATE_HOST=1 steers from
+     * the host instead): every later phase is planned now for the whole
+     * batch, and a compaction kernel lists the networks that yielded, so the
+     * relaxation is stream work only, with no host round trip between
+     * phases, and a stream capture records it into a graph.  A phase whose
+     * list is empty launches clusters that exit at once. */
+    std::vector<DsmPlan> later;
+    const char *eh = knob("NR_ESCALATE_HOST");
+    bool device_side = frac > 0 && !(eh && atoi(eh) != 0);
+    for (int C = 2 * pl.C; device_side && C <= kDsmParts; C *= 2) {
+        DsmPlan p2;
+        if (!dsm_plan(S, C, 0, p2)) device_side = false;
+        else later.push_back(p2);
+    }
+    if (device_side) {
+        if (n_small > 0) NR_CUDA_TRY(cudaEventRecord(S.ev_fork, stream));
+        NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_run, pl.C, pl.bmax, pl.emax, pl.tmax, pl.ebmax,
+                                     pl.etmax, pl.resident, later.empty() ? 0.0 : frac, cap, to_dev(prm), S.queue,
+                                     order_dev, stream));
+        S.launches++;
+        if (n_small > 0) {
+            NR_CUDA_TRY(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
+            NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_small, 1, ps.bmax, ps.emax, ps.tmax, ps.ebmax,
+                                         ps.etmax, ps.resident, later.empty() ? 0.0 : frac, 0, to_dev(prm),
+                                         S.queue + 4, S.order + (S.n_nets - n_small), S.side));
+            S.launches++;
+            NR_CUDA_TRY(cudaEventRecord(S.ev_join, S.side));
+            NR_CUDA_TRY(cudaStreamWaitEvent(stream, S.ev_join, 0));
+        }
+        for (size_t k = 0; k < later.size(); ++k) {
+            const DsmPlan &p2 = later[k];
+            const bool last = k + 1 == later.size();
+            NR_CUDA_TRY(launch_compact_yielded(S.st, S.n_nets, S.order2, S.queue + 8, stream));
+            NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, S.n_nets, p2.C, p2.bmax, p2.emax, p2.tmax, p2.ebmax,
+                                         p2.etmax, p2.resident, last ? 0.0 : frac, 0, to_dev(prm), S.queue, S.order2,
+                                         stream, S.queue + 8));
+            S.launches += 2;
+        }
+        return NR_OK;
+    }
+    if (capture && frac > 0 && pl.C < kDsmParts)
+        return fail(NR_ERR_INVALID, "batch relaxation: escalation steered from the host (NR_ESCALATE_HOST, or no "
+                                    "plan for the larger clusters) cannot be recorded in a graph");
     for (int phase = 0;; ++phase) {
         const bool last = pl.C >= kDsmParts || frac <= 0;
         /* the side stream starts after the work queued so far, not after
@@ -918,7 +962,10 @@ static int fp64_batch_cluster(int max_nodes) {
     return max_nodes <= 2304 ? 1 : 8;
 }
 
-static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
+/* Enqueues one relaxation of every network of S (FIRE states zeroed, the
+ * kernels) without waiting for it.  capture: stream work only, as a stream
+ * capture needs (fails when escalation would be steered from the host). */
+static int enqueue_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, bool capture) {
     NR_CUDA_TRY(cudaMemsetAsync(S.st, 0, sizeof(FireState) * S.n_nets, stream));
     S.launches = 0;
     if (prm.precision == NR_MIXED) {
@@ -926,7 +973,7 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
         const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
         DsmPlan pl;
         if (dsm_plan(S, env ? cluster : 0, cluster, pl)) {
-            const int st = relax_dsm_phases(S, prm, pl, stream);
+            const int st = relax_dsm_phases(S, prm, pl, stream, capture);
             if (st != NR_OK) return st;
         } else if (cluster > 1) {
             NR_CUDA_TRY(launch_mixed_cluster(S.dev_array, S.n_nets, cluster, to_dev(prm), S.queue, S.order, stream));
@@ -952,15 +999,27 @@ static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t
         }
         S.launches++;
     }
-    std::vector<FireState> st(S.n_nets);
-    NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
-    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    return NR_OK;
+}
+
+/* Reports of n networks from their FIRE states; the worst status. */
+static int reports_of(const DeviceSet &S, const FireState *st, nr_report *reps) {
     int worst = NR_OK;
     for (int i = 0; i < S.n_nets; ++i) {
         fill_report(st[i], S.dev[i], &reps[i]);
         if (reps[i].status < 0) worst = reps[i].status;
         else if (worst == NR_OK && reps[i].status == NR_NOT_CONVERGED) worst = NR_NOT_CONVERGED;
     }
+    return worst;
+}
+
+static int relax_set_batch(DeviceSet &S, const nr_fire_params &prm, cudaStream_t stream, nr_report *reps) {
+    int rc = enqueue_set_batch(S, prm, stream, false);
+    if (rc != NR_OK) return rc;
+    std::vector<FireState> st(S.n_nets);
+    NR_CUDA_TRY(cudaMemcpyAsync(st.data(), S.st, sizeof(FireState) * S.n_nets, cudaMemcpyDeviceToHost, stream));
+    NR_CUDA_TRY(cudaStreamSynchronize(stream));
+    const int worst = reports_of(S, st.data(), reps);
     if (worst < 0) return fail(worst, "a network in the batch failed");
     return worst;
 }
@@ -1790,6 +1849,103 @@ int nr_batch_affine_displace(nr_batch *b, const double *miny, const double *yran
     NR_CUDA_TRY(launch_affine_batch(b->set.dev_array, b->set.affine_prm, b->set.n_nets, as_stream(stream)));
     NR_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
     return NR_OK;
+}
+
+int nr_batch_sweep(nr_batch *b, const nr_fire_params *params, const double compr[3], const double shear[3],
+                   nr_step_record *records, int max_steps, int *n_steps, int graph, void *stream) {
+    if (!b || !compr || !shear || !n_steps || (max_steps > 0 && !records))
+        return fail(NR_ERR_INVALID, "nr_batch_sweep: null argument");
+    int rc = check_params(params);
+    if (rc != NR_OK) return rc;
+    clear_error();
+    *n_steps = 0;
+    DeviceSet &S = b->set;
+    const int n = S.n_nets;
+    std::vector<SweepStep> steps;
+    rc = sweep_steps(1.0, compr, shear, steps); /* in strain units: the same steps for every network */
+    if (rc != NR_OK || steps.empty()) return rc;
+    /* per network and kind of step, the affine increment in its own
+     * displacement units (strain x (maxy - miny)) */
+    std::vector<double4> prm(2 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const double H = S.maxy[i] - S.miny[i];
+        for (int kind = 0; kind < 2; ++kind) {
+            const SweepStep *t = nullptr;
+            for (const SweepStep &q : steps)
+                if (q.is_shear == kind) {
+                    t = &q;
+                    break;
+                }
+            prm[(size_t)kind * n + i] = make_double4(S.miny[i], H, t ? t->xdisp * H : 0.0, t ? t->ydisp * H : 0.0);
+        }
+    }
+    cudaStream_t user = as_stream(stream);
+    struct Res {
+        cudaStream_t cs = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t e = nullptr;
+        double4 *prm = nullptr;
+        FireState *st = nullptr;
+        ~Res() {
+            if (e) cudaGraphExecDestroy(e);
+            if (g) cudaGraphDestroy(g);
+            if (prm) cudaFree(prm);
+            if (st) cudaFree(st);
+            if (cs) cudaStreamDestroy(cs);
+        }
+    } r;
+    const size_t ns = steps.size();
+    NR_CUDA_TRY(cudaStreamSynchronize(user));
+    NR_CUDA_TRY(cudaMalloc(&r.prm, sizeof(double4) * prm.size()));
+    NR_CUDA_TRY(cudaMalloc(&r.st, sizeof(FireState) * n * ns));
+    NR_CUDA_TRY(cudaMemcpy(r.prm, prm.data(), sizeof(double4) * prm.size(), cudaMemcpyHostToDevice));
+    NR_CUDA_TRY(cudaStreamCreateWithFlags(&r.cs, cudaStreamNonBlocking));
+    if (graph) NR_CUDA_TRY(cudaStreamBeginCapture(r.cs, cudaStreamCaptureModeThreadLocal));
+    int launches = 0;
+    for (size_t k = 0; k < ns && rc == NR_OK; ++k) {
+        cudaError_t e = launch_affine_batch(S.dev_array, r.prm + (size_t)steps[k].is_shear * n, n, r.cs);
+        if (e != cudaSuccess) {
+            rc = fail(NR_ERR_CUDA, std::string("nr_batch_sweep: ") + cudaGetErrorString(e));
+            break;
+        }
+        rc = enqueue_set_batch(S, *params, r.cs, graph != 0);
+        if (rc != NR_OK) break;
+        launches += 1 + S.launches;
+        e = cudaMemcpyAsync(r.st + k * n, S.st, sizeof(FireState) * n, cudaMemcpyDeviceToDevice, r.cs);
+        if (e != cudaSuccess) rc = fail(NR_ERR_CUDA, std::string("nr_batch_sweep: ") + cudaGetErrorString(e));
+    }
+    if (graph) {
+        const cudaError_t ec = cudaStreamEndCapture(r.cs, &r.g);
+        if (rc != NR_OK) return rc;
+        if (ec != cudaSuccess) return fail(NR_ERR_CUDA, std::string("nr_batch_sweep capture: ") + cudaGetErrorString(ec));
+        NR_CUDA_TRY(cudaGraphInstantiate(&r.e, r.g, 0));
+        NR_CUDA_TRY(cudaGraphLaunch(r.e, r.cs));
+    } else if (rc != NR_OK) {
+        cudaStreamSynchronize(r.cs);
+        return rc;
+    }
+    std::vector<FireState> st(n * ns);
+    NR_CUDA_TRY(cudaMemcpyAsync(st.data(), r.st, sizeof(FireState) * n * ns, cudaMemcpyDeviceToHost, r.cs));
+    NR_CUDA_TRY(cudaStreamSynchronize(r.cs));
+    S.launches = launches;
+    int worst = NR_OK;
+    std::vector<nr_report> reps(n);
+    for (size_t k = 0; k < ns; ++k) {
+        const int w = reports_of(S, st.data() + k * n, reps.data());
+        if (w < 0 && worst >= 0) worst = w;
+        else if (w == NR_NOT_CONVERGED && worst == NR_OK) worst = w;
+        if ((int)k < max_steps)
+            for (int i = 0; i < n; ++i) {
+                const double H = S.maxy[i] - S.miny[i];
+                SweepStep t = steps[k];
+                t.curr *= H;
+                t.maxc *= H;
+                record_step(t, reps[i], records[k * n + i]);
+            }
+    }
+    *n_steps = (int)ns;
+    if (worst < 0) return fail(worst, "nr_batch_sweep: a network failed");
+    return worst;
 }
 
 int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports, void *stream) {

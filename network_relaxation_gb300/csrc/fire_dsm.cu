@@ -175,8 +175,8 @@ __device__ __forceinline__ T ldro(const T *p) {
 
 template <int NT, bool RES>
 __global__ void __launch_bounds__(NT, 1)
-    k_fire_dsm_mixed(const NetDev *nets, const NetDsm *dsms, int n_nets, FireParamsDev p, int *queue,
-                     const int *order, DsmSizes z, int yield_at) {
+    k_fire_dsm_mixed(const NetDev *nets, const NetDsm *dsms, int n_nets, const int *n_dev, FireParamsDev p,
+                     int *queue, const int *order, DsmSizes z, int yield_at, int yield_pm) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     extern __shared__ float4 s_dyn[];
@@ -215,8 +215,19 @@ __global__ void __launch_bounds__(NT, 1)
         s_ab[threadIdx.x] = dsm_addr(s_bdf, threadIdx.x);
         s_at[threadIdx.x] = dsm_addr(s_tdf, threadIdx.x);
     }
+    /* n_dev: the count of this launch's networks, written on the device by
+     * an earlier kernel (device-side escalation); the escalation threshold
+     * is then yield_pm / 1000 of the clusters that get a network */
+    if (n_dev && yield_pm > 0) {
+        const int n_eff = *(volatile const int *)n_dev, clusters = (int)(gridDim.x / C);
+        yield_at = max(1, yield_pm * min(clusters, n_eff) / 1000);
+    }
+    bool ran = false; /* this cluster relaxed a network in this launch */
     for (;;) {
-        if (rank == 0 && threadIdx.x == 0) s_slot = atomicAdd(queue, 1);
+        if (rank == 0 && threadIdx.x == 0) {
+            const int sl = atomicAdd(queue, 1);
+            s_slot = n_dev && sl >= *(volatile const int *)n_dev ? n_nets : sl;
+        }
         cl.sync();
         const int slot = *cl.map_shared_rank(&s_slot, 0);
         /* every CTA has read rank 0's slot before any CTA may exit (a CTA's
@@ -224,9 +235,12 @@ __global__ void __launch_bounds__(NT, 1)
          * overwrites it for the next network */
         cl.sync();
         if (slot >= n_nets) {
-            if (rank == 0 && threadIdx.x == 0) atomicAdd(queue + 1, 1); /* one more idle cluster */
+            /* one more idle cluster (one that never got a network does not
+             * count: it was never busy) */
+            if (rank == 0 && threadIdx.x == 0 && (ran || !n_dev)) atomicAdd(queue + 1, 1);
             return;
         }
+        ran = true;
         if (threadIdx.x == 0) {
             const int idx = order ? order[slot] : slot;
             s_d = nets[idx];
@@ -609,9 +623,9 @@ static cudaError_t dsm_config(int cluster, const DsmSizes &z, cudaLaunchConfig_t
 }
 
 template <int NT, bool RES>
-static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster,
-                                 const DsmSizes &z, double escalate, int cap, const FireParamsDev &p, int *queue_dev,
-                                 const int *order_dev, cudaStream_t stream) {
+static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, const int *n_dev,
+                                 int cluster, const DsmSizes &z, double escalate, int cap, const FireParamsDev &p,
+                                 int *queue_dev, const int *order_dev, cudaStream_t stream) {
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr[1];
     int max_clusters = 0;
@@ -623,9 +637,10 @@ static cudaError_t launch_dsm_nt(const NetDev *nets_dev, const NetDsm *dsm_dev, 
     cfg.gridDim = dim3(clusters * cluster);
     cfg.stream = stream;
     const int yield_at = escalate > 0 ? std::max(1, (int)(escalate * clusters)) : 0;
+    const int yield_pm = escalate > 0 ? std::max(1, (int)(1000.0 * escalate)) : 0;
     if ((e = cudaMemsetAsync(queue_dev, 0, 2 * sizeof(int), stream)) != cudaSuccess) return e;
-    return cudaLaunchKernelEx(&cfg, k_fire_dsm_mixed<NT, RES>, nets_dev, dsm_dev, n_nets, p, queue_dev, order_dev, z,
-                              yield_at);
+    return cudaLaunchKernelEx(&cfg, k_fire_dsm_mixed<NT, RES>, nets_dev, dsm_dev, n_nets, n_dev, p, queue_dev,
+                              order_dev, z, yield_at, n_dev ? yield_pm : 0);
 }
 
 /* Threads per CTA: NR_MIX_THREADS (512 or 1024), else 1024 when the state
@@ -640,19 +655,53 @@ static int dsm_threads(bool resident) {
 
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
                              int emax, int tmax, int ebmax, int etmax, int resident, double escalate, int cap,
-                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream) {
+                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream,
+                             const int *n_dev) {
     if (cluster < 1 || cluster > kDsmParts || (kDsmParts % cluster) != 0) return cudaErrorInvalidValue;
     const DsmSizes z{bmax, emax, tmax, ebmax, etmax, resident};
     const bool wide = dsm_threads(resident != 0) == 1024;
     if (resident)
-        return wide ? launch_dsm_nt<1024, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
-                                                order_dev, stream)
-                    : launch_dsm_nt<512, true>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
-                                               order_dev, stream);
-    return wide ? launch_dsm_nt<1024, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
+        return wide ? launch_dsm_nt<1024, true>(nets_dev, dsm_dev, n_nets, n_dev, cluster, z, escalate, cap, p,
+                                                queue_dev, order_dev, stream)
+                    : launch_dsm_nt<512, true>(nets_dev, dsm_dev, n_nets, n_dev, cluster, z, escalate, cap, p,
+                                               queue_dev, order_dev, stream);
+    return wide ? launch_dsm_nt<1024, false>(nets_dev, dsm_dev, n_nets, n_dev, cluster, z, escalate, cap, p, queue_dev,
                                              order_dev, stream)
-                : launch_dsm_nt<512, false>(nets_dev, dsm_dev, n_nets, cluster, z, escalate, cap, p, queue_dev,
+                : launch_dsm_nt<512, false>(nets_dev, dsm_dev, n_nets, n_dev, cluster, z, escalate, cap, p, queue_dev,
                                             order_dev, stream);
+}
+
+/* Device-side escalation: the networks of a batch that left their last
+ * launch at an anchor (FireState.yielded), in index order, into order_out,
+ * and their count into *count_out.  One CTA; a block-wide scan per chunk of
+ * blockDim networks. */
+__global__ void k_compact_yielded(const FireState *st, int n, int *order_out, int *count_out) {
+    __shared__ int s_warp[32];
+    __shared__ int s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) s_base = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+        const int i = c0 + threadIdx.x;
+        const int flag = i < n && ((volatile const FireState *)st)[i].yielded ? 1 : 0;
+        const unsigned bal = __ballot_sync(kFull, flag);
+        const int in_warp = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) s_warp[warp] = __popc(bal);
+        __syncthreads();
+        int before = s_base;
+        for (int w = 0; w < warp; ++w) before += s_warp[w];
+        if (flag) order_out[before + in_warp] = i;
+        __syncthreads();
+        if (threadIdx.x == 0)
+            for (int w = 0; w < nw; ++w) s_base += s_warp[w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count_out = s_base;
+}
+
+cudaError_t launch_compact_yielded(const FireState *st, int n, int *order_out, int *count_out, cudaStream_t stream) {
+    k_compact_yielded<<<1, 256, 0, stream>>>(st, n, order_out, count_out);
+    return cudaGetLastError();
 }
 
 cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out) {

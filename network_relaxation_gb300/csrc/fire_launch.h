@@ -82,7 +82,12 @@ size_t dsm_smem_limit();
  * 2 ints (next slot, idle clusters). */
 cudaError_t launch_mixed_dsm(const NetDev *nets_dev, const NetDsm *dsm_dev, int n_nets, int cluster, int bmax,
                              int emax, int tmax, int ebmax, int etmax, int resident, double escalate, int cap,
-                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream);
+                             const FireParamsDev &p, int *queue_dev, const int *order_dev, cudaStream_t stream,
+                             const int *n_dev = nullptr);
+/* (launch_mixed_dsm: n_dev, when given, holds the launch's network count on
+ * the device, at most n_nets.)  The yielded networks of a batch, compacted
+ * on the device in index order: order_out and *count_out. */
+cudaError_t launch_compact_yielded(const FireState *st, int n, int *order_out, int *count_out, cudaStream_t stream);
 /* (launch_mixed_dsm: cap > 0 limits the number of clusters launched.)
  * Clusters of the given plan that fit the GPU at once. */
 cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out);

@@ -218,22 +218,24 @@ def test_sweep_graph_mixed_grid_equals_step_by_step(cuda):
     assert np.array_equal(pos, ppos)
 
 
-@pytest.mark.parametrize("case", ["jitter", "mikado"])
+@pytest.mark.parametrize("case", ["jitter", "per_item"])
 def test_mixed_tile_kernel_certified(cuda, case, monkeypatch):
     """The tiled kernel on a jittered lattice with generator triples (rest
-    angles) and on a Mikado network (per-bond k, per-triple kb, wraps):
-    every state certified by the oracle's FP64 force, energies within the
-    bar, and the tiled sweep as one CUDA graph equal to the step-by-step
-    sweep."""
+    angles), and on one with a stiffness per bond and per triple (random in
+    [0.5, 2] and [1e-3, 1e-2], as Mikado networks have): every state
+    certified by the oracle's FP64 force, energies within the bar, and the
+    tiled sweep as one CUDA graph equal to the step-by-step sweep."""
     monkeypatch.setenv("NR_TILE_MIN_NODES", "1000")
     monkeypatch.setenv("NR_TILE_NODES", "128")
-    if case == "jitter":
-        h = nr.HostNetwork.lattice(70, 70, 0.8, 0.05, 17, line_triples=True)
-        ks, kb, fire = 1.0, 1e-2, dict(FIRE)
-    else:
-        h = nr.HostNetwork.mikado(1400, 0.1, 1.0, 1e-3, 8)
-        ks, kb = 1.0, 1.0
-        fire = dict(FIRE, dt_max=0.05 * float(np.sqrt(h.arrays()["edge_l0"].min())))
+    h = nr.HostNetwork.lattice(70, 70, 0.8, 0.05, 17 if case == "jitter" else 19, line_triples=True)
+    ks, kb, fire = 1.0, 1e-2, dict(FIRE)
+    if case == "per_item":
+        rng = np.random.default_rng(3)
+        a0 = h.arrays()
+        h.set_bond_k(rng.uniform(0.5, 2.0, len(a0["edge_l0"])))
+        h.set_triples(a0["tri_hjk"], a0["tri_wrap"], kb=10 ** rng.uniform(-3, -2, len(a0["tri_hjk"])),
+                      phi0=a0["tri_phi0"])
+        kb = 1.0
     a = h.arrays()
     assert len(a["points"]) > 4096  # above the one-CTA size: a grid-wide kernel
     H = a["maxy"] - a["miny"]
@@ -257,3 +259,53 @@ def test_mixed_tile_kernel_certified(cuda, case, monkeypatch):
     r2, p2 = net3.sweep((0.0, 0.0, 0.0), (0.01, 0.02, 0.01), prm, keep_positions=True, graph=True)
     assert [(r.e_stretch, r.e_bend, r.steps) for r in r1] == [(r.e_stretch, r.e_bend, r.steps) for r in r2]
     assert all(np.array_equal(u, w) for u, w in zip(p1, p2))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batch_sweep_graph(cuda, precision):
+    """nr_batch_sweep: the shear protocol on every network of a batch at once,
+    the whole protocol as one CUDA graph (escalation decided on the device)
+    and enqueued directly, against each network swept alone (FP64: the same
+    bits as the oracle's sweep; mixed: certified and within the energy bar of
+    the FP64 oracle's sweep)."""
+    rng = np.random.default_rng(21)
+    hosts, arrs, kb = [], [], []
+    for i, L in enumerate([14, 40, 22, 56, 9]):
+        h = nr.HostNetwork.lattice(L, L, float(rng.uniform(0.65, 0.8)), 0.0, 300 + i).get_triples()
+        hosts.append(h)
+        arrs.append(h.arrays())
+        kb.append(float(10 ** rng.uniform(-3, -2)))
+    prm = nr.fire_params(fcut=1e-10, criterion="max", precision=precision, **FIRE)
+    shear = (0.01, 0.03, 0.01)
+    res = {}
+    for graph in (True, False):
+        b = nr.Batch(hosts, 1.0, np.array(kb))
+        res[graph] = (b.sweep((0.0, 0.0, 0.0), shear, prm, graph=graph), b.positions(), b.offsets)
+        b.close()
+    recs, X, off = res[True]
+    assert len(recs) == 3
+    if precision == "fp64":  # deterministic: graph and direct enqueue agree bit for bit
+        recs2, X2, _ = res[False]
+        assert np.array_equal(X, X2)
+        assert [[(r.e_stretch, r.e_bend, r.steps) for r in s] for s in recs] == \
+               [[(r.e_stretch, r.e_bend, r.steps) for r in s] for s in recs2]
+    for i, a in enumerate(arrs):
+        m = oracle.Model(a, 1.0, kb[i])
+        H = a["maxy"] - a["miny"]
+        orecs, opos, ox = m.sweep(a["points"], a["miny"], H, oracle.params(fcut=1e-10, criterion="max", **FIRE),
+                                  [0.0, 0.0, 0.0], list(shear))
+        x = X[off[i]:off[i + 1]]
+        for k in range(3):
+            r = recs[k][i]
+            assert r.status == nr.NR_OK and r.is_shear == 1
+            assert abs(r.curr_disp - orecs[k][0]) <= 1e-12 * H
+            e_or = orecs[k][2] + orecs[k][3]
+            if precision == "fp64":
+                assert (r.e_stretch, r.e_bend, r.steps) == (orecs[k][2], orecs[k][3], int(orecs[k][6]))
+            else:
+                assert r.max_force < 1e-10
+                assert abs(r.e_stretch + r.e_bend - e_or) <= energy_bar(m, opos[k], e_or)
+        if precision == "fp64":
+            assert np.array_equal(x, ox)
+        else:
+            assert np.sqrt((m.forces(x) ** 2).sum(1)).max() < 1e-10
