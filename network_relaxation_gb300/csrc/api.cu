@@ -188,60 +188,69 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
 
 /* Networks of at least NR_TILE_MIN_NODES nodes (default 131072) relaxed
  * alone in mixed precision use the tiled kernel, tiles of about
- * NR_TILE_NODES nodes (default 1024). */
+ * NR_TILE_NODES nodes (default 512). */
 static int tile_min_nodes() {
     const char *env = knob("NR_TILE_MIN_NODES");
     return env ? std::max(1, atoi(env)) : 131072;
 }
 static int tile_target_nodes() {
     const char *env = knob("NR_TILE_NODES");
-    const int v = env ? atoi(env) : 1024;
-    return v >= 64 && v <= 8192 ? v : 1024;
+    const int v = env ? atoi(env) : 512;
+    return v >= 64 && v <= 8192 ? v : 512;
 }
 
 /* Builds and uploads the tiled layout of network 0 of S (one allocation);
  * leaves S.tile_ctas = 0 when the network does not fit its encoding or the
- * kernel cannot launch. */
-static int build_tile_set(const nr_host_network &h, const Incidence &inc, DeviceSet &S, cudaStream_t stream) {
-    int dev = 0, sms = 0;
+ * kernel cannot launch.  One CTA per SM; the tile size is the largest of
+ * NR_TILE_NODES, half of it, a quarter ... whose two stage buffers and
+ * working arrays fit shared memory. */
+static int build_tile_set(const nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, DeviceSet &S,
+                          cudaStream_t stream) {
+    int dev = 0, sms = 0, optin = 0;
     NR_CUDA_TRY(cudaGetDevice(&dev));
     NR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    NR_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     const NetDev &d = S.dev[0];
     TileHost th;
-    /* two CTAs per SM is the design point (tiles of ~1000 nodes fit twice) */
-    if (build_tile_layout(h, inc, d.use_bonds != 0, d.use_triples != 0, 2 * sms, tile_target_nodes(), th) != NR_OK)
-        return NR_OK;
     NetTile &tl = S.tile;
-    tl = NetTile{};
-    tl.n_tiles = th.n_tiles;
-    tl.max_nodes = th.max_nodes;
-    tl.max_bonds = th.max_bonds;
-    tl.max_tris = th.max_tris;
+    bool ok = false;
+    for (int target = tile_target_nodes(); target >= 64 && !ok; target /= 2) {
+        if (build_tile_layout(h, inc, fcodes, d.use_bonds != 0, d.use_triples != 0, sms, target, th) != NR_OK)
+            return NR_OK;
+        tl = NetTile{};
+        tl.n_tiles = th.n_tiles;
+        tl.n_pos = th.n_pos;
+        tl.max_nodes = th.max_nodes;
+        tl.max_bonds = th.max_bonds;
+        tl.max_tris = th.max_tris;
+        tl.max_ro = th.max_ro;
+        ok = tile_smem(tl) + 8192 <= (size_t)optin;
+    }
+    if (!ok) return NR_OK;
+    /* every tile record is a whole number of 16-byte units at a 16-byte
+     * offset, as cp.async.bulk requires */
+    for (const TileDesc &td : th.desc)
+        if (td.ro_off % 16 != 0 || tile_segs(td.nb, td.nt, td.no, td.ni, td.nh).total % 16 != 0)
+            return fail(NR_ERR_INVALID, "tile layout: record not 16-byte aligned");
     const int ctas = tile_grid_ctas(tile_smem(tl));
     if (ctas < 1) {
         cudaGetLastError();
         return NR_OK;
     }
     Image img;
-    const size_t o_node_off = img.put(th.node_off.data(), th.node_off.size());
-    const size_t o_n_own = img.put(th.n_own.data(), th.n_own.size());
-    const size_t o_n_halo = img.put(th.n_halo.data(), th.n_halo.size());
-    const size_t o_own_off = img.put(th.own_off.data(), th.own_off.size());
-    const size_t o_bond_off = img.put(th.bond_off.data(), th.bond_off.size());
-    const size_t o_tri_off = img.put(th.tri_off.data(), th.tri_off.size());
-    const size_t o_inc_off = img.put(th.inc_off.data(), th.inc_off.size());
-    const size_t o_node = img.put(th.node.data(), th.node.size());
-    const size_t o_bref = img.put(th.bref.data(), th.bref.size());
-    const size_t o_tref = img.put(th.tref.data(), th.tref.size());
+    const size_t np = (size_t)th.n_pos;
+    const size_t o_desc = img.put(th.desc.data(), th.desc.size());
+    const size_t o_ro = img.put(th.ro.data(), th.ro.size());
+    const size_t o_nop = img.put(th.node_of_pos.data(), th.node_of_pos.size());
     const size_t o_bid = img.put(th.bid.data(), th.bid.size());
     const size_t o_tid = img.put(th.tid.data(), th.tid.size());
-    const size_t o_iptr = img.put(th.iptr.data(), th.iptr.size());
-    const size_t o_inc = img.put(th.inc.data(), th.inc.size());
-    const size_t nb = th.bid.size(), nt = th.tid.size(), nn = (size_t)d.n;
-    const size_t o_mb = img.add(sizeof(float4) * nb), o_sk = img.add(sizeof(float2) * nb);
-    const size_t o_arms = img.add(sizeof(float4) * nt), o_pk = img.add(sizeof(float2) * nt);
-    const size_t o_u1 = img.add(sizeof(float4) * nn), o_v1 = img.add(sizeof(float2) * nn),
-                 o_f1 = img.add(sizeof(float2) * nn);
+    size_t o_u[2], o_v[2], o_f[2];
+    for (int c = 0; c < 2; ++c) {
+        o_u[c] = img.add(sizeof(float4) * np);
+        o_v[c] = img.add(sizeof(float2) * np);
+        o_f[c] = img.add(sizeof(float2) * np);
+    }
+    const size_t o_fah = img.add(sizeof(float2) * np), o_fal = img.add(sizeof(float2) * np);
     const size_t o_cpart = img.add(sizeof(float) * 5 * 2 * (size_t)ctas);
     const size_t o_dpart = img.add(sizeof(double) * 2 * (size_t)ctas);
     const size_t o_bar = img.add(sizeof(unsigned long long));
@@ -254,30 +263,18 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, Device
     NR_CUDA_TRY(cudaMemcpyAsync(S.tile_mem, img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
     char *b = S.tile_mem;
-    tl.node_off = (const int *)(b + o_node_off);
-    tl.n_own = (const int *)(b + o_n_own);
-    tl.n_halo = (const int *)(b + o_n_halo);
-    tl.own_off = (const int *)(b + o_own_off);
-    tl.bond_off = (const int *)(b + o_bond_off);
-    tl.tri_off = (const int *)(b + o_tri_off);
-    tl.inc_off = (const int *)(b + o_inc_off);
-    tl.node = (const int *)(b + o_node);
-    tl.bref = (const unsigned *)(b + o_bref);
-    tl.tref = (const uint2 *)(b + o_tref);
+    tl.desc = (const TileDesc *)(b + o_desc);
+    tl.ro = (unsigned char *)(b + o_ro);
+    tl.node_of_pos = (const int *)(b + o_nop);
     tl.bid = (const int *)(b + o_bid);
     tl.tid = (const int *)(b + o_tid);
-    tl.iptr = (const unsigned short *)(b + o_iptr);
-    tl.inc = (const unsigned short *)(b + o_inc);
-    tl.mb = (float4 *)(b + o_mb);
-    tl.sk = (float2 *)(b + o_sk);
-    tl.arms = (float4 *)(b + o_arms);
-    tl.pk = (float2 *)(b + o_pk);
-    tl.u[0] = d.u;
-    tl.v[0] = d.vf;
-    tl.f[0] = d.ff;
-    tl.u[1] = (float4 *)(b + o_u1);
-    tl.v[1] = (float2 *)(b + o_v1);
-    tl.f[1] = (float2 *)(b + o_f1);
+    for (int c = 0; c < 2; ++c) {
+        tl.u[c] = (float4 *)(b + o_u[c]);
+        tl.v[c] = (float2 *)(b + o_v[c]);
+        tl.f[c] = (float2 *)(b + o_f[c]);
+    }
+    tl.fa_hi = (float2 *)(b + o_fah);
+    tl.fa_lo = (float2 *)(b + o_fal);
     tl.cpart = (float *)(b + o_cpart);
     tl.dpart = (double *)(b + o_dpart);
     tl.bar = (unsigned long long *)(b + o_bar);
@@ -322,6 +319,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
     std::vector<NetOff> off(n);
     const bool want_tile = n == 1 && nets[0]->n_points >= tile_min_nodes();
     Incidence inc0;
+    std::vector<unsigned char> fc0;
     for (int i = 0; i < n; ++i) {
         const nr_host_network &h = *nets[i];
         memcpy(img.bytes.data() + x_off + sizeof(double2) * S.node_off[i], h.points.data(),
@@ -396,7 +394,10 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.eent = img.put(eent.data(), eent.size());
         o.partner = img.put(partner.data(), partner.size());
         build_dsm_layout(h, inc, img, o, S.dsm[i]);
-        if (want_tile && i == 0) inc0 = std::move(inc);
+        if (want_tile && i == 0) {
+            inc0 = std::move(inc);
+            fc0 = fc;
+        }
         if (S.dsm[i].bsub <= 0) S.dsm_ok = false;
         S.max_nodes = std::max(S.max_nodes, h.n_points);
         const int tiles = (h.n_points + kTile - 1) / kTile;
@@ -510,7 +511,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         NR_CUDA_TRY(launch_inv_mats((const double *)S.dev[i].x, (const int *)S.gel[i].elem, 4, S.dev[i].n_elems,
                                     S.gel[i].elem_inv, stream));
     NR_CUDA_TRY(cudaStreamSynchronize(stream));
-    if (want_tile) return build_tile_set(*nets[0], inc0, S, stream);
+    if (want_tile) return build_tile_set(*nets[0], inc0, fc0.data(), S, stream);
     return NR_OK;
 }
 

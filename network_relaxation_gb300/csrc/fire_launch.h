@@ -93,17 +93,17 @@ cudaError_t launch_compact_yielded(const FireState *st, int n, int *order_out, i
 cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out);
 /* Host arrays of a NetTile layout (fire_tile.cu). */
 struct TileHost {
-    int n_tiles = 0, max_nodes = 0, max_bonds = 0, max_tris = 0;
-    std::vector<int> node_off, n_own, n_halo, own_off, bond_off, tri_off, inc_off, node, bid, tid;
-    std::vector<unsigned> bref;
-    std::vector<uint2> tref;
-    std::vector<unsigned short> iptr, inc;
+    int n_tiles = 0, n_pos = 0, max_nodes = 0, max_bonds = 0, max_tris = 0;
+    unsigned max_ro = 0;
+    std::vector<TileDesc> desc;
+    std::vector<unsigned char> ro;
+    std::vector<int> node_of_pos, bid, tid;
 };
 struct Incidence;
 /* The tiled mixed-precision kernel for one large network: layout, launch
  * width (co-resident CTAs for its shared memory) and launch. */
-int build_tile_layout(const ::nr_host_network &h, const Incidence &inc, bool use_bonds, bool use_triples,
-                      int ctas, int target_nodes, TileHost &out);
+int build_tile_layout(const ::nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, bool use_bonds,
+                      bool use_triples, int ctas, int target_nodes, TileHost &out);
 size_t tile_smem(const NetTile &tl);
 int tile_grid_ctas(size_t smem);
 cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas,

@@ -1,40 +1,47 @@
 /*
  * Mixed-precision FIRE for one large network over the whole GPU, in spatial
- * tiles, with ONE grid barrier per FIRE step.
+ * tiles, with ONE grid barrier per FIRE step and every tile's read-only data
+ * streamed into shared memory by TMA bulk copies.
  *
  * The cooperative grid kernel of fire_mixed.cu runs a step as four passes
  * separated by grid barriers (drift, item pass writing every bond's and
  * triple's FP32 force change to global memory, gather reading them back,
- * reduction by the last CTA) and is bound by the latency of those passes and
- * barriers.  Here a CTA takes whole tiles (NetTile, nr_device.cuh: a spatial
- * block of nodes, its halo and every item touching it, stored tile-major)
- * and does the whole step of a tile on chip:
- *   1. load u, v, F of the tile's own and halo nodes (from the step's input
- *      copy of the double-buffered state) into shared memory;
+ * reduction by the last CTA); it is bound by the latency of those passes and
+ * barriers.  Here one CTA per SM takes whole tiles (NetTile, nr_device.cuh)
+ * and does a tile's whole step on chip:
+ *   0. the tile's record (item references, anchor records, incidence,
+ *      fcodes, halo list: one contiguous block) arrives in shared memory by
+ *      one cp.async.bulk, issued while the previous tile computes (two
+ *      stage buffers, an mbarrier each);
+ *   1. u, v, F of the own nodes (contiguous in tile order) and of the halo;
  *   2. pass A (mixing, drift, half kick) for own AND halo nodes: the halo's
  *      drift is recomputed from the same inputs with the same operations as
- *      its owner's, so it has the same bits, and no barrier is needed
- *      between the drift and the items;
- *   3. the item pass: the FP32 force change of every bond and triple of the
- *      tile into shared memory (boundary items are evaluated by each tile
- *      they touch, identically);
- *   4. the gather of the tile's own nodes in the canonical incidence order,
- *      half kick, writes of u, v, F to the step's output copy, and the
- *      step's partial sums.
- * Then one grid barrier; every CTA combines the CTAs' partial sums in CTA
- * order itself and advances an identical copy of the FIRE scalars.  The
+ *      its owner's, so it has the same bits and needs no barrier;
+ *   3. the item pass: every bond's and triple's FP32 force change into
+ *      shared memory (boundary items are evaluated by each tile they touch);
+ *   4. the gather of the own nodes in the canonical incidence order, half
+ *      kick, the next step's u, v, F written, the step's partial sums.
+ * Then one grid barrier; every CTA combines the CTAs' partials in CTA order
+ * itself and advances an identical copy of the FIRE scalars.  The
  * arithmetic (double-float u, bond_dforce, tri_dforce, FP32 FIRE step, FP64
  * anchors and certification) is mixed_common.cuh's; per node the force is
  * the same sum in the same order as in the other mixed kernels.  Anchors
  * (rare) take two more barriers: X += u, then the FP64 force and the tile
- * items' FP32 anchor records.
+ * records' anchor data.
+ *
+ * Every wait is bounded: the grid barrier by a %globaltimer budget, the
+ * mbarrier waits by the same budget; a wait that runs out sets the
+ * network's abort flag (NR_ERR_TIMEOUT on the host), waits (bounded) for the
+ * CTA's copy in flight, and returns.
  *
  * Compiled with --fmad=false; FP32 expressions use explicit fmaf().
  */
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
+#include "fire_launch.h"
 #include "mixed_common.cuh"
 #include "nr_internal.h"
 
@@ -44,7 +51,7 @@ namespace nr {
 
 /* Arrives at barrier number `epoch` (1, 2, ...) of the launch and waits
  * until all G CTAs have; false when the wait exceeded budget_ns or another
- * CTA gave up (st->abort_flag), every thread of the CTA sees the same
+ * CTA gave up (st->abort_flag); every thread of the CTA sees the same
  * result. */
 __device__ inline bool tile_barrier(const NetTile &tl, FireState *st, unsigned G, unsigned long long epoch,
                                     unsigned long long budget_ns, unsigned site) {
@@ -81,77 +88,50 @@ __device__ inline bool tile_barrier(const NetTile &tl, FireState *st, unsigned G
     return ok != 0;
 }
 
-/* Dynamic shared memory of a CTA: one tile's state and item results. */
-struct TileSmem {
-    float4 *u, *tdf;
-    float2 *v, *bdf;
-};
-__host__ __device__ inline size_t tile_smem_bytes(int max_nodes, int max_bonds, int max_tris) {
-    return 16 * (size_t)max_nodes + 16 * (size_t)max_tris + 8 * (size_t)max_nodes + 8 * (size_t)max_bonds;
+/* ----- TMA bulk copy into shared memory, completion on an mbarrier ----- */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
 }
 
-/* FP64 anchor evaluation: X += u was done; every node's canonical FP64
- * force (d.f), its double-float copy (fa) and F = fa_hi in the current state
- * copy; the FP32 anchor records of the CTA's tiles' items.  Returns the CTA
- * partials of |F|^2 (sum) and max |F|^2 in thread 0. */
-static __device__ __noinline__ void tile_anchor_eval(const NetDev &d, const NetTile &tl, int cur, double *dslots,
-                                                     double &tF2, double &tM2) {
-    const double W = d.width;
-    double F2 = 0.0, M2 = 0.0;
-    const int G = gridDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += G * blockDim.x) {
-        double fx, fy;
-        node_force_fp64_own<false>(d, i, fx, fy);
-        d.f[i] = make_double2(fx, fy);
-        const float hx = (float)fx, hy = (float)fy;
-        d.fa_hi[i] = make_float2(hx, hy);
-        d.fa_lo[i] = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));
-        tl.f[cur][i] = make_float2(hx, hy);
-        const double t = dot2(fx, fy, fx, fy);
-        F2 += t;
-        M2 = fmax(M2, t);
-    }
-    for (int t = blockIdx.x; t < tl.n_tiles; t += G) {
-        if (d.use_bonds)
-            for (int k = tl.bond_off[t] + threadIdx.x; k < tl.bond_off[t + 1]; k += blockDim.x) {
-                const int b = tl.bid[k];
-                const int4 r = d.bond[b];
-                const double2 p1 = d.x[r.x], p2 = d.x[r.y];
-                const double rx = (p2.x + wrap_shift(r.z, W)) - p1.x, ry = p2.y - p1.y;
-                const double kk = d.bond_k ? d.bond_k[b] : d.ks;
-                const float hx = (float)rx, hy = (float)ry;
-                tl.mb[k] = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
-                tl.sk[k] = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)kk);
-            }
-        if (d.use_triples)
-            for (int k = tl.tri_off[t] + threadIdx.x; k < tl.tri_off[t + 1]; k += blockDim.x) {
-                const int tt = tl.tid[k];
-                const int4 r = d.tri[tt];
-                const double2 ph = d.x[r.x], pj = d.x[r.y], pk = d.x[r.z];
-                const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
-                const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
-                const double bx = (pk.x + wrap_shift(wk, W)) - ph.x, by = pk.y - ph.y;
-                const double kb = d.tri_kb ? d.tri_kb[tt] : d.kb;
-                const double phi0 = d.tri_phi0 ? d.tri_phi0[tt] : 0.0;
-                tl.arms[k] = make_float4((float)ax, (float)ay, (float)bx, (float)by);
-                tl.pk[k] = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
-            }
-    }
-    anchor_reduce(F2, M2, dslots, tF2, tM2);
+/* One thread: expect `bytes` and copy them from global src to shared dst
+ * (both 16-byte aligned, bytes a multiple of 16: the host checks the
+ * layout). */
+__device__ __forceinline__ void tma_load(void *dst, const void *src, unsigned bytes, unsigned long long *mbar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
 }
 
-/* Totals of the CTAs' FP64 anchor partials, in CTA order (thread 0). */
-static __device__ __noinline__ void tile_anchor_totals(const NetTile &tl, int G, double &F2, double &M2) {
-    double s = 0.0, m = 0.0;
-    for (int c = 0; c < G; ++c) {
-        s = s + __ldcg(tl.dpart + 2 * c);
-        m = fmax(m, __ldcg(tl.dpart + 2 * c + 1));
-    }
-    F2 = s;
-    M2 = m;
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *mbar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(mbar)), "r"(parity)
+        : "memory");
+    return ok != 0;
 }
 
-/* Pass A of one node held in shared memory (mixed_pass_a's operations). */
+/* Waits (every thread) until the mbarrier's phase `parity` completed, at
+ * most budget_ns; false when it ran out. */
+__device__ inline bool mbar_wait(unsigned long long *mbar, unsigned parity, unsigned long long budget_ns) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned spins = 0;; ++spins) {
+        if (mbar_try_wait(mbar, parity)) return true;
+        if ((spins & 15u) == 15u && global_ns() - t0 > budget_ns) return false;
+    }
+}
+
+/* ----- per-tile pieces ----- */
+
+/* Pass A of one node (mixed_pass_a's operations). */
 __device__ __forceinline__ void tile_pass_a(const Coef &c, float4 &w, float2 &v, const float2 F) {
     if (c.mix_pending) {
         v.x = fmaf(c.na, v.x, v.x);
@@ -168,27 +148,117 @@ __device__ __forceinline__ void tile_pass_a(const Coef &c, float4 &w, float2 &v,
     }
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT, 2)
+/* FP64 anchor evaluation: X += u was done; every node's canonical FP64
+ * force (d.f), its double-float copy fa and F = fa_hi in the current state
+ * copy (tile order); the anchor data of the CTA's tiles' records.  Returns
+ * the CTA partials of |F|^2 (sum) and max |F|^2 in thread 0. */
+static __device__ __noinline__ void tile_anchor_eval(const NetDev &d, const NetTile &tl, int cur, double *dslots,
+                                                     double &tF2, double &tM2) {
+    const double W = d.width;
+    double F2 = 0.0, M2 = 0.0;
+    const int G = gridDim.x;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < tl.n_pos; p += G * blockDim.x) {
+        const int i = tl.node_of_pos[p];
+        if (i < 0) continue;
+        double fx, fy;
+        node_force_fp64_own<false>(d, i, fx, fy);
+        d.f[i] = make_double2(fx, fy);
+        const float hx = (float)fx, hy = (float)fy;
+        tl.fa_hi[p] = make_float2(hx, hy);
+        tl.fa_lo[p] = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));
+        tl.f[cur][p] = make_float2(hx, hy);
+        const double t = dot2(fx, fy, fx, fy);
+        F2 += t;
+        M2 = fmax(M2, t);
+    }
+    for (int t = blockIdx.x; t < tl.n_tiles; t += G) {
+        const TileDesc td = tl.desc[t];
+        const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+        unsigned char *rec = tl.ro + td.ro_off;
+        float4 *mb = reinterpret_cast<float4 *>(rec + g.mb);
+        float2 *sk = reinterpret_cast<float2 *>(rec + g.sk);
+        float4 *arms = reinterpret_cast<float4 *>(rec + g.arms);
+        float2 *pk = reinterpret_cast<float2 *>(rec + g.pk);
+        if (d.use_bonds)
+            for (int k = threadIdx.x; k < td.nb; k += blockDim.x) {
+                const int b = tl.bid[td.bond_off + k];
+                const int4 r = d.bond[b];
+                const double2 p1 = d.x[r.x], p2 = d.x[r.y];
+                const double rx = (p2.x + wrap_shift(r.z, W)) - p1.x, ry = p2.y - p1.y;
+                const double kk = d.bond_k ? d.bond_k[b] : d.ks;
+                const float hx = (float)rx, hy = (float)ry;
+                mb[k] = make_float4(hx, hy, (float)(rx - (double)hx), (float)(ry - (double)hy));
+                sk[k] = make_float2((float)(sqrt(fma(rx, rx, ry * ry)) - d.bond_l0[b]), (float)kk);
+            }
+        if (d.use_triples)
+            for (int k = threadIdx.x; k < td.nt; k += blockDim.x) {
+                const int tt = tl.tid[td.tri_off + k];
+                const int4 r = d.tri[tt];
+                const double2 ph = d.x[r.x], pj = d.x[r.y], pkk = d.x[r.z];
+                const int wj = (signed char)(r.w & 0xff), wk = (signed char)((r.w >> 8) & 0xff);
+                const double ax = (pj.x + wrap_shift(wj, W)) - ph.x, ay = pj.y - ph.y;
+                const double bx = (pkk.x + wrap_shift(wk, W)) - ph.x, by = pkk.y - ph.y;
+                const double kb = d.tri_kb ? d.tri_kb[tt] : d.kb;
+                const double phi0 = d.tri_phi0 ? d.tri_phi0[tt] : 0.0;
+                arms[k] = make_float4((float)ax, (float)ay, (float)bx, (float)by);
+                pk[k] = make_float2((float)bend_dtheta(ax, ay, bx, by, phi0), (float)kb);
+            }
+    }
+    /* the records are read later by bulk copies (the async proxy) */
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    anchor_reduce(F2, M2, dslots, tF2, tM2);
+}
+
+/* Totals of the CTAs' FP64 anchor partials, in CTA order (thread 0). */
+static __device__ __noinline__ void tile_anchor_totals(const NetTile &tl, int G, double &F2, double &M2) {
+    double s = 0.0, m = 0.0;
+    for (int c = 0; c < G; ++c) {
+        s = s + __ldcg(tl.dpart + 2 * c);
+        m = fmax(m, __ldcg(tl.dpart + 2 * c + 1));
+    }
+    F2 = s;
+    M2 = m;
+}
+
+constexpr int kTileThreads = 512;
+
+/* Dynamic shared memory of a CTA: two stage buffers of max_ro bytes, then
+ * the working arrays of one tile. */
+__host__ __device__ inline size_t tile_smem_bytes(unsigned max_ro, int max_nodes, int max_bonds, int max_tris) {
+    return 2 * (size_t)max_ro + 16 * (size_t)max_nodes + 16 * (size_t)max_tris + 8 * (size_t)max_nodes +
+           8 * (size_t)max_bonds;
+}
+
+__global__ void __launch_bounds__(kTileThreads, 1)
     k_fire_tile_mixed(NetDev d, NetTile tl, FireParamsDev p, unsigned long long budget_ns) {
     extern __shared__ float4 s_dyn[];
     __shared__ MixShared sh;
+    __shared__ __align__(8) unsigned long long s_mbar[2];
+    __shared__ int s_fail;
+    /* FIRE scalars, advanced by thread 0 of every CTA (identical copies) */
+    __shared__ MixScal s;
+    __shared__ MixParams q;
+    constexpr int NT = kTileThreads;
     unsigned char *dyn = reinterpret_cast<unsigned char *>(s_dyn);
-    TileSmem sm;
-    sm.u = reinterpret_cast<float4 *>(dyn);
-    sm.tdf = sm.u + tl.max_nodes;
-    sm.v = reinterpret_cast<float2 *>(sm.tdf + tl.max_tris);
-    sm.bdf = sm.v + tl.max_nodes;
+    unsigned char *const stage0 = dyn, *const stage1 = dyn + tl.max_ro;
+    float4 *s_u = reinterpret_cast<float4 *>(dyn + 2 * (size_t)tl.max_ro);
+    float4 *s_tdf = s_u + tl.max_nodes;
+    float2 *s_v = reinterpret_cast<float2 *>(s_tdf + tl.max_tris);
+    float2 *s_bdf = s_v + tl.max_nodes;
     const unsigned G = gridDim.x;
     FireState *st = d.st;
     unsigned long long epoch = 0;
-    /* FIRE scalars, advanced by thread 0 of every CTA (identical copies);
-     * kept in shared memory, out of the step loop's registers */
-    __shared__ MixScal s;
-    __shared__ MixParams q;
-    if (threadIdx.x == 0) q = mix_params(p, d.sqrt_dof);
+    unsigned uses0 = 0u, uses1 = 0u; /* completed phases of each stage buffer's mbarrier */
+    if (threadIdx.x == 0) {
+        q = mix_params(p, d.sqrt_dof);
+        mbar_init(&s_mbar[0]);
+        mbar_init(&s_mbar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+    }
+    __syncthreads();
     int cur = 0;
-    for (int i = blockIdx.x * NT + threadIdx.x; i < d.n; i += G * NT) {
+    for (int i = blockIdx.x * NT + threadIdx.x; i < tl.n_pos; i += G * NT) {
         tl.u[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
         tl.v[0][i] = make_float2(0.f, 0.f);
     }
@@ -207,84 +277,127 @@ __global__ void __launch_bounds__(NT, 2)
         sh.coef = coef_of(s, 0);
     }
     __syncthreads();
+    const int n_mine = (int)blockIdx.x < tl.n_tiles ? (tl.n_tiles - 1 - (int)blockIdx.x) / (int)G + 1 : 0;
     for (;;) {
         const Coef &c = sh.coef;
         if (c.done) {
             /* the last pass A: mixing of v only (u is 0 after the certifying
              * anchor); the FP64 velocities out */
-            for (int i = blockIdx.x * NT + threadIdx.x; i < d.n; i += G * NT) {
-                float4 w = tl.u[cur][i];
-                float2 v = tl.v[cur][i];
-                tile_pass_a(c, w, v, tl.f[cur][i]);
+            for (int pp = blockIdx.x * NT + threadIdx.x; pp < tl.n_pos; pp += G * NT) {
+                const int i = tl.node_of_pos[pp];
+                if (i < 0) continue;
+                float4 w = tl.u[cur][pp];
+                float2 v = tl.v[cur][pp];
+                tile_pass_a(c, w, v, tl.f[cur][pp]);
                 d.v[i] = make_double2((double)v.x, (double)v.y);
             }
             break;
         }
         const int nxt = cur ^ 1;
         float P = 0.f, V2 = 0.f, Fs = 0.f, M2f = 0.f, A = 0.f;
-        for (int t = blockIdx.x; t < tl.n_tiles; t += G) {
-            const int n0 = tl.node_off[t], no = tl.n_own[t], nn = no + tl.n_halo[t];
-            const int b0 = tl.bond_off[t], nb = tl.bond_off[t + 1] - b0;
-            const int t0 = tl.tri_off[t], ntr = tl.tri_off[t + 1] - t0;
-            /* 1 + 2: state of own and halo nodes, then their pass A */
-            for (int k = threadIdx.x; k < nn; k += NT) {
-                const int i = __ldg(tl.node + n0 + k);
-                float4 w = tl.u[cur][i];
-                float2 v = tl.v[cur][i];
-                const float2 F = tl.f[cur][i];
-                tile_pass_a(c, w, v, F);
-                sm.u[k] = w;
-                sm.v[k] = v;
+        if (threadIdx.x == 0 && n_mine > 0) {
+            const TileDesc td0 = tl.desc[blockIdx.x];
+            tma_load(stage0, tl.ro + td0.ro_off, tile_segs(td0.nb, td0.nt, td0.no, td0.ni, td0.nh).total,
+                     &s_mbar[0]);
+        }
+        for (int k = 0; k < n_mine; ++k) {
+            const int t = (int)blockIdx.x + k * (int)G, b = k & 1;
+            const TileDesc td = tl.desc[t];
+            /* the next tile's record into the other buffer (free: the
+             * previous tile ended with a barrier) */
+            if (threadIdx.x == 0 && k + 1 < n_mine) {
+                const TileDesc tn = tl.desc[t + (int)G];
+                tma_load(b ? stage0 : stage1, tl.ro + tn.ro_off, tile_segs(tn.nb, tn.nt, tn.no, tn.ni, tn.nh).total,
+                         &s_mbar[b ^ 1]);
+            }
+            const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+            const int no = td.no, nh = td.nh, op = td.own_pos;
+            /* 1 + 2 for the own nodes (no wait on the stage) */
+            for (int kk = threadIdx.x; kk < no; kk += NT) {
+                float4 w = tl.u[cur][op + kk];
+                float2 v = tl.v[cur][op + kk];
+                tile_pass_a(c, w, v, tl.f[cur][op + kk]);
+                s_u[kk] = w;
+                s_v[kk] = v;
+            }
+            const unsigned parity = (b ? uses1 : uses0) & 1u;
+            if (b) ++uses1;
+            else ++uses0;
+            if (!mbar_wait(&s_mbar[b], parity, budget_ns)) s_fail = 1;
+            __syncthreads();
+            if (s_fail) {
+                if (threadIdx.x == 0) {
+                    atomicExch(&st->abort_flag, 1u);
+                    atomicExch(&st->timeout_site, 25u);
+                }
+                /* the other buffer's copy may still be in flight: wait for
+                 * it, bounded, before the shared memory goes away */
+                if (k + 1 < n_mine) mbar_wait(&s_mbar[b ^ 1], (b ? uses0 : uses1) & 1u, budget_ns);
+                return;
+            }
+            const unsigned char *rec = b ? stage1 : stage0;
+            const int *halo = reinterpret_cast<const int *>(rec + g.halo);
+            for (int h = threadIdx.x; h < nh; h += NT) {
+                const int pp = halo[h];
+                float4 w = tl.u[cur][pp];
+                float2 v = tl.v[cur][pp];
+                tile_pass_a(c, w, v, tl.f[cur][pp]);
+                s_u[no + h] = w;
+                s_v[no + h] = v;
             }
             __syncthreads();
             /* 3: item pass into shared memory */
-            if (d.use_bonds)
-                for (int k = threadIdx.x; k < nb; k += NT) {
-                    const unsigned r = __ldg(tl.bref + b0 + k);
-                    const float4 ra = tl.mb[b0 + k];
-                    const float2 sk = tl.sk[b0 + k];
-                    const float4 ui = sm.u[r & 0xffffu], uj = sm.u[r >> 16];
+            if (d.use_bonds) {
+                const unsigned *bref = reinterpret_cast<const unsigned *>(rec + g.bref);
+                const float4 *mb = reinterpret_cast<const float4 *>(rec + g.mb);
+                const float2 *sk = reinterpret_cast<const float2 *>(rec + g.sk);
+                for (int kk = threadIdx.x; kk < td.nb; kk += NT) {
+                    const unsigned r = bref[kk];
+                    const float4 ui = s_u[r & 0xffffu], uj = s_u[r >> 16];
                     float2 dh, dlo;
                     u_diff2(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), make_float2(ui.x, ui.y),
                             make_float2(ui.z, ui.w), dh, dlo);
-                    sm.bdf[k] = bond_dforce(ra, sk, dh, dlo);
+                    s_bdf[kk] = bond_dforce(mb[kk], sk[kk], dh, dlo);
                 }
-            if (d.use_triples)
-                for (int k = threadIdx.x; k < ntr; k += NT) {
-                    const uint2 r = __ldg(tl.tref + t0 + k);
-                    const float4 arms = tl.arms[t0 + k];
-                    const float2 pk = tl.pk[t0 + k];
-                    const float4 uh = sm.u[r.x & 0xffffu], uj = sm.u[r.x >> 16], uk = sm.u[r.y];
+            }
+            if (d.use_triples) {
+                const uint2 *tref = reinterpret_cast<const uint2 *>(rec + g.tref);
+                const float4 *arms = reinterpret_cast<const float4 *>(rec + g.arms);
+                const float2 *pk = reinterpret_cast<const float2 *>(rec + g.pk);
+                for (int kk = threadIdx.x; kk < td.nt; kk += NT) {
+                    const uint2 r = tref[kk];
+                    const float4 uh = s_u[r.x & 0xffffu], uj = s_u[r.x >> 16], uk = s_u[r.y];
                     const float2 hh = make_float2(uh.x, uh.y), hl = make_float2(uh.z, uh.w);
                     float2 dFj, dFk;
-                    tri_dforce(arms, pk, u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
+                    tri_dforce(arms[kk], pk[kk], u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
                                u_diff(make_float2(uk.x, uk.y), make_float2(uk.z, uk.w), hh, hl), dFj, dFk);
-                    sm.tdf[k] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
+                    s_tdf[kk] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
                 }
+            }
             __syncthreads();
             /* 4: gather of the own nodes, half kick, the next step's state */
-            const unsigned short *ip = tl.iptr + tl.own_off[t] + t;
-            const unsigned short *inc = tl.inc + tl.inc_off[t];
-            for (int k = threadIdx.x; k < no; k += NT) {
-                const int i = __ldg(tl.node + n0 + k);
-                const unsigned fc = __ldg(d.fcode + i);
-                const int e0 = __ldg(ip + k), e1 = __ldg(ip + k + 1);
-                const float2 ah = d.fa_hi[i], al = d.fa_lo[i];
+            const unsigned short *iptr = reinterpret_cast<const unsigned short *>(rec + g.iptr);
+            const unsigned short *inc = reinterpret_cast<const unsigned short *>(rec + g.inc);
+            const unsigned char *fcode = rec + g.fcode;
+            for (int kk = threadIdx.x; kk < no; kk += NT) {
+                const unsigned fc = fcode[kk];
+                const int e0 = iptr[kk], e1 = iptr[kk + 1];
+                const float2 ah = tl.fa_hi[op + kk], al = tl.fa_lo[op + kk];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
                     float2 dF = make_float2(0.f, 0.f);
                     float mag = 0.f;
                     for (int e = e0; e < e1; ++e) {
-                        const unsigned code = __ldg(inc + e);
+                        const unsigned code = inc[e];
                         if (!(code & 0x8000u)) {
-                            float2 df = sm.bdf[code >> 1];
+                            float2 df = s_bdf[code >> 1];
                             if (code & 1) df = make_float2(-df.x, -df.y);
                             dF.x += df.x;
                             dF.y += df.y;
                             mag += fabsf(df.x) + fabsf(df.y);
                         } else {
                             const int role = code & 3;
-                            const float4 qv = sm.tdf[(code & 0x7fffu) >> 2];
+                            const float4 qv = s_tdf[(code & 0x7fffu) >> 2];
                             float gx, gy, mg;
                             if (role == 0) {
                                 gx = -(qv.x + qv.z);
@@ -306,12 +419,12 @@ __global__ void __launch_bounds__(NT, 2)
                     if (!(fc & 1)) F.x = 0.f;
                     if (!(fc & 2)) F.y = 0.f;
                 }
-                float2 v = sm.v[k];
+                float2 v = s_v[kk];
                 v.x = fmaf(c.dtm, F.x, v.x);
                 v.y = fmaf(c.dtm, F.y, v.y);
-                tl.u[nxt][i] = sm.u[k];
-                tl.v[nxt][i] = v;
-                tl.f[nxt][i] = F;
+                tl.u[nxt][op + kk] = s_u[kk];
+                tl.v[nxt][op + kk] = v;
+                tl.f[nxt][op + kk] = F;
                 P += fmaf(v.x, F.x, v.y * F.y);
                 V2 += fmaf(v.x, v.x, v.y * v.y);
                 const float f2 = fmaf(F.x, F.x, F.y * F.y);
@@ -341,8 +454,8 @@ __global__ void __launch_bounds__(NT, 2)
             /* lane l accumulates CTAs l, l + 32, ... in order, then the
              * butterfly: the same totals in every CTA */
             Part t{0.f, 0.f, 0.f, 0.f, 0.f};
-            for (int k = threadIdx.x; k < (int)G; k += 32) {
-                const float *cp = tl.cpart + 5 * ((size_t)cur * G + k);
+            for (int kk = threadIdx.x; kk < (int)G; kk += 32) {
+                const float *cp = tl.cpart + 5 * ((size_t)cur * G + kk);
                 t.P += __ldcg(cp);
                 t.V2 += __ldcg(cp + 1);
                 t.F2 += __ldcg(cp + 2);
@@ -359,13 +472,15 @@ __global__ void __launch_bounds__(NT, 2)
         cur = nxt;
         if (sh.coef.anchor) {
             /* X += u (FP64), u = 0, then the FP64 anchor */
-            for (int i = blockIdx.x * NT + threadIdx.x; i < d.n; i += G * NT) {
-                const float4 w = tl.u[cur][i];
+            for (int pp = blockIdx.x * NT + threadIdx.x; pp < tl.n_pos; pp += G * NT) {
+                const int i = tl.node_of_pos[pp];
+                if (i < 0) continue;
+                const float4 w = tl.u[cur][pp];
                 double2 x = d.x[i];
                 x.x = x.x + ((double)w.x + (double)w.z);
                 x.y = x.y + ((double)w.y + (double)w.w);
                 d.x[i] = x;
-                tl.u[cur][i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                tl.u[cur][pp] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             if (!tile_barrier(tl, st, G, ++epoch, budget_ns, 23)) return;
             tile_anchor_eval(d, tl, cur, sh.dslots, tF2, tM2);
@@ -392,77 +507,80 @@ __global__ void __launch_bounds__(NT, 2)
 /* Host side: layout and launch                                         */
 /* ------------------------------------------------------------------ */
 
-constexpr int kTileThreads = 512;
+size_t tile_smem(const NetTile &tl) { return tile_smem_bytes(tl.max_ro, tl.max_nodes, tl.max_bonds, tl.max_tris); }
 
-/* CTAs of the cooperative launch: co-resident CTAs per SM times SMs
- * (0 when the kernel cannot launch with this shared memory). */
+/* CTAs of the cooperative launch: co-resident CTAs per SM times SMs (0 when
+ * the kernel cannot launch with this shared memory). */
 int tile_grid_ctas(size_t smem) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaFuncSetAttribute(k_fire_tile_mixed<kTileThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_fire_tile_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_tile_mixed<kTileThreads>, kTileThreads, smem) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_tile_mixed, kTileThreads, smem) != cudaSuccess)
         return 0;
     return per_sm * sms;
 }
 
-size_t tile_smem(const NetTile &tl) { return tile_smem_bytes(tl.max_nodes, tl.max_bonds, tl.max_tris); }
-
 cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas,
                               unsigned long long budget_ns, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(tl.bar, 0, sizeof(unsigned long long), stream);
+    cudaError_t e = cudaFuncSetAttribute(k_fire_tile_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tile_smem(tl));
     if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(tl.bar, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
     NetDev dd = d;
     NetTile tt = tl;
     FireParamsDev pp = p;
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &tt, &pp, &bb};
-    return launch_cooperative((const void *)k_fire_tile_mixed<kTileThreads>, ctas, kTileThreads, args, tile_smem(tl),
-                              stream);
+    return launch_cooperative((const void *)k_fire_tile_mixed, ctas, kTileThreads, args, tile_smem(tl), stream);
 }
 
 /* Spatial tiles of one network (see NetTile): about target_nodes nodes per
  * tile, the tile count a multiple of `ctas` (each CTA takes the same number
  * of tiles), cells of the box [0, width) x [miny, maxy] with the box's
- * aspect ratio.  Returns NR_OK with the layout in `out` (host arrays),
- * or NR_ERR_CAPACITY when a tile exceeds the 16-bit local encoding. */
-int build_tile_layout(const nr_host_network &h, const Incidence &inc, bool use_bonds, bool use_triples, int ctas,
-                      int target_nodes, TileHost &out) {
+ * aspect ratio.  Returns NR_OK with the layout in `out` (host arrays), or
+ * NR_ERR_CAPACITY when a tile exceeds the 16-bit local encoding. */
+int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, bool use_bonds,
+                      bool use_triples, int ctas, int target_nodes, TileHost &out) {
     const int n = h.n_points, ne = h.n_edges(), nt = h.n_triples();
     const double W = h.offset, y0 = h.miny, H = std::max(h.maxy - h.miny, 1e-300);
     if (n <= 0 || !(W > 0) || ctas < 1) return NR_ERR_INVALID;
     const long per = (long)ctas * target_nodes;
     const long want = (long)ctas * std::max(1L, (n + per - 1) / per);
-    int ny = std::max(1, (int)std::lround(std::sqrt((double)want * H / W)));
-    int nx = std::max(1, (int)((want + ny - 1) / ny));
-    std::vector<int> cell(n), count((size_t)nx * ny + 1, 0);
+    const int ny = std::max(1, (int)std::lround(std::sqrt((double)want * H / W)));
+    const int nx = std::max(1, (int)((want + ny - 1) / ny));
+    std::vector<int> cell(n), count((size_t)nx * ny, 0);
     for (int i = 0; i < n; ++i) {
         double x = h.points[2 * i], y = h.points[2 * i + 1];
         x -= W * std::floor(x / W);
-        int cx = std::min(nx - 1, std::max(0, (int)(x / W * nx)));
-        int cy = std::min(ny - 1, std::max(0, (int)((y - y0) / H * ny)));
+        const int cx = std::min(nx - 1, std::max(0, (int)(x / W * nx)));
+        const int cy = std::min(ny - 1, std::max(0, (int)((y - y0) / H * ny)));
         cell[i] = cy * nx + cx;
-        count[cell[i] + 1]++;
+        count[cell[i]]++;
     }
-    /* compact the non-empty cells into tiles, cells in row order */
     std::vector<int> tile_of_cell((size_t)nx * ny, -1);
     int T = 0;
-    for (int cidx = 0; cidx < nx * ny; ++cidx)
-        if (count[cidx + 1] > 0) tile_of_cell[cidx] = T++;
+    for (int c = 0; c < nx * ny; ++c)
+        if (count[c] > 0) tile_of_cell[c] = T++;
     std::vector<std::vector<int>> own(T);
     for (int i = 0; i < n; ++i) own[tile_of_cell[cell[i]]].push_back(i); /* ascending */
     out = TileHost();
     out.n_tiles = T;
-    out.node_off.push_back(0);
-    out.own_off.push_back(0);
-    out.bond_off.push_back(0);
-    out.tri_off.push_back(0);
-    out.inc_off.push_back(0);
+    /* tile-order positions: each tile's own range starts on a multiple of 16 */
+    std::vector<int> pos_of(n), own_pos(T);
+    int P = 0;
+    for (int t = 0; t < T; ++t) {
+        own_pos[t] = P;
+        for (size_t k = 0; k < own[t].size(); ++k) pos_of[own[t][k]] = P + (int)k;
+        P += (int)((own[t].size() + 15) / 16 * 16);
+    }
+    out.n_pos = P;
+    out.node_of_pos.assign(P, -1);
+    for (int i = 0; i < n; ++i) out.node_of_pos[pos_of[i]] = i;
     std::vector<int> loc(n, -1), bslot(use_bonds ? ne : 0, -1), tslot(use_triples ? nt : 0, -1);
     std::vector<int> bl, tlist, halo;
+    std::vector<unsigned short> iptr, incv;
     for (int t = 0; t < T; ++t) {
         const std::vector<int> &o = own[t];
         for (size_t k = 0; k < o.size(); ++k) loc[o[k]] = (int)k;
@@ -480,7 +598,7 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, bool use_b
         std::sort(tlist.begin(), tlist.end());
         tlist.erase(std::unique(tlist.begin(), tlist.end()), tlist.end());
         auto touch = [&](int v) {
-            if (loc[v] < 0) {
+            if (loc[v] == -1) {
                 loc[v] = -2; /* halo, numbered below */
                 halo.push_back(v);
             }
@@ -489,66 +607,85 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, bool use_b
             touch(h.edge_ij[2 * b]);
             touch(h.edge_ij[2 * b + 1]);
         }
-        for (int q : tlist)
-            for (int r = 0; r < 3; ++r) touch(h.tri_hjk[3 * q + r]);
+        for (int qq : tlist)
+            for (int r = 0; r < 3; ++r) touch(h.tri_hjk[3 * qq + r]);
         std::sort(halo.begin(), halo.end());
         for (size_t k = 0; k < halo.size(); ++k) loc[halo[k]] = (int)(o.size() + k);
-        const size_t nn = o.size() + halo.size();
-        if (nn > 0xffff || bl.size() >= 0x4000 || tlist.size() >= 0x2000) {
+        auto reset = [&]() {
             for (int v : o) loc[v] = -1;
             for (int v : halo) loc[v] = -1;
+            for (int b : bl) bslot[b] = -1;
+            for (int qq : tlist) tslot[qq] = -1;
+        };
+        const size_t nn = o.size() + halo.size();
+        if (nn > 0xffff || bl.size() >= 0x4000 || tlist.size() >= 0x2000) {
+            reset();
             return NR_ERR_CAPACITY;
         }
-        out.n_own.push_back((int)o.size());
-        out.n_halo.push_back((int)halo.size());
-        out.node.insert(out.node.end(), o.begin(), o.end());
-        out.node.insert(out.node.end(), halo.begin(), halo.end());
+        for (size_t k = 0; k < bl.size(); ++k) bslot[bl[k]] = (int)k;
+        for (size_t k = 0; k < tlist.size(); ++k) tslot[tlist[k]] = (int)k;
+        /* incidence of the own nodes, canonical order: bonds, then triples */
+        iptr.clear();
+        incv.clear();
+        for (int i : o) {
+            iptr.push_back((unsigned short)incv.size());
+            if (use_bonds)
+                for (int e = inc.bptr[i]; e < inc.bptr[i + 1]; ++e)
+                    incv.push_back((unsigned short)((bslot[inc.bent[e] >> 1] << 1) | (inc.bent[e] & 1)));
+            if (use_triples)
+                for (int e = inc.tptr[i]; e < inc.tptr[i + 1]; ++e)
+                    incv.push_back((unsigned short)(0x8000 | (tslot[inc.tent[e] >> 2] << 2) | (inc.tent[e] & 3)));
+            if (incv.size() > 0xffff) {
+                reset();
+                return NR_ERR_CAPACITY;
+            }
+        }
+        iptr.push_back((unsigned short)incv.size());
+        TileDesc td;
+        td.ro_off = (long long)out.ro.size();
+        td.own_pos = own_pos[t];
+        td.no = (int)o.size();
+        td.nh = (int)halo.size();
+        td.nb = (int)bl.size();
+        td.nt = (int)tlist.size();
+        td.ni = (int)incv.size();
+        td.bond_off = (int)out.bid.size();
+        td.tri_off = (int)out.tid.size();
+        td.pad = 0;
+        const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+        out.ro.resize(out.ro.size() + g.total, 0);
+        unsigned char *rec = out.ro.data() + td.ro_off;
         for (size_t k = 0; k < bl.size(); ++k) {
             const int b = bl[k];
-            bslot[b] = (int)k;
-            out.bref.push_back((unsigned)loc[h.edge_ij[2 * b]] | ((unsigned)loc[h.edge_ij[2 * b + 1]] << 16));
+            const unsigned r = (unsigned)loc[h.edge_ij[2 * b]] | ((unsigned)loc[h.edge_ij[2 * b + 1]] << 16);
+            memcpy(rec + g.bref + 4 * k, &r, 4);
             out.bid.push_back(b);
         }
         for (size_t k = 0; k < tlist.size(); ++k) {
-            const int q = tlist[k];
-            tslot[q] = (int)k;
-            out.tref.push_back(make_uint2((unsigned)loc[h.tri_hjk[3 * q]] | ((unsigned)loc[h.tri_hjk[3 * q + 1]] << 16),
-                                          (unsigned)loc[h.tri_hjk[3 * q + 2]]));
-            out.tid.push_back(q);
+            const int qq = tlist[k];
+            const uint2 r = make_uint2((unsigned)loc[h.tri_hjk[3 * qq]] | ((unsigned)loc[h.tri_hjk[3 * qq + 1]] << 16),
+                                       (unsigned)loc[h.tri_hjk[3 * qq + 2]]);
+            memcpy(rec + g.tref + 8 * k, &r, 8);
+            out.tid.push_back(qq);
         }
-        /* incidence of the own nodes, canonical order: bonds, then triples */
-        const size_t ibase = out.inc.size();
-        for (int i : o) {
-            out.iptr.push_back((unsigned short)(out.inc.size() - ibase));
-            if (use_bonds)
-                for (int e = inc.bptr[i]; e < inc.bptr[i + 1]; ++e) {
-                    const int b = inc.bent[e] >> 1, role = inc.bent[e] & 1;
-                    out.inc.push_back((unsigned short)((bslot[b] << 1) | role));
-                }
-            if (use_triples)
-                for (int e = inc.tptr[i]; e < inc.tptr[i + 1]; ++e) {
-                    const int q = inc.tent[e] >> 2, role = inc.tent[e] & 3;
-                    out.inc.push_back((unsigned short)(0x8000 | (tslot[q] << 2) | role));
-                }
+        memcpy(rec + g.iptr, iptr.data(), 2 * iptr.size());
+        if (!incv.empty()) memcpy(rec + g.inc, incv.data(), 2 * incv.size());
+        for (size_t k = 0; k < o.size(); ++k) rec[g.fcode + k] = fcodes[o[k]];
+        for (size_t k = 0; k < halo.size(); ++k) {
+            const int pp = pos_of[halo[k]];
+            memcpy(rec + g.halo + 4 * k, &pp, 4);
         }
-        if (out.inc.size() - ibase > 0xffff) return NR_ERR_CAPACITY;
-        out.iptr.push_back((unsigned short)(out.inc.size() - ibase));
+        out.desc.push_back(td);
         out.max_nodes = std::max(out.max_nodes, (int)nn);
-        out.max_bonds = std::max(out.max_bonds, (int)bl.size());
-        out.max_tris = std::max(out.max_tris, (int)tlist.size());
-        out.node_off.push_back((int)out.node.size());
-        out.own_off.push_back(out.own_off.back() + (int)o.size());
-        out.bond_off.push_back((int)out.bid.size());
-        out.tri_off.push_back((int)out.tid.size());
-        out.inc_off.push_back((int)out.inc.size());
-        for (int v : o) loc[v] = -1;
-        for (int v : halo) loc[v] = -1;
-        for (int b : bl) bslot[b] = -1;
-        for (int q : tlist) tslot[q] = -1;
+        out.max_bonds = std::max(out.max_bonds, td.nb);
+        out.max_tris = std::max(out.max_tris, td.nt);
+        out.max_ro = std::max(out.max_ro, g.total);
+        reset();
     }
     out.max_nodes = std::max(out.max_nodes, 1);
     out.max_bonds = std::max(out.max_bonds, 1);
     out.max_tris = std::max(out.max_tris, 1);
+    out.max_ro = std::max(out.max_ro, 16u);
     return NR_OK;
 }
 

@@ -154,46 +154,77 @@ struct NetDsm {
 };
 
 /* Layout of one large network for the tiled mixed-precision kernel
- * (fire_tile.cu).  Nodes are binned into spatial tiles; a tile lists its own
- * nodes (ascending index) and then its halo: the other nodes that the
- * tile's items reach.  The tile's items are every bond with an endpoint and
- * every triple with a node among its own nodes (ascending global index; an
+ * (fire_tile.cu).  Nodes are binned into spatial tiles; a tile owns its
+ * nodes and reaches a halo of other tiles' nodes through its items: every
+ * bond with an endpoint and every triple with a node among its own nodes (an
  * item on a tile boundary belongs to every tile it touches and is evaluated
- * by each of them).  Everything a tile reads in a FIRE step is stored
- * tile-major, so a step streams through it:
- *   node_off[t] .. node_off[t] + n_own[t] + n_halo[t]   node ids (own, then halo)
- *   bond_off[t] .. bond_off[t+1]   bond items: local node refs {i, j}, anchor
- *                                  record {ra hi, lo}, {|ra| - l0, k}, bond id
- *   tri_off[t]  .. tri_off[t+1]    triple items: local refs {h, j, k},
- *                                  anchor arms, {theta_a - pi, kb}, triple id
- *   inc_off[t]  .. per own node its entries in the canonical incidence
- *                                  order (bonds, then triples): bond entry
- *                                  slot << 1 | role, triple entry 0x8000 |
- *                                  slot << 2 | role (slots local to the tile);
- *                                  node k of the tile's own nodes has entries
- *                                  iptr[own_off[t] + t + k] .. [.. + k + 1]
- *                                  (offsets relative to inc_off[t])
- * State of a step is double buffered ({u, v, F} read from one copy and the
- * next step's written to the other), so a tile may recompute the drift of
- * its halo nodes from the step's inputs while their owners write theirs. */
+ * by each of them, identically).
+ *
+ * Node state lives in TILE ORDER: tile t's own nodes occupy positions
+ * own_pos .. own_pos + no (ascending node id; own_pos a multiple of 16, the
+ * range padded to whole 16s with unused positions), so a tile's own state is
+ * contiguous; node_of_pos maps back to node ids (-1 for padding).
+ *
+ * Everything read-only that a tile reads in a FIRE step is one contiguous,
+ * 16-byte aligned record in `ro`, staged into shared memory by TMA bulk
+ * copies (cp.async.bulk), segments in this order, each padded to 16 bytes:
+ *   bref  nb x u32      local i | local j << 16
+ *   mb    nb x float4   anchor vector i -> j {hi.x, hi.y, lo.x, lo.y}
+ *   sk    nb x float2   {|r_anchor| - l0, k}
+ *   tref  nt x uint2    {local h | local j << 16, local k}
+ *   arms  nt x float4   anchor arms {a.x, a.y, b.x, b.y}
+ *   pk    nt x float2   {theta_anchor - pi, kb}
+ *   iptr  (no+1) x u16  incidence range of each own node (relative)
+ *   inc   ni x u16      entries in the canonical order (bonds, then
+ *                       triples): bond slot << 1 | role, triple 0x8000 |
+ *                       slot << 2 | role
+ *   fcode no x u8
+ *   halo  nh x i32      tile-order position of each halo node
+ * (local node k < no: own node k; no + h: halo node h).  The anchor records
+ * (mb, sk, arms, pk) are rewritten there at every anchor.  The state
+ * (u, v, F) is double buffered: a step reads one copy and writes the other,
+ * so a tile can recompute its halo nodes' drift from the step's inputs while
+ * their owners write theirs. */
+struct TileDesc {
+    long long ro_off; /* byte offset of the tile's record in ro */
+    int own_pos, no, nh, nb, nt, ni;
+    int bond_off, tri_off; /* first entry of the tile in bid / tid */
+    int pad;
+};
+struct TileSegs {
+    unsigned bref, mb, sk, tref, arms, pk, iptr, inc, fcode, halo, total; /* byte offsets in a tile record */
+};
+__host__ __device__ inline unsigned tile_pad16(unsigned b) { return (b + 15u) & ~15u; }
+__host__ __device__ inline TileSegs tile_segs(int nb, int nt, int no, int ni, int nh) {
+    TileSegs g;
+    unsigned o = 0;
+    g.bref = o;  o += tile_pad16(4u * nb);
+    g.mb = o;    o += 16u * nb;
+    g.sk = o;    o += tile_pad16(8u * nb);
+    g.tref = o;  o += tile_pad16(8u * nt);
+    g.arms = o;  o += 16u * nt;
+    g.pk = o;    o += tile_pad16(8u * nt);
+    g.iptr = o;  o += tile_pad16(2u * (no + 1));
+    g.inc = o;   o += tile_pad16(2u * ni);
+    g.fcode = o; o += tile_pad16(1u * no);
+    g.halo = o;  o += tile_pad16(4u * nh);
+    g.total = o;
+    return g;
+}
 struct NetTile {
-    int n_tiles, max_nodes, max_bonds, max_tris; /* max_nodes: own + halo */
-    const int *node_off, *n_own, *n_halo, *own_off, *bond_off, *tri_off, *inc_off;
-    const int *node;          /* node ids */
-    const unsigned *bref;     /* per bond item: local i | local j << 16 */
-    const uint2 *tref;        /* per triple item: local h | local j << 16, local k */
-    const int *bid, *tid;     /* global bond / triple id of each item */
-    float4 *mb;               /* per bond item: anchor vector i -> j, {hi.x, hi.y, lo.x, lo.y} */
-    float2 *sk;               /* per bond item: {|ra| - l0, k} */
-    float4 *arms;             /* per triple item: anchor arms {a.x, a.y, b.x, b.y} */
-    float2 *pk;               /* per triple item: {theta_a - pi, kb} */
-    const unsigned short *iptr; /* per own node (tile-major): first entry, relative to inc_off; n_own + 1 per tile */
-    const unsigned short *inc;  /* incidence entries */
-    float4 *u[2];             /* double-buffered state, by node */
+    int n_tiles, n_pos;                  /* tiles; tile-order positions (with padding) */
+    int max_nodes, max_bonds, max_tris;  /* per tile: own + halo nodes, bond items, triple items */
+    unsigned max_ro;                     /* largest tile record, bytes */
+    const TileDesc *desc;
+    unsigned char *ro;                   /* tile records (anchor records rewritten in place) */
+    const int *node_of_pos;              /* node id of each tile-order position (-1: padding) */
+    const int *bid, *tid;                /* global bond / triple id of each tile item */
+    float4 *u[2];                        /* double-buffered state, tile order */
     float2 *v[2], *f[2];
-    float *cpart;             /* per CTA step totals (5 floats each) */
-    double *dpart;            /* per CTA FP64 anchor totals (2 doubles each) */
-    unsigned long long *bar;  /* grid barrier counter (monotonic) */
+    float2 *fa_hi, *fa_lo;               /* double-float anchor force, tile order */
+    float *cpart;                        /* per CTA step totals (5 floats, two copies) */
+    double *dpart;                       /* per CTA FP64 anchor totals (2 doubles each) */
+    unsigned long long *bar;             /* grid barrier counter (monotonic) */
 };
 
 /* ----- reductions ----- */
