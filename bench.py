@@ -473,7 +473,8 @@ def main():
             "fp64_anchor_evals_median": float(np.median([r.fp64_steps for r in reps])),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
-                         "kernel": kname, "cluster_ctas": kcl},
+                         "kernel": kname, "cluster_ctas": kcl, "plan": batch.plan(args.precision)},
+            "tuning_table": nr.lib().nr_tuning_source().decode() or None,
             "clocks": clk,
             "wall_s_timed_region": wall,
         }
@@ -548,6 +549,7 @@ def fp64_batched(nr, hosts, kappa, gamma, batch_idx, c4, sp, mixed_reps, mixed_p
     prm = fire_params(nr, "fp64")
     reps_arr = (nr.Report * b.n)()
     lib = nr.lib()
+    plan64 = b.plan("fp64")
     stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -573,7 +575,7 @@ def fp64_batched(nr, hosts, kappa, gamma, batch_idx, c4, sp, mixed_reps, mixed_p
     b.close()
     unc = oracle_uncertainty(batch_idx)
     return {"value": len(hosts) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": 1,
-            "kernel": "k_fire_cluster (8 CTAs per network)", "bit_identical_to_oracle": "%d of %d" % (same, len(rows)),
+            "kernel": plan64, "bit_identical_to_oracle": "%d of %d" % (same, len(rows)),
             "mixed_vs_fp64_batched": mixed_value / (len(hosts) / (ms / 1e3)),
             "mixed_errors_vs_fp64": {
                 "energy": error_stats(emx, e64, unc),
@@ -642,6 +644,7 @@ def single_network_arm(args):
     sx, sy = SINGLE[args.workload][2]
     net.affine_displace(net.miny, H, sx * H, sy * H)
     x0 = net.positions()
+    plan = net.plan(args.precision)
     cap = min(args.max_steps, args.fire_cap)
     prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
                          max_steps=cap, criterion="max", precision=args.precision)
@@ -687,7 +690,7 @@ def single_network_arm(args):
                        "precision": args.precision},
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "kernel": "k_fire_grid_mixed" if args.precision == "mixed" else "k_fire_grid"},
+                         "traffic": None, "kernel": plan},
             **extra,
         }))
     return 0

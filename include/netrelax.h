@@ -546,6 +546,7 @@ const char *nr_tuning_source(void);
  * cluster=16" (NUL-terminated, truncated to cap). */
 int nr_network_plan(nr_network *dnet, int precision, char *buf, size_t cap);
 
+
 /* ------------------------------------------------------------------ */
 /* Batched relaxation of many independent networks in one launch       */
 /* ------------------------------------------------------------------ */
@@ -562,6 +563,10 @@ int nr_batch_size(const nr_batch *b);
  * per escalation of long-running networks to larger thread-block clusters).
  * No counterpart in the reference, which relaxes one network at a time. */
 int nr_batch_last_launches(const nr_batch *b);
+/* No reference counterpart: the launch plan nr_batch_relax picks for this
+ * batch and precision (kernel, CTAs per network, residency, single-CTA
+ * networks, escalation), as nr_network_plan's text. */
+int nr_batch_plan(nr_batch *b, int precision, char *buf, size_t cap);
 int nr_batch_total_points(const nr_batch *b);
 /* Positions of all networks, concatenated in network order (host or
  * device pointer). */

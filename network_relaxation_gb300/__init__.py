@@ -461,6 +461,13 @@ class Batch:
         check(st, "nr_batch_relax")
         return [reps[i] for i in range(self.n)]
 
+    def plan(self, precision="mixed"):
+        """The launch plan of nr_batch_relax for this batch (nr_batch_plan)."""
+        buf = C.create_string_buffer(256)
+        check(self._lib.nr_batch_plan(self._h, {"fp64": NR_FP64, "mixed": NR_MIXED}[precision], buf, 256),
+              "nr_batch_plan")
+        return buf.value.decode()
+
     def sweep(self, compr, shear, params=None, graph=True, max_steps=100000, stream=None):
         """The strain protocol on every network at once (nr_batch_sweep);
         returns records[step][network].  graph=True records the whole

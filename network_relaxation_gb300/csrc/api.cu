@@ -1561,6 +1561,38 @@ int nr_network_plan(nr_network *d, int precision, char *buf, size_t cap) {
     return NR_OK;
 }
 
+int nr_batch_plan(nr_batch *b, int precision, char *buf, size_t cap) {
+    if (!b || !buf || cap == 0 || (precision != NR_FP64 && precision != NR_MIXED))
+        return fail(NR_ERR_INVALID, "nr_batch_plan: bad arguments");
+    const DeviceSet &S = b->set;
+    char out[256];
+    if (precision == NR_MIXED) {
+        const char *env = knob("NR_CLUSTER");
+        const int cluster = env ? std::max(1, std::min(16, atoi(env))) : mixed_cluster_size(S.max_nodes);
+        DsmPlan pl, ps;
+        if (dsm_plan(S, env ? cluster : 0, cluster, pl)) {
+            int cap_clusters = 0;
+            const int n_small = solo_split(S, pl, ps, cap_clusters);
+            const char *eh = knob("NR_ESCALATE_HOST");
+            snprintf(out, sizeof out,
+                     "k_fire_dsm_mixed cluster=%d resident=%d solo_networks=%d escalation=%g (%s)", pl.C, pl.resident,
+                     n_small, escalate_fraction(), eh && atoi(eh) != 0 ? "host" : "device");
+        } else {
+            snprintf(out, sizeof out, "%s cluster=%d", cluster > 1 ? "k_fire_cluster_mixed" : "k_fire_batch_mixed",
+                     cluster);
+        }
+    } else {
+        const int c = fp64_batch_cluster(S.max_nodes);
+        int bmax = 0, emax = 0, tmax = 0;
+        if (c > 1 && fp64_kernel_choice() == 0 && fp64_dsm_plan(S, c, bmax, emax, tmax))
+            snprintf(out, sizeof out, "k_fire_dsm64 cluster=%d", c);
+        else if (c > 1) snprintf(out, sizeof out, "k_fire_cluster cluster=%d", c);
+        else snprintf(out, sizeof out, "k_fire_batch (one CTA per network)");
+    }
+    snprintf(buf, cap, "%s", out);
+    return NR_OK;
+}
+
 int nr_stress(nr_network *d, double stress[3], double energies[2], void *stream) {
     if (!d || !stress || !energies) return fail(NR_ERR_INVALID, "nr_stress: null argument");
     const NetDev &dv = d->set.dev[0];
