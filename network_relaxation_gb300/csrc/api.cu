@@ -223,6 +223,7 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
         tl.max_nodes = th.max_nodes;
         tl.max_bonds = th.max_bonds;
         tl.max_tris = th.max_tris;
+        tl.max_own = th.max_own;
         tl.max_ro = th.max_ro;
         ok = tile_smem(tl) + 8192 <= (size_t)optin;
     }

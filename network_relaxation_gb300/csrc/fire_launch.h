@@ -93,7 +93,7 @@ cudaError_t launch_compact_yielded(const FireState *st, int n, int *order_out, i
 cudaError_t dsm_max_active(int cluster, int bmax, int emax, int tmax, int ebmax, int etmax, int resident, int *out);
 /* Host arrays of a NetTile layout (fire_tile.cu). */
 struct TileHost {
-    int n_tiles = 0, n_pos = 0, max_nodes = 0, max_bonds = 0, max_tris = 0;
+    int n_tiles = 0, n_pos = 0, max_nodes = 0, max_bonds = 0, max_tris = 0, max_own = 0;
     unsigned max_ro = 0;
     std::vector<TileDesc> desc;
     std::vector<unsigned char> ro;

@@ -129,7 +129,65 @@ __device__ inline bool mbar_wait(unsigned long long *mbar, unsigned parity, unsi
     }
 }
 
+/* ----- per-thread asynchronous copies into shared memory (cp.async) ----- */
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 /* ----- per-tile pieces ----- */
+
+/* A tile's node state in shared memory: u, v, F of its own nodes (local 0
+ * .. no - 1) and halo nodes (no .. no + nh - 1), the own nodes' anchor
+ * force.  Two of them: the next tile's state is copied in while the current
+ * tile computes. */
+struct TileState {
+    float4 *u;
+    float2 *v, *f, *fah, *fal;
+};
+__host__ __device__ inline size_t tile_state_bytes(int max_nodes, int max_own) {
+    return 32 * (size_t)max_nodes + 16 * (size_t)max_own;
+}
+__device__ inline TileState tile_state_at(unsigned char *base, int max_nodes, int max_own) {
+    TileState t;
+    t.u = reinterpret_cast<float4 *>(base);
+    t.v = reinterpret_cast<float2 *>(base + 16 * (size_t)max_nodes);
+    t.f = t.v + max_nodes;
+    t.fah = t.f + max_nodes;
+    t.fal = t.fah + max_own;
+    return t;
+}
+
+/* Starts the copies of tile td's own state (state copy `cur`). */
+__device__ __forceinline__ void issue_own(const NetTile &tl, const TileDesc &td, int cur, const TileState &ts) {
+    for (int k = threadIdx.x; k < td.no; k += blockDim.x) {
+        const int p = td.own_pos + k;
+        cp_async16(ts.u + k, tl.u[cur] + p);
+        cp_async8(ts.v + k, tl.v[cur] + p);
+        cp_async8(ts.f + k, tl.f[cur] + p);
+        cp_async8(ts.fah + k, tl.fa_hi + p);
+        cp_async8(ts.fal + k, tl.fa_lo + p);
+    }
+}
+/* Starts the copies of tile td's halo state (its record already in shared
+ * memory). */
+__device__ __forceinline__ void issue_halo(const NetTile &tl, const TileDesc &td, const unsigned char *rec, int cur,
+                                           const TileState &ts) {
+    const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+    const int *halo = reinterpret_cast<const int *>(rec + g.halo);
+    for (int h = threadIdx.x; h < td.nh; h += blockDim.x) {
+        const int pp = halo[h];
+        cp_async16(ts.u + td.no + h, tl.u[cur] + pp);
+        cp_async8(ts.v + td.no + h, tl.v[cur] + pp);
+        cp_async8(ts.f + td.no + h, tl.f[cur] + pp);
+    }
+}
 
 /* Pass A of one node (mixed_pass_a's operations). */
 __device__ __forceinline__ void tile_pass_a(const Coef &c, float4 &w, float2 &v, const float2 F) {
@@ -222,10 +280,11 @@ static __device__ __noinline__ void tile_anchor_totals(const NetTile &tl, int G,
 
 constexpr int kTileThreads = 512;
 
-/* Dynamic shared memory of a CTA: two stage buffers of max_ro bytes, then
- * the working arrays of one tile. */
-__host__ __device__ inline size_t tile_smem_bytes(unsigned max_ro, int max_nodes, int max_bonds, int max_tris) {
-    return 2 * (size_t)max_ro + 16 * (size_t)max_nodes + 16 * (size_t)max_tris + 8 * (size_t)max_nodes +
+/* Dynamic shared memory of a CTA: two record buffers of max_ro bytes, two
+ * node-state buffers, the item results of one tile. */
+__host__ __device__ inline size_t tile_smem_bytes(unsigned max_ro, int max_nodes, int max_own, int max_bonds,
+                                                  int max_tris) {
+    return 2 * (size_t)max_ro + 2 * tile_state_bytes(max_nodes, max_own) + 16 * (size_t)max_tris +
            8 * (size_t)max_bonds;
 }
 
@@ -241,14 +300,16 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     constexpr int NT = kTileThreads;
     unsigned char *dyn = reinterpret_cast<unsigned char *>(s_dyn);
     unsigned char *const stage0 = dyn, *const stage1 = dyn + tl.max_ro;
-    float4 *s_u = reinterpret_cast<float4 *>(dyn + 2 * (size_t)tl.max_ro);
-    float4 *s_tdf = s_u + tl.max_nodes;
-    float2 *s_v = reinterpret_cast<float2 *>(s_tdf + tl.max_tris);
-    float2 *s_bdf = s_v + tl.max_nodes;
+    const size_t sbytes = tile_state_bytes(tl.max_nodes, tl.max_own);
+    const TileState ts0 = tile_state_at(dyn + 2 * (size_t)tl.max_ro, tl.max_nodes, tl.max_own);
+    const TileState ts1 = tile_state_at(dyn + 2 * (size_t)tl.max_ro + sbytes, tl.max_nodes, tl.max_own);
+    float4 *s_tdf = reinterpret_cast<float4 *>(dyn + 2 * (size_t)tl.max_ro + 2 * sbytes);
+    float2 *s_bdf = reinterpret_cast<float2 *>(s_tdf + tl.max_tris);
     const unsigned G = gridDim.x;
     FireState *st = d.st;
     unsigned long long epoch = 0;
     unsigned uses0 = 0u, uses1 = 0u; /* completed phases of each stage buffer's mbarrier */
+    unsigned iss0 = 0u, iss1 = 0u;   /* record copies issued into each stage buffer */
     if (threadIdx.x == 0) {
         q = mix_params(p, d.sqrt_dof);
         mbar_init(&s_mbar[0]);
@@ -295,65 +356,78 @@ __global__ void __launch_bounds__(kTileThreads, 1)
         }
         const int nxt = cur ^ 1;
         float P = 0.f, V2 = 0.f, Fs = 0.f, M2f = 0.f, A = 0.f;
-        if (threadIdx.x == 0 && n_mine > 0) {
+        /* the pipeline: the record (TMA) and the node state (cp.async) of
+         * tile k + 1 are in flight while tile k computes */
+        if (n_mine > 0) {
             const TileDesc td0 = tl.desc[blockIdx.x];
-            tma_load(stage0, tl.ro + td0.ro_off, tile_segs(td0.nb, td0.nt, td0.no, td0.ni, td0.nh).total,
-                     &s_mbar[0]);
+            if (threadIdx.x == 0)
+                tma_load(stage0, tl.ro + td0.ro_off, tile_segs(td0.nb, td0.nt, td0.no, td0.ni, td0.nh).total,
+                         &s_mbar[0]);
+            ++iss0;
+            issue_own(tl, td0, cur, ts0);
+            cp_async_commit();
+            if (mbar_wait(&s_mbar[0], uses0 & 1u, budget_ns)) {
+                ++uses0;
+                issue_halo(tl, td0, stage0, cur, ts0); /* only from a record that arrived */
+            } else {
+                s_fail = 1;
+            }
+            cp_async_commit();
         }
+        /* a wait that ran out: record the timeout, let every copy in flight
+         * land (record copies: bounded waits), leave */
+        auto abort_tiles = [&]() {
+            if (threadIdx.x == 0) {
+                atomicExch(&st->abort_flag, 1u);
+                atomicExch(&st->timeout_site, 25u);
+            }
+            cp_async_wait_all();
+            if (iss0 > uses0) mbar_wait(&s_mbar[0], uses0 & 1u, budget_ns);
+            if (iss1 > uses1) mbar_wait(&s_mbar[1], uses1 & 1u, budget_ns);
+        };
         for (int k = 0; k < n_mine; ++k) {
             const int t = (int)blockIdx.x + k * (int)G, b = k & 1;
             const TileDesc td = tl.desc[t];
-            /* the next tile's record into the other buffer (free: the
-             * previous tile ended with a barrier) */
-            if (threadIdx.x == 0 && k + 1 < n_mine) {
-                const TileDesc tn = tl.desc[t + (int)G];
-                tma_load(b ? stage0 : stage1, tl.ro + tn.ro_off, tile_segs(tn.nb, tn.nt, tn.no, tn.ni, tn.nh).total,
-                         &s_mbar[b ^ 1]);
-            }
-            const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
-            const int no = td.no, nh = td.nh, op = td.own_pos;
-            /* 1 + 2 for the own nodes (no wait on the stage) */
-            for (int kk = threadIdx.x; kk < no; kk += NT) {
-                float4 w = tl.u[cur][op + kk];
-                float2 v = tl.v[cur][op + kk];
-                tile_pass_a(c, w, v, tl.f[cur][op + kk]);
-                s_u[kk] = w;
-                s_v[kk] = v;
-            }
-            const unsigned parity = (b ? uses1 : uses0) & 1u;
-            if (b) ++uses1;
-            else ++uses0;
-            if (!mbar_wait(&s_mbar[b], parity, budget_ns)) s_fail = 1;
+            const bool more = k + 1 < n_mine;
+            const TileDesc tn = more ? tl.desc[t + (int)G] : td;
+            const TileState &sc = b ? ts1 : ts0, &sn = b ? ts0 : ts1;
+            unsigned char *const rec_n = b ? stage0 : stage1;
             __syncthreads();
             if (s_fail) {
-                if (threadIdx.x == 0) {
-                    atomicExch(&st->abort_flag, 1u);
-                    atomicExch(&st->timeout_site, 25u);
-                }
-                /* the other buffer's copy may still be in flight: wait for
-                 * it, bounded, before the shared memory goes away */
-                if (k + 1 < n_mine) mbar_wait(&s_mbar[b ^ 1], (b ? uses0 : uses1) & 1u, budget_ns);
+                abort_tiles();
                 return;
             }
+            if (more) {
+                if (threadIdx.x == 0)
+                    tma_load(rec_n, tl.ro + tn.ro_off, tile_segs(tn.nb, tn.nt, tn.no, tn.ni, tn.nh).total,
+                             &s_mbar[b ^ 1]);
+                if (b) ++iss0;
+                else ++iss1;
+                issue_own(tl, tn, cur, sn);
+            }
+            cp_async_commit();
+            cp_async_wait1(); /* this tile's own and halo state is in */
+            __syncthreads();
+            const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+            const int no = td.no, nn = no + td.nh, op = td.own_pos;
             const unsigned char *rec = b ? stage1 : stage0;
-            const int *halo = reinterpret_cast<const int *>(rec + g.halo);
-            for (int h = threadIdx.x; h < nh; h += NT) {
-                const int pp = halo[h];
-                float4 w = tl.u[cur][pp];
-                float2 v = tl.v[cur][pp];
-                tile_pass_a(c, w, v, tl.f[cur][pp]);
-                s_u[no + h] = w;
-                s_v[no + h] = v;
+            /* pass A of own and halo nodes, in place */
+            for (int kk = threadIdx.x; kk < nn; kk += NT) {
+                float4 w = sc.u[kk];
+                float2 v = sc.v[kk];
+                tile_pass_a(c, w, v, sc.f[kk]);
+                sc.u[kk] = w;
+                sc.v[kk] = v;
             }
             __syncthreads();
-            /* 3: item pass into shared memory */
+            /* item pass into shared memory */
             if (d.use_bonds) {
                 const unsigned *bref = reinterpret_cast<const unsigned *>(rec + g.bref);
                 const float4 *mb = reinterpret_cast<const float4 *>(rec + g.mb);
                 const float2 *sk = reinterpret_cast<const float2 *>(rec + g.sk);
                 for (int kk = threadIdx.x; kk < td.nb; kk += NT) {
                     const unsigned r = bref[kk];
-                    const float4 ui = s_u[r & 0xffffu], uj = s_u[r >> 16];
+                    const float4 ui = sc.u[r & 0xffffu], uj = sc.u[r >> 16];
                     float2 dh, dlo;
                     u_diff2(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), make_float2(ui.x, ui.y),
                             make_float2(ui.z, ui.w), dh, dlo);
@@ -366,7 +440,7 @@ __global__ void __launch_bounds__(kTileThreads, 1)
                 const float2 *pk = reinterpret_cast<const float2 *>(rec + g.pk);
                 for (int kk = threadIdx.x; kk < td.nt; kk += NT) {
                     const uint2 r = tref[kk];
-                    const float4 uh = s_u[r.x & 0xffffu], uj = s_u[r.x >> 16], uk = s_u[r.y];
+                    const float4 uh = sc.u[r.x & 0xffffu], uj = sc.u[r.x >> 16], uk = sc.u[r.y];
                     const float2 hh = make_float2(uh.x, uh.y), hl = make_float2(uh.z, uh.w);
                     float2 dFj, dFk;
                     tri_dforce(arms[kk], pk[kk], u_diff(make_float2(uj.x, uj.y), make_float2(uj.z, uj.w), hh, hl),
@@ -374,15 +448,31 @@ __global__ void __launch_bounds__(kTileThreads, 1)
                     s_tdf[kk] = make_float4(dFj.x, dFj.y, dFk.x, dFk.y);
                 }
             }
+            /* the next tile's record is in by now (bounded wait): start its
+             * halo state */
+            if (more) {
+                if (mbar_wait(&s_mbar[b ^ 1], (b ? uses0 : uses1) & 1u, budget_ns)) {
+                    if (b) ++uses0;
+                    else ++uses1;
+                    issue_halo(tl, tn, rec_n, cur, sn); /* only from a record that arrived */
+                } else {
+                    s_fail = 1;
+                }
+            }
+            cp_async_commit();
             __syncthreads();
-            /* 4: gather of the own nodes, half kick, the next step's state */
+            if (s_fail) {
+                abort_tiles();
+                return;
+            }
+            /* gather of the own nodes, half kick, the next step's state */
             const unsigned short *iptr = reinterpret_cast<const unsigned short *>(rec + g.iptr);
             const unsigned short *inc = reinterpret_cast<const unsigned short *>(rec + g.inc);
             const unsigned char *fcode = rec + g.fcode;
             for (int kk = threadIdx.x; kk < no; kk += NT) {
                 const unsigned fc = fcode[kk];
                 const int e0 = iptr[kk], e1 = iptr[kk + 1];
-                const float2 ah = tl.fa_hi[op + kk], al = tl.fa_lo[op + kk];
+                const float2 ah = sc.fah[kk], al = sc.fal[kk];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
                     float2 dF = make_float2(0.f, 0.f);
@@ -419,10 +509,10 @@ __global__ void __launch_bounds__(kTileThreads, 1)
                     if (!(fc & 1)) F.x = 0.f;
                     if (!(fc & 2)) F.y = 0.f;
                 }
-                float2 v = s_v[kk];
+                float2 v = sc.v[kk];
                 v.x = fmaf(c.dtm, F.x, v.x);
                 v.y = fmaf(c.dtm, F.y, v.y);
-                tl.u[nxt][op + kk] = s_u[kk];
+                tl.u[nxt][op + kk] = sc.u[kk];
                 tl.v[nxt][op + kk] = v;
                 tl.f[nxt][op + kk] = F;
                 P += fmaf(v.x, F.x, v.y * F.y);
@@ -433,6 +523,7 @@ __global__ void __launch_bounds__(kTileThreads, 1)
             }
             __syncthreads();
         }
+        cp_async_wait_all();
         warp_part(Part{P, V2, Fs, M2f, A}, sh.slots);
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -507,7 +598,9 @@ __global__ void __launch_bounds__(kTileThreads, 1)
 /* Host side: layout and launch                                         */
 /* ------------------------------------------------------------------ */
 
-size_t tile_smem(const NetTile &tl) { return tile_smem_bytes(tl.max_ro, tl.max_nodes, tl.max_bonds, tl.max_tris); }
+size_t tile_smem(const NetTile &tl) {
+    return tile_smem_bytes(tl.max_ro, tl.max_nodes, tl.max_own, tl.max_bonds, tl.max_tris);
+}
 
 /* CTAs of the cooperative launch: co-resident CTAs per SM times SMs (0 when
  * the kernel cannot launch with this shared memory). */
@@ -677,12 +770,14 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
         }
         out.desc.push_back(td);
         out.max_nodes = std::max(out.max_nodes, (int)nn);
+        out.max_own = std::max(out.max_own, td.no);
         out.max_bonds = std::max(out.max_bonds, td.nb);
         out.max_tris = std::max(out.max_tris, td.nt);
         out.max_ro = std::max(out.max_ro, g.total);
         reset();
     }
     out.max_nodes = std::max(out.max_nodes, 1);
+    out.max_own = std::max(out.max_own, 1);
     out.max_bonds = std::max(out.max_bonds, 1);
     out.max_tris = std::max(out.max_tris, 1);
     out.max_ro = std::max(out.max_ro, 16u);

@@ -214,6 +214,7 @@ __host__ __device__ inline TileSegs tile_segs(int nb, int nt, int no, int ni, in
 struct NetTile {
     int n_tiles, n_pos;                  /* tiles; tile-order positions (with padding) */
     int max_nodes, max_bonds, max_tris;  /* per tile: own + halo nodes, bond items, triple items */
+    int max_own;                         /* per tile: own nodes */
     unsigned max_ro;                     /* largest tile record, bytes */
     const TileDesc *desc;
     unsigned char *ro;                   /* tile records (anchor records rewritten in place) */
