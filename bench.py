@@ -293,7 +293,9 @@ def main():
     ap.add_argument("--reorder", default="none", choices=["none", "morton", "rcm"],
                     help="renumber every network's nodes (nr_host_network_reorder) before the batch is built")
     ap.add_argument("--side", type=int, default=0,
-                    help="profiling case: lattice side of the L1 workload (default 1024; not a bench line)")
+                    help="lattice side of the L1 workload (default 1024; a profiling case, not a bench line) or of "
+                         "the P5 protocol's network (default 1024, C5; a smaller side runs the same protocol on a "
+                         "smaller lattice of the same kind)")
     ap.add_argument("--fcut", type=float, default=1e-10,
                     help="C4 stop criterion max|F| < fcut of the measured precision (at most 1e-10: the metric's "
                          "criterion is met at any tighter value)")
@@ -306,7 +308,7 @@ def main():
     args = ap.parse_args()
     if not args.fcut <= 1e-10:
         ap.error("--fcut must be at most 1e-10")
-    profiling_case = args.largest > 0 or args.max_steps != 10_000_000 or args.side > 0
+    profiling_case = args.largest > 0 or args.max_steps != 10_000_000 or (args.side > 0 and args.workload == "L1")
     if profiling_case:
         args.no_cpu = args.no_fp64 = True
     if args.warmup < 3:
@@ -806,8 +808,11 @@ def protocol_arm(args):
     import network_relaxation_gb300 as nr
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    pr = PROTOCOLS[args.workload]
+    pr = dict(PROTOCOLS[args.workload])
     h, kb, dt_max = single_network(nr, pr["net"])
+    if args.workload == "P5" and args.side > 0:  # the same protocol on a smaller lattice of the same kind
+        h = nr.HostNetwork.lattice(args.side, args.side, 0.65, 0.05, 5, line_triples=True)
+        pr["what"] = pr["what"].replace("C5 network", "C5-kind lattice %dx%d" % (args.side, args.side))
     info = h.info()
     compr, shear = list(pr["compr"]), list(pr["shear"])
     k = args.strain_steps
@@ -826,7 +831,7 @@ def protocol_arm(args):
     cap = min(args.max_steps, args.fire_cap) if args.fire_cap != 2000 else args.max_steps
     stream = torch.cuda.current_stream()
     out = {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed",) if args.no_fp64 else ("mixed", "fp64"):
         net = nr.Network(h, 1.0, kb)
         x0 = net.positions()
         prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
@@ -841,7 +846,7 @@ def protocol_arm(args):
         out[prec] = (e0.elapsed_time(e1), recs)
         net.close()
     ms_m, rm = out["mixed"]
-    ms_d, rd = out["fp64"]
+    ms_d, rd = out.get("fp64", (float("nan"), []))
     n = info.n_points
     bpn = 73 + 24 * info.n_edges / n + 12 * info.n_triples / n
     fire_m = sum(r.steps for r in rm)
@@ -866,9 +871,12 @@ def protocol_arm(args):
         "config": {"workload": "%s: %s; N=%d E=%d T=%d; FIRE to max|F|<1e-10, at most %d steps per strain step"
                                % (args.workload, pr["what"], n, info.n_edges, info.n_triples, cap),
                    "strain_steps_run": len(rm), "compression": compr, "shear": shear},
-        "fp64": {"value": len(rd) / (ms_d / 1e3), "ms_per_protocol": ms_d, "fire_steps": sum(r.steps for r in rd)},
+        "fp64": ({"value": len(rd) / (ms_d / 1e3), "ms_per_protocol": ms_d, "fire_steps": sum(r.steps for r in rd)}
+                 if rd else None),
         "mixed_fire_steps": fire_m, "us_per_fire_step_mixed": 1e3 * ms_m / max(1, fire_m),
-        "us_per_fire_step_fp64": 1e3 * ms_d / max(1, sum(r.steps for r in rd)),
+        "us_per_fire_step_fp64": 1e3 * ms_d / max(1, sum(r.steps for r in rd)) if rd else None,
+        "converged_mixed": sum(1 for r in rm if r.status == 0),
+        "converged_fp64": sum(1 for r in rd if r.status == 0) if rd else None,
         "converged_both": len(both),
         "mixed_vs_fp64": {"energy_rel_max": max(e_err) if e_err else None,
                           "stress_xy_rel_max": max(sxy_err) if sxy_err else None,

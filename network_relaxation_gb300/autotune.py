@@ -7,11 +7,12 @@ default.  This module measures the candidates of each knob on synthetic
 networks of each size class, with CUDA events, and writes the table the
 library loads by default on that GPU model:
 
-    python -m network_relaxation_gb300.autotune [--out PATH] [--quick]
+    python -m network_relaxation_gb300.autotune [--out PATH] [--quick] [--only CLASSES] [--merge TABLE]
 
 (default PATH: network_relaxation_gb300/tuning/<device name>.txt, next to
 libnetrelax.so).  A JSON record of every measurement goes beside it
-(<PATH>.json).  Knobs and size classes:
+(<PATH>.json); --merge starts from an earlier table and replaces only the
+classes tuned now.  Knobs and size classes:
 
   FP64, one network      NR_FP64_KERNEL (dsm | l2), NR_FP64_CLUSTER (CTAs per
                          cluster), NR_FP64_CLUSTER_NODES (largest network run
@@ -125,7 +126,7 @@ def tune_fp64_single(nr, torch, log, quick):
 
 def tune_mixed_single(nr, torch, log, quick):
     sides = [128, 256, 512, 1024] if not quick else [256, 1024]
-    tiles = [512, 1024, 2048]
+    tiles = [256, 384, 512]  # larger targets are halved to fit shared memory anyway
     res = {}
     for L in sides:
         h = nr.HostNetwork.lattice(L, L, 0.65, 0.05, 5, line_triples=True)
@@ -232,6 +233,8 @@ def main(argv=None):
     ap.add_argument("--out", default="")
     ap.add_argument("--quick", action="store_true", help="fewer size classes and candidates")
     ap.add_argument("--only", default="", help="comma-separated subset: fp64,mixed,batch,fp64batch")
+    ap.add_argument("--merge", default="",
+                    help="start from this table (its .json record): the classes tuned now replace their entries")
     args = ap.parse_args(argv)
     import torch
 
@@ -244,6 +247,12 @@ def main(argv=None):
     nr._capi.check(nr.lib().nr_tuning_load(empty.encode()), "nr_tuning_load")
     only = set(args.only.split(",")) if args.only else {"fp64", "mixed", "batch", "fp64batch"}
     log, table, summary = [], {}, {}
+    if args.merge:
+        with open(args.merge + ".json") as f:
+            prev = json.load(f)
+        table, summary, log = dict(prev["table"]), dict(prev["summary"]), list(prev["measurements"])
+        tuned = {"fp64": "fp64 single", "mixed": "mixed single", "batch": "mixed batch", "fp64batch": "fp64 batch"}
+        log = [m for m in log if m.get("class") not in {tuned[k] for k in only}]
     t0 = time.time()
     if "fp64" in only:
         out, _ = tune_fp64_single(nr, torch, log, args.quick)

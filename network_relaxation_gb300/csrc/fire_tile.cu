@@ -629,32 +629,51 @@ cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FirePara
     return launch_cooperative((const void *)k_fire_tile_mixed, ctas, kTileThreads, args, tile_smem(tl), stream);
 }
 
-/* Spatial tiles of one network (see NetTile): about target_nodes nodes per
- * tile, the tile count a multiple of `ctas` (each CTA takes the same number
- * of tiles), cells of the box [0, width) x [miny, maxy] with the box's
- * aspect ratio.  Returns NR_OK with the layout in `out` (host arrays), or
- * NR_ERR_CAPACITY when a tile exceeds the 16-bit local encoding. */
+/* Spatial tiles of one network (see NetTile): at most about target_nodes
+ * nodes per tile, the tile count a multiple of `ctas`, equal-count cells in
+ * strips of the box [0, width) x [miny, maxy] with the box's aspect ratio.
+ * Returns NR_OK with the layout in `out` (host arrays), or NR_ERR_CAPACITY
+ * when a tile exceeds the 16-bit local encoding. */
 int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, bool use_bonds,
                       bool use_triples, int ctas, int target_nodes, TileHost &out) {
     const int n = h.n_points, ne = h.n_edges(), nt = h.n_triples();
-    const double W = h.offset, y0 = h.miny, H = std::max(h.maxy - h.miny, 1e-300);
+    const double W = h.offset, H = std::max(h.maxy - h.miny, 1e-300);
     if (n <= 0 || !(W > 0) || ctas < 1) return NR_ERR_INVALID;
     const long per = (long)ctas * target_nodes;
     const long want = (long)ctas * std::max(1L, (n + per - 1) / per);
-    const int ny = std::max(1, (int)std::lround(std::sqrt((double)want * H / W)));
-    const int nx = std::max(1, (int)((want + ny - 1) / ny));
-    std::vector<int> cell(n), count((size_t)nx * ny, 0);
+    const int ny = (int)std::min(want, std::max(1L, std::lround(std::sqrt((double)want * H / W))));
+    /* equal-count cells: ny strips of consecutive y, strip s cut into the
+     * cells [want s / ny, want (s + 1) / ny) of consecutive x (periodic x
+     * folded into [0, W)), each strip holding nodes in proportion to its
+     * cells: exactly `want` cells (a multiple of ctas), each owning n / want
+     * nodes however unevenly the nodes are spread (fibre networks), so no
+     * tile's record is much larger than the mean and every CTA takes the
+     * same number of tiles */
+    const long ncells = want;
+    std::vector<int> cell(n), count((size_t)ncells, 0), idx(n);
+    std::vector<double> xs(n);
     for (int i = 0; i < n; ++i) {
-        double x = h.points[2 * i], y = h.points[2 * i + 1];
-        x -= W * std::floor(x / W);
-        const int cx = std::min(nx - 1, std::max(0, (int)(x / W * nx)));
-        const int cy = std::min(ny - 1, std::max(0, (int)((y - y0) / H * ny)));
-        cell[i] = cy * nx + cx;
-        count[cell[i]]++;
+        idx[i] = i;
+        xs[i] = h.points[2 * i] - W * std::floor(h.points[2 * i] / W);
     }
-    std::vector<int> tile_of_cell((size_t)nx * ny, -1);
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+        const double ya = h.points[2 * a + 1], yb = h.points[2 * b + 1];
+        return ya < yb || (ya == yb && a < b);
+    });
+    for (int sy = 0; sy < ny; ++sy) {
+        const long c0 = ncells * sy / ny, c1 = ncells * (sy + 1) / ny;
+        const long lo = (long)n * c0 / ncells, hi = (long)n * c1 / ncells;
+        std::sort(idx.begin() + lo, idx.begin() + hi,
+                  [&](int a, int b) { return xs[a] < xs[b] || (xs[a] == xs[b] && a < b); });
+        for (long k = lo; k < hi; ++k) {
+            const long c = c0 + (k - lo) * (c1 - c0) / std::max(1L, hi - lo);
+            cell[idx[k]] = (int)c;
+            count[c]++;
+        }
+    }
+    std::vector<int> tile_of_cell((size_t)ncells, -1);
     int T = 0;
-    for (int c = 0; c < nx * ny; ++c)
+    for (long c = 0; c < ncells; ++c)
         if (count[c] > 0) tile_of_cell[c] = T++;
     std::vector<std::vector<int>> own(T);
     for (int i = 0; i < n; ++i) own[tile_of_cell[cell[i]]].push_back(i); /* ascending */

@@ -112,15 +112,32 @@ __device__ __forceinline__ float2 bond_dforce(float4 ra, float2 sk, float2 dh, f
     const float dd = s + lo;
     const float dx = dh.x + dlo.x, dy = dh.y + dlo.y;
     const float rx = rax + dx, ry = ray + dy;
-    const float rl = sqrtf(fmaf(rx, rx, ry * ry));
-    const float ral = sqrtf(fmaf(rax, rax, ray * ray));
-    const float inv_rl = 1.0f / rl;
-    const float dl = dd / (rl + ral);
+    /* hardware reciprocal square roots and an approximate quotient (a few
+     * ulp): their error is relative to the force CHANGE, like every other
+     * FP32 rounding here, and all of them are even in (ra, d) */
+    const float q2 = fmaf(rx, rx, ry * ry), qa2 = fmaf(rax, rax, ray * ray);
+    const float inv_rl = rsqrtf(q2), inv_ral = rsqrtf(qa2);
+    const float rl = q2 * inv_rl, ral = qa2 * inv_ral;
+    const float dl = __fdividef(dd, rl + ral);
     const float c1 = (dl + sk.x) * inv_rl;
     const float l0 = ral - sk.x;
-    const float c2 = l0 * dl * inv_rl / ral;
+    const float c2 = ((l0 * dl) * inv_rl) * inv_ral;
     const float k = sk.y;
     return make_float2(k * fmaf(dx, c1, rax * c2), k * fmaf(dy, c1, ray * c2));
+}
+
+/* atan2(im, re) for the bending-angle change since the anchor.  That
+ * change is small in nearly every call (re > 0, |im| <= re / 8): there the
+ * Taylor series atan t = t - t^3/3 + t^5/5 - t^7/7 + t^9/9 of t = im / re,
+ * whose next term is below 1e-10 t, replaces the full-range function;
+ * anything else goes to atan2f. */
+__device__ __forceinline__ float small_atan2(float im, float re) {
+    if (re > 0.0f && fabsf(im) <= 0.125f * re) {
+        const float t = __fdividef(im, re), z = t * t;
+        const float q = fmaf(fmaf(fmaf(fmaf(z, 1.0f / 9.0f, -1.0f / 7.0f), z, 1.0f / 5.0f), z, -1.0f / 3.0f), z, 0.0f);
+        return fmaf(t, q, t);
+    }
+    return atan2f(im, re);
 }
 
 __device__ __forceinline__ void tri_dforce(float4 arms, float2 pk, float2 dj, float2 dk, float2 &dFj, float2 &dFk) {
@@ -132,11 +149,12 @@ __device__ __forceinline__ void tri_dforce(float4 arms, float2 pk, float2 dj, fl
     const float zb_re = bb2 + db_dot, zb_im = fmaf(bax, dk.y, -(bay * dk.x));
     const float re = fmaf(zb_re, za_re, zb_im * za_im);
     const float im = fmaf(zb_im, za_re, -(zb_re * za_im));
-    const float dth = atan2f(im, re);
+    const float dth = small_atan2(im, re);
     const float ax = aax + dj.x, ay = aay + dj.y, bx = bax + dk.x, by = bay + dk.y;
-    const float ia2 = 1.0f / fmaf(ax, ax, ay * ay), ib2 = 1.0f / fmaf(bx, bx, by * by);
-    const float qa = fmaf(2.0f, da_dot, fmaf(dj.x, dj.x, dj.y * dj.y)) * ia2 / aa2;
-    const float qb = fmaf(2.0f, db_dot, fmaf(dk.x, dk.x, dk.y * dk.y)) * ib2 / bb2;
+    /* approximate reciprocals (a few ulp, relative to the change) */
+    const float ia2 = __fdividef(1.0f, fmaf(ax, ax, ay * ay)), ib2 = __fdividef(1.0f, fmaf(bx, bx, by * by));
+    const float qa = fmaf(2.0f, da_dot, fmaf(dj.x, dj.x, dj.y * dj.y)) * (ia2 * __fdividef(1.0f, aa2));
+    const float qb = fmaf(2.0f, db_dot, fmaf(dk.x, dk.x, dk.y * dk.y)) * (ib2 * __fdividef(1.0f, bb2));
     const float dgax = fmaf(-dj.y, ia2, aay * qa), dgay = fmaf(dj.x, ia2, -(aax * qa));
     const float dgbx = fmaf(-dk.y, ib2, bay * qb), dgby = fmaf(dk.x, ib2, -(bax * qb));
     const float gax = -ay * ia2, gay = ax * ia2, gbx = -by * ib2, gby = bx * ib2;

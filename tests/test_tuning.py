@@ -1,7 +1,7 @@
 """The launch-policy tuning table (tuning.cu): parsing, precedence of the
 environment over the table, errors; and the committed table of the GB300
-parses.  The table is process-wide state, so each test restores an empty
-table at the end."""
+parses.  The table is process-wide state, so each test loads the table in
+effect before it again at the end (an empty one if there was none)."""
 import math
 import os
 
@@ -15,10 +15,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 @pytest.fixture
 def lib(built, tmp_path):
     L = nr.lib()
+    before = L.nr_tuning_source().decode()
     yield L
-    empty = tmp_path / "empty.txt"
-    empty.write_text("")
-    assert L.nr_tuning_load(str(empty).encode()) == 0
+    if before:
+        assert L.nr_tuning_load(before.encode()) >= 0
+    else:
+        empty = tmp_path / "empty.txt"
+        empty.write_text("")
+        assert L.nr_tuning_load(str(empty).encode()) == 0
 
 
 def test_table_values_and_env_precedence(lib, tmp_path, monkeypatch):
