@@ -476,7 +476,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "algorithmic_bytes": bytes_launch, "peak_source": peak_kind,
                          "kernel": kname, "cluster_ctas": kcl, "plan": batch.plan(args.precision)},
-            "tuning_table": nr.lib().nr_tuning_source().decode() or None,
+            "tuning_table": tuning_table_name(nr),
             "clocks": clk,
             "wall_s_timed_region": wall,
         }
@@ -794,6 +794,16 @@ PROTOCOLS = {
 }
 
 
+def tuning_table_name(nr):
+    """The launch-policy table the library loaded, relative to the
+    repository when it lies inside it (None: built-in defaults)."""
+    src = nr.lib().nr_tuning_source().decode()
+    if not src:
+        return None
+    rel = os.path.relpath(os.path.realpath(src), os.path.realpath(ROOT))
+    return src if rel.startswith("..") else rel
+
+
 def protocol_arm(args):
     """--workload P5|P3: the strain protocol of C5 / C3 run end to end as
     one CUDA graph per precision (nr_sweep_graph: affine increment, FIRE
@@ -830,9 +840,10 @@ def protocol_arm(args):
                 break
     cap = min(args.max_steps, args.fire_cap) if args.fire_cap != 2000 else args.max_steps
     stream = torch.cuda.current_stream()
-    out = {}
+    out, plans = {}, {}
     for prec in ("mixed",) if args.no_fp64 else ("mixed", "fp64"):
         net = nr.Network(h, 1.0, kb)
+        plans[prec] = net.plan(prec)
         x0 = net.positions()
         prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
                              max_steps=cap, criterion="max", precision=prec)
@@ -882,7 +893,8 @@ def protocol_arm(args):
                           "stress_xy_rel_max": max(sxy_err) if sxy_err else None,
                           "stress_yy_rel_max": max(syy_err) if syy_err else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "k_fire_tile_mixed (mixed sweep)"},
+                     "traffic": None, "kernel": plans["mixed"]},
+        "plan_fp64": plans.get("fp64"),
         "curve_mixed": curve(rm), "curve_fp64": curve(rd),
         "gpu_launches": 4 * (len(rm) + len(rd)),
     }))

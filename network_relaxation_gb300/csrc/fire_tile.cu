@@ -467,41 +467,45 @@ __global__ void __launch_bounds__(kTileThreads, 1)
             }
             /* gather of the own nodes, half kick, the next step's state */
             const unsigned short *iptr = reinterpret_cast<const unsigned short *>(rec + g.iptr);
+            const unsigned short *ibe = reinterpret_cast<const unsigned short *>(rec + g.ibe);
             const unsigned short *inc = reinterpret_cast<const unsigned short *>(rec + g.inc);
             const unsigned char *fcode = rec + g.fcode;
             for (int kk = threadIdx.x; kk < no; kk += NT) {
                 const unsigned fc = fcode[kk];
-                const int e0 = iptr[kk], e1 = iptr[kk + 1];
+                const int e0 = iptr[kk], eb = ibe[kk], e1 = iptr[kk + 1];
                 const float2 ah = sc.fah[kk], al = sc.fal[kk];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
+                    /* the node's bond entries, then its triple entries (the
+                     * canonical order), each list without a branch per
+                     * entry; own nodes are ordered by list lengths */
                     float2 dF = make_float2(0.f, 0.f);
                     float mag = 0.f;
-                    for (int e = e0; e < e1; ++e) {
+                    for (int e = e0; e < eb; ++e) {
                         const unsigned code = inc[e];
-                        if (!(code & 0x8000u)) {
-                            float2 df = s_bdf[code >> 1];
-                            if (code & 1) df = make_float2(-df.x, -df.y);
-                            dF.x += df.x;
-                            dF.y += df.y;
-                            mag += fabsf(df.x) + fabsf(df.y);
+                        float2 df = s_bdf[code >> 1];
+                        if (code & 1) df = make_float2(-df.x, -df.y);
+                        dF.x += df.x;
+                        dF.y += df.y;
+                        mag += fabsf(df.x) + fabsf(df.y);
+                    }
+                    for (int e = eb; e < e1; ++e) {
+                        const unsigned code = inc[e];
+                        const int role = code & 3;
+                        const float4 qv = s_tdf[(code & 0x7fffu) >> 2];
+                        float gx, gy, mg;
+                        if (role == 0) {
+                            gx = -(qv.x + qv.z);
+                            gy = -(qv.y + qv.w);
+                            mg = fabsf(qv.x) + fabsf(qv.y) + fabsf(qv.z) + fabsf(qv.w);
                         } else {
-                            const int role = code & 3;
-                            const float4 qv = s_tdf[(code & 0x7fffu) >> 2];
-                            float gx, gy, mg;
-                            if (role == 0) {
-                                gx = -(qv.x + qv.z);
-                                gy = -(qv.y + qv.w);
-                                mg = fabsf(qv.x) + fabsf(qv.y) + fabsf(qv.z) + fabsf(qv.w);
-                            } else {
-                                gx = role == 1 ? qv.x : qv.z;
-                                gy = role == 1 ? qv.y : qv.w;
-                                mg = fabsf(gx) + fabsf(gy);
-                            }
-                            dF.x += gx;
-                            dF.y += gy;
-                            mag += mg;
+                            gx = role == 1 ? qv.x : qv.z;
+                            gy = role == 1 ? qv.y : qv.w;
+                            mg = fabsf(gx) + fabsf(gy);
                         }
+                        dF.x += gx;
+                        dF.y += gy;
+                        mag += mg;
                     }
                     A = fmaxf(A, mag);
                     F.x = ah.x + (al.x + dF.x);
@@ -521,7 +525,8 @@ __global__ void __launch_bounds__(kTileThreads, 1)
                 Fs += f2;
                 M2f = fmaxf(M2f, f2);
             }
-            __syncthreads();
+            /* the next tile's first barrier orders this gather's reads of the
+             * stage and state buffers before they are refilled */
         }
         cp_async_wait_all();
         warp_part(Part{P, V2, Fs, M2f, A}, sh.slots);
@@ -677,6 +682,17 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
         if (count[c] > 0) tile_of_cell[c] = T++;
     std::vector<std::vector<int>> own(T);
     for (int i = 0; i < n; ++i) own[tile_of_cell[cell[i]]].push_back(i); /* ascending */
+    /* within a tile, own nodes by their numbers of triple and bond entries:
+     * the lanes of a warp gather (nearly) equally long incidence lists */
+    auto entries = [&](int i, bool tri) {
+        if (tri) return use_triples ? inc.tptr[i + 1] - inc.tptr[i] : 0;
+        return use_bonds ? inc.bptr[i + 1] - inc.bptr[i] : 0;
+    };
+    for (std::vector<int> &o : own)
+        std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+            const int ta = entries(a, true), tb = entries(b, true);
+            return ta != tb ? ta > tb : entries(a, false) > entries(b, false);
+        });
     out = TileHost();
     out.n_tiles = T;
     /* tile-order positions: each tile's own range starts on a multiple of 16 */
@@ -692,7 +708,7 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
     for (int i = 0; i < n; ++i) out.node_of_pos[pos_of[i]] = i;
     std::vector<int> loc(n, -1), bslot(use_bonds ? ne : 0, -1), tslot(use_triples ? nt : 0, -1);
     std::vector<int> bl, tlist, halo;
-    std::vector<unsigned short> iptr, incv;
+    std::vector<unsigned short> iptr, ibe, incv;
     for (int t = 0; t < T; ++t) {
         const std::vector<int> &o = own[t];
         for (size_t k = 0; k < o.size(); ++k) loc[o[k]] = (int)k;
@@ -738,12 +754,14 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
         for (size_t k = 0; k < tlist.size(); ++k) tslot[tlist[k]] = (int)k;
         /* incidence of the own nodes, canonical order: bonds, then triples */
         iptr.clear();
+        ibe.clear();
         incv.clear();
         for (int i : o) {
             iptr.push_back((unsigned short)incv.size());
             if (use_bonds)
                 for (int e = inc.bptr[i]; e < inc.bptr[i + 1]; ++e)
                     incv.push_back((unsigned short)((bslot[inc.bent[e] >> 1] << 1) | (inc.bent[e] & 1)));
+            ibe.push_back((unsigned short)incv.size());
             if (use_triples)
                 for (int e = inc.tptr[i]; e < inc.tptr[i + 1]; ++e)
                     incv.push_back((unsigned short)(0x8000 | (tslot[inc.tent[e] >> 2] << 2) | (inc.tent[e] & 3)));
@@ -781,6 +799,7 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
             out.tid.push_back(qq);
         }
         memcpy(rec + g.iptr, iptr.data(), 2 * iptr.size());
+        if (!ibe.empty()) memcpy(rec + g.ibe, ibe.data(), 2 * ibe.size());
         if (!incv.empty()) memcpy(rec + g.inc, incv.data(), 2 * incv.size());
         for (size_t k = 0; k < o.size(); ++k) rec[g.fcode + k] = fcodes[o[k]];
         for (size_t k = 0; k < halo.size(); ++k) {

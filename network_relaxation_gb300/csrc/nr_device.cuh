@@ -161,9 +161,10 @@ struct NetDsm {
  * by each of them, identically).
  *
  * Node state lives in TILE ORDER: tile t's own nodes occupy positions
- * own_pos .. own_pos + no (ascending node id; own_pos a multiple of 16, the
+ * own_pos .. own_pos + no (own_pos a multiple of 16, the
  * range padded to whole 16s with unused positions), so a tile's own state is
- * contiguous; node_of_pos maps back to node ids (-1 for padding).
+ * contiguous; node_of_pos maps back to node ids (-1 for padding).  Own nodes
+ * are ordered within their tile by their numbers of incidence entries.
  *
  * Everything read-only that a tile reads in a FIRE step is one contiguous,
  * 16-byte aligned record in `ro`, staged into shared memory by TMA bulk
@@ -175,6 +176,8 @@ struct NetDsm {
  *   arms  nt x float4   anchor arms {a.x, a.y, b.x, b.y}
  *   pk    nt x float2   {theta_anchor - pi, kb}
  *   iptr  (no+1) x u16  incidence range of each own node (relative)
+ *   ibe   no x u16      end of each own node's bond entries (its triple
+ *                       entries follow up to the next iptr)
  *   inc   ni x u16      entries in the canonical order (bonds, then
  *                       triples): bond slot << 1 | role, triple 0x8000 |
  *                       slot << 2 | role
@@ -192,7 +195,7 @@ struct TileDesc {
     int pad;
 };
 struct TileSegs {
-    unsigned bref, mb, sk, tref, arms, pk, iptr, inc, fcode, halo, total; /* byte offsets in a tile record */
+    unsigned bref, mb, sk, tref, arms, pk, iptr, ibe, inc, fcode, halo, total; /* byte offsets in a tile record */
 };
 __host__ __device__ inline unsigned tile_pad16(unsigned b) { return (b + 15u) & ~15u; }
 __host__ __device__ inline TileSegs tile_segs(int nb, int nt, int no, int ni, int nh) {
@@ -205,6 +208,7 @@ __host__ __device__ inline TileSegs tile_segs(int nb, int nt, int no, int ni, in
     g.arms = o;  o += 16u * nt;
     g.pk = o;    o += tile_pad16(8u * nt);
     g.iptr = o;  o += tile_pad16(2u * (no + 1));
+    g.ibe = o;   o += tile_pad16(2u * no);
     g.inc = o;   o += tile_pad16(2u * ni);
     g.fcode = o; o += tile_pad16(1u * no);
     g.halo = o;  o += tile_pad16(4u * nh);
