@@ -485,6 +485,14 @@ def main():
             e_or = np.array([float.fromhex(r["e_stretch"]) + float.fromhex(r["e_bend"]) for r in rows])
             e_gpu = np.array([r.e_stretch + r.e_bend for r in reps])
             line["energy_rel_err_vs_fp64_oracle"] = error_stats(e_gpu, e_or, oracle_uncertainty(batch_idx))
+            e_min = converged_energies(batch_idx)
+            if e_min is not None:
+                d_gpu = np.abs(e_gpu - e_min) / np.abs(e_min)
+                d_or = np.abs(e_or - e_min) / np.abs(e_min)
+                line["energy_vs_converged_fp64_minimum"] = {
+                    "what": "relative distance from the FP64 oracle's energy continued to max|F| < 1e-12",
+                    "this_run": error_stats(e_gpu, e_min), "fp64_oracle_at_1e-10": error_stats(e_or, e_min),
+                    "n_farther_than_max_1e-10_and_oracle": int((d_gpu > np.maximum(1e-10, d_or)).sum())}
             line["fp64_node_iterations"] = c4["node_iterations"]
     if rank == 0 and not args.no_fp64 and c4 is not None and args.precision == "mixed":
         line["fp64_batched"] = fp64_batched(nr, hosts, kappa, gamma, batch_idx, c4, sp, reps, out_host.numpy(),
@@ -521,6 +529,19 @@ def oracle_uncertainty(batch_idx):
         r = pol.get(i)
         out.append(abs(r["rel_change"]) if r else None)
     return out
+
+
+def converged_energies(batch_idx):
+    """Per network, the FP64 oracle's energy continued to max|F| < 1e-12
+    (tests/golden/c4_oracle_polish.json), or None when the fixture is
+    absent."""
+    path = os.path.join(ROOT, "tests", "golden", "c4_oracle_polish.json")
+    if not os.path.exists(path):
+        return None
+    pol = {r["index"]: r for r in json.load(open(path))["networks"]}
+    if any(i not in pol for i in batch_idx):
+        return None
+    return np.array([float.fromhex(pol[i]["e_stretch"]) + float.fromhex(pol[i]["e_bend"]) for i in batch_idx])
 
 
 def error_stats(got, ref, uncertainty=None, bar=1e-10):

@@ -67,7 +67,7 @@ struct Image {
 
 struct NetOff {
     size_t mb_data, mb_sk, bdf, mt_arms, mt_pk, tdf, bfrc, tfrc;
-    size_t dsm_bref, dsm_bidx, dsm_tref, dsm_bent, dsm_tent;
+    size_t dsm_bref, dsm_bidx, dsm_tref, dsm_bent, dsm_tent, dsm_grec;
     size_t fcode, bond, bond_l0, bond_k, tri, tri_kb, tri_phi0, bptr, bent, tptr, tent, part, epart;
     size_t elem, elem_inv, elem_area, efrc, eptr, eent, partner;
     bool has_bond_k, has_tri_kb, has_tri_phi0;
@@ -124,9 +124,11 @@ struct DeviceSet {
 /* Sub-block layout of one network for the distributed-shared-memory kernels
  * (NetDsm, nr_device.cuh): item slots grouped by the sub-block of the
  * bond's node i / the triple's hinge, in index order within a group; node
- * references and resolved incidence entries.  m.bsub = 0 when the network
- * is too large for the encoding (more than 2^20 nodes). */
-static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Image &img, NetOff &o, NetDsm &m) {
+ * references and resolved incidence entries; per node, in gather order,
+ * its gather record.  m.bsub = 0 when the network is too large for the
+ * encoding (more than 2^20 nodes). */
+static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, Image &img,
+                             NetOff &o, NetDsm &m) {
     const int n = h.n_points, ne = h.n_edges(), nt = h.n_triples();
     memset(&m, 0, sizeof(m));
     /* sub-blocks of a whole number of 32-node chunks: a CTA's nodes then
@@ -138,7 +140,7 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
     auto ref = [&](int v) { return (part(v) << 16) | (v % bsub); };
     std::vector<int2> bref(fits ? ne : 0);
     std::vector<int> bidx(fits ? ne : 0), bslot(fits ? ne : 0), dbent(fits ? inc.bent.size() : 0);
-    std::vector<int4> tref(fits ? nt : 0);
+    std::vector<int4> tref(fits ? nt : 0), grec(fits ? n : 0);
     std::vector<int> tslot(fits ? nt : 0), dtent(fits ? inc.tent.size() : 0);
     if (fits) {
         int cnt[kDsmParts + 1] = {0};
@@ -177,6 +179,25 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
             m.be[g] = inc.bptr[v];
             m.te[g] = inc.tptr[v];
         }
+        /* gather records: within each sub-block the nodes ordered by their
+         * numbers of triple and bond entries, so the lanes of a warp walk
+         * (nearly) equally long lists */
+        std::vector<int> ord;
+        for (int g = 0; g * bsub < n; ++g) {
+            const int v0 = g * bsub, v1 = std::min(n, v0 + bsub);
+            ord.resize(v1 - v0);
+            for (int v = v0; v < v1; ++v) ord[v - v0] = v;
+            auto nbe = [&](int v) { return inc.bptr[v + 1] - inc.bptr[v]; };
+            auto nte = [&](int v) { return inc.tptr[v + 1] - inc.tptr[v]; };
+            std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+                return nte(a) != nte(b) ? nte(a) > nte(b) : nbe(a) > nbe(b);
+            });
+            for (int k = 0; k < v1 - v0; ++k) {
+                const int v = ord[k];
+                grec[v0 + k] = make_int4(v | ((int)(fcodes[v] & 3u) << 28), inc.bptr[v], nbe(v) | (nte(v) << 16),
+                                         inc.tptr[v]);
+            }
+        }
         m.bsub = bsub;
     }
     o.dsm_bref = img.put(bref.data(), bref.size());
@@ -184,6 +205,7 @@ static void build_dsm_layout(const nr_host_network &h, const Incidence &inc, Ima
     o.dsm_tref = img.put(tref.data(), tref.size());
     o.dsm_bent = img.put(dbent.data(), dbent.size());
     o.dsm_tent = img.put(dtent.data(), dtent.size());
+    o.dsm_grec = img.put(grec.data(), grec.size());
 }
 
 /* Networks of at least NR_TILE_MIN_NODES nodes (default 131072) relaxed
@@ -394,7 +416,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         o.eptr = img.put(eptr.data(), eptr.size());
         o.eent = img.put(eent.data(), eent.size());
         o.partner = img.put(partner.data(), partner.size());
-        build_dsm_layout(h, inc, img, o, S.dsm[i]);
+        build_dsm_layout(h, inc, fc.data(), img, o, S.dsm[i]);
         if (want_tile && i == 0) {
             inc0 = std::move(inc);
             fc0 = fc;
@@ -501,6 +523,7 @@ static int build_set(int n, const nr_host_network *const *nets, const double *ks
         m.tref = (const int4 *)(base + o.dsm_tref);
         m.bent = (const int *)(base + o.dsm_bent);
         m.tent = (const int *)(base + o.dsm_tent);
+        m.grec = (const int4 *)(base + o.dsm_grec);
     }
     S.dsm_array = (NetDsm *)(base + dsm_off);
     memcpy(img.bytes.data() + dsm_off, S.dsm.data(), sizeof(NetDsm) * n);

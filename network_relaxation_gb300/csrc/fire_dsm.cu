@@ -67,7 +67,7 @@ struct DsmSizes {
     int resident;
 };
 struct DsmLayout {
-    size_t u, tdf, mb, arms, tref, v, f, bdf, fahi, falo, sk, pk, bref, bptr, tptr, bent, tent, total;
+    size_t u, tdf, mb, arms, tref, grec, v, f, bdf, fahi, falo, sk, pk, bref, bent, tent, total;
 };
 __host__ __device__ inline DsmLayout dsm_layout(const DsmSizes &z) {
     const size_t R = z.resident ? 1 : 0, bm = (size_t)z.bmax, em = (size_t)z.emax, tm = (size_t)z.tmax;
@@ -78,6 +78,7 @@ __host__ __device__ inline DsmLayout dsm_layout(const DsmSizes &z) {
     L.mb = o;   o += R * 16 * em;
     L.arms = o; o += R * 16 * tm;
     L.tref = o; o += R * 16 * tm;
+    L.grec = o; o += R * 16 * bm;
     L.v = o;    o += 8 * bm;
     L.f = o;    o += 8 * bm;
     L.bdf = o;  o += 8 * em;
@@ -86,8 +87,6 @@ __host__ __device__ inline DsmLayout dsm_layout(const DsmSizes &z) {
     L.sk = o;   o += R * 8 * em;
     L.pk = o;   o += R * 8 * tm;
     L.bref = o; o += R * 8 * em;
-    L.bptr = o; o += R * 4 * (bm + 1);
-    L.tptr = o; o += R * 4 * (bm + 1);
     L.bent = o; o += R * 4 * (size_t)z.ebmax;
     L.tent = o; o += R * 4 * (size_t)z.etmax;
     L.total = o;
@@ -195,8 +194,7 @@ __global__ void __launch_bounds__(NT, 1)
                      reinterpret_cast<float2 *>(dyn + L.fahi), reinterpret_cast<float2 *>(dyn + L.falo)};
     int4 *s_tref = reinterpret_cast<int4 *>(dyn + L.tref);
     int2 *s_bref = reinterpret_cast<int2 *>(dyn + L.bref);
-    int *s_bptr = reinterpret_cast<int *>(dyn + L.bptr);
-    int *s_tptr = reinterpret_cast<int *>(dyn + L.tptr);
+    int4 *s_grec = reinterpret_cast<int4 *>(dyn + L.grec);
     int *s_bent = reinterpret_cast<int *>(dyn + L.bent);
     int *s_tent = reinterpret_cast<int *>(dyn + L.tent);
     __shared__ MixShared sh;
@@ -256,11 +254,7 @@ __global__ void __launch_bounds__(NT, 1)
         const int eb0 = m.be[rank * spr], eb1 = m.be[(rank + 1) * spr];
         const int et0 = m.te[rank * spr], et1 = m.te[(rank + 1) * spr];
         if (R) { /* the CTA's read-only slices into shared memory */
-            if (nloc > 0)
-                for (int k = threadIdx.x; k <= nloc; k += NT) {
-                    s_bptr[k] = d.bptr[n0 + k];
-                    s_tptr[k] = d.tptr[n0 + k];
-                }
+            for (int k = threadIdx.x; k < nloc; k += NT) s_grec[k] = m.grec[n0 + k];
             for (int k = threadIdx.x; k < eb1 - eb0; k += NT) s_bent[k] = m.bent[eb0 + k];
             for (int k = threadIdx.x; k < et1 - et0; k += NT) s_tent[k] = m.tent[et0 + k];
             if (d.use_bonds)
@@ -275,8 +269,7 @@ __global__ void __launch_bounds__(NT, 1)
         const int4 *Tref = R ? s_tref : m.tref + t0;
         const float4 *Arms = R ? res.arms : d.mt_arms + t0;
         const float2 *Pk = R ? res.pk : d.mt_pk + t0;
-        const int *Bp = R ? s_bptr : d.bptr + n0;
-        const int *Tp = R ? s_tptr : d.tptr + n0;
+        const int4 *Gr = R ? s_grec : m.grec + n0;
         const int *Be = R ? s_bent : m.bent + eb0;
         const int *Te = R ? s_tent : m.tent + et0;
         const float2 *FaH = R ? res.fahi : d.fa_hi + n0;
@@ -433,14 +426,18 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
             cl.sync();
-            /* gather: F = F(X) + the node's entries in incidence order, half kick */
+            /* gather: F = F(X) + the node's entries in incidence order, half
+             * kick; the nodes in gather-record order (lanes of a warp take
+             * nodes with equally long entry lists) */
             float P = 0.f, V2 = 0.f, Fs = 0.f, M2f = 0.f, A = 0.f;
-            for (int li = threadIdx.x; li < nloc; li += NT) {
-                const int i = n0 + li;
-                /* the node's independent global loads first: one round trip */
-                const unsigned fc = __ldg(d.fcode + i);
-                const int bq0 = ldro<RES>(Bp + li) - eb0, bq1 = ldro<RES>(Bp + li + 1) - eb0;
-                const int tq0 = ldro<RES>(Tp + li) - et0, tq1 = ldro<RES>(Tp + li + 1) - et0;
+            for (int k = threadIdx.x; k < nloc; k += NT) {
+                /* one record load gives the node, its fcode and both entry
+                 * ranges */
+                const int4 g = ldro<RES>(Gr + k);
+                const int li = (g.x & 0x0fffffff) - n0;
+                const unsigned fc = (unsigned)g.x >> 28;
+                const int bq0 = g.y - eb0, bq1 = bq0 + (g.z & 0xffff);
+                const int tq0 = g.w - et0, tq1 = tq0 + ((unsigned)g.z >> 16);
                 const float2 ah = FaH[li], al = FaL[li];
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {

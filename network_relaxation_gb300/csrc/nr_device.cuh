@@ -151,6 +151,11 @@ struct NetDsm {
     const int *bidx;                          /* per bond slot: bond index */
     const int4 *tref;                         /* per triple slot: references of h, j, k; triple index */
     const int *bent, *tent;
+    /* gather records, per node slot: within each sub-block the nodes by
+     * decreasing numbers of triple, then bond entries; {node | fcode << 28,
+     * first bond entry, bond entries | triple entries << 16, first triple
+     * entry} (entries: indices into bent / tent) */
+    const int4 *grec;
 };
 
 /* Layout of one large network for the tiled mixed-precision kernel
