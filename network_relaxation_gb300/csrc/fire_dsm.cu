@@ -276,8 +276,12 @@ __global__ void __launch_bounds__(NT, 1)
         const float2 *FaL = R ? res.falo : d.fa_lo + n0;
         if (threadIdx.x == 0) s_flag = ((volatile FireState *)d.st)->yielded;
         __syncthreads();
-        MixScal s; /* replicated in thread 0 of every CTA */
-        MixParams q;
+        /* the FIRE scalars, advanced by thread 0 of every CTA (identical
+         * copies), in shared memory: registers stay free for the passes */
+        __shared__ MixScal s_mix;
+        __shared__ MixParams s_mq;
+        MixScal &s = s_mix;
+        MixParams &q = s_mq;
         double F2, M2, tF2, tM2;
         if (s_flag) {
             /* resume a network a smaller cluster left at an anchor: u = 0,
@@ -430,6 +434,11 @@ __global__ void __launch_bounds__(NT, 1)
              * kick; the nodes in gather-record order (lanes of a warp take
              * nodes with equally long entry lists) */
             float P = 0.f, V2 = 0.f, Fs = 0.f, M2f = 0.f, A = 0.f;
+            /* rank 0 reads the idle-cluster count now; its global-memory
+             * latency passes during the gather instead of before the
+             * cluster barrier */
+            int idle = 0;
+            if (rank == 0 && threadIdx.x == 0 && yield_at > 0) idle = *(volatile int *)(queue + 1);
             for (int k = threadIdx.x; k < nloc; k += NT) {
                 /* one record load gives the node, its fcode and both entry
                  * ranges */
@@ -502,7 +511,7 @@ __global__ void __launch_bounds__(NT, 1)
                 const Part t = block_totals(sh.slots);
                 if (threadIdx.x == 0) {
                     s_part = t;
-                    if (rank == 0) s_yield = yield_at > 0 && *(volatile int *)(queue + 1) >= yield_at;
+                    if (rank == 0) s_yield = yield_at > 0 && idle >= yield_at;
                 }
             }
             cl.sync();
