@@ -19,7 +19,8 @@ classes tuned now.  Knobs and size classes:
                          on a cluster instead of the grid kernel): time per
                          FIRE step on lattices of 32^2 .. 181^2 nodes
   mixed, one network     NR_TILE_MIN_NODES (smallest network run on the tiled
-                         kernel), NR_TILE_NODES (nodes per tile): time per
+                         kernel), NR_TILE_THREADS (512: one CTA per SM, 256:
+                         two), NR_TILE_NODES (nodes per tile): time per
                          FIRE step on lattices of 128^2 .. 1024^2 nodes
   mixed, batches         NR_CLUSTER (CTAs per network in the first phase),
                          NR_ESCALATE (idle fraction that triggers escalation),
@@ -126,7 +127,10 @@ def tune_fp64_single(nr, torch, log, quick):
 
 def tune_mixed_single(nr, torch, log, quick):
     sides = [128, 256, 512, 1024] if not quick else [256, 1024]
-    tiles = [256, 384, 512]  # larger targets are halved to fit shared memory anyway
+    # (threads per CTA, tile nodes): one 512-thread CTA per SM, or two
+    # 256-thread CTAs per SM with smaller tiles; larger targets are cut down
+    # to fit shared memory anyway
+    tiles = [(512, 512), (512, 384), (256, 256), (256, 192)]
     res = {}
     for L in sides:
         h = nr.HostNetwork.lattice(L, L, 0.65, 0.05, 5, line_triples=True)
@@ -134,18 +138,19 @@ def tune_mixed_single(nr, torch, log, quick):
             us, plan = per_step_us(nr, torch, h, 1e-4, "mixed", 1000)
         res[(L, "grid")] = us
         log.append({"class": "mixed single", "nodes": L * L, "kernel": "grid", "us_per_step": us, "plan": plan})
-        for t in tiles:
-            with knobs(NR_MIX_KERNEL=None, NR_TILE_MIN_NODES=1, NR_TILE_NODES=t):
+        for th, t in tiles:
+            with knobs(NR_MIX_KERNEL=None, NR_TILE_MIN_NODES=1, NR_TILE_THREADS=th, NR_TILE_NODES=t):
                 us, plan = per_step_us(nr, torch, h, 1e-4, "mixed", 1000)
-            res[(L, "tile", t)] = us
-            log.append({"class": "mixed single", "nodes": L * L, "kernel": "tile", "tile_nodes": t,
+            res[(L, "tile", th, t)] = us
+            log.append({"class": "mixed single", "nodes": L * L, "kernel": "tile", "threads": th, "tile_nodes": t,
                         "us_per_step": us, "plan": plan})
     out = {}
     big = sides[-1]
-    out["NR_TILE_NODES"] = min(tiles, key=lambda t: res[(big, "tile", t)])
+    best = min(tiles, key=lambda v: res[(big, "tile") + v])
+    out["NR_TILE_THREADS"], out["NR_TILE_NODES"] = best
     thr = None
     for L in sides:
-        if min(res[(L, "tile", t)] for t in tiles) < res[(L, "grid")]:
+        if res[(L, "tile") + best] < res[(L, "grid")]:
             thr = L * L if thr is None else thr
         else:
             thr = None  # the tiled kernel must win from its threshold upwards

@@ -112,6 +112,7 @@ struct DeviceSet {
     NetTile tile{};
     char *tile_mem = nullptr;
     int tile_ctas = 0;
+    int tile_threads = 512;
     ~DeviceSet() {
         if (tile_mem) cudaFree(tile_mem);
         if (arena) cudaFree(arena);
@@ -220,24 +221,38 @@ static int tile_target_nodes() {
     const int v = env ? atoi(env) : 512;
     return v >= 64 && v <= 8192 ? v : 512;
 }
+/* Threads per CTA of the tiled kernel (NR_TILE_THREADS): 512, one CTA per
+ * SM (default), or 256, two CTAs per SM. */
+static int tile_threads() {
+    const char *env = knob("NR_TILE_THREADS");
+    return env && atoi(env) == 256 ? 256 : 512;
+}
 
 /* Builds and uploads the tiled layout of network 0 of S (one allocation);
  * leaves S.tile_ctas = 0 when the network does not fit its encoding or the
- * kernel cannot launch.  One CTA per SM; the tile size is the largest of
- * NR_TILE_NODES, half of it, a quarter ... whose two stage buffers and
- * working arrays fit shared memory. */
+ * kernel cannot launch.  One or two CTAs per SM (NR_TILE_THREADS); the
+ * tile size is the largest of NR_TILE_NODES, 4/5 of it, 16/25 ... whose two
+ * stage buffers and working arrays fit the CTA's shared memory. */
 static int build_tile_set(const nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, DeviceSet &S,
                           cudaStream_t stream) {
     int dev = 0, sms = 0, optin = 0;
     NR_CUDA_TRY(cudaGetDevice(&dev));
     NR_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     NR_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    int per_sm_smem = 0;
+    NR_CUDA_TRY(cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    const int threads = tile_threads(), per_sm = threads == 256 ? 2 : 1;
+    /* dynamic shared memory a CTA may take: the opt-in maximum less a
+     * margin, or, when two CTAs share the SM, half of it less the per-CTA
+     * reservation and the kernel's static shared memory */
+    const size_t limit = per_sm == 1 ? (size_t)optin - 8192 : (size_t)per_sm_smem / 2 - 3072;
     const NetDev &d = S.dev[0];
     TileHost th;
     NetTile &tl = S.tile;
     bool ok = false;
-    for (int target = tile_target_nodes(); target >= 64 && !ok; target /= 2) {
-        if (build_tile_layout(h, inc, fcodes, d.use_bonds != 0, d.use_triples != 0, sms, target, th) != NR_OK)
+    for (int target = tile_target_nodes(); target >= 64 && !ok; target = target * 4 / 5) {
+        if (build_tile_layout(h, inc, fcodes, d.use_bonds != 0, d.use_triples != 0, per_sm * sms, target, th) !=
+            NR_OK)
             return NR_OK;
         tl = NetTile{};
         tl.n_tiles = th.n_tiles;
@@ -247,7 +262,7 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
         tl.max_tris = th.max_tris;
         tl.max_own = th.max_own;
         tl.max_ro = th.max_ro;
-        ok = tile_smem(tl) + 8192 <= (size_t)optin;
+        ok = tile_smem(tl) <= limit;
     }
     if (!ok) return NR_OK;
     /* every tile record is a whole number of 16-byte units at a 16-byte
@@ -255,7 +270,7 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
     for (const TileDesc &td : th.desc)
         if (td.ro_off % 16 != 0 || tile_segs(td.nb, td.nt, td.no, td.ni, td.nh).total % 16 != 0)
             return fail(NR_ERR_INVALID, "tile layout: record not 16-byte aligned");
-    const int ctas = tile_grid_ctas(tile_smem(tl));
+    const int ctas = tile_grid_ctas(tile_smem(tl), threads);
     if (ctas < 1) {
         cudaGetLastError();
         return NR_OK;
@@ -302,6 +317,7 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
     tl.dpart = (double *)(b + o_dpart);
     tl.bar = (unsigned long long *)(b + o_bar);
     S.tile_ctas = ctas;
+    S.tile_threads = threads;
     return NR_OK;
 }
 
@@ -605,6 +621,7 @@ struct GridPlan {
     bool mixed;
     bool tile;   /* mixed: the tiled kernel (fire_tile.cu) */
     NetTile tl;
+    int tile_threads = 512;
     /* FP64 on a cluster: the distributed-shared-memory kernel (dsm64) with
      * its per-CTA maxima, else the L2 one */
     bool dsm64;
@@ -687,6 +704,7 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
         g.tile = true;
         g.tl = S.tile;
         g.blocks = S.tile_ctas;
+        g.tile_threads = S.tile_threads;
     } else if (mixed) {
         g.blocks = mixed_grid_blocks(g.d.n);
         if (g.blocks <= 0) return fail(NR_ERR_CUDA, "occupancy query failed");
@@ -725,7 +743,9 @@ static int grid_plan(const DeviceSet &S, int i, bool mixed, GridPlan &g) {
  * capture records it into a graph. */
 static int enqueue_grid(const GridPlan &g, const nr_fire_params &prm, cudaStream_t stream) {
     NR_CUDA_TRY(cudaMemsetAsync(g.d.st, 0, sizeof(FireState), stream));
-    if (g.tile) NR_CUDA_TRY(launch_mixed_tile(g.d, g.tl, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
+    if (g.tile)
+        NR_CUDA_TRY(
+            launch_mixed_tile(g.d, g.tl, to_dev(prm), g.blocks, g.tile_threads, barrier_budget_ns(), stream));
     else if (g.mixed) NR_CUDA_TRY(launch_mixed_grid(g.d, to_dev(prm), g.blocks, barrier_budget_ns(), stream));
     else if (g.cluster > 0) {
         /* the cluster kernels take their energies themselves */
@@ -1575,8 +1595,8 @@ int nr_network_plan(nr_network *d, int precision, char *buf, size_t cap) {
         const int rc = grid_plan(d->set, 0, precision == NR_MIXED, g);
         if (rc != NR_OK) return rc;
         if (g.tile)
-            snprintf(out, sizeof out, "k_fire_tile_mixed ctas=%d tiles=%d max_tile_nodes=%d", g.blocks, g.tl.n_tiles,
-                     g.tl.max_nodes);
+            snprintf(out, sizeof out, "k_fire_tile_mixed ctas=%d threads=%d tiles=%d max_tile_nodes=%d", g.blocks,
+                     g.tile_threads, g.tl.n_tiles, g.tl.max_nodes);
         else if (g.mixed) snprintf(out, sizeof out, "k_fire_grid_mixed ctas=%d", g.blocks);
         else if (g.cluster > 0) snprintf(out, sizeof out, "%s cluster=%d", g.dsm64 ? "k_fire_dsm64" : "k_fire_cluster", g.cluster);
         else snprintf(out, sizeof out, "k_fire_grid ctas=%d sub=%d", g.blocks, g.d.sub);

@@ -105,8 +105,8 @@ struct Incidence;
 int build_tile_layout(const ::nr_host_network &h, const Incidence &inc, const unsigned char *fcodes, bool use_bonds,
                       bool use_triples, int ctas, int target_nodes, TileHost &out);
 size_t tile_smem(const NetTile &tl);
-int tile_grid_ctas(size_t smem);
-cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas,
+int tile_grid_ctas(size_t smem, int threads);
+cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas, int threads,
                               unsigned long long budget_ns, cudaStream_t stream);
 int mixed_grid_blocks(int n);
 cudaError_t launch_mixed_grid(const NetDev &d, const FireParamsDev &p, int blocks, unsigned long long budget_ns,

@@ -278,7 +278,9 @@ static __device__ __noinline__ void tile_anchor_totals(const NetTile &tl, int G,
     M2 = m;
 }
 
-constexpr int kTileThreads = 512;
+/* Instantiated for 512 threads per CTA with one CTA per SM, and for 256
+ * threads with two CTAs per SM (smaller tiles; one CTA's barriers overlap
+ * the other's work). */
 
 /* Dynamic shared memory of a CTA: two record buffers of max_ro bytes, two
  * node-state buffers, the item results of one tile. */
@@ -288,7 +290,8 @@ __host__ __device__ inline size_t tile_smem_bytes(unsigned max_ro, int max_nodes
            8 * (size_t)max_bonds;
 }
 
-__global__ void __launch_bounds__(kTileThreads, 1)
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     k_fire_tile_mixed(NetDev d, NetTile tl, FireParamsDev p, unsigned long long budget_ns) {
     extern __shared__ float4 s_dyn[];
     __shared__ MixShared sh;
@@ -297,7 +300,6 @@ __global__ void __launch_bounds__(kTileThreads, 1)
     /* FIRE scalars, advanced by thread 0 of every CTA (identical copies) */
     __shared__ MixScal s;
     __shared__ MixParams q;
-    constexpr int NT = kTileThreads;
     unsigned char *dyn = reinterpret_cast<unsigned char *>(s_dyn);
     unsigned char *const stage0 = dyn, *const stage1 = dyn + tl.max_ro;
     const size_t sbytes = tile_state_bytes(tl.max_nodes, tl.max_own);
@@ -607,23 +609,28 @@ size_t tile_smem(const NetTile &tl) {
     return tile_smem_bytes(tl.max_ro, tl.max_nodes, tl.max_own, tl.max_bonds, tl.max_tris);
 }
 
+/* The kernel instantiation for `threads` per CTA (512 or 256). */
+static const void *tile_kernel(int threads) {
+    return threads == 256 ? (const void *)k_fire_tile_mixed<256, 2> : (const void *)k_fire_tile_mixed<512, 1>;
+}
+
 /* CTAs of the cooperative launch: co-resident CTAs per SM times SMs (0 when
  * the kernel cannot launch with this shared memory). */
-int tile_grid_ctas(size_t smem) {
+int tile_grid_ctas(size_t smem, int threads) {
     int dev = 0, sms = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaFuncSetAttribute(k_fire_tile_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fire_tile_mixed, kTileThreads, smem) != cudaSuccess)
+    const void *k = tile_kernel(threads);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads == 256 ? 256 : 512, smem) != cudaSuccess)
         return 0;
     return per_sm * sms;
 }
 
-cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas,
+cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FireParamsDev &p, int ctas, int threads,
                               unsigned long long budget_ns, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(k_fire_tile_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tile_smem(tl));
+    const void *k = tile_kernel(threads);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem(tl));
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(tl.bar, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
     NetDev dd = d;
@@ -631,7 +638,7 @@ cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FirePara
     FireParamsDev pp = p;
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &tt, &pp, &bb};
-    return launch_cooperative((const void *)k_fire_tile_mixed, ctas, kTileThreads, args, tile_smem(tl), stream);
+    return launch_cooperative(k, ctas, threads == 256 ? 256 : 512, args, tile_smem(tl), stream);
 }
 
 /* Spatial tiles of one network (see NetTile): at most about target_nodes

@@ -218,15 +218,18 @@ def test_sweep_graph_mixed_grid_equals_step_by_step(cuda):
     assert np.array_equal(pos, ppos)
 
 
+@pytest.mark.parametrize("threads", ["512", "256"])
 @pytest.mark.parametrize("case", ["jitter", "per_item"])
-def test_mixed_tile_kernel_certified(cuda, case, monkeypatch):
-    """The tiled kernel on a jittered lattice with generator triples (rest
-    angles), and on one with a stiffness per bond and per triple (random in
-    [0.5, 2] and [1e-3, 1e-2], as Mikado networks have): every state
-    certified by the oracle's FP64 force, energies within the bar, and the
-    tiled sweep as one CUDA graph equal to the step-by-step sweep."""
+def test_mixed_tile_kernel_certified(cuda, case, threads, monkeypatch):
+    """The tiled kernel (one 512-thread CTA or two 256-thread CTAs per SM)
+    on a jittered lattice with generator triples (rest angles), and on one
+    with a stiffness per bond and per triple (random in [0.5, 2] and
+    [1e-3, 1e-2], as Mikado networks have): every state certified by the
+    oracle's FP64 force, energies within the bar, and the tiled sweep as one
+    CUDA graph equal to the step-by-step sweep."""
     monkeypatch.setenv("NR_TILE_MIN_NODES", "1000")
     monkeypatch.setenv("NR_TILE_NODES", "128")
+    monkeypatch.setenv("NR_TILE_THREADS", threads)
     h = nr.HostNetwork.lattice(70, 70, 0.8, 0.05, 17 if case == "jitter" else 19, line_triples=True)
     ks, kb, fire = 1.0, 1e-2, dict(FIRE)
     if case == "per_item":
@@ -240,6 +243,7 @@ def test_mixed_tile_kernel_certified(cuda, case, monkeypatch):
     assert len(a["points"]) > 4096  # above the one-CTA size: a grid-wide kernel
     H = a["maxy"] - a["miny"]
     net = nr.Network(h, ks, kb)
+    assert net.plan("mixed").startswith("k_fire_tile_mixed") and ("threads=%s" % threads) in net.plan("mixed")
     net.affine_displace(a["miny"], H, 0.02 * H, 0.0)
     prm = nr.fire_params(fcut=1e-10, criterion="max", precision="mixed", **fire)
     rep = net.relax(prm)
