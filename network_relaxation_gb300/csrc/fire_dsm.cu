@@ -28,26 +28,6 @@
 
 namespace nr {
 
-/* 32-bit shared::cluster address of shared-memory location p in CTA `rank`. */
-__device__ __forceinline__ unsigned dsm_addr(const void *p, unsigned rank) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    unsigned r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-    return r;
-}
-__device__ __forceinline__ float2 dsm_ld2(unsigned a) {
-    float2 v;
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
-    return v;
-}
-__device__ __forceinline__ float4 dsm_ld4(unsigned a) {
-    float4 v;
-    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "r"(a));
-    return v;
-}
-
 /* Shared::cluster address of the u of node reference `ref` (sub-block << 16
  * | index in it) when each CTA owns spr = 2^lg sub-blocks of bsub nodes;
  * au[r] = address of CTA r's s_u. */
@@ -201,9 +181,12 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ NetDev s_d;
     __shared__ NetDsm s_m;
     __shared__ int s_slot;
-    __shared__ Part s_part;
-    __shared__ double s_anc[2];
-    __shared__ int s_yield; /* rank 0: half the clusters are idle, escalate */
+    /* every CTA's step totals and rank 0's escalation flag, pushed into
+     * every CTA of the cluster before the barrier that ends the step: each
+     * CTA then reads them from its own shared memory */
+    __shared__ float s_parts[kDsmParts][5];
+    __shared__ int s_yield_all;
+    __shared__ double s_ancs[kDsmParts][2]; /* every CTA's FP64 anchor totals (pushed) */
     __shared__ int s_flag;  /* network start: resume a yielded network; in the loop: leave after this anchor */
     __shared__ unsigned s_au[kDsmParts], s_ab[kDsmParts], s_at[kDsmParts];
     const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
@@ -322,14 +305,11 @@ __global__ void __launch_bounds__(NT, 1)
             }
             anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, res, F2, M2);
             anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
-            if (threadIdx.x == 0) {
-                s_anc[0] = tF2;
-                s_anc[1] = tM2;
-            }
+            if (threadIdx.x == 0) anchor_push(s_ancs, rank, C, tF2, tM2);
             cl.sync();
             if (threadIdx.x == 0) {
                 double t[2];
-                anchor_totals(cl, s_anc, t);
+                anchor_totals(s_ancs, C, t);
                 q = mix_params(p, d.sqrt_dof);
                 mix_init(s, q);
                 mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
@@ -509,20 +489,33 @@ __global__ void __launch_bounds__(NT, 1)
             __syncthreads();
             if (threadIdx.x < 32) {
                 const Part t = block_totals(sh.slots);
-                if (threadIdx.x == 0) {
-                    s_part = t;
-                    if (rank == 0) s_yield = yield_at > 0 && idle >= yield_at;
+                /* rank 0's escalation flag: thread 0 read the idle count, so
+                 * lane 0's decision goes to every lane before any is pushed
+                 * (every CTA must take the same branch) */
+                const int yv = __shfl_sync(kFull, (int)(yield_at > 0 && idle >= yield_at), 0);
+                /* lane r pushes this CTA's totals into CTA r (remote stores
+                 * complete before the cluster barrier releases) */
+                if ((int)threadIdx.x < C) {
+                    const unsigned a = dsm_addr(&s_parts[rank][0], threadIdx.x);
+                    dsm_st1(a, t.P);
+                    dsm_st1(a + 4u, t.V2);
+                    dsm_st1(a + 8u, t.F2);
+                    dsm_st1(a + 12u, t.M2);
+                    dsm_st1(a + 16u, t.A);
+                    if (rank == 0) dsm_st1i(dsm_addr(&s_yield_all, threadIdx.x), yv);
                 }
             }
             cl.sync();
             if (threadIdx.x < 32) {
                 /* lane r takes rank r's totals: the same butterfly in every CTA */
                 Part t{0.f, 0.f, 0.f, 0.f, 0.f};
-                if ((int)threadIdx.x < C) t = *cl.map_shared_rank(&s_part, (int)threadIdx.x);
+                if ((int)threadIdx.x < C)
+                    t = Part{s_parts[threadIdx.x][0], s_parts[threadIdx.x][1], s_parts[threadIdx.x][2],
+                             s_parts[threadIdx.x][3], s_parts[threadIdx.x][4]};
                 t = warp_reduce(t);
                 if (threadIdx.x == 0) {
                     /* rank 0's escalation flag, the same in every CTA */
-                    const int y = *cl.map_shared_rank(&s_yield, 0);
+                    const int y = s_yield_all;
                     mix_step(s, q, t);
                     sh.coef = coef_of(s, need_anchor(s, q, t) || y);
                     s_flag = y;
@@ -543,14 +536,11 @@ __global__ void __launch_bounds__(NT, 1)
                 cl.sync();
                 anchor_eval_dsm(d, m, n0, nloc, b0, b1, t0, t1, s_f, res, F2, M2);
                 anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
-                if (threadIdx.x == 0) {
-                    s_anc[0] = tF2;
-                    s_anc[1] = tM2;
-                }
+                if (threadIdx.x == 0) anchor_push(s_ancs, rank, C, tF2, tM2);
                 cl.sync();
                 if (threadIdx.x == 0) {
                     double t[2];
-                    anchor_totals(cl, s_anc, t);
+                    anchor_totals(s_ancs, C, t);
                     mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
                     sh.coef = coef_of(s, 0);
                     s_flag = s_flag && !s.done;

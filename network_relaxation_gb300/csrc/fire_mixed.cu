@@ -99,8 +99,8 @@ __global__ void __launch_bounds__(NT, 1) k_fire_batch_mixed(const NetDev *nets, 
 /* A network relaxed by the C CTAs of one cluster (C SMs): nodes and items
  * are split over the CTAs (interleaved), u lives in global memory
  * (L2-resident), the hardware cluster barrier orders the passes, and each
- * CTA's totals are read by every other CTA through distributed shared
- * memory.  Thread 0 of every CTA advances an identical copy of the FIRE
+ * CTA pushes its totals into every other CTA's shared memory (distributed
+ * shared memory stores before the barrier).  Thread 0 of every CTA advances an identical copy of the FIRE
  * scalars from the same totals combined in the same order, so no broadcast
  * is needed. */
 
@@ -112,8 +112,8 @@ __global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets
     __shared__ MixShared sh;
     __shared__ NetDev s_d;
     __shared__ int s_slot;
-    __shared__ Part s_part;   /* this CTA's step totals */
-    __shared__ double s_anc[2]; /* this CTA's FP64 anchor totals */
+    __shared__ float s_parts[kDsmParts][5];  /* every CTA's step totals (pushed) */
+    __shared__ double s_ancs[kDsmParts][2]; /* every CTA's FP64 anchor totals (pushed) */
     const int rank = (int)cl.block_rank(), C = (int)cl.num_blocks();
     for (;;) {
         if (rank == 0 && threadIdx.x == 0) s_slot = atomicAdd(queue, 1);
@@ -138,14 +138,11 @@ __global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets
         double F2, M2, tF2, tM2;
         anchor_eval(d, tm, F2, M2);
         anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
-        if (threadIdx.x == 0) {
-            s_anc[0] = tF2;
-            s_anc[1] = tM2;
-        }
+        if (threadIdx.x == 0) anchor_push(s_ancs, rank, C, tF2, tM2);
         cl.sync();
         if (threadIdx.x == 0) {
             double t[2];
-            anchor_totals(cl, s_anc, t);
+            anchor_totals(s_ancs, C, t);
             q = mix_params(p, d.sqrt_dof);
             mix_init(s, q);
             mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
@@ -163,13 +160,23 @@ __global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets
             __syncthreads();
             if (threadIdx.x < 32) {
                 const Part t = block_totals(sh.slots);
-                if (threadIdx.x == 0) s_part = t;
+                /* lane r pushes this CTA's totals into CTA r */
+                if ((int)threadIdx.x < C) {
+                    const unsigned a = dsm_addr(&s_parts[rank][0], threadIdx.x);
+                    dsm_st1(a, t.P);
+                    dsm_st1(a + 4u, t.V2);
+                    dsm_st1(a + 8u, t.F2);
+                    dsm_st1(a + 12u, t.M2);
+                    dsm_st1(a + 16u, t.A);
+                }
             }
             cl.sync();
             if (threadIdx.x < 32) {
                 /* lane r takes rank r's totals: the same butterfly in every CTA */
                 Part t{0.f, 0.f, 0.f, 0.f, 0.f};
-                if ((int)threadIdx.x < C) t = *cl.map_shared_rank(&s_part, (int)threadIdx.x);
+                if ((int)threadIdx.x < C)
+                    t = Part{s_parts[threadIdx.x][0], s_parts[threadIdx.x][1], s_parts[threadIdx.x][2],
+                             s_parts[threadIdx.x][3], s_parts[threadIdx.x][4]};
                 t = warp_reduce(t);
                 if (threadIdx.x == 0) {
                     mix_step(s, q, t);
@@ -182,14 +189,11 @@ __global__ void __launch_bounds__(NT, 1) k_fire_cluster_mixed(const NetDev *nets
                 cl.sync();
                 anchor_eval(d, tm, F2, M2);
                 anchor_reduce(F2, M2, sh.dslots, tF2, tM2);
-                if (threadIdx.x == 0) {
-                    s_anc[0] = tF2;
-                    s_anc[1] = tM2;
-                }
+                if (threadIdx.x == 0) anchor_push(s_ancs, rank, C, tF2, tM2);
                 cl.sync();
                 if (threadIdx.x == 0) {
                     double t[2];
-                    anchor_totals(cl, s_anc, t);
+                    anchor_totals(s_ancs, C, t);
                     mix_certify(s, p, d.sqrt_dof, t[0], t[1]);
                     sh.coef = coef_of(s, 0);
                 }

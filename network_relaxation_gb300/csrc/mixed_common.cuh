@@ -652,15 +652,63 @@ static __device__ __noinline__ void mixed_energies(const NetDev &d, double *s_re
     }
 }
 
-/* FP64 anchor totals (sum of F2, max of M2) over the ranks, in rank order. */
-static __device__ void anchor_totals(cooperative_groups::cluster_group &cl, double *s_anc, double *t) {
-    const int C = (int)cl.num_blocks();
+/* ----- distributed shared memory (thread-block clusters) ----- */
+
+/* 32-bit shared::cluster address of shared-memory location p in CTA `rank`. */
+__device__ __forceinline__ unsigned dsm_addr(const void *p, unsigned rank) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float2 dsm_ld2(unsigned a) {
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void dsm_st1(unsigned a, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void dsm_st1i(unsigned a, int v) {
+    asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void dsm_st1d(unsigned a, double v) {
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ float4 dsm_ld4(unsigned a) {
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(a));
+    return v;
+}
+
+/* Cross-CTA totals are PUSHED: each CTA stores its value into its own slot
+ * of every CTA's array before the cluster barrier that ends the phase (the
+ * barrier's release / acquire orders the remote stores), and afterwards
+ * every CTA reads the C slots from its own shared memory: no remote load
+ * on the critical path after the barrier.  The next push into the same
+ * slots comes after at least one more cluster barrier, which every CTA
+ * reaches only after it has read them. */
+
+/* Thread 0: this CTA's FP64 anchor totals into slot `rank` of s_ancs in
+ * each of the cluster's C CTAs. */
+__device__ __forceinline__ void anchor_push(double (*s_ancs)[2], int rank, int C, double tF2, double tM2) {
+    for (int r = 0; r < C; ++r) {
+        const unsigned a = dsm_addr(&s_ancs[rank][0], (unsigned)r);
+        dsm_st1d(a, tF2);
+        dsm_st1d(a + 8u, tM2);
+    }
+}
+
+/* FP64 anchor totals (sum of F2, max of M2) over the ranks, in rank order,
+ * from the pushed slots. */
+__device__ __forceinline__ void anchor_totals(const double (*s_ancs)[2], int C, double *t) {
     t[0] = 0.0;
     t[1] = 0.0;
     for (int r = 0; r < C; ++r) {
-        const double *rp = cl.map_shared_rank(s_anc, r);
-        t[0] = t[0] + rp[0];
-        t[1] = fmax(t[1], rp[1]);
+        t[0] = t[0] + s_ancs[r][0];
+        t[1] = fmax(t[1], s_ancs[r][1]);
     }
 }
 
