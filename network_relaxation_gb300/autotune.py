@@ -19,8 +19,8 @@ classes tuned now.  Knobs and size classes:
                          on a cluster instead of the grid kernel): time per
                          FIRE step on lattices of 32^2 .. 181^2 nodes
   mixed, one network     NR_TILE_MIN_NODES (smallest network run on the tiled
-                         kernel), NR_TILE_THREADS (512: one CTA per SM, 256:
-                         two), NR_TILE_NODES (nodes per tile): time per
+                         kernel), NR_TILE_THREADS (512 or 768: one CTA per
+                         SM, 256: two), NR_TILE_NODES (nodes per tile): time per
                          FIRE step on lattices of 128^2 .. 1024^2 nodes
   mixed, batches         NR_CLUSTER (CTAs per network in the first phase),
                          NR_ESCALATE (idle fraction that triggers escalation),
@@ -127,10 +127,10 @@ def tune_fp64_single(nr, torch, log, quick):
 
 def tune_mixed_single(nr, torch, log, quick):
     sides = [128, 256, 512, 1024] if not quick else [256, 1024]
-    # (threads per CTA, tile nodes): one 512-thread CTA per SM, or two
-    # 256-thread CTAs per SM with smaller tiles; larger targets are cut down
-    # to fit shared memory anyway
-    tiles = [(512, 512), (512, 384), (256, 256), (256, 192)]
+    # (threads per CTA, tile nodes): one 512- or 768-thread CTA per SM, or
+    # two 256-thread CTAs per SM with smaller tiles; larger targets are cut
+    # down to fit shared memory anyway
+    tiles = [(512, 512), (512, 384), (768, 512), (256, 256), (256, 192)]
     res = {}
     for L in sides:
         h = nr.HostNetwork.lattice(L, L, 0.65, 0.05, 5, line_triples=True)

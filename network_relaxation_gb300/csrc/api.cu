@@ -221,11 +221,12 @@ static int tile_target_nodes() {
     const int v = env ? atoi(env) : 512;
     return v >= 64 && v <= 8192 ? v : 512;
 }
-/* Threads per CTA of the tiled kernel (NR_TILE_THREADS): 512, one CTA per
- * SM (default), or 256, two CTAs per SM. */
+/* Threads per CTA of the tiled kernel (NR_TILE_THREADS): 512 (default) or
+ * 768, one CTA per SM, or 256, two CTAs per SM. */
 static int tile_threads() {
     const char *env = knob("NR_TILE_THREADS");
-    return env && atoi(env) == 256 ? 256 : 512;
+    const int v = env ? atoi(env) : 512;
+    return v == 256 || v == 768 ? v : 512;
 }
 
 /* Builds and uploads the tiled layout of network 0 of S (one allocation);

@@ -278,9 +278,10 @@ static __device__ __noinline__ void tile_anchor_totals(const NetTile &tl, int G,
     M2 = m;
 }
 
-/* Instantiated for 512 threads per CTA with one CTA per SM, and for 256
- * threads with two CTAs per SM (smaller tiles; one CTA's barriers overlap
- * the other's work). */
+/* Instantiated for 512 or 768 threads per CTA with one CTA per SM (768: more
+ * warps to hide latency, fewer registers per thread), and for 256 threads
+ * with two CTAs per SM (smaller tiles; one CTA's barriers overlap the
+ * other's work). */
 
 /* Dynamic shared memory of a CTA: two record buffers of max_ro bytes, two
  * node-state buffers, the item results of one tile. */
@@ -609,9 +610,11 @@ size_t tile_smem(const NetTile &tl) {
     return tile_smem_bytes(tl.max_ro, tl.max_nodes, tl.max_own, tl.max_bonds, tl.max_tris);
 }
 
-/* The kernel instantiation for `threads` per CTA (512 or 256). */
+/* The kernel instantiation for `threads` per CTA (512, 768 or 256). */
 static const void *tile_kernel(int threads) {
-    return threads == 256 ? (const void *)k_fire_tile_mixed<256, 2> : (const void *)k_fire_tile_mixed<512, 1>;
+    if (threads == 256) return (const void *)k_fire_tile_mixed<256, 2>;
+    if (threads == 768) return (const void *)k_fire_tile_mixed<768, 1>;
+    return (const void *)k_fire_tile_mixed<512, 1>;
 }
 
 /* CTAs of the cooperative launch: co-resident CTAs per SM times SMs (0 when
@@ -622,8 +625,7 @@ int tile_grid_ctas(size_t smem, int threads) {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
     const void *k = tile_kernel(threads);
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads == 256 ? 256 : 512, smem) != cudaSuccess)
-        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem) != cudaSuccess) return 0;
     return per_sm * sms;
 }
 
@@ -638,7 +640,7 @@ cudaError_t launch_mixed_tile(const NetDev &d, const NetTile &tl, const FirePara
     FireParamsDev pp = p;
     unsigned long long bb = budget_ns;
     void *args[] = {&dd, &tt, &pp, &bb};
-    return launch_cooperative(k, ctas, threads == 256 ? 256 : 512, args, tile_smem(tl), stream);
+    return launch_cooperative(k, ctas, threads, args, tile_smem(tl), stream);
 }
 
 /* Spatial tiles of one network (see NetTile): at most about target_nodes

@@ -218,10 +218,11 @@ def test_sweep_graph_mixed_grid_equals_step_by_step(cuda):
     assert np.array_equal(pos, ppos)
 
 
-@pytest.mark.parametrize("threads", ["512", "256"])
+@pytest.mark.parametrize("threads", ["512", "768", "256"])
 @pytest.mark.parametrize("case", ["jitter", "per_item"])
 def test_mixed_tile_kernel_certified(cuda, case, threads, monkeypatch):
-    """The tiled kernel (one 512-thread CTA or two 256-thread CTAs per SM)
+    """The tiled kernel (one 512- or 768-thread CTA, or two 256-thread CTAs,
+    per SM)
     on a jittered lattice with generator triples (rest angles), and on one
     with a stiffness per bond and per triple (random in [0.5, 2] and
     [1e-3, 1e-2], as Mikado networks have): every state certified by the
