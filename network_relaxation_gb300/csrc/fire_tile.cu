@@ -291,6 +291,8 @@ __host__ __device__ inline size_t tile_smem_bytes(unsigned max_ro, int max_nodes
            8 * (size_t)max_bonds;
 }
 
+constexpr int kDescCache = 32;
+
 template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
     k_fire_tile_mixed(NetDev d, NetTile tl, FireParamsDev p, unsigned long long budget_ns) {
@@ -301,6 +303,9 @@ __global__ void __launch_bounds__(NT, MINB)
     /* FIRE scalars, advanced by thread 0 of every CTA (identical copies) */
     __shared__ MixScal s;
     __shared__ MixParams q;
+    /* the descriptors of the CTA's first kDescCache tiles, loaded once: a
+     * tile's first instructions then wait on shared memory, not on L2 */
+    __shared__ TileDesc s_desc[kDescCache];
     unsigned char *dyn = reinterpret_cast<unsigned char *>(s_dyn);
     unsigned char *const stage0 = dyn, *const stage1 = dyn + tl.max_ro;
     const size_t sbytes = tile_state_bytes(tl.max_nodes, tl.max_own);
@@ -342,6 +347,9 @@ __global__ void __launch_bounds__(NT, MINB)
     }
     __syncthreads();
     const int n_mine = (int)blockIdx.x < tl.n_tiles ? (tl.n_tiles - 1 - (int)blockIdx.x) / (int)G + 1 : 0;
+    for (int k = threadIdx.x; k < min(n_mine, kDescCache); k += NT) s_desc[k] = tl.desc[blockIdx.x + k * G];
+    __syncthreads();
+    auto desc = [&](int k) -> TileDesc { return k < kDescCache ? s_desc[k] : tl.desc[blockIdx.x + k * G]; };
     for (;;) {
         const Coef &c = sh.coef;
         if (c.done) {
@@ -362,7 +370,7 @@ __global__ void __launch_bounds__(NT, MINB)
         /* the pipeline: the record (TMA) and the node state (cp.async) of
          * tile k + 1 are in flight while tile k computes */
         if (n_mine > 0) {
-            const TileDesc td0 = tl.desc[blockIdx.x];
+            const TileDesc td0 = desc(0);
             if (threadIdx.x == 0)
                 tma_load(stage0, tl.ro + td0.ro_off, tile_segs(td0.nb, td0.nt, td0.no, td0.ni, td0.nh).total,
                          &s_mbar[0]);
@@ -389,10 +397,10 @@ __global__ void __launch_bounds__(NT, MINB)
             if (iss1 > uses1) mbar_wait(&s_mbar[1], uses1 & 1u, budget_ns);
         };
         for (int k = 0; k < n_mine; ++k) {
-            const int t = (int)blockIdx.x + k * (int)G, b = k & 1;
-            const TileDesc td = tl.desc[t];
+            const int b = k & 1;
+            const TileDesc td = desc(k);
             const bool more = k + 1 < n_mine;
-            const TileDesc tn = more ? tl.desc[t + (int)G] : td;
+            const TileDesc tn = more ? desc(k + 1) : td;
             const TileState &sc = b ? ts1 : ts0, &sn = b ? ts0 : ts1;
             unsigned char *const rec_n = b ? stage0 : stage1;
             __syncthreads();
