@@ -895,6 +895,20 @@ static int solo_split(const DeviceSet &S, const DsmPlan &pl, DsmPlan &ps, int &c
     return (int)small.size();
 }
 
+/* CTAs of the single-CTA launch beside `cap_clusters` clusters of C: the
+ * SMs the clusters leave (NR_SOLO_CTAS; 0: one per SM, oversubscribed),
+ * so that both launches are resident together from the start and the
+ * placement of the clusters does not depend on which launch the hardware
+ * schedules first. */
+static int solo_ctas(int cap_clusters, int C) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const char *env = knob("NR_SOLO_CTAS");
+    if (env) return std::max(0, atoi(env));
+    return std::max(1, sms - cap_clusters * C);
+}
+
 static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl, cudaStream_t stream,
                             bool capture = false) {
     const double frac = escalate_fraction();
@@ -936,8 +950,8 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
         if (n_small > 0) {
             NR_CUDA_TRY(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
             NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_small, 1, ps.bmax, ps.emax, ps.tmax, ps.ebmax,
-                                         ps.etmax, ps.resident, later.empty() ? 0.0 : frac, 0, to_dev(prm),
-                                         S.queue + 4, S.order + (S.n_nets - n_small), S.side));
+                                         ps.etmax, ps.resident, later.empty() ? 0.0 : frac, solo_ctas(cap, pl.C),
+                                         to_dev(prm), S.queue + 4, S.order + (S.n_nets - n_small), S.side));
             S.launches++;
             NR_CUDA_TRY(cudaEventRecord(S.ev_join, S.side));
             NR_CUDA_TRY(cudaStreamWaitEvent(stream, S.ev_join, 0));
@@ -970,8 +984,8 @@ static int relax_dsm_phases(DeviceSet &S, const nr_fire_params &prm, DsmPlan pl,
              * the side stream, with their own queue counters */
             NR_CUDA_TRY(cudaStreamWaitEvent(S.side, S.ev_fork, 0));
             NR_CUDA_TRY(launch_mixed_dsm(S.dev_array, S.dsm_array, n_small, 1, ps.bmax, ps.emax, ps.tmax, ps.ebmax,
-                                         ps.etmax, ps.resident, last ? 0.0 : frac, 0, to_dev(prm), S.queue + 4,
-                                         S.order + (S.n_nets - n_small), S.side));
+                                         ps.etmax, ps.resident, last ? 0.0 : frac, solo_ctas(cap, pl.C),
+                                         to_dev(prm), S.queue + 4, S.order + (S.n_nets - n_small), S.side));
             S.launches++;
             NR_CUDA_TRY(cudaEventRecord(S.ev_join, S.side));
             NR_CUDA_TRY(cudaStreamWaitEvent(stream, S.ev_join, 0));
@@ -1620,8 +1634,10 @@ int nr_batch_plan(nr_batch *b, int precision, char *buf, size_t cap) {
             const int n_small = solo_split(S, pl, ps, cap_clusters);
             const char *eh = knob("NR_ESCALATE_HOST");
             snprintf(out, sizeof out,
-                     "k_fire_dsm_mixed cluster=%d resident=%d solo_networks=%d escalation=%g (%s)", pl.C, pl.resident,
-                     n_small, escalate_fraction(), eh && atoi(eh) != 0 ? "host" : "device");
+                     "k_fire_dsm_mixed cluster=%d clusters=%d resident=%d solo_networks=%d solo_ctas=%d escalation=%g "
+                     "(%s)",
+                     pl.C, cap_clusters, pl.resident, n_small, n_small > 0 ? solo_ctas(cap_clusters, pl.C) : 0,
+                     escalate_fraction(), eh && atoi(eh) != 0 ? "host" : "device");
         } else {
             snprintf(out, sizeof out, "%s cluster=%d", cluster > 1 ? "k_fire_cluster_mixed" : "k_fire_batch_mixed",
                      cluster);
