@@ -283,13 +283,12 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
     const size_t o_nop = img.put(th.node_of_pos.data(), th.node_of_pos.size());
     const size_t o_bid = img.put(th.bid.data(), th.bid.size());
     const size_t o_tid = img.put(th.tid.data(), th.tid.size());
-    size_t o_u[2], o_v[2], o_f[2];
+    size_t o_u[2], o_vf[2];
     for (int c = 0; c < 2; ++c) {
         o_u[c] = img.add(sizeof(float4) * np);
-        o_v[c] = img.add(sizeof(float2) * np);
-        o_f[c] = img.add(sizeof(float2) * np);
+        o_vf[c] = img.add(sizeof(float4) * np);
     }
-    const size_t o_fah = img.add(sizeof(float2) * np), o_fal = img.add(sizeof(float2) * np);
+    const size_t o_fa = img.add(sizeof(float4) * np);
     const size_t o_cpart = img.add(sizeof(float) * 5 * 2 * (size_t)ctas);
     const size_t o_dpart = img.add(sizeof(double) * 2 * (size_t)ctas);
     const size_t o_bar = img.add(sizeof(unsigned long long));
@@ -309,11 +308,9 @@ static int build_tile_set(const nr_host_network &h, const Incidence &inc, const 
     tl.tid = (const int *)(b + o_tid);
     for (int c = 0; c < 2; ++c) {
         tl.u[c] = (float4 *)(b + o_u[c]);
-        tl.v[c] = (float2 *)(b + o_v[c]);
-        tl.f[c] = (float2 *)(b + o_f[c]);
+        tl.vf[c] = (float4 *)(b + o_vf[c]);
     }
-    tl.fa_hi = (float2 *)(b + o_fah);
-    tl.fa_lo = (float2 *)(b + o_fal);
+    tl.fa = (float4 *)(b + o_fa);
     tl.cpart = (float *)(b + o_cpart);
     tl.dpart = (double *)(b + o_dpart);
     tl.bar = (unsigned long long *)(b + o_bar);

@@ -148,8 +148,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
  * force.  Two of them: the next tile's state is copied in while the current
  * tile computes. */
 struct TileState {
-    float4 *u;
-    float2 *v, *f, *fah, *fal;
+    float4 *u;  /* double-float u {hi.x, hi.y, lo.x, lo.y} */
+    float4 *vf; /* {v.x, v.y, F.x, F.y} */
+    float4 *fa; /* own nodes: double-float anchor force {hi.x, hi.y, lo.x, lo.y} */
 };
 __host__ __device__ inline size_t tile_state_bytes(int max_nodes, int max_own) {
     return 32 * (size_t)max_nodes + 16 * (size_t)max_own;
@@ -157,10 +158,8 @@ __host__ __device__ inline size_t tile_state_bytes(int max_nodes, int max_own) {
 __device__ inline TileState tile_state_at(unsigned char *base, int max_nodes, int max_own) {
     TileState t;
     t.u = reinterpret_cast<float4 *>(base);
-    t.v = reinterpret_cast<float2 *>(base + 16 * (size_t)max_nodes);
-    t.f = t.v + max_nodes;
-    t.fah = t.f + max_nodes;
-    t.fal = t.fah + max_own;
+    t.vf = t.u + max_nodes;
+    t.fa = t.vf + max_nodes;
     return t;
 }
 
@@ -169,10 +168,8 @@ __device__ __forceinline__ void issue_own(const NetTile &tl, const TileDesc &td,
     for (int k = threadIdx.x; k < td.no; k += blockDim.x) {
         const int p = td.own_pos + k;
         cp_async16(ts.u + k, tl.u[cur] + p);
-        cp_async8(ts.v + k, tl.v[cur] + p);
-        cp_async8(ts.f + k, tl.f[cur] + p);
-        cp_async8(ts.fah + k, tl.fa_hi + p);
-        cp_async8(ts.fal + k, tl.fa_lo + p);
+        cp_async16(ts.vf + k, tl.vf[cur] + p);
+        cp_async16(ts.fa + k, tl.fa + p);
     }
 }
 /* Starts the copies of tile td's halo state (its record already in shared
@@ -184,8 +181,7 @@ __device__ __forceinline__ void issue_halo(const NetTile &tl, const TileDesc &td
     for (int h = threadIdx.x; h < td.nh; h += blockDim.x) {
         const int pp = halo[h];
         cp_async16(ts.u + td.no + h, tl.u[cur] + pp);
-        cp_async8(ts.v + td.no + h, tl.v[cur] + pp);
-        cp_async8(ts.f + td.no + h, tl.f[cur] + pp);
+        cp_async16(ts.vf + td.no + h, tl.vf[cur] + pp);
     }
 }
 
@@ -222,9 +218,11 @@ static __device__ __noinline__ void tile_anchor_eval(const NetDev &d, const NetT
         node_force_fp64_own<false>(d, i, fx, fy);
         d.f[i] = make_double2(fx, fy);
         const float hx = (float)fx, hy = (float)fy;
-        tl.fa_hi[p] = make_float2(hx, hy);
-        tl.fa_lo[p] = make_float2((float)(fx - (double)hx), (float)(fy - (double)hy));
-        tl.f[cur][p] = make_float2(hx, hy);
+        tl.fa[p] = make_float4(hx, hy, (float)(fx - (double)hx), (float)(fy - (double)hy));
+        float4 q = tl.vf[cur][p]; /* v stays, F = the anchor force */
+        q.z = hx;
+        q.w = hy;
+        tl.vf[cur][p] = q;
         const double t = dot2(fx, fy, fx, fy);
         F2 += t;
         M2 = fmax(M2, t);
@@ -329,7 +327,7 @@ __global__ void __launch_bounds__(NT, MINB)
     int cur = 0;
     for (int i = blockIdx.x * NT + threadIdx.x; i < tl.n_pos; i += G * NT) {
         tl.u[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        tl.v[0][i] = make_float2(0.f, 0.f);
+        tl.vf[0][i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     double tF2, tM2;
     tile_anchor_eval(d, tl, cur, sh.dslots, tF2, tM2);
@@ -359,8 +357,9 @@ __global__ void __launch_bounds__(NT, MINB)
                 const int i = tl.node_of_pos[pp];
                 if (i < 0) continue;
                 float4 w = tl.u[cur][pp];
-                float2 v = tl.v[cur][pp];
-                tile_pass_a(c, w, v, tl.f[cur][pp]);
+                const float4 q = tl.vf[cur][pp];
+                float2 v = make_float2(q.x, q.y);
+                tile_pass_a(c, w, v, make_float2(q.z, q.w));
                 d.v[i] = make_double2((double)v.x, (double)v.y);
             }
             break;
@@ -425,10 +424,11 @@ __global__ void __launch_bounds__(NT, MINB)
             /* pass A of own and halo nodes, in place */
             for (int kk = threadIdx.x; kk < nn; kk += NT) {
                 float4 w = sc.u[kk];
-                float2 v = sc.v[kk];
-                tile_pass_a(c, w, v, sc.f[kk]);
+                const float4 q = sc.vf[kk];
+                float2 v = make_float2(q.x, q.y);
+                tile_pass_a(c, w, v, make_float2(q.z, q.w));
                 sc.u[kk] = w;
-                sc.v[kk] = v;
+                sc.vf[kk] = make_float4(v.x, v.y, q.z, q.w);
             }
             __syncthreads();
             /* item pass into shared memory */
@@ -484,7 +484,8 @@ __global__ void __launch_bounds__(NT, MINB)
             for (int kk = threadIdx.x; kk < no; kk += NT) {
                 const unsigned fc = fcode[kk];
                 const int e0 = iptr[kk], eb = ibe[kk], e1 = iptr[kk + 1];
-                const float2 ah = sc.fah[kk], al = sc.fal[kk];
+                const float4 fa = sc.fa[kk];
+                const float2 ah = make_float2(fa.x, fa.y), al = make_float2(fa.z, fa.w);
                 float2 F = make_float2(0.f, 0.f);
                 if (fc != 0) {
                     /* the node's bond entries, then its triple entries (the
@@ -524,12 +525,12 @@ __global__ void __launch_bounds__(NT, MINB)
                     if (!(fc & 1)) F.x = 0.f;
                     if (!(fc & 2)) F.y = 0.f;
                 }
-                float2 v = sc.v[kk];
+                const float4 q = sc.vf[kk];
+                float2 v = make_float2(q.x, q.y);
                 v.x = fmaf(c.dtm, F.x, v.x);
                 v.y = fmaf(c.dtm, F.y, v.y);
                 tl.u[nxt][op + kk] = sc.u[kk];
-                tl.v[nxt][op + kk] = v;
-                tl.f[nxt][op + kk] = F;
+                tl.vf[nxt][op + kk] = make_float4(v.x, v.y, F.x, F.y);
                 P += fmaf(v.x, F.x, v.y * F.y);
                 V2 += fmaf(v.x, v.x, v.y * v.y);
                 const float f2 = fmaf(F.x, F.x, F.y * F.y);

@@ -229,9 +229,9 @@ struct NetTile {
     unsigned char *ro;                   /* tile records (anchor records rewritten in place) */
     const int *node_of_pos;              /* node id of each tile-order position (-1: padding) */
     const int *bid, *tid;                /* global bond / triple id of each tile item */
-    float4 *u[2];                        /* double-buffered state, tile order */
-    float2 *v[2], *f[2];
-    float2 *fa_hi, *fa_lo;               /* double-float anchor force, tile order */
+    float4 *u[2];                        /* double-buffered state, tile order: u {hi, lo}, */
+    float4 *vf[2];                       /* and {v, F} */
+    float4 *fa;                          /* double-float anchor force {hi, lo}, tile order */
     float *cpart;                        /* per CTA step totals (5 floats, two copies) */
     double *dpart;                       /* per CTA FP64 anchor totals (2 doubles each) */
     unsigned long long *bar;             /* grid barrier counter (monotonic) */
