@@ -546,6 +546,18 @@ const char *nr_tuning_source(void);
  * cluster=16" (NUL-terminated, truncated to cap). */
 int nr_network_plan(nr_network *dnet, int precision, char *buf, size_t cap);
 
+/* No reference counterpart; host only (no GPU needed): builds the spatial
+ * tile layout that the tiled mixed-precision kernel would use for this
+ * network with `ctas` CTAs and about `target_nodes` nodes per tile, and
+ * checks every invariant the kernel relies on (each node owned by exactly
+ * one tile, every local reference and incidence entry inside its tile,
+ * bond entries before triple entries per node, 16-byte aligned records,
+ * fcodes copied).  stats[0..5]: tiles, tile-order positions, largest tile
+ * (own + halo nodes), largest record (bytes), halo nodes over all tiles,
+ * violations found.  Returns NR_OK (violations counted in stats[5]) or
+ * the builder's error (NR_ERR_CAPACITY, NR_ERR_INVALID). */
+int nr_tile_layout_check(const nr_host_network *net, int ctas, int target_nodes, long long stats[6]);
+
 
 /* ------------------------------------------------------------------ */
 /* Batched relaxation of many independent networks in one launch       */

@@ -178,6 +178,16 @@ class HostNetwork:
                                          C.byref(out)), "nr_gen_mikado")
         return cls(out)
 
+    def tile_layout_check(self, ctas=152, target_nodes=512):
+        """Builds the tiled kernel's spatial layout on the host and checks
+        its invariants (nr_tile_layout_check): a dict of tiles, positions,
+        largest tile, largest record (bytes), halo nodes, violations."""
+        st = (C.c_longlong * 6)()
+        check(_capi.load().nr_tile_layout_check(self.handle, int(ctas), int(target_nodes), st),
+              "nr_tile_layout_check")
+        keys = ("tiles", "positions", "max_tile_nodes", "max_record_bytes", "halo_nodes", "violations")
+        return dict(zip(keys, (int(v) for v in st)))
+
     def get_triples(self):
         """get_triples (large_strain_relax.cu:116) into this network."""
         check(_capi.load().nr_get_triples(self._h), "get_triples")

@@ -841,3 +841,90 @@ int build_tile_layout(const nr_host_network &h, const Incidence &inc, const unsi
 }
 
 }  // namespace nr
+
+extern "C" int nr_tile_layout_check(const nr_host_network *h, int ctas, int target_nodes, long long stats[6]) {
+    using namespace nr;
+    if (!h || !stats || ctas < 1 || target_nodes < 1) return NR_ERR_INVALID;
+    for (int k = 0; k < 6; ++k) stats[k] = 0;
+    const int n = h->n_points, ne = h->n_edges(), nt = h->n_triples();
+    Incidence inc;
+    build_incidence(n, h->edge_ij.data(), ne, h->tri_hjk.data(), nt, true, true, inc);
+    std::vector<unsigned char> fc(n);
+    nr_host_network_fcodes(h, fc.data());
+    TileHost th;
+    const int rc = build_tile_layout(*h, inc, fc.data(), true, true, ctas, target_nodes, th);
+    if (rc != NR_OK) return rc;
+    long long bad = 0, halo_total = 0;
+    std::vector<int> owned(n, 0);
+    for (int t = 0; t < th.n_tiles; ++t) {
+        const TileDesc &td = th.desc[t];
+        const TileSegs g = tile_segs(td.nb, td.nt, td.no, td.ni, td.nh);
+        if (td.ro_off % 16 || g.total % 16 || td.ro_off + (long long)g.total > (long long)th.ro.size() ||
+            g.total > th.max_ro) {
+            ++bad;
+            continue;
+        }
+        if (td.own_pos % 16 || td.own_pos + td.no > th.n_pos || td.no + td.nh > th.max_nodes ||
+            td.nb > th.max_bonds || td.nt > th.max_tris || td.no > th.max_own)
+            ++bad;
+        const unsigned char *rec = th.ro.data() + td.ro_off;
+        const int nn = td.no + td.nh;
+        for (int k = 0; k < td.no; ++k) {
+            const int i = th.node_of_pos[td.own_pos + k];
+            if (i < 0 || i >= n) {
+                ++bad;
+                continue;
+            }
+            owned[i]++;
+            if (rec[g.fcode + k] != fc[i]) ++bad;
+        }
+        for (int k = 0; k < td.nb; ++k) {
+            unsigned r;
+            memcpy(&r, rec + g.bref + 4 * k, 4);
+            if ((int)(r & 0xffffu) >= nn || (int)(r >> 16) >= nn) ++bad;
+            const int b = th.bid[td.bond_off + k];
+            if (b < 0 || b >= ne) ++bad;
+        }
+        for (int k = 0; k < td.nt; ++k) {
+            unsigned r[2];
+            memcpy(r, rec + g.tref + 8 * k, 8);
+            if ((int)(r[0] & 0xffffu) >= nn || (int)(r[0] >> 16) >= nn || (int)r[1] >= nn) ++bad;
+            const int q = th.tid[td.tri_off + k];
+            if (q < 0 || q >= nt) ++bad;
+        }
+        for (int k = 0; k < td.nh; ++k) {
+            int pp;
+            memcpy(&pp, rec + g.halo + 4 * k, 4);
+            if (pp < 0 || pp >= th.n_pos || th.node_of_pos[pp] < 0) ++bad;
+        }
+        for (int k = 0; k < td.no; ++k) {
+            unsigned short a, b, e;
+            memcpy(&a, rec + g.iptr + 2 * k, 2);
+            memcpy(&e, rec + g.iptr + 2 * k + 2, 2);
+            memcpy(&b, rec + g.ibe + 2 * k, 2);
+            if (!(a <= b && b <= e && e <= td.ni)) {
+                ++bad;
+                continue;
+            }
+            for (int x = a; x < e; ++x) {
+                unsigned short c;
+                memcpy(&c, rec + g.inc + 2 * x, 2);
+                const bool tri = (c & 0x8000u) != 0;
+                if (tri != (x >= b)) ++bad;
+                if (!tri && (c >> 1) >= (unsigned)td.nb) ++bad;
+                if (tri && (((c & 0x7fffu) >> 2) >= (unsigned)td.nt || (c & 3u) > 2u)) ++bad;
+            }
+        }
+        halo_total += td.nh;
+    }
+    for (int i = 0; i < n; ++i)
+        if (owned[i] != 1) ++bad;
+    stats[0] = th.n_tiles;
+    stats[1] = th.n_pos;
+    stats[2] = th.max_nodes;
+    stats[3] = th.max_ro;
+    stats[4] = halo_total;
+    stats[5] = bad;
+    return NR_OK;
+}
+
