@@ -392,8 +392,8 @@ void or_energies(const or_model *m, const double *pos, double *e_stretch, double
 }
 
 /* Virial W = -sum_n r_n (x) F_n of the stretch and bending forces (no
- * counterpart in the reference, which reports no stress; the benchmark spec's
- * "stresses" output).  Per bond, with r = r_j - r_i (minimum image) and f the
+ * counterpart in the reference, which reports no stress; the library's
+ * stress output).  Per bond, with r = r_j - r_i (minimum image) and f the
  * stretch force on i of large_strain_relax.cu:386-414: W_ab = r_a f_b.  Per
  * triple, with arms a = r_hj, b = r_hk and the bending forces F_j, F_k of
  * :417-469: W_ab = -(a_a F_j,b + b_a F_k,b).  Each component is summed over
