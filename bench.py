@@ -276,6 +276,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU work per CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-c5", action="store_true", help="C4: skip the single-network C5 leg")
     ap.add_argument("--largest", type=int, default=0,
                     help="profiling case: only the K largest networks of the batch (not a bench line)")
     ap.add_argument("--strain-steps", type=int, default=0,
@@ -500,6 +501,15 @@ def main():
     if rank == 0 and not args.no_fp64 and c4 is not None:
         line["fp64"] = fp64_network_by_network(nr, hosts, prm_list, c4, sp)
         line["batched_vs_fp64_network_by_network"] = value / line["fp64"]["value"]
+    if rank == 0 and not args.no_c5 and not profiling_case:
+        # the single-network kernel beside the batch: C5's first shear
+        # increment, 1000 FIRE steps, W = 3
+        _, us, ms5, roof5, last5, _, _, _, _ = single_network_measure(nr, torch, "C5", "mixed", 1000, 3, 1)
+        line["c5_single_network"] = {
+            "what": "C5: one 1 048 576-node lattice (p=0.65, jitter 0.05, seed 5), first shear increment 0.0025, "
+                    "1000 FIRE steps, mixed precision, inputs larger than L2",
+            "us_per_fire_step": us, "ms_per_relaxation": ms5, "roofline": roof5,
+            "max_force_after_1000_steps": last5.max_force}
     if rank == 0 and not args.no_cpu and c4 is not None:
         n_threads = os.cpu_count() or 1
         v, rate, wall_cpu, desc = run_cpu_baseline(c4, n_threads, args.cpu_budget)
@@ -646,34 +656,28 @@ def mesh_cpu_baseline(h, gel, sx, sy, steps, threads=1):
     return len(a["points"]) * rep.steps / dt, rep.steps, dt
 
 
-def single_network_arm(args):
-    """--workload C2|C3|C5|M1: one large network relaxed by the cooperative
-    grid kernel (the whole GPU), FIRE steps capped: node-iterations/s.  M1
-    carries a gel (FP64 path)."""
-    import torch
-
-    import network_relaxation_gb300 as nr
-
-    rank = int(os.environ.get("RANK", "0"))
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    h, kb, dt_max = single_network(nr, args.workload)
+def single_network_measure(nr, torch, workload, precision, cap, warmup, steps):
+    """One large network (C2 / C3 / C5 / M1) relaxed from the first strain
+    increment of its protocol, FIRE steps capped at `cap`, timed with CUDA
+    events on the current stream: (node-iterations/s, us per FIRE step,
+    the roofline dict, the last report, network info, gel info, plan)."""
+    h, kb, dt_max = single_network(nr, workload)
     info = h.info()
     mesh = h.mesh_info()
     net = nr.Network(h, 1.0, kb)
-    if args.workload == "M1":
+    if workload == "M1":
         net.set_gel(*GEL_M1)
-        args.precision = "fp64"  # gel-coupled networks relax on the FP64 path
+        precision = "fp64"  # gel-coupled networks relax on the FP64 path
     H = net.maxy - net.miny
-    sx, sy = SINGLE[args.workload][2]
+    sx, sy = SINGLE[workload][2]
     net.affine_displace(net.miny, H, sx * H, sy * H)
     x0 = net.positions()
-    plan = net.plan(args.precision)
-    cap = min(args.max_steps, args.fire_cap)
+    plan = net.plan(precision)
     prm = nr.fire_params(alpha0=0.1, falpha=0.99, dt_max=dt_max, finc=1.1, fdec=0.5, nmin=5, mass=1.0, fcut=1e-10,
-                         max_steps=cap, criterion="max", precision=args.precision)
+                         max_steps=cap, criterion="max", precision=precision)
     stream = torch.cuda.current_stream()
-    times, steps = [], 0
-    for s in range(args.warmup + args.steps):
+    times, fire_steps, last = [], 0, None
+    for s in range(warmup + steps):
         net.set_positions(x0)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -681,39 +685,59 @@ def single_network_arm(args):
         rep = net.relax(prm)
         e1.record(stream)
         e1.synchronize()
-        if s >= args.warmup:
+        if s >= warmup:
             times.append(e0.elapsed_time(e1))
-            steps = rep.steps
+            fire_steps = rep.steps
             last = rep
+    net.close()
     ms = float(np.mean(times))
     n, e, t = info.n_points, info.n_edges / info.n_points, info.n_triples / info.n_points
-    g = mesh.n_facets / info.n_points if args.workload == "M1" else 0.0
-    bpn = (145 + 17 * e + 14 * t + 168 * g) if args.precision == "fp64" else (73 + 24 * e + 12 * t)
+    g = mesh.n_facets / info.n_points if workload == "M1" else 0.0
+    bpn = (145 + 17 * e + 14 * t + 168 * g) if precision == "fp64" else (73 + 24 * e + 12 * t)
     hbm = (json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs")
            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else None) or 6800.0
-    rate = n * steps / (ms / 1e3)
+    rate = n * fire_steps / (ms / 1e3)
     achieved = bpn * rate / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": plan}
+    return rate, 1e3 * ms / fire_steps, ms, roof, last, info, mesh, h, precision
+
+
+def single_network_arm(args):
+    """--workload C2|C3|C5|M1: one large network relaxed on the whole GPU
+    (the tiled kernel, or the grid kernel below its size threshold), FIRE
+    steps capped: node-iterations/s.  M1 carries a gel (FP64 path)."""
+    import torch
+
+    import network_relaxation_gb300 as nr
+
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    cap = min(args.max_steps, args.fire_cap)
+    rate, us, ms, roof, last, info, mesh, h, precision = single_network_measure(
+        nr, torch, args.workload, args.precision, cap, args.warmup, args.steps)
     extra = {}
     if args.workload == "M1" and rank == 0 and not args.no_cpu:
+        sx, sy = SINGLE["M1"][2]
         cpu_rate, cpu_steps, cpu_s = mesh_cpu_baseline(h, GEL_M1, sx, sy, 20)
         extra["cpu_baseline"] = {"value": cpu_rate, "unit": "node-iterations/s", "cores": 1, "kind": "port",
                                  "sample": "the oracle's FP64 FIRE with the gel, %d iterations of the same network "
                                            "and strain step (%.1f s)" % (cpu_steps, cpu_s)}
     if rank == 0:
+        n = info.n_points
         print(json.dumps({
             "metric": "node-iterations/s, one network (%s), first strain step, FIRE capped at %d steps"
                       % (args.workload, cap),
             "value": rate, "unit": "node-iterations/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "us_per_fire_step": 1e3 * ms / steps, "higher_is_better": True, "scaling": "replicas",
-            "relaxation": {"fire_steps": steps, "status": last.status, "max_force": last.max_force,
+            "ms_per_step": ms, "us_per_fire_step": us, "higher_is_better": True, "scaling": "replicas",
+            "relaxation": {"fire_steps": last.steps, "status": last.status, "max_force": last.max_force,
                            "energy": last.e_stretch + last.e_bend, "stress_xy": last.stress_xy},
-            "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32+f64" if precision == "mixed" else "f64", "data": "synthetic",
             "config": {"workload": "%s: %s, N=%d E=%d T=%d F=%d" % (args.workload, SINGLE[args.workload][0], n,
                                                                      info.n_edges, info.n_triples, mesh.n_facets),
-                       "precision": args.precision},
+                       "precision": precision},
             "gpu_launches": 3 * args.steps,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "kernel": plan},
+            "roofline": roof,
             **extra,
         }))
     return 0
