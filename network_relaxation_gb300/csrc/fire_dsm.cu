@@ -454,15 +454,7 @@ __global__ void __launch_bounds__(NT, 1)
                             const int ls = (int)((code >> 2) & 0x3ffffffu) - s_m.to[r * spr];
                             const float4 qv = dsm_ld4(s_at[r] + 16u * (unsigned)ls);
                             float gx, gy, mg;
-                            if (role == 0) {
-                                gx = -(qv.x + qv.z);
-                                gy = -(qv.y + qv.w);
-                                mg = fabsf(qv.x) + fabsf(qv.y) + fabsf(qv.z) + fabsf(qv.w);
-                            } else {
-                                gx = role == 1 ? qv.x : qv.z;
-                                gy = role == 1 ? qv.y : qv.w;
-                                mg = fabsf(gx) + fabsf(gy);
-                            }
+                            tri_entry(qv, role, gx, gy, mg);
                             dF.x += gx;
                             dF.y += gy;
                             mag += mg;

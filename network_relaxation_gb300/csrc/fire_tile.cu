@@ -506,15 +506,7 @@ __global__ void __launch_bounds__(NT, MINB)
                         const int role = code & 3;
                         const float4 qv = s_tdf[(code & 0x7fffu) >> 2];
                         float gx, gy, mg;
-                        if (role == 0) {
-                            gx = -(qv.x + qv.z);
-                            gy = -(qv.y + qv.w);
-                            mg = fabsf(qv.x) + fabsf(qv.y) + fabsf(qv.z) + fabsf(qv.w);
-                        } else {
-                            gx = role == 1 ? qv.x : qv.z;
-                            gy = role == 1 ? qv.y : qv.w;
-                            mg = fabsf(gx) + fabsf(gy);
-                        }
+                        tri_entry(qv, role, gx, gy, mg);
                         dF.x += gx;
                         dF.y += gy;
                         mag += mg;

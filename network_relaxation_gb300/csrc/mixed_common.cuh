@@ -193,6 +193,21 @@ struct UView {
     }
 };
 
+/* A triple entry's FP32 force change on its node, q = the triple's
+ * {dF_j, dF_k}: role 0 (the hinge) -(dF_j + dF_k), role 1 dF_j, role 2
+ * dF_k; m = the sum of the |components| involved.  Selects instead of a
+ * branch per role (the lanes of a warp hold different roles), with the
+ * case-by-case form's values and summation order. */
+__device__ __forceinline__ void tri_entry(const float4 q, int role, float &gx, float &gy, float &m) {
+    const bool h = role == 0, k2 = role == 2;
+    const float sx = (k2 ? q.z : q.x) + (h ? q.z : 0.f);
+    const float sy = (k2 ? q.w : q.y) + (h ? q.w : 0.f);
+    gx = h ? -sx : sx;
+    gy = h ? -sy : sy;
+    const float ax = fabsf(q.x), ay = fabsf(q.y), az = fabsf(q.z), aw = fabsf(q.w);
+    m = (((k2 ? az : ax) + (k2 ? aw : ay)) + (h ? az : 0.f)) + (h ? aw : 0.f);
+}
+
 /* FP32 force change since the anchor for node i, gathered from the item
  * results bdf/tdf in incidence order; mag = sum of the entries' |df|. */
 __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag) {
@@ -218,15 +233,7 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
             const int role = code & 3;
             const float4 q = d.tdf[code >> 2];
             float gx, gy, m;
-            if (role == 0) {
-                gx = -(q.x + q.z);
-                gy = -(q.y + q.w);
-                m = fabsf(q.x) + fabsf(q.y) + fabsf(q.z) + fabsf(q.w);
-            } else {
-                gx = role == 1 ? q.x : q.z;
-                gy = role == 1 ? q.y : q.w;
-                m = fabsf(gx) + fabsf(gy);
-            }
+            tri_entry(q, role, gx, gy, m);
             F.x += gx;
             F.y += gy;
             mag += m;
