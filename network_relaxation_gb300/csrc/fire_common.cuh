@@ -229,16 +229,11 @@ __device__ __forceinline__ void node_force_items_own(const NetDev &d, int i, dou
             const int code = d.tent[e];
             const double4 f = d.tfrc[code >> 2];
             const int role = code & 3;
-            if (role == 0) {
-                fx = fx + ((-f.x) - f.z);
-                fy = fy + ((-f.y) - f.w);
-            } else if (role == 1) {
-                fx = fx + f.x;
-                fy = fy + f.y;
-            } else {
-                fx = fx + f.z;
-                fy = fy + f.w;
-            }
+            /* selects, not a branch per role (lanes hold different roles):
+             * the hinge takes -(F_j + F_k) as (-F_j) - F_k, j F_j, k F_k */
+            const double hx = (-f.x) - f.z, hy = (-f.y) - f.w;
+            fx = fx + (role == 0 ? hx : (role == 1 ? f.x : f.z));
+            fy = fy + (role == 0 ? hy : (role == 1 ? f.y : f.w));
         }
     }
     if (kGel && d.use_gel) {

@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(NT, 1)
                             const int r = (int)(code >> 28) >> lg;
                             const int ls = (int)((code >> 1) & 0x7ffffffu) - s_m.bo[r * spr];
                             float2 df = dsm_ld2(s_ab[r] + 8u * (unsigned)ls);
-                            if (code & 1) df = make_float2(-df.x, -df.y);
+                            df = neg_if(df, code);
                             dF.x += df.x;
                             dF.y += df.y;
                             mag += fabsf(df.x) + fabsf(df.y);

@@ -260,16 +260,12 @@ __global__ void __launch_bounds__(kDsm64Threads, 1)
                                 const int role = code & 3;
                                 const int ls = (int)((code >> 2) & 0x3ffffffu) - m.to[r * spr];
                                 const double4 f = cl_ld4d(s_atf[r] + 32u * (unsigned)ls);
-                                if (role == 0) {
-                                    fx = fx + ((-f.x) - f.z);
-                                    fy = fy + ((-f.y) - f.w);
-                                } else if (role == 1) {
-                                    fx = fx + f.x;
-                                    fy = fy + f.y;
-                                } else {
-                                    fx = fx + f.z;
-                                    fy = fy + f.w;
-                                }
+                                /* selects, not a branch per role: the same
+                                 * operands and operations as the oracle's
+                                 * case-by-case sum */
+                                const double hx = (-f.x) - f.z, hy = (-f.y) - f.w;
+                                fx = fx + (role == 0 ? hx : (role == 1 ? f.x : f.z));
+                                fy = fy + (role == 0 ? hy : (role == 1 ? f.y : f.w));
                             }
                         }
                         if (!(fc & 1)) fx = 0.0;

@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(NT, MINB)
                     for (int e = e0; e < eb; ++e) {
                         const unsigned code = inc[e];
                         float2 df = s_bdf[code >> 1];
-                        if (code & 1) df = make_float2(-df.x, -df.y);
+                        df = neg_if(df, code);
                         dF.x += df.x;
                         dF.y += df.y;
                         mag += fabsf(df.x) + fabsf(df.y);

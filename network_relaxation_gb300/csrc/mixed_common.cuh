@@ -193,6 +193,13 @@ struct UView {
     }
 };
 
+/* -v when the entry's role bit is set, else v: the sign bit flipped
+ * exactly, without a branch (the lanes of a warp hold different roles). */
+__device__ __forceinline__ float2 neg_if(float2 v, unsigned code) {
+    const unsigned sg = (code & 1u) << 31;
+    return make_float2(__uint_as_float(__float_as_uint(v.x) ^ sg), __uint_as_float(__float_as_uint(v.y) ^ sg));
+}
+
 /* A triple entry's FP32 force change on its node, q = the triple's
  * {dF_j, dF_k}: role 0 (the hinge) -(dF_j + dF_k), role 1 dF_j, role 2
  * dF_k; m = the sum of the |components| involved.  Selects instead of a
@@ -219,7 +226,7 @@ __device__ __forceinline__ float2 node_dforce(const NetDev &d, int i, float &mag
         for (int e = __ldg(d.bptr + i); e < e1; ++e) {
             const int code = __ldg(d.bent + e);
             float2 df = d.bdf[code >> 1];
-            if (code & 1) df = make_float2(-df.x, -df.y);
+            df = neg_if(df, (unsigned)code);
             F.x += df.x;
             F.y += df.y;
             mag += fabsf(df.x) + fabsf(df.y);
