@@ -214,13 +214,9 @@ __device__ __forceinline__ void node_force_items_own(const NetDev &d, int i, dou
         for (int e = d.bptr[i]; e < e1; ++e) {
             const int code = d.bent[e];
             const double2 f = d.bfrc[code >> 1];
-            if (code & 1) {
-                fx = fx + (-f.x);
-                fy = fy + (-f.y);
-            } else {
-                fx = fx + f.x;
-                fy = fy + f.y;
-            }
+            /* a select, not a branch: the same sum */
+            fx = fx + ((code & 1) ? -f.x : f.x);
+            fy = fy + ((code & 1) ? -f.y : f.y);
         }
     }
     if (d.use_triples) {

@@ -243,13 +243,9 @@ __global__ void __launch_bounds__(kDsm64Threads, 1)
                                 const int r = (int)(code >> 28) >> lg;
                                 const int ls = (int)((code >> 1) & 0x7ffffffu) - m.bo[r * spr];
                                 const double2 f = cl_ld2d(s_abf[r] + 16u * (unsigned)ls);
-                                if (code & 1) {
-                                    fx = fx + (-f.x);
-                                    fy = fy + (-f.y);
-                                } else {
-                                    fx = fx + f.x;
-                                    fy = fy + f.y;
-                                }
+                                /* a select, not a branch: the same sum */
+                                fx = fx + ((code & 1) ? -f.x : f.x);
+                                fy = fy + ((code & 1) ? -f.y : f.y);
                             }
                         }
                         if (d.use_triples) {
