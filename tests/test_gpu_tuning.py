@@ -100,3 +100,21 @@ def test_table_sets_the_batch_cluster(lib, tmp_path):
         b = nr.Batch(hs, ks=1.0, kb=1e-3)
         assert ("cluster=%d" % c) in b.plan("mixed"), b.plan("mixed")
         assert ("cluster=%d" % c) in b.plan("fp64"), b.plan("fp64")
+
+
+def test_table_sets_the_single_cta_launch(lib, tmp_path):
+    """NR_SOLO_CTAS sizes the one-network-per-CTA launch beside the
+    clusters (default: the SMs the clusters leave)."""
+    hs = []
+    for L in (60, 60, 20, 20, 20):  # two networks on clusters, three small ones on single CTAs
+        h = nr.HostNetwork.lattice(L, L, 0.7, 0.0, 30 + L)
+        h.get_triples()
+        hs.append(h)
+    b = nr.Batch(hs, ks=1.0, kb=1e-3)
+    plan = b.plan("mixed")
+    if "solo_networks=0" in plan:
+        pytest.skip("no single-CTA split for this batch: " + plan)
+    t = tmp_path / "s.txt"
+    t.write_text("NR_SOLO_CTAS 7\n")
+    assert lib.nr_tuning_load(str(t).encode()) == 1
+    assert "solo_ctas=7" in b.plan("mixed"), b.plan("mixed")
