@@ -493,6 +493,7 @@ __global__ void __launch_bounds__(NT, MINB)
                      * entry; own nodes are ordered by list lengths */
                     float2 dF = make_float2(0.f, 0.f);
                     float mag = 0.f;
+#pragma unroll 4
                     for (int e = e0; e < eb; ++e) {
                         const unsigned code = inc[e];
                         float2 df = s_bdf[code >> 1];
@@ -501,6 +502,7 @@ __global__ void __launch_bounds__(NT, MINB)
                         dF.y += df.y;
                         mag += fabsf(df.x) + fabsf(df.y);
                     }
+#pragma unroll 4
                     for (int e = eb; e < e1; ++e) {
                         const unsigned code = inc[e];
                         const int role = code & 3;
