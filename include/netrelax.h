@@ -536,7 +536,9 @@ int nr_energies_noalloc(int n_points, int npairs, int ntriples, double width, do
  * nr_tuning_load replaces the table (returns the entry count, NR_ERR_IO or
  * NR_ERR_PARSE); nr_tuning_value returns a knob's numeric value as the
  * library sees it (NaN when unset); nr_tuning_source names the table in use
- * ("" for none; valid until the next nr_tuning_load). */
+ * ("" for none; the string stays valid for the life of the process, as
+ * does every table loaded, so a load on one thread never invalidates what
+ * another thread read). */
 int nr_tuning_load(const char *path);
 double nr_tuning_value(const char *name);
 const char *nr_tuning_source(void);

@@ -24,19 +24,34 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <vector>
 
 #include "nr_internal.h"
 
 namespace nr {
 namespace {
 
+/* Every table and source name ever loaded stays allocated for the life of
+ * the process: knob() and nr_tuning_source() hand out pointers into them,
+ * which a later nr_tuning_load on another thread must not invalidate. */
+using Table = std::map<std::string, std::string>;
 std::mutex g_mu;
-std::map<std::string, std::string> g_table;
+std::vector<std::unique_ptr<Table>> g_tables;
+std::vector<std::unique_ptr<std::string>> g_sources;
+const Table *g_table = nullptr;
+const std::string *g_source = nullptr;
 bool g_loaded = false;
-std::string g_source;
+
+void install_locked(Table &&t, const std::string &source) {
+    g_tables.push_back(std::unique_ptr<Table>(new Table(std::move(t))));
+    g_sources.push_back(std::unique_ptr<std::string>(new std::string(source)));
+    g_table = g_tables.back().get();
+    g_source = g_sources.back().get();
+}
 
 int parse_table(const std::string &path, std::map<std::string, std::string> &out) {
     std::ifstream in(path);
@@ -82,11 +97,8 @@ void load_default_locked() {
     const char *env = getenv("NR_TUNING_FILE");
     const std::string path = env ? std::string(env) : default_table_path();
     if (path.empty()) return;
-    std::map<std::string, std::string> t;
-    if (parse_table(path, t) >= 0) {
-        g_table.swap(t);
-        g_source = path;
-    }
+    Table t;
+    if (parse_table(path, t) >= 0) install_locked(std::move(t), path);
 }
 
 }  // namespace
@@ -96,8 +108,9 @@ const char *knob(const char *name) {
     if (env) return env;
     std::lock_guard<std::mutex> lock(g_mu);
     load_default_locked();
-    auto it = g_table.find(name);
-    return it == g_table.end() ? nullptr : it->second.c_str();
+    if (!g_table) return nullptr;
+    auto it = g_table->find(name);
+    return it == g_table->end() ? nullptr : it->second.c_str();
 }
 
 }  // namespace nr
@@ -108,14 +121,13 @@ extern "C" {
 
 int nr_tuning_load(const char *path) {
     if (!path) return fail(NR_ERR_INVALID, "nr_tuning_load: null path");
-    std::map<std::string, std::string> t;
+    Table t;
     const int n = parse_table(path, t);
     if (n == NR_ERR_IO) return fail(NR_ERR_IO, std::string("cannot open ") + path);
     if (n < 0) return fail(NR_ERR_PARSE, std::string("malformed tuning table ") + path);
     std::lock_guard<std::mutex> lock(g_mu);
-    g_table.swap(t);
+    install_locked(std::move(t), path);
     g_loaded = true;
-    g_source = path;
     return n;
 }
 
@@ -131,7 +143,7 @@ double nr_tuning_value(const char *name) {
 const char *nr_tuning_source(void) {
     std::lock_guard<std::mutex> lock(g_mu);
     load_default_locked();
-    return g_source.c_str();
+    return g_source ? g_source->c_str() : "";
 }
 
 }  // extern "C"
