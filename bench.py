@@ -19,17 +19,32 @@ Also reported in the same JSON line:
   roofline      the batch kernel's algorithmic bytes / its event-timed
                 duration vs the measured HBM copy bandwidth; traffic = DRAM
                 bytes per launch from the committed ncu summary
-  fp64          plain FP64 path, network by network (grid kernel), on a
-                stratified sample, extrapolated by FP64 work to the batch
+  energy_rel_err_vs_fp64_oracle / energy_vs_converged_fp64_minimum
+                the mixed energies against the FP64 oracle's at max|F| <
+                1e-10 and against its relaxation continued to 1e-12
+  fp64_batched  the plain FP64 path on the same batch in one launch (the
+                oracle's bits, checked), and the mixed results' errors
+                against it: energy, shear stress, secant modulus, positions
+  fp64          plain FP64 path, network by network, on a stratified
+                sample, extrapolated by FP64 work to the batch
+  c5_single_network
+                one 1 048 576-node network on the tiled kernel, 1000 FIRE
+                steps, with its roofline (--no-c5 skips it)
   cpu_baseline  the CPU oracle (FP64 restatement of run_fire_md) on all host
-                threads, on a bounded sample, extrapolated by FP64 work
+                threads, on a bounded sample of the batch plus its longest
+                network timed on one thread (the makespan is the larger)
   clocks        nvidia-smi samples during the timed region
 --impl reference times the CPU restatement alone (the reference's own GPU
 code cannot run on this machine; its CPU path sparse_relax needs SuiteSparse).
+Other workloads (--workload): C2 / C3 / C5 / M1 one large network, P3 / P5
+the strain protocols as CUDA graphs (mixed and FP64), S1 the C1 sweep, L1
+the linear-response solve, A1 the analyses, IO the file readers.
 
-Multi-GPU (torchrun): every rank relaxes its own 512-network batch (seeds
-offset by rank), no collective on the data path; value = all networks /
-max-over-ranks time ("scaling": "weak").
+Multi-GPU (torchrun): --shard weak (default): every rank relaxes its own
+512-network batch (seeds offset by rank), "scaling": "weak"; --shard
+split: ONE batch partitioned across the ranks by expected cost,
+"scaling": "strong".  No collective on the data path; value = all
+networks / max-over-ranks time.
 """
 import argparse
 import ctypes as C
