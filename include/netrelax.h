@@ -560,6 +560,18 @@ int nr_network_plan(nr_network *dnet, int precision, char *buf, size_t cap);
  * the builder's error (NR_ERR_CAPACITY, NR_ERR_INVALID). */
 int nr_tile_layout_check(const nr_host_network *net, int ctas, int target_nodes, long long stats[6]);
 
+/* No reference counterpart; host only: builds the sub-block layout of the
+ * thread-block-cluster kernels for this network and checks it: every node
+ * in exactly one gather record of its own sub-block, records ordered by
+ * decreasing triple then bond entry counts, each record's entry ranges,
+ * counts and fcode equal to the incidence lists, every bond and triple
+ * slot owned by the sub-block of its first node / hinge, every resolved
+ * incidence entry pointing at the item slot and role it came from.
+ * stats[0..3]: sub-block size (nodes), sub-blocks in use, nodes,
+ * violations found.  Returns NR_OK, or NR_ERR_CAPACITY when the network
+ * exceeds the layout's encoding. */
+int nr_dsm_layout_check(const nr_host_network *net, long long stats[4]);
+
 
 /* ------------------------------------------------------------------ */
 /* Batched relaxation of many independent networks in one launch       */

@@ -178,6 +178,15 @@ class HostNetwork:
                                          C.byref(out)), "nr_gen_mikado")
         return cls(out)
 
+    def dsm_layout_check(self):
+        """Builds the cluster kernels' sub-block layout (item slots, resolved
+        incidence, gather records) on the host and checks it
+        (nr_dsm_layout_check): a dict of sub-block size, sub-blocks, nodes,
+        violations."""
+        st = (C.c_longlong * 4)()
+        check(_capi.load().nr_dsm_layout_check(self.handle, st), "nr_dsm_layout_check")
+        return dict(zip(("sub_block_nodes", "sub_blocks", "nodes", "violations"), (int(v) for v in st)))
+
     def tile_layout_check(self, ctas=152, target_nodes=512):
         """Builds the tiled kernel's spatial layout on the host and checks
         its invariants (nr_tile_layout_check): a dict of tiles, positions,

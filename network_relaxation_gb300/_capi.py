@@ -132,6 +132,7 @@ SIGNATURES = {
     "nr_tuning_source": (C.c_char_p, []),
     "nr_network_plan": (C.c_int, [P, C.c_int, C.c_char_p, C.c_size_t]),
     "nr_tile_layout_check": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_longlong)]),
+    "nr_dsm_layout_check": (C.c_int, [P, C.POINTER(C.c_longlong)]),
     "nr_batch_plan": (C.c_int, [P, C.c_int, C.c_char_p, C.c_size_t]),
     "nr_sweep": (C.c_int, [P, C.c_double, C.c_double, C.POINTER(FireParams), c_double_p, c_double_p,
                            C.POINTER(StepRecord), C.c_int, c_int_p, c_double_p, P]),

@@ -2048,3 +2048,99 @@ int nr_batch_relax(nr_batch *b, const nr_fire_params *params, nr_report *reports
 }
 
 }  // extern "C"
+
+extern "C" int nr_dsm_layout_check(const nr_host_network *h, long long stats[4]) {
+    if (!h || !stats) return fail(NR_ERR_INVALID, "nr_dsm_layout_check: null argument");
+    for (int k = 0; k < 4; ++k) stats[k] = 0;
+    const int n = h->n_points, ne = h->n_edges(), nt = h->n_triples();
+    Incidence inc;
+    build_incidence(n, h->edge_ij.data(), ne, h->tri_hjk.data(), nt, true, true, inc);
+    std::vector<unsigned char> fc(n);
+    nr_host_network_fcodes(h, fc.data());
+    Image img;
+    NetOff o;
+    memset(&o, 0, sizeof o);
+    NetDsm m;
+    build_dsm_layout(*h, inc, fc.data(), img, o, m);
+    if (m.bsub <= 0) return NR_ERR_CAPACITY;
+    const char *base = img.bytes.data();
+    const int2 *bref = (const int2 *)(base + o.dsm_bref);
+    const int *bidx = (const int *)(base + o.dsm_bidx);
+    const int4 *tref = (const int4 *)(base + o.dsm_tref);
+    const int *bent = (const int *)(base + o.dsm_bent);
+    const int *tent = (const int *)(base + o.dsm_tent);
+    const int4 *grec = (const int4 *)(base + o.dsm_grec);
+    const int bsub = m.bsub;
+    long long bad = 0;
+    auto ref_of = [&](int v) { return ((v / bsub) << 16) | (v % bsub); };
+    std::vector<int> seen(n, 0);
+    int parts = 0;
+    for (int g = 0; g * bsub < n; ++g) {
+        ++parts;
+        const int v0 = g * bsub, v1 = std::min(n, v0 + bsub);
+        for (int k = v0; k < v1; ++k) {
+            const int4 r = grec[k];
+            const int v = r.x & 0x0fffffff, f = (int)((unsigned)r.x >> 28);
+            if (v < v0 || v >= v1) {
+                ++bad;
+                continue;
+            }
+            seen[v]++;
+            const int nbe = inc.bptr[v + 1] - inc.bptr[v], nte = inc.tptr[v + 1] - inc.tptr[v];
+            if (f != (fc[v] & 3) || r.y != inc.bptr[v] || r.w != inc.tptr[v] || (r.z & 0xffff) != nbe ||
+                ((unsigned)r.z >> 16) != (unsigned)nte)
+                ++bad;
+            if (k > v0) {
+                const int u = grec[k - 1].x & 0x0fffffff;
+                if (u >= v0 && u < v1) {
+                    const int pnb = inc.bptr[u + 1] - inc.bptr[u], pnt = inc.tptr[u + 1] - inc.tptr[u];
+                    if (pnt < nte || (pnt == nte && pnb < nbe)) ++bad; /* order: decreasing (triples, bonds) */
+                }
+            }
+        }
+    }
+    for (int v = 0; v < n; ++v)
+        if (seen[v] != 1) ++bad;
+    /* item slots: owned by the sub-block of the bond's first node / the
+     * triple's hinge, with that item's node references */
+    for (int g = 0; g < kDsmParts; ++g) {
+        for (int sl = m.bo[g]; sl < m.bo[g + 1]; ++sl) {
+            const int b = bidx[sl];
+            if (b < 0 || b >= ne) {
+                ++bad;
+                continue;
+            }
+            const int i = h->edge_ij[2 * b], j = h->edge_ij[2 * b + 1];
+            if (i / bsub != g || bref[sl].x != ref_of(i) || bref[sl].y != ref_of(j)) ++bad;
+        }
+        for (int sl = m.to[g]; sl < m.to[g + 1]; ++sl) {
+            const int4 r = tref[sl];
+            if (r.w < 0 || r.w >= nt) {
+                ++bad;
+                continue;
+            }
+            const int hh = h->tri_hjk[3 * r.w], jj = h->tri_hjk[3 * r.w + 1], kk = h->tri_hjk[3 * r.w + 2];
+            if (hh / bsub != g || r.x != ref_of(hh) || r.y != ref_of(jj) || r.z != ref_of(kk)) ++bad;
+        }
+    }
+    /* resolved incidence entries: owner sub-block, slot, role of the entry
+     * they replace */
+    for (size_t e = 0; e < inc.bent.size(); ++e) {
+        const unsigned c = (unsigned)bent[e];
+        const int g = (int)(c >> 28), sl = (int)((c >> 1) & 0x7ffffffu);
+        const int b = inc.bent[e] >> 1;
+        if ((int)(c & 1u) != (inc.bent[e] & 1) || sl < m.bo[g] || sl >= m.bo[g + 1] || bidx[sl] != b) ++bad;
+    }
+    for (size_t e = 0; e < inc.tent.size(); ++e) {
+        const unsigned c = (unsigned)tent[e];
+        const int g = (int)(c >> 28), sl = (int)((c >> 2) & 0x3ffffffu);
+        const int t = inc.tent[e] >> 2;
+        if ((int)(c & 3u) != (inc.tent[e] & 3) || sl < m.to[g] || sl >= m.to[g + 1] || tref[sl].w != t) ++bad;
+    }
+    stats[0] = bsub;
+    stats[1] = parts;
+    stats[2] = n;
+    stats[3] = bad;
+    return NR_OK;
+}
+
